@@ -1,0 +1,396 @@
+#!/usr/bin/env python3
+"""Benchmark of the RVGP pipeline on one GB300: fit + predict wall time.
+
+Workload (default): torus R=1, r=0.35, n=20000 points with N(0, 0.01²) jitter,
+k=20, m=200 eigenpairs; field = rotational ∂/∂φ + a smoothed random field
+(t=50); train on a seeded 30 % (the fit's own 80/20 split inside, as in the
+reference), 200 Adam steps on the log marginal likelihood with the
+hand-written adjoint, predict mean and variance at the remaining 70 %.
+
+A step = the whole pipeline from points to posterior: kNN graph, gauges,
+connections, Laplacians, eigenpairs of L and Lc, lift, GP fit, GP predict.
+``value`` = seconds per step of the mixed-precision form with inputs resident
+in HBM (CUDA events on the launching stream, L2 flushed between steps).
+``fp64_form_s`` = the same step in the plain FP64 form; ``pred_rel_err`` = the
+relative L2 difference of the two forms' posterior means.  ``e2e`` = the same
+step through the public API with host numpy inputs and outputs.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+import os
+
+_THREADS = str(os.cpu_count() or 1)
+for _v in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
+    os.environ.setdefault(_v, _THREADS)
+
+import argparse  # noqa: E402
+import json  # noqa: E402
+import subprocess  # noqa: E402
+import sys  # noqa: E402
+import threading  # noqa: E402
+import time  # noqa: E402
+
+import numpy as np  # noqa: E402
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    "torus_n20000_k20_m200": dict(kind="torus", n=20000, k=20, m=200, train_frac=0.3, t_smooth=50.0, adam=200,
+                                  rotational=True),
+    "sphere_n2000_k10_m50": dict(kind="sphere", n=2000, k=10, m=50, train_frac=0.5, t_smooth=100.0, adam=200,
+                                 rotational=False),
+}
+METRIC = "RVGP fit+predict wall s (mixed vs FP64 GPU, equal pred. error); HBM GB/s"
+
+
+def make_inputs(wl, seed=0):
+    from rvgp_gb300.workloads import make_points, rotational_field, split
+    X = make_points(wl["kind"], wl["n"], seed=seed)
+    train, test = split(wl["n"], wl["train_frac"], seed=seed)
+    return X, train, test
+
+
+def make_field(X, wl, seed=0):
+    """Ground-truth field (outside the timed region): rotational + smoothed random tangent field."""
+    import rvgp_gb300 as RVGP
+    from rvgp_gb300.workloads import rotational_field
+    d = RVGP.create_data_object(X, n_neighbors=wl["k"], n_eigenpairs=wl["m"], verbose=False)
+    d.random_vector_field(seed=seed)
+    d.smooth_vector_field(t=wl["t_smooth"])
+    v = d.vectors
+    if wl["rotational"]:
+        import torch
+        from rvgp_gb300 import _core
+        rot = torch.as_tensor(rotational_field(X), device="cuda")
+        rot = _core.frame_map(d._dev.T, d.dim_man, rot, "project")
+        v = v + rot.cpu().numpy()
+    return np.ascontiguousarray(v)
+
+
+# ------------------------------------------------------------------------------ our arm
+def pipeline(X, V, train, test, wl, precision):
+    """One step through the public API; returns (mean, var) on the device."""
+    import rvgp_gb300 as RVGP
+    d = RVGP.create_data_object(X, n_neighbors=wl["k"], n_eigenpairs=wl["m"], precision=precision, verbose=False)
+    d.vectors = V
+    gp = RVGP.fit(d, train_ind=train, epochs=wl["adam"], optimizer="adam", lr=0.05, verbose=False)
+    return gp.predict_points(test)
+
+
+def flush_l2(buf):
+    buf.add_(1.0)
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons during the timed region."""
+
+    FIELDS = ["clocks.sm", "clocks.max.sm", "clocks_event_reasons.active", "clocks_event_reasons.hw_slowdown",
+              "clocks_event_reasons.hw_thermal_slowdown", "clocks_event_reasons.sw_thermal_slowdown",
+              "clocks_event_reasons.sw_power_cap"]
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + ",".join(self.FIELDS),
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait(timeout=5)
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[3:7]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def spmm_roofline(d, wl, peaks, reps=50):
+    """Achieved HBM bandwidth of the eigensolver's Chebyshev-step SpMM (FP32,
+    block width p) on this workload's connection Laplacian, timed with CUDA
+    events on the launching stream."""
+    import torch
+    from rvgp_gb300 import _core
+    dev = d._dev
+    n, k = d.n, d.dim_man
+    N = n * k
+    p = _core.block_size(wl["m"], N)
+    X = torch.randn((N, p), dtype=torch.float32, device="cuda")
+    Z = torch.randn_like(X)
+    Y = torch.empty_like(X)
+    for _ in range(3):
+        _core.bspmm(dev.indptr, dev.indices, dev.Lc_vals32, X, Y, Z, 0.1, -0.2, 0.3)
+    s = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(s)
+    for _ in range(reps):
+        _core.bspmm(dev.indptr, dev.indices, dev.Lc_vals32, X, Y, Z, 0.1, -0.2, 0.3)
+    e1.record(s)
+    torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) / 1e3 / reps
+    E = dev.indices.numel()
+    alg = E * (k * k * 4 + 4) + (n + 1) * 4 + 3 * N * p * 4  # values + indices + read X, read Z, write Y
+    achieved = alg / t / 1e9
+    return {"kernel": "bspmm_kernel<float,2> (Chebyshev step, Lc x block)", "bound": "hbm",
+            "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
+            "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": None, "algorithmic_bytes": int(alg),
+            "avg_launch_us": round(t * 1e6, 2), "block_width": p}
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+    from rvgp_gb300 import _core
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    _core.require_cuda()
+    wl = WORKLOADS[args.workload]
+    X, train, test = make_inputs(wl, seed=rank)
+    V = make_field(X, wl, seed=rank)
+    Xd = torch.as_tensor(X, device="cuda")
+    Vd = torch.as_tensor(V, device="cuda")
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MiB > L2
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        pipeline(Xd, Vd, train, test, wl, "mixed")
+    barrier()
+    stream = torch.cuda.current_stream()
+    times = []
+    launches0 = _core.launch_count()
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush_l2(flush)
+            barrier()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            mean_mixed, _ = pipeline(Xd, Vd, train, test, wl, "mixed")
+            e1.record(stream)
+            barrier()
+            times.append(e0.elapsed_time(e1) / 1e3)
+    launches = _core.launch_count() - launches0
+    t_step = float(np.mean(times))
+    if world > 1:
+        tt = torch.tensor([t_step], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_step = float(tt.item())
+    out = {}
+    if rank == 0:
+        # the plain FP64 form of the same step, for the metric's comparison
+        fp64_times = []
+        mean64 = None
+        if not args.skip_fp64:
+            pipeline(Xd, Vd, train, test, wl, "fp64")
+            for _ in range(max(1, min(args.steps, 2))):
+                flush_l2(flush)
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                mean64, _ = pipeline(Xd, Vd, train, test, wl, "fp64")
+                e1.record(stream)
+                torch.cuda.synchronize()
+                fp64_times.append(e0.elapsed_time(e1) / 1e3)
+        # end to end through the public API with host buffers
+        e2e_times = []
+        for _ in range(2):
+            import rvgp_gb300 as RVGP
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            d = RVGP.create_data_object(X, n_neighbors=wl["k"], n_eigenpairs=wl["m"], verbose=False)
+            d.vectors = V
+            gp = RVGP.fit(d, train_ind=train, epochs=wl["adam"], optimizer="adam", lr=0.05, verbose=False)
+            mean_h, var_h = gp.transform(d, test)
+            torch.cuda.synchronize()
+            e2e_times.append(time.perf_counter() - t0)
+        peaks, src = measured_peaks()
+        d = __import__("rvgp_gb300").create_data_object(Xd, n_neighbors=wl["k"], n_eigenpairs=wl["m"], verbose=False)
+        roof = spmm_roofline(d, wl, peaks)
+        roof["peak_source"] = src
+        pred_err = None
+        if mean64 is not None:
+            pred_err = float(torch.linalg.vector_norm(mean_mixed - mean64) / torch.linalg.vector_norm(mean64))
+        out = {
+            "metric": METRIC, "value": round(t_step, 5), "unit": "s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(t_step * 1e3, 3), "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+            "config": {"workload": args.workload, "n": wl["n"], "D": 3, "k": wl["k"], "m": wl["m"],
+                       "train_frac": wl["train_frac"], "adam_steps": wl["adam"], "parallelism": f"replicas{world}",
+                       "l2": "flushed between steps (256 MiB write)"},
+            "fp64_form_s": round(float(np.mean(fp64_times)), 5) if fp64_times else None,
+            "mixed_speedup_vs_fp64": round(float(np.mean(fp64_times)) / t_step, 3) if fp64_times else None,
+            "pred_rel_err_vs_fp64": pred_err,
+            "pipelines_per_s": round(world / t_step, 4),
+            "e2e": {"value": round(float(np.mean(e2e_times)), 5), "unit": "s",
+                    "h2d_bytes_per_step": int(X.nbytes + V.nbytes),
+                    "d2h_bytes_per_step": int(mean_h.nbytes + var_h.nbytes)},
+            "roofline": roof,
+            "clocks": clk.summary(),
+            "gpu_launches": int(launches),
+        }
+        if not args.skip_cpu:
+            out["cpu_baseline"] = cpu_baseline(wl, X, V, train, test, budget=args.cpu_budget)
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+    return out
+
+
+# ------------------------------------------------------------------------------ CPU baseline (oracle port)
+def cpu_stage_times(wl, X, V, train, test, budget=240.0):
+    """Per-stage seconds of the reference algorithm's CPU restatement (oracle):
+    brute-force kNN, heap Dijkstra gauges, LAPACK SVDs, connections,
+    Laplacians, ARPACK eigsh(which='SM') for L and Lc, one dense GPflow-GPR
+    LML + gradient evaluation (scaled by the number of optimiser steps) and the
+    dense predict."""
+    import math
+    from oracle import rvgp_oracle as O
+    n, k, m = wl["n"], wl["k"], wl["m"]
+    T = {}
+    t0 = time.perf_counter()
+    nn = O.knn(X, k)
+    ip, ix = O.symmetrised_csr(nn, n)
+    T["graph"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    K = int(k * 1.5)
+    nbh = O.geodesic_neighbourhoods(ip, ix, K)
+    Tg, S = O.tangent_frames(X, nbh, min(3, K + 1))
+    T["gauges"] = time.perf_counter() - t0
+    d = O.manifold_dimension(S, 0.8)
+    Tg = np.ascontiguousarray(Tg[:, :, :d])
+    t0 = time.perf_counter()
+    R = O.connections(Tg, ip, ix)
+    T["connections"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    L = O.laplacian(ip, ix, n)
+    Lc = O.connection_laplacian(L, R, ip, ix, d)
+    T["laplacians"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    O.spectrum(L, m)
+    T["eigsh_L"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    ev, U = O.spectrum(Lc, m)
+    T["eigsh_Lc"] = time.perf_counter() - t0
+    evecs = O.lift(Tg, U, m)
+    tr, te = O.train_test_split_indices(len(train), 0.2, 0)
+    pts = train[tr]
+    Phi = evecs.reshape(n, -1)[pts].reshape(-1, m)
+    y = V[pts].reshape(-1)
+    Sk = O.eval_S(ev, 1.5, 5.0, 1.0, evecs.shape[0])
+    t0 = time.perf_counter()
+    O.lml_dense(Phi, y, Sk, 1.0)
+    O.lml_grad_S_noise(Phi, y, Sk, 1.0)
+    one = time.perf_counter() - t0
+    T["gp_fit"] = one * wl["adam"]
+    Phi_te = evecs.reshape(n, -1)[test].reshape(-1, m)
+    sample = min(len(Phi_te), 2000)
+    t0 = time.perf_counter()
+    O.predict_f(Phi, y, Sk, 1.0, Phi_te[:sample])
+    T["gp_predict"] = (time.perf_counter() - t0) * len(Phi_te) / sample  # linear in the test rows
+    return T, one
+
+
+def cpu_baseline(wl, X, V, train, test, budget=240.0):
+    T, one = cpu_stage_times(wl, X, V, train, test, budget)
+    measured = sum(v for k_, v in T.items() if k_ != "gp_fit") + one
+    return {"value": round(sum(T.values()), 3), "unit": "s", "cores": os.cpu_count(), "kind": "port",
+            "sample": (f"one pass of every stage on the full workload (measured {measured:.1f} s of CPU time); "
+                       f"the GP fit is one dense LML+gradient evaluation scaled by {wl['adam']} optimiser steps; "
+                       f"the dense predict is timed on 2000 test rows and scaled to all of them"),
+            "stages_s": {k_: round(v, 3) for k_, v in T.items()}}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    wl = WORKLOADS[args.workload]
+    X, train, test = make_inputs(wl, seed=0)
+    rng = np.random.default_rng(0)
+    V = rng.standard_normal(X.shape)  # the CPU timing does not depend on the field values
+    # warm-up steps exercise the cheap stages only; the timed work is one full stage pass
+    from oracle import rvgp_oracle as O
+    O.build_c()
+    for _ in range(args.warmup):
+        O.knn(X[:2000], wl["k"])
+    t0 = time.perf_counter()
+    base = cpu_baseline(wl, X, V, train, test, budget=args.cpu_budget)
+    wall = time.perf_counter() - t0
+    out = {"metric": METRIC, "value": base["value"], "unit": "s", "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(base["value"] * 1e3, 1),
+           "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": args.workload, "n": wl["n"], "D": 3, "k": wl["k"], "m": wl["m"],
+                      "train_frac": wl["train_frac"], "adam_steps": wl["adam"]},
+           "impl": "reference", "cpu_baseline": {**base, "wall_s": round(wall, 2)},
+           "e2e": {"value": base["value"], "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="torus_n20000_k20_m200")
+    ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--cpu-budget", type=float, default=240.0)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,184 @@
+/*
+ * librvgp_gb300 — C ABI of the GB300 (sm_103a) RVGP numerical core.
+ *
+ * Conventions for every entry point:
+ *  - pointers are device pointers unless stated; the caller owns all memory;
+ *  - `stream` is a cudaStream_t passed as void*; work is stream-ordered and
+ *    asynchronous unless a function says it synchronises;
+ *  - functions that need scratch take (workspace, ws_bytes) and have a
+ *    matching *_workspace() size query;
+ *  - return 0 on success, > 0 for numerical information (documented per
+ *    function), < 0 for bad arguments (-1), launch failures (-2), short
+ *    workspace (-3) or unsupported sizes (-4); rvgp_last_error() gives the
+ *    message of the last failure on the calling host thread.
+ *
+ * Reference paths below are inside the agosztolai/RVGP checkout.
+ */
+#ifndef RVGP_GB300_H
+#define RVGP_GB300_H
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+const char* rvgp_last_error(void);
+int rvgp_abi_version(void);
+/* Kernels launched by this library since it was loaded (all host threads). */
+long long rvgp_launch_count(void);
+
+/* ---- graph ------------------------------------------------------------ */
+
+/* Exact kNN, FP64 distances, ties to the lower index, self excluded.
+ * Replaces sklearn.neighbors.kneighbors_graph(X, k, mode='connectivity',
+ * include_self=False) at RVGP/geometry.py:103-110.  X: (n, D) f64 row-major;
+ * idx: (n, k) int32, each row ascending by (distance, index). */
+size_t rvgp_knn_workspace(int n, int D, int k);
+int rvgp_knn(const double* X, int n, int D, int k, int* idx, void* workspace, size_t ws_bytes, void* stream);
+/* Rows the last rvgp_knn on this workspace settled by the exact fallback scan
+ * (synchronises the stream; diagnostics only). */
+int rvgp_knn_fallback_rows(int n, int D, int k, void* workspace, void* stream);
+
+/* Symmetrised CSR of kNN + I with sorted columns and unit weights.  Replaces
+ * A += I; nx.from_scipy_sparse_array(A) (RVGP/geometry.py:111-112) and the
+ * max(A, Aᵀ) symmetrisation of RVGP/lib/ptu_dijkstra.pyx:84-103.
+ * indptr: n+1; indices: capacity n*(2k+1); e_out, maxdeg_out: one device int
+ * each (stored entries; largest degree without the self-loop). */
+size_t rvgp_graph_workspace(int n, int k);
+int rvgp_graph_build(const int* knn, int n, int k, int* indptr, int* indices, int* e_out, int* maxdeg_out,
+                     void* workspace, size_t ws_bytes, void* stream);
+
+/* Values of L = D - A on that pattern (deg on the diagonal, -1 elsewhere).
+ * Replaces nx.laplacian_matrix(G) at RVGP/geometry.py:55-63. */
+int rvgp_laplacian_values(const int* indptr, const int* indices, int n, double* vals, void* stream);
+
+/* ---- gauges and connections ------------------------------------------- */
+
+/* Geodesic-neighbourhood local PCA.  Replaces
+ * ptu_dijkstra.tangent_frames(X, G, d, K) (RVGP/lib/ptu_dijkstra.pyx:33-125,
+ * kernel pyx:300-437).  tangents: (n, D, d_out); sigma: (n, min(D, K+1));
+ * nbh_out (optional): (n, K+1) scan order.  status: 3 device ints, left
+ * >= n when fine, else [0] = first point whose component has fewer than K+1
+ * nodes, [2] = first point whose heap pool overflowed. */
+size_t rvgp_gauges_workspace(int n, int D, int K, int maxdeg);
+int rvgp_gauges(const double* X, int n, int D, const int* indptr, const int* indices, int K, int maxdeg, int d_out,
+                double* tangents, double* sigma, int* nbh_out, int* status, void* workspace, size_t ws_bytes,
+                void* stream);
+
+/* Per-edge transports R_ij = polar(T_iᵀ T_j) in CSR order and the block
+ * connection Laplacian values (deg R_ii diagonal, -R_ij off-diagonal).
+ * Replaces ptu_dijkstra.connections(tangents, G, d) (pyx:128-199, kernel
+ * pyx:221-293) and compute_connection_laplacian (RVGP/geometry.py:14-52).
+ * T: (n, D, ld) f64 (first d columns used); R, lc64: (E, d, d) f64; lc32:
+ * (E, d, d) f32; any output may be null. */
+int rvgp_connections(const double* T, int n, int D, int ld, int d, const int* indptr, const int* indices, double* R,
+                     double* lc64, float* lc32, void* stream);
+
+/* ---- sparse products -------------------------------------------------- */
+
+/* Y = alpha*(A X) + beta*X + gamma*Z, A block-CSR with DB x DB blocks
+ * (DB in 1..4), X/Y/Z (n*DB) x b row-major, leading dimension ld.  b and ld
+ * multiples of 4 (f32) or 2 (f64); 16-byte aligned.  The products scipy's
+ * eigsh performs inside compute_spectrum (RVGP/geometry.py:73). */
+int rvgp_bspmm_f32(int n, int DB, const int* indptr, const int* indices, const float* vals, const float* X, float* Y,
+                   const float* Z, int b, int ld, float alpha, float beta, float gamma, void* stream);
+int rvgp_bspmm_f64(int n, int DB, const int* indptr, const int* indices, const double* vals, const double* X,
+                   double* Y, const double* Z, int b, int ld, double alpha, double beta, double gamma, void* stream);
+
+/* ---- eigensolver ------------------------------------------------------ */
+
+/* m smallest eigenpairs of a symmetric PSD block-CSR matrix by Chebyshev-
+ * filtered subspace iteration.  Replaces compute_spectrum (ARPACK eigsh,
+ * which="SM") at RVGP/geometry.py:66-80 for L and Lc.  mode 0: all FP64;
+ * mode 1: FP32 SpMM / tall products (FP64-reduced Grams), FP64 p x p
+ * Cholesky and Rayleigh-Ritz, then FP64 refinement.  p: block size
+ * (m < p <= n*DB, multiple of 4).  tol / tol32: residual tolerances relative to
+ * the Gershgorin bound.  evals ascending (m); evecs N x m (ld_evecs) times
+ * `scale` (the reference scales by sqrt(N)).  stats: 8 host ints (iterations,
+ * SpMMs, Jacobi sweeps, converged, refinement iterations, Cholesky rescues).
+ * Returns 0, or the number of unconverged pairs.  Synchronises the stream. */
+size_t rvgp_eigsh_workspace(int n, int DB, int m, int p, int mode);
+int rvgp_eigsh(const int* indptr, const int* indices, const double* vals64, const float* vals32, int n, int DB, int m,
+               int p, int mode, double tol, double tol32, int max_iter, unsigned long long seed, double* evals,
+               double* evecs, int ld_evecs, double scale, int* stats, void* workspace, size_t ws_bytes, void* stream);
+
+/* ---- spectral kernel and GP ------------------------------------------- */
+
+/* S_l = sigma_f * n_rows * s_l / sum(s), s_l = (λ_l + 2ν/κ²)^(-ν) (typ 0,
+ * Matérn) or exp(-λ_l κ²/2) (typ 1, SE), and dS (3 x m) = dS/d(ν, κ, σ_f).
+ * theta (device) = [nu, kappa, sigma_f, noise].  tmp3m: 3m doubles scratch.
+ * Replaces ManifoldKernel.eval_S (RVGP/kernels.py:41-53). */
+int rvgp_spectral_S(const double* evals, int m, const double* theta, double n_rows, int typ, double* S, double* dS,
+                    double* tmp3m, void* stream);
+/* evecs_Lc[(i*D+a), j] = sum_q T[i,a,q] U[(i*d+q), j]: RVGP/dataclass.py:57-59. */
+int rvgp_lift(const double* T, int n, int D, int ld, int d, const double* U, int m, double* out, void* stream);
+/* GP rows (point, coordinate) of the selected points, as RVGP/main.py:31,47-50
+ * builds them: Phi[(t*D+a), :] = src[(idx[t]*D+a), :], y[(t*D+a)] = vec[idx[t]*D+a]. */
+int rvgp_gather_rows(const double* src, int m, int D, const int* idx, int nt, const double* vec, double* Phi,
+                     float* Phi32, double* y, void* stream);
+/* C = PhiᵀPhi, b = Phiᵀy, yy = yᵀy (mode 1: C from FP32 Phi32, FP64-reduced). */
+size_t rvgp_gp_prepare_workspace(long long N, int m);
+int rvgp_gp_prepare(const double* Phi, const float* Phi32, const double* y, long long N, int m, int mode, double* C,
+                    double* b, double* yy, void* workspace, size_t ws_bytes, void* stream);
+/* Log marginal likelihood of GPflow GPR (RVGP/main.py:55-95; training_loss =
+ * -LML) with Φ S Φᵀ + σ² I, through the exact rank-m (Woodbury) algebra, and
+ * its gradient w.r.t. [nu, kappa, sigma_f, noise].  out (device, 5 doubles);
+ * state (device, rvgp_gp_state_size(m) doubles) feeds rvgp_gp_predict.  No
+ * host synchronisation. */
+size_t rvgp_gp_lml_workspace(int m);
+size_t rvgp_gp_state_size(int m);
+int rvgp_gp_lml(const double* C, const double* b, const double* yy, long long N, int m, const double* evals,
+                double n_rows, int typ, const double* theta, double* out, double* state, void* workspace,
+                size_t ws_bytes, void* stream);
+/* predict_f(full_cov=False) mean and variance at Nte rows (RVGP/main.py:102-116). */
+size_t rvgp_gp_predict_workspace(long long Nte, int m, int mode);
+int rvgp_gp_predict(const double* Phi_star, const float* Phi_star32, long long Nte, int m, int mode,
+                    const double* state, double* mean, double* var, void* workspace, size_t ws_bytes, void* stream);
+/* K = (X S) X2ᵀ and diag((X S) Xᵀ): ManifoldKernel.K / K_diag (RVGP/kernels.py:55-67). */
+int rvgp_kernel_matrix(const double* X, long long N1, const double* X2, long long N2, int m, const double* S,
+                       double* K, void* stream);
+int rvgp_kernel_diag(const double* X, long long N, int m, const double* S, double* out, void* stream);
+
+/* ---- fields and diffusion --------------------------------------------- */
+
+/* manifold_dimension (RVGP/geometry.py:83-97): var_exp (c), dim (device int,
+ * -1 when no column reaches frac). */
+int rvgp_manifold_dimension(const double* sigma, int n, int c, double frac, double* var_exp, int* dim, void* stream);
+/* mode 0: T Tᵀ v (project_to_manifold, RVGP/geometry.py:165-168); 1: Tᵀ v;
+ * 2: T c (express_in_local_frame, RVGP/geometry.py:171-175). */
+int rvgp_frame_map(const double* T, int n, int D, int ld, int d, const double* v, int mode, double* out, void* stream);
+int rvgp_normalise_rows(double* v, int n, int D, void* stream);
+/* exp(-tA) X without forming the exponential (scipy.linalg.expm(-t A) @ x at
+ * RVGP/smoothing.py:13-15); A block-CSR with spectrum in [0, bound], b <= 4. */
+size_t rvgp_expm_action_workspace(int n, int DB, int b);
+int rvgp_expm_action(const int* indptr, const int* indices, const double* vals, int n, int DB, const double* X, int b,
+                     double t, double bound, double* Y, void* workspace, size_t ws_bytes, void* stream);
+/* vector_diffusion(x, t, Lc, L, method="matrix_exp", normalise=True)
+ * (RVGP/smoothing.py:37-63) on the local-frame field x_loc (n, d). */
+size_t rvgp_vector_diffusion_workspace(int n, int d);
+int rvgp_vector_diffusion(const int* indptr, const int* indices, const double* L_vals, const double* Lc_vals, int n,
+                          int d, const double* x_loc, double t, double bound_L, double bound_Lc, double* out,
+                          void* workspace, size_t ws_bytes, void* stream);
+/* Y = Φ diag(exp(-tλ)) Φᵀ X with orthonormal Φ (the spectral branch of
+ * RVGP/smoothing.py:17-32). */
+size_t rvgp_spectral_diffusion_workspace(long long N, int m, int b);
+int rvgp_spectral_diffusion(const double* Phi, long long N, int m, const double* lam, const double* X, int b, double t,
+                            double* Y, void* workspace, size_t ws_bytes, void* stream);
+
+/* ---- sampling --------------------------------------------------------- */
+
+/* Greedy furthest-point sampling, exact FP64 distances, first-index argmax
+ * (furthest_point_sampling, RVGP/geometry.py:126-162).  perm (N_max ints),
+ * lambdas (N_max doubles).  diam (device, optional): stop when
+ * lambda/diam < spacing; count (device int) = points taken, -1 when all N_max. */
+size_t rvgp_fps_workspace(int n);
+int rvgp_fps(const double* X, int n, int D, int N_max, int start, const double* diam, double spacing, int* perm,
+             double* lambdas, int* count, void* workspace, size_t ws_bytes, void* stream);
+/* Largest pairwise exact distance (D.max() at RVGP/geometry.py:143). */
+size_t rvgp_diameter_workspace(int n);
+int rvgp_diameter(const double* X, int n, int D, double* out, void* workspace, size_t ws_bytes, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RVGP_GB300_H */

@@ -420,7 +420,7 @@ def lml_grad_S_noise(Phi, y, S, noise):
     Kinv = np.linalg.inv(Ky)
     alpha = Kinv @ y
     pa = Phi.T @ alpha
-    gS = 0.5 * (pa ** 2 - np.einsum("il,ij,jl->l", Phi, Kinv, Phi))
+    gS = 0.5 * (pa ** 2 - ((Kinv @ Phi) * Phi).sum(0))
     gn = 0.5 * (alpha @ alpha - np.trace(Kinv))
     return gS, gn
 

@@ -1,0 +1,452 @@
+"""ctypes bindings of librvgp_gb300.so (the C ABI in include/rvgp_gb300.h).
+
+Every wrapper takes and returns torch tensors on the current CUDA device and
+launches on torch's current stream.  There is no CPU path: without the built
+library or a CUDA device these functions raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import torch
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "librvgp_gb300.so")
+
+c_int, c_size_t, c_void_p, c_double, c_float = (ctypes.c_int, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_double,
+                                                ctypes.c_float)
+P = c_void_p
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "rvgp_last_error": (ctypes.c_char_p, []),
+    "rvgp_abi_version": (c_int, []),
+    "rvgp_launch_count": (ctypes.c_longlong, []),
+    "rvgp_knn_workspace": (c_size_t, [c_int, c_int, c_int]),
+    "rvgp_knn": (c_int, [P, c_int, c_int, c_int, P, P, c_size_t, P]),
+    "rvgp_knn_fallback_rows": (c_int, [c_int, c_int, c_int, P, P]),
+    "rvgp_graph_workspace": (c_size_t, [c_int, c_int]),
+    "rvgp_graph_build": (c_int, [P, c_int, c_int, P, P, P, P, P, c_size_t, P]),
+    "rvgp_laplacian_values": (c_int, [P, P, c_int, P, P]),
+    "rvgp_gauges_workspace": (c_size_t, [c_int, c_int, c_int, c_int]),
+    "rvgp_gauges": (c_int, [P, c_int, c_int, P, P, c_int, c_int, c_int, P, P, P, P, P, c_size_t, P]),
+    "rvgp_connections": (c_int, [P, c_int, c_int, c_int, c_int, P, P, P, P, P, P]),
+    "rvgp_bspmm_f32": (c_int, [c_int, c_int, P, P, P, P, P, P, c_int, c_int, c_float, c_float, c_float, P]),
+    "rvgp_bspmm_f64": (c_int, [c_int, c_int, P, P, P, P, P, P, c_int, c_int, c_double, c_double, c_double, P]),
+    "rvgp_eigsh_workspace": (c_size_t, [c_int, c_int, c_int, c_int, c_int]),
+    "rvgp_spectral_S": (c_int, [P, c_int, P, c_double, c_int, P, P, P, P]),
+    "rvgp_lift": (c_int, [P, c_int, c_int, c_int, c_int, P, c_int, P, P]),
+    "rvgp_gather_rows": (c_int, [P, c_int, c_int, P, c_int, P, P, P, P, P]),
+    "rvgp_gp_prepare_workspace": (c_size_t, [ctypes.c_longlong, c_int]),
+    "rvgp_gp_prepare": (c_int, [P, P, P, ctypes.c_longlong, c_int, c_int, P, P, P, P, c_size_t, P]),
+    "rvgp_gp_lml_workspace": (c_size_t, [c_int]),
+    "rvgp_gp_state_size": (c_size_t, [c_int]),
+    "rvgp_gp_lml": (c_int, [P, P, P, ctypes.c_longlong, c_int, P, c_double, c_int, P, P, P, P, c_size_t, P]),
+    "rvgp_gp_predict_workspace": (c_size_t, [ctypes.c_longlong, c_int, c_int]),
+    "rvgp_gp_predict": (c_int, [P, P, ctypes.c_longlong, c_int, c_int, P, P, P, P, c_size_t, P]),
+    "rvgp_kernel_matrix": (c_int, [P, ctypes.c_longlong, P, ctypes.c_longlong, c_int, P, P, P]),
+    "rvgp_kernel_diag": (c_int, [P, ctypes.c_longlong, c_int, P, P, P]),
+    "rvgp_manifold_dimension": (c_int, [P, c_int, c_int, c_double, P, P, P]),
+    "rvgp_frame_map": (c_int, [P, c_int, c_int, c_int, c_int, P, c_int, P, P]),
+    "rvgp_normalise_rows": (c_int, [P, c_int, c_int, P]),
+    "rvgp_expm_action_workspace": (c_size_t, [c_int, c_int, c_int]),
+    "rvgp_expm_action": (c_int, [P, P, P, c_int, c_int, P, c_int, c_double, c_double, P, P, c_size_t, P]),
+    "rvgp_vector_diffusion_workspace": (c_size_t, [c_int, c_int]),
+    "rvgp_vector_diffusion": (c_int, [P, P, P, P, c_int, c_int, P, c_double, c_double, c_double, P, P, c_size_t, P]),
+    "rvgp_spectral_diffusion_workspace": (c_size_t, [ctypes.c_longlong, c_int, c_int]),
+    "rvgp_spectral_diffusion": (c_int, [P, ctypes.c_longlong, c_int, P, P, c_int, c_double, P, P, c_size_t, P]),
+    "rvgp_fps_workspace": (c_size_t, [c_int]),
+    "rvgp_fps": (c_int, [P, c_int, c_int, c_int, c_int, P, c_double, P, P, P, P, c_size_t, P]),
+    "rvgp_diameter_workspace": (c_size_t, [c_int]),
+    "rvgp_diameter": (c_int, [P, c_int, c_int, P, P, c_size_t, P]),
+    "rvgp_eigsh": (c_int, [P, P, P, P, c_int, c_int, c_int, c_int, c_int, c_double, c_double, c_int, ctypes.c_ulonglong,
+                           P, P, c_int, c_double, P, P, c_size_t, P]),
+}
+
+_LIB = None
+
+
+def lib():
+    """Load the library (once) and declare every exported signature."""
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with `python -m rvgp_gb300.build`")
+        handle = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(handle, name)
+            f.restype = res
+            f.argtypes = args
+        _LIB = handle
+    return _LIB
+
+
+def launch_count():
+    """Kernels launched by librvgp_gb300 in this process so far."""
+    return int(lib().rvgp_launch_count())
+
+
+def require_cuda():
+    if not torch.cuda.is_available():
+        raise RuntimeError("rvgp_gb300 runs on a CUDA GPU only (no CPU fallback) and none is available")
+
+
+def ptr(t):
+    return None if t is None else c_void_p(t.data_ptr())
+
+
+def stream():
+    return c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def check(status, what):
+    if status != 0:
+        msg = lib().rvgp_last_error().decode()
+        if status == -1 and ("must be" in msg or "Expected" in msg):
+            raise ValueError(msg)
+        raise RuntimeError(f"{what} failed ({status}): {msg}")
+
+
+def workspace(nbytes, device):
+    return torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)
+
+
+def _dev(t, dtype, name):
+    if not t.is_cuda:
+        raise ValueError(f"{name} must be a CUDA tensor")
+    if t.dtype != dtype:
+        raise ValueError(f"{name} must be {dtype}, got {t.dtype}")
+    return t.contiguous()
+
+
+# ---------------------------------------------------------------------------- graph
+def knn(X, k):
+    """(n, D) f64 CUDA tensor -> (n, k) int32 neighbour indices (exact, ties to lower index)."""
+    X = _dev(X, torch.float64, "X")
+    n, D = X.shape
+    idx = torch.empty((n, k), dtype=torch.int32, device=X.device)
+    L = lib()
+    ws = workspace(L.rvgp_knn_workspace(n, D, k), X.device)
+    check(L.rvgp_knn(ptr(X), n, D, k, ptr(idx), ptr(ws), ws.numel(), stream()), "rvgp_knn")
+    knn.last_ws = ws
+    return idx
+
+
+def graph_build(knn_idx):
+    """kNN (n, k) int32 -> (indptr (n+1,), indices (E,), maxdeg int) of the symmetrised graph + I."""
+    knn_idx = _dev(knn_idx, torch.int32, "knn")
+    n, k = knn_idx.shape
+    dev = knn_idx.device
+    indptr = torch.empty(n + 1, dtype=torch.int32, device=dev)
+    indices = torch.empty(n * (2 * k + 1), dtype=torch.int32, device=dev)
+    scal = torch.empty(2, dtype=torch.int32, device=dev)
+    L = lib()
+    ws = workspace(L.rvgp_graph_workspace(n, k), dev)
+    check(L.rvgp_graph_build(ptr(knn_idx), n, k, ptr(indptr), ptr(indices), ptr(scal[0:1]), ptr(scal[1:2]),
+                             ptr(ws), ws.numel(), stream()), "rvgp_graph_build")
+    E, maxdeg = (int(v) for v in scal.cpu())
+    return indptr, indices[:E].clone(), maxdeg
+
+
+def laplacian_values(indptr, indices):
+    n = indptr.numel() - 1
+    vals = torch.empty(indices.numel(), dtype=torch.float64, device=indices.device)
+    check(lib().rvgp_laplacian_values(ptr(indptr), ptr(indices), n, ptr(vals), stream()), "rvgp_laplacian_values")
+    return vals
+
+
+# ---------------------------------------------------------------------------- gauges
+def gauges(X, indptr, indices, K, maxdeg, d_out, return_nbh=False):
+    """Geodesic-neighbourhood PCA: (tangents (n, D, d_out), sigma (n, min(D, K+1)), nbh or None)."""
+    X = _dev(X, torch.float64, "X")
+    n, D = X.shape
+    if K >= n:
+        raise ValueError("Geodesic neighborhood size must be less than the total number of samples")
+    dev = X.device
+    c = min(D, K + 1)
+    T = torch.empty((n, D, d_out), dtype=torch.float64, device=dev)
+    S = torch.empty((n, c), dtype=torch.float64, device=dev)
+    nbh = torch.empty((n, K + 1), dtype=torch.int32, device=dev) if return_nbh else None
+    status = torch.empty(3, dtype=torch.int32, device=dev)
+    L = lib()
+    ws = workspace(L.rvgp_gauges_workspace(n, D, K, maxdeg), dev)
+    check(L.rvgp_gauges(ptr(X), n, D, ptr(indptr), ptr(indices), K, maxdeg, d_out, ptr(T), ptr(S), ptr(nbh),
+                        ptr(status), ptr(ws), ws.numel(), stream()), "rvgp_gauges")
+    st = status.cpu().tolist()
+    if st[0] < n:
+        raise RuntimeError(f"the graph component of point {st[0]} holds fewer than K+1={K + 1} points")
+    if st[2] < n:
+        raise RuntimeError(f"geodesic neighbourhood search overflowed its node pool at point {st[2]}")
+    return T, S, nbh
+
+
+def connections(T, d, indptr, indices, want_R=True, want64=True, want32=True):
+    """Per-edge transports (E, d, d) and block connection-Laplacian values (f64 / f32)."""
+    T = _dev(T, torch.float64, "tangents")
+    n, D, ld = T.shape
+    E = indices.numel()
+    dev = T.device
+    R = torch.empty((E, d, d), dtype=torch.float64, device=dev) if want_R else None
+    v64 = torch.empty((E, d, d), dtype=torch.float64, device=dev) if want64 else None
+    v32 = torch.empty((E, d, d), dtype=torch.float32, device=dev) if want32 else None
+    check(lib().rvgp_connections(ptr(T), n, D, ld, d, ptr(indptr), ptr(indices), ptr(R), ptr(v64), ptr(v32),
+                                 stream()), "rvgp_connections")
+    return R, v64, v32
+
+
+# ---------------------------------------------------------------------------- products
+def bspmm(indptr, indices, vals, X, Y=None, Z=None, alpha=1.0, beta=0.0, gamma=0.0):
+    """Y = alpha*(A X) + beta*X + gamma*Z for block-CSR A with square blocks."""
+    n = indptr.numel() - 1
+    DB = 1 if vals.dim() == 1 else vals.shape[-1]
+    rows, b = X.shape
+    if rows != n * DB:
+        raise ValueError("X rows must equal n * block size")
+    Y = torch.empty_like(X) if Y is None else Y
+    f = lib().rvgp_bspmm_f32 if X.dtype == torch.float32 else lib().rvgp_bspmm_f64
+    check(f(n, DB, ptr(indptr), ptr(indices), ptr(vals), ptr(X), ptr(Y), ptr(Z), b, X.stride(0), alpha, beta, gamma,
+            stream()), "rvgp_bspmm")
+    return Y
+
+
+# ---------------------------------------------------------------------------- eigensolver
+def block_size(m, N):
+    """Subspace block: m plus a guard of max(16, m/8) vectors, a multiple of 4, at most N."""
+    p = m + max(16, m // 8)
+    p = (p + 3) // 4 * 4
+    return min(p, N - N % 4)
+
+
+def eigsh(indptr, indices, vals64, vals32=None, m=10, mode="mixed", tol=1e-11, tol32=2e-5, max_iter=60, seed=0,
+          scale=None, p=None):
+    """m smallest eigenpairs of the block-CSR matrix: (evals (m,), evecs (N, m), stats dict).
+
+    evecs are orthonormal times ``scale`` (default 1).  mode: "mixed" (FP32
+    bulk + FP64 refinement) or "fp64" (plain FP64).
+    """
+    n = indptr.numel() - 1
+    DB = 1 if vals64.dim() == 1 else vals64.shape[-1]
+    N = n * DB
+    if m >= N - 1:
+        raise ValueError(f"k must be less than ndim(A)-1, got k={m}")
+    p = block_size(m, N) if p is None else p
+    imode = 1 if mode == "mixed" else 0
+    if imode == 1 and vals32 is None:
+        vals32 = vals64.float()
+    dev = vals64.device
+    evals = torch.empty(m, dtype=torch.float64, device=dev)
+    evecs = torch.empty((N, m), dtype=torch.float64, device=dev)
+    stats = (ctypes.c_int * 8)()
+    L = lib()
+    ws = workspace(L.rvgp_eigsh_workspace(n, DB, m, p, imode), dev)
+    st = L.rvgp_eigsh(ptr(indptr), ptr(indices), ptr(vals64), ptr(vals32), n, DB, m, p, imode, tol, tol32, max_iter,
+                      seed, ptr(evals), ptr(evecs), m, 1.0 if scale is None else float(scale), stats, ptr(ws),
+                      ws.numel(), stream())
+    info = dict(iters=stats[0], spmm=stats[1], sweeps=stats[2], converged=stats[3], refine_iters=stats[4],
+                chol_rescues=stats[5], p=p)
+    if st < 0:
+        check(st, "rvgp_eigsh")
+    if st > 0:
+        raise RuntimeError(f"ARPACK-equivalent no convergence: {lib().rvgp_last_error().decode()}")
+    return evals, evecs, info
+
+
+# ---------------------------------------------------------------------------- GP
+KERNEL_TYPES = {"matern": 0, "se": 1}
+
+
+def spectral_S(evals, theta, n_rows, typ="matern", want_grad=True):
+    """S (m,) and dS (3, m) for theta = [nu, kappa, sigma_f, noise] (CUDA f64)."""
+    m = evals.numel()
+    S = torch.empty(m, dtype=torch.float64, device=evals.device)
+    dS = torch.empty((3, m), dtype=torch.float64, device=evals.device) if want_grad else None
+    tmp = torch.empty(3 * m, dtype=torch.float64, device=evals.device)
+    check(lib().rvgp_spectral_S(ptr(evals), m, ptr(theta), float(n_rows), KERNEL_TYPES[typ], ptr(S), ptr(dS),
+                                ptr(tmp), stream()), "rvgp_spectral_S")
+    return S, dS
+
+
+def lift(T, d, U):
+    """evecs_Lc[(i*D + a), j] = Σ_q T[i, a, q] U[(i*d + q), j]  -> (n*D, m)."""
+    n, D, ld = T.shape
+    m = U.shape[1]
+    out = torch.empty((n * D, m), dtype=torch.float64, device=T.device)
+    check(lib().rvgp_lift(ptr(T), n, D, ld, d, ptr(U.contiguous()), m, ptr(out), stream()), "rvgp_lift")
+    return out
+
+
+def gather_rows(src, D, idx, vec=None, want64=True, want32=False):
+    """Rows (point, coordinate) of src for the points in idx: (Phi (nt*D, m), Phi32, y)."""
+    m = src.shape[1]
+    nt = idx.numel()
+    dev = src.device
+    Phi = torch.empty((nt * D, m), dtype=torch.float64, device=dev) if want64 else None
+    Phi32 = torch.empty((nt * D, m), dtype=torch.float32, device=dev) if want32 else None
+    y = torch.empty(nt * D, dtype=torch.float64, device=dev) if vec is not None else None
+    check(lib().rvgp_gather_rows(ptr(src), m, D, ptr(idx.to(torch.int32).contiguous()), nt,
+                                 ptr(None if vec is None else vec.contiguous()), ptr(Phi), ptr(Phi32), ptr(y),
+                                 stream()), "rvgp_gather_rows")
+    return Phi, Phi32, y
+
+
+def gp_prepare(Phi, y, Phi32=None, mode="fp64"):
+    N, m = Phi.shape
+    dev = Phi.device
+    C = torch.empty((m, m), dtype=torch.float64, device=dev)
+    b = torch.empty(m, dtype=torch.float64, device=dev)
+    yy = torch.empty(1, dtype=torch.float64, device=dev)
+    L = lib()
+    ws = workspace(L.rvgp_gp_prepare_workspace(N, m), dev)
+    check(L.rvgp_gp_prepare(ptr(Phi), ptr(Phi32), ptr(y), N, m, 1 if mode == "mixed" else 0, ptr(C), ptr(b), ptr(yy),
+                            ptr(ws), ws.numel(), stream()), "rvgp_gp_prepare")
+    return C, b, yy
+
+
+class LMLWorkspace:
+    """Device buffers reused across likelihood evaluations of one problem."""
+
+    def __init__(self, m, device):
+        L = lib()
+        self.m = m
+        self.ws = workspace(L.rvgp_gp_lml_workspace(m), device)
+        self.state = torch.empty(int(L.rvgp_gp_state_size(m)), dtype=torch.float64, device=device)
+        self.out = torch.empty(5, dtype=torch.float64, device=device)
+
+
+def gp_lml(C, b, yy, N, evals, n_rows, theta, typ="matern", work=None):
+    """[LML, d/dnu, d/dkappa, d/dsigma_f, d/dnoise] on the device (no host sync)."""
+    m = evals.numel()
+    work = work or LMLWorkspace(m, evals.device)
+    check(lib().rvgp_gp_lml(ptr(C), ptr(b), ptr(yy), int(N), m, ptr(evals), float(n_rows), KERNEL_TYPES[typ],
+                            ptr(theta), ptr(work.out), ptr(work.state), ptr(work.ws), work.ws.numel(), stream()),
+          "rvgp_gp_lml")
+    return work.out, work
+
+
+def gp_predict(Phi_star, state, m, Phi_star32=None, mode="fp64"):
+    Nte = Phi_star.shape[0]
+    dev = Phi_star.device
+    mean = torch.empty(Nte, dtype=torch.float64, device=dev)
+    var = torch.empty(Nte, dtype=torch.float64, device=dev)
+    imode = 1 if mode == "mixed" else 0
+    if imode == 1 and Phi_star32 is None:
+        Phi_star32 = Phi_star.float()
+    L = lib()
+    ws = workspace(L.rvgp_gp_predict_workspace(Nte, m, imode), dev)
+    check(L.rvgp_gp_predict(ptr(Phi_star), ptr(Phi_star32), Nte, m, imode, ptr(state), ptr(mean), ptr(var), ptr(ws),
+                            ws.numel(), stream()), "rvgp_gp_predict")
+    return mean, var
+
+
+def kernel_matrix(X, S, X2=None):
+    X = X.contiguous()
+    X2 = X if X2 is None else X2.contiguous()
+    K = torch.empty((X.shape[0], X2.shape[0]), dtype=torch.float64, device=X.device)
+    check(lib().rvgp_kernel_matrix(ptr(X), X.shape[0], ptr(X2), X2.shape[0], X.shape[1], ptr(S), ptr(K), stream()),
+          "rvgp_kernel_matrix")
+    return K
+
+
+def kernel_diag(X, S):
+    X = X.contiguous()
+    out = torch.empty(X.shape[0], dtype=torch.float64, device=X.device)
+    check(lib().rvgp_kernel_diag(ptr(X), X.shape[0], X.shape[1], ptr(S), ptr(out), stream()), "rvgp_kernel_diag")
+    return out
+
+
+# ---------------------------------------------------------------------------- fields / diffusion
+def manifold_dimension(sigma, frac):
+    """(dim, var_exp) of RVGP/geometry.py:83-97 computed on the device."""
+    n, c = sigma.shape
+    var = torch.empty(c, dtype=torch.float64, device=sigma.device)
+    dim = torch.empty(1, dtype=torch.int32, device=sigma.device)
+    check(lib().rvgp_manifold_dimension(ptr(sigma.contiguous()), n, c, float(frac), ptr(var), ptr(dim), stream()),
+          "rvgp_manifold_dimension")
+    return int(dim.item()), var
+
+
+FRAME_MODES = {"project": 0, "to_local": 1, "from_local": 2}
+
+
+def frame_map(T, d, v, mode):
+    n, D, ld = T.shape
+    out_cols = d if mode == "to_local" else D
+    out = torch.empty((n, out_cols), dtype=torch.float64, device=T.device)
+    check(lib().rvgp_frame_map(ptr(T), n, D, ld, d, ptr(v.contiguous()), FRAME_MODES[mode], ptr(out), stream()),
+          "rvgp_frame_map")
+    return out
+
+
+def normalise_rows(v):
+    v = v.contiguous()
+    check(lib().rvgp_normalise_rows(ptr(v), v.shape[0], v.shape[1], stream()), "rvgp_normalise_rows")
+    return v
+
+
+def expm_action(indptr, indices, vals, X, t, bound):
+    """exp(-t A) X for block-CSR A (spectrum in [0, bound]); X: (N, b <= 4)."""
+    n = indptr.numel() - 1
+    DB = 1 if vals.dim() == 1 else vals.shape[-1]
+    X = X.contiguous()
+    b = X.shape[1]
+    Y = torch.empty_like(X)
+    L = lib()
+    ws = workspace(L.rvgp_expm_action_workspace(n, DB, b), X.device)
+    check(L.rvgp_expm_action(ptr(indptr), ptr(indices), ptr(vals), n, DB, ptr(X), b, float(t), float(bound), ptr(Y),
+                             ptr(ws), ws.numel(), stream()), "rvgp_expm_action")
+    return Y
+
+
+def vector_diffusion(indptr, indices, L_vals, Lc_vals, x_loc, t, bound_L, bound_Lc):
+    n, d = x_loc.shape
+    out = torch.empty_like(x_loc)
+    L = lib()
+    ws = workspace(L.rvgp_vector_diffusion_workspace(n, d), x_loc.device)
+    check(L.rvgp_vector_diffusion(ptr(indptr), ptr(indices), ptr(L_vals), ptr(Lc_vals), n, d, ptr(x_loc.contiguous()),
+                                  float(t), float(bound_L), float(bound_Lc), ptr(out), ptr(ws), ws.numel(), stream()),
+          "rvgp_vector_diffusion")
+    return out
+
+
+def spectral_diffusion(Phi, lam, X, t):
+    N, m = Phi.shape
+    X = X.contiguous()
+    b = X.shape[1]
+    Y = torch.empty_like(X)
+    L = lib()
+    ws = workspace(L.rvgp_spectral_diffusion_workspace(N, m, b), X.device)
+    check(L.rvgp_spectral_diffusion(ptr(Phi.contiguous()), N, m, ptr(lam), ptr(X), b, float(t), ptr(Y), ptr(ws),
+                                    ws.numel(), stream()), "rvgp_spectral_diffusion")
+    return Y
+
+
+# ---------------------------------------------------------------------------- sampling
+def diameter(X):
+    X = _dev(X, torch.float64, "X")
+    n, D = X.shape
+    out = torch.empty(1, dtype=torch.float64, device=X.device)
+    L = lib()
+    ws = workspace(L.rvgp_diameter_workspace(n), X.device)
+    check(L.rvgp_diameter(ptr(X), n, D, ptr(out), ptr(ws), ws.numel(), stream()), "rvgp_diameter")
+    return out
+
+
+def fps(X, N=None, spacing=0.1, start_idx=0):
+    """(perm int32, lambdas f64) on the device: RVGP/geometry.py:126-162."""
+    X = _dev(X, torch.float64, "X")
+    n, D = X.shape
+    N_max = n if N is None else int(N)
+    dev = X.device
+    perm = torch.empty(N_max, dtype=torch.int32, device=dev)
+    lam = torch.empty(N_max, dtype=torch.float64, device=dev)
+    count = torch.empty(1, dtype=torch.int32, device=dev)
+    diam = diameter(X) if N is None else None
+    L = lib()
+    ws = workspace(L.rvgp_fps_workspace(n), dev)
+    check(L.rvgp_fps(ptr(X), n, D, N_max, int(start_idx), ptr(diam), float(spacing), ptr(perm), ptr(lam),
+                     ptr(count), ptr(ws), ws.numel(), stream()), "rvgp_fps")
+    c = int(count.item())
+    if c >= 0:
+        perm, lam = perm[:c], lam[:c]
+    return perm, lam

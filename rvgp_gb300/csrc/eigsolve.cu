@@ -1,0 +1,487 @@
+// Smallest eigenpairs of a sparse symmetric positive semi-definite block-CSR
+// matrix by Chebyshev-filtered subspace iteration.
+//
+// Replaces compute_spectrum (RVGP/geometry.py:66-80), which calls ARPACK
+// eigsh(which="SM") on the graph Laplacian L (n x n) and the connection
+// Laplacian Lc (nd x nd).  Same result contract: the m algebraically smallest
+// eigenvalues in ascending order and orthonormal eigenvectors (the caller
+// applies the reference's sqrt(N) scaling through `scale`).
+//
+// Iteration (block of p = m + guard vectors, all bulk work on the device):
+//   filter  : V <- p_k(A) V, the scaled Chebyshev polynomial of degree k that
+//             damps [a, b] (a = largest Ritz value, b = Gershgorin bound) and
+//             grows [0, a); 3-term recurrence fused into the SpMM.
+//   orth    : column scaling + Cholesky QR twice (G = VᵀV, V <- V L⁻ᵀ).
+//   RR      : W = A V, H = Vᵀ W, H = Q Θ Qᵀ (Jacobi), V <- V Q, W <- W Q.
+//   check   : residuals |W_j - θ_j V_j|; stop when the first m are below
+//             tol * b.
+// Two precisions:
+//   plain (mode 0): everything in FP64;
+//   mixed (mode 1): SpMM and the tall products in FP32 (Gram partial sums
+//             reduced in FP64), the p x p Cholesky / Rayleigh-Ritz eigensolve in
+//             FP64, then FP64 refinement iterations starting from the FP32
+//             subspace until the FP64 tolerance is met.
+#include "common.cuh"
+#include "linalg.cuh"
+#include <math.h>
+#include <float.h>
+#include <vector>
+#include <algorithm>
+
+namespace rvgp {
+int bspmm_f32(int n, int DB, const int* indptr, const int* indices, const float* vals, const float* X, float* Y,
+              const float* Z, int b, int ld, float alpha, float beta, float gamma, cudaStream_t st);
+int bspmm_f64(int n, int DB, const int* indptr, const int* indices, const double* vals, const double* X, double* Y,
+              const double* Z, int b, int ld, double alpha, double beta, double gamma, cudaStream_t st);
+
+namespace {
+
+inline int spmm(int n, int DB, const int* ip, const int* ix, const float* v, const float* X, float* Y, const float* Z,
+                int b, int ld, double al, double be, double ga, cudaStream_t st) {
+  return bspmm_f32(n, DB, ip, ix, v, X, Y, Z, b, ld, (float)al, (float)be, (float)ga, st);
+}
+inline int spmm(int n, int DB, const int* ip, const int* ix, const double* v, const double* X, double* Y,
+                const double* Z, int b, int ld, double al, double be, double ga, cudaStream_t st) {
+  return bspmm_f64(n, DB, ip, ix, v, X, Y, Z, b, ld, al, be, ga, st);
+}
+
+__global__ void gershgorin_kernel(int n, int DB, const int* __restrict__ indptr, const double* __restrict__ vals,
+                                  double* __restrict__ part) {
+  __shared__ double sh[256];
+  double mx = 0.0;
+  for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < (long long)n * DB;
+       r += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(r / DB), p = (int)(r % DB);
+    double s = 0.0;
+    for (int t = indptr[i]; t < indptr[i + 1]; ++t)
+      for (int q = 0; q < DB; ++q) s += fabs(vals[((size_t)t * DB + p) * DB + q]);
+    mx = fmax(mx, s);
+  }
+  sh[threadIdx.x] = mx;
+  __syncthreads();
+  for (int s = 128; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sh[threadIdx.x] = fmax(sh[threadIdx.x], sh[threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+__device__ __forceinline__ double hash_uniform(unsigned long long seed, unsigned long long a) {
+  unsigned long long z = seed + 0x9E3779B97F4A7C15ull * (a + 1);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  return (double)(z >> 11) * (1.0 / 9007199254740992.0) - 0.5;
+}
+
+template <typename T>
+__global__ void random_block(T* __restrict__ V, long long N, int p, int ld, unsigned long long seed) {
+  const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e >= N * p) return;
+  const long long r = e / p;
+  const int j = (int)(e % p);
+  V[r * ld + j] = (T)hash_uniform(seed, (unsigned long long)e);
+}
+
+// B (p x p, type T) = Linvᵀ, i.e. B[k][j] = Linv[j][k]
+template <typename T>
+__global__ void transpose_to(const double* __restrict__ A, int p, T* __restrict__ B) {
+  const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e >= (long long)p * p) return;
+  const int k = (int)(e / p), j = (int)(e % p);
+  B[e] = (T)A[(size_t)j * p + k];
+}
+
+template <typename T>
+__global__ void copy_to(const double* __restrict__ A, long long cnt, T* __restrict__ B) {
+  const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e < cnt) B[e] = (T)A[e];
+}
+
+// add shift * trace(G)/p to the diagonal (rescue for a numerically singular Gram)
+__global__ void shift_diag(double* __restrict__ G, int p, double rel) {
+  __shared__ double tr;
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int i = 0; i < p; ++i) s += G[(size_t)i * p + i];
+    tr = s / p;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < p; i += blockDim.x) G[(size_t)i * p + i] += rel * tr;
+}
+
+template <typename T>
+__global__ void resid_partial(const T* __restrict__ W, const T* __restrict__ V, const double* __restrict__ theta,
+                              int ld, long long N, int b, long long chunk, double* __restrict__ part) {
+  const long long r0 = blockIdx.x * chunk, r1 = min(N, r0 + chunk);
+  for (int j = threadIdx.x; j < b; j += blockDim.x) {
+    const double th = theta[j];
+    double s = 0.0;
+    for (long long r = r0; r < r1; ++r) {
+      double d = (double)W[r * ld + j] - th * (double)V[r * ld + j];
+      s += d * d;
+    }
+    part[(size_t)blockIdx.x * b + j] = s;
+  }
+}
+
+__global__ void resid_final(const double* __restrict__ part, int nchunk, int b, double* __restrict__ out) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= b) return;
+  double s = 0.0;
+  for (int c = 0; c < nchunk; ++c) s += part[(size_t)c * b + j];
+  out[j] = sqrt(s);
+}
+
+template <typename T>
+__global__ void write_output(const T* __restrict__ V, int ldv, long long N, int m, double scale, double* __restrict__ out,
+                             int ldo) {
+  const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e >= N * m) return;
+  const long long r = e / m;
+  const int j = (int)(e % m);
+  out[r * ldo + j] = scale * (double)V[r * ldv + j];
+}
+
+int resid_chunks(long long N) { return (int)std::max<long long>(1, std::min<long long>(512, N / 128)); }
+
+// ------------------------------------------------------------------------------ solver state
+template <typename T>
+struct Block {
+  T *V, *W, *T1, *T2;  // N x p each, ld = p
+};
+
+struct Small {
+  double *G, *H, *Q, *Linv, *theta, *res, *norms64;
+  double *gersh, *resid_part;
+  int* info;
+  void* gram_ws;
+  size_t gram_bytes;
+  void* jac_ws;
+  size_t jac_bytes;
+  void* cn_ws;
+  size_t cn_bytes;
+  float* Bf;
+  double* Bd;
+  float* nf;
+  double* nd;
+};
+
+struct Problem {
+  int n, DB;
+  long long N;
+  const int *indptr, *indices;
+  const double* v64;
+  const float* v32;
+  int m, p;
+};
+
+template <typename T>
+const T* vals_of(const Problem& P);
+template <>
+const float* vals_of<float>(const Problem& P) { return P.v32; }
+template <>
+const double* vals_of<double>(const Problem& P) { return P.v64; }
+
+template <typename T>
+T* Bmat(Small& s);
+template <>
+float* Bmat<float>(Small& s) { return s.Bf; }
+template <>
+double* Bmat<double>(Small& s) { return s.Bd; }
+template <typename T>
+T* nrm(Small& s);
+template <>
+float* nrm<float>(Small& s) { return s.nf; }
+template <>
+double* nrm<double>(Small& s) { return s.nd; }
+
+inline int gram_any(const float* A, const float* B, long long N, int p, double* C, Small& s, cudaStream_t st) {
+  return gram_f32_out64(A, p, B, p, N, p, p, C, p, 1.0, 0.0, s.gram_ws, s.gram_bytes, st);
+}
+inline int gram_any(const double* A, const double* B, long long N, int p, double* C, Small& s, cudaStream_t st) {
+  return gram<double>(A, p, B, p, N, p, p, C, p, 1.0, 0.0, s.gram_ws, s.gram_bytes, st);
+}
+
+#define TRY(x)                  \
+  do {                          \
+    int _s = (x);               \
+    if (_s != RVGP_OK) return _s; \
+  } while (0)
+
+struct Stats {
+  int iters = 0, spmm = 0, sweeps = 0, conv = 0, refine_iters = 0, chol_rescues = 0;
+};
+
+// Chebyshev filter of degree deg on [a, b] with lower bound a0; result pointer returned in *out.
+template <typename T>
+int filter(const Problem& P, Block<T>& B, int deg, double a, double b, double a0, Stats& stt, cudaStream_t st) {
+  const double e = (b - a) / 2, c = (b + a) / 2;
+  double sigma = e / (a0 - c);
+  const double tau = 2.0 / sigma;
+  T *X = B.V, *Y = B.T1, *Z = B.T2;
+  const T* vals = vals_of<T>(P);
+  TRY(spmm(P.n, P.DB, P.indptr, P.indices, vals, X, Y, (const T*)nullptr, P.p, P.p, sigma / e, -c * sigma / e, 0.0, st));
+  ++stt.spmm;
+  for (int i = 2; i <= deg; ++i) {
+    const double sn = 1.0 / (tau - sigma);
+    TRY(spmm(P.n, P.DB, P.indptr, P.indices, vals, Y, Z, X, P.p, P.p, 2 * sn / e, -2 * c * sn / e, -sigma * sn, st));
+    ++stt.spmm;
+    T* t = X;
+    X = Y;
+    Y = Z;
+    Z = t;
+    sigma = sn;
+  }
+  // result in Y; make it V
+  B.V = Y;
+  B.T1 = X;
+  B.T2 = Z;
+  return RVGP_OK;
+}
+
+// V <- orthonormal basis of span(V): column scaling + Cholesky QR (twice).
+template <typename T>
+int orthonormalise(const Problem& P, Block<T>& B, Small& s, Stats& stt, cudaStream_t st) {
+  const long long N = P.N;
+  const int p = P.p;
+  int rescues = 0;
+  for (int pass = 0; pass < 2; ++pass) {
+    TRY(col_norms<T>(B.V, p, N, p, nrm<T>(s), s.cn_ws, s.cn_bytes, st));
+    TRY(scale_cols<T>(B.V, p, N, p, nrm<T>(s), true, st));
+    TRY(gram_any(B.V, B.V, N, p, s.G, s, st));
+    TRY(cholesky<double>(s.G, p, p, s.info, st));
+    int info = 0;
+    cudaMemcpyAsync(&info, s.info, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return check_launch("orthonormalise");
+    if (info != 0) {
+      // numerically rank-deficient block: shifted Cholesky QR on a fresh Gram
+      ++stt.chol_rescues;
+      if (++rescues > 3) {
+        set_error("eigensolver: Cholesky QR failed repeatedly (block lost rank)");
+        return 1;
+      }
+      TRY(gram_any(B.V, B.V, N, p, s.G, s, st));
+      rvgp::note_launch(); shift_diag<<<1, 256, 0, st>>>(s.G, p, 1e-6);
+      TRY(cholesky<double>(s.G, p, p, s.info, st));
+      cudaMemcpyAsync(&info, s.info, sizeof(int), cudaMemcpyDeviceToHost, st);
+      if (cudaStreamSynchronize(st) != cudaSuccess) return check_launch("orthonormalise");
+      if (info != 0) {
+        set_error("eigensolver: Cholesky QR failed (block lost rank)");
+        return 1;
+      }
+      pass = -1;  // two clean passes after the rescue
+    }
+    TRY(tri_inv_lower<double>(s.G, p, p, s.Linv, p, st));
+    rvgp::note_launch(); transpose_to<T><<<ceil_div((long long)p * p, 256), 256, 0, st>>>(s.Linv, p, Bmat<T>(s));
+    TRY(gemm_nn<T>(B.V, p, Bmat<T>(s), p, N, p, p, B.T1, p, T(1), T(0), st));
+    std::swap(B.V, B.T1);
+  }
+  return RVGP_OK;
+}
+
+// Rayleigh-Ritz: V, W = A V rotated to Ritz vectors; theta, residuals to host.
+template <typename T>
+int rayleigh_ritz(const Problem& P, Block<T>& B, Small& s, Stats& stt, int max_sweeps, std::vector<double>& theta,
+                  std::vector<double>& res, cudaStream_t st) {
+  const long long N = P.N;
+  const int p = P.p;
+  TRY(spmm(P.n, P.DB, P.indptr, P.indices, vals_of<T>(P), B.V, B.W, (const T*)nullptr, p, p, 1.0, 0.0, 0.0, st));
+  ++stt.spmm;
+  TRY(gram_any(B.V, B.W, N, p, s.H, s, st));
+  int used = 0;
+  TRY(jacobi_eigh<double>(s.H, p, s.theta, s.Q, max_sweeps, 1e-15, &used, s.jac_ws, s.jac_bytes, st));
+  stt.sweeps += used;
+  rvgp::note_launch(); copy_to<T><<<ceil_div((long long)p * p, 256), 256, 0, st>>>(s.Q, (long long)p * p, Bmat<T>(s));
+  TRY(gemm_nn<T>(B.V, p, Bmat<T>(s), p, N, p, p, B.T1, p, T(1), T(0), st));
+  TRY(gemm_nn<T>(B.W, p, Bmat<T>(s), p, N, p, p, B.T2, p, T(1), T(0), st));
+  std::swap(B.V, B.T1);
+  std::swap(B.W, B.T2);
+  const int nc = resid_chunks(N);
+  const long long chunk = (N + nc - 1) / nc;
+  rvgp::note_launch(); resid_partial<T><<<nc, 256, 0, st>>>(B.W, B.V, s.theta, p, N, p, chunk, s.resid_part);
+  rvgp::note_launch(); resid_final<<<ceil_div(p, 256), 256, 0, st>>>(s.resid_part, nc, p, s.res);
+  theta.resize(p);
+  res.resize(p);
+  cudaMemcpyAsync(theta.data(), s.theta, sizeof(double) * p, cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(res.data(), s.res, sizeof(double) * p, cudaMemcpyDeviceToHost, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess) return check_launch("rayleigh_ritz");
+  return check_launch("rayleigh_ritz");
+}
+
+int choose_degree(const std::vector<double>& th, int m, double a, double b, double range, int cap) {
+  const double e = (b - a) / 2, c = (b + a) / 2;
+  const double xm = std::max(1.0 + 1e-6, (c - th[m - 1]) / e);
+  const double x0 = std::max(xm, (c - std::min(th[0], th[m - 1])) / e);
+  int deg = (int)ceil(log(2e4) / acosh(xm));
+  const double gap = acosh(x0) - acosh(xm);
+  if (gap > 0) deg = std::min(deg, (int)floor(log(range) / gap));
+  return std::max(4, std::min(deg, cap));
+}
+
+// Runs iterations in precision T from the current B.V (orthonormalised inside).
+template <typename T>
+int iterate(const Problem& P, Block<T>& B, Small& s, Stats& stt, double bup, double tol, int max_iter, int first_deg,
+            double range, std::vector<double>& theta, std::vector<double>& res, bool have_ritz, int* nconv_out,
+            cudaStream_t st) {
+  const int m = P.m, p = P.p;
+  int nconv = 0;
+  double a, a0;
+  int deg = first_deg;
+  if (have_ritz) {
+    a = theta[p - 1];
+    a0 = std::min(theta[0], 0.0) - 1e-3 * bup;
+    deg = choose_degree(theta, m, a, bup, range, sizeof(T) == 4 ? 60 : 250);
+  } else {
+    a = bup * std::min(0.5, std::max(4.0 * p / (double)P.N, 0.01));
+    a0 = -1e-3 * bup;
+  }
+  for (int it = 0; it < max_iter; ++it) {
+    if (a >= bup * 0.999) a = bup * 0.5;
+    TRY(filter<T>(P, B, deg, a, bup, a0, stt, st));
+    TRY(orthonormalise<T>(P, B, s, stt, st));
+    TRY(rayleigh_ritz<T>(P, B, s, stt, 60, theta, res, st));
+    ++stt.iters;
+    nconv = 0;
+    for (int j = 0; j < m; ++j)
+      if (res[j] <= tol * bup) ++nconv;
+    if (nconv == m) break;
+    a = theta[p - 1];
+    a0 = std::min(theta[0], 0.0) - 1e-3 * bup;
+    deg = choose_degree(theta, m, a, bup, range, sizeof(T) == 4 ? 60 : 250);
+  }
+  *nconv_out = nconv;
+  return RVGP_OK;
+}
+
+struct Layout {
+  Block<float> f;
+  Block<double> d;
+  Small s;
+};
+
+Layout carve(Workspace& ws, long long N, int p, int mode) {
+  Layout L{};
+  const size_t blk = (size_t)N * p;
+  if (mode == 1) {
+    L.f.V = ws.take<float>(blk);
+    L.f.W = ws.take<float>(blk);
+    L.f.T1 = ws.take<float>(blk);
+    L.f.T2 = ws.take<float>(blk);
+  }
+  L.d.V = ws.take<double>(blk);
+  L.d.W = ws.take<double>(blk);
+  L.d.T1 = ws.take<double>(blk);
+  L.d.T2 = ws.take<double>(blk);
+  Small& s = L.s;
+  const size_t pp = (size_t)p * p;
+  s.G = ws.take<double>(pp);
+  s.H = ws.take<double>(pp);
+  s.Q = ws.take<double>(pp);
+  s.Linv = ws.take<double>(pp);
+  s.theta = ws.take<double>(p);
+  s.res = ws.take<double>(p);
+  s.norms64 = ws.take<double>(p);
+  s.gersh = ws.take<double>(kNumSMs * 2);
+  s.resid_part = ws.take<double>((size_t)resid_chunks(N) * p);
+  s.info = ws.take<int>(4);
+  s.Bf = ws.take<float>(pp);
+  s.Bd = ws.take<double>(pp);
+  s.nf = ws.take<float>(p);
+  s.nd = ws.take<double>(p);
+  s.gram_bytes = std::max(gram_workspace<float>(N, p, p), gram_workspace<double>(N, p, p));
+  s.gram_ws = ws.take<char>(s.gram_bytes);
+  s.jac_bytes = jacobi_workspace<double>(p);
+  s.jac_ws = ws.take<char>(s.jac_bytes);
+  s.cn_bytes = std::max(col_norms_workspace<float>(N, p), col_norms_workspace<double>(N, p));
+  s.cn_ws = ws.take<char>(s.cn_bytes);
+  return L;
+}
+
+}  // namespace
+}  // namespace rvgp
+
+using namespace rvgp;
+
+RVGP_API size_t rvgp_eigsh_workspace(int n, int DB, int m, int p, int mode) {
+  Workspace ws(nullptr, 0);
+  carve(ws, (long long)n * DB, p, mode);
+  return ws.used;
+}
+
+// Smallest m eigenpairs of the block-CSR matrix (n block rows, DB x DB blocks).
+// vals64 is always required (Gershgorin bound, FP64 iterations); vals32 for
+// mode 1.  p: block size (m < p <= N, p % 4 == 0).  mode: 0 plain FP64, 1 mixed.
+// tol: FP64 residual tolerance relative to the Gershgorin bound; tol32 the
+// FP32 stage's.  evals: m doubles ascending; evecs: N x m (ld_evecs) times
+// `scale`.  stats (host, 8 ints, may be null): iterations, SpMM count, Jacobi
+// sweeps, converged, FP64 refinement iterations, Cholesky rescues.
+// Returns 0, or the number of unconverged eigenpairs (> 0).  Synchronises.
+RVGP_API int rvgp_eigsh(const int* indptr, const int* indices, const double* vals64, const float* vals32, int n,
+                        int DB, int m, int p, int mode, double tol, double tol32, int max_iter,
+                        unsigned long long seed, double* evals, double* evecs, int ld_evecs, double scale, int* stats,
+                        void* workspace, size_t ws_bytes, void* stream) {
+  const long long N = (long long)n * DB;
+  RVGP_CHECK_ARG(indptr && indices && vals64 && evals && evecs, "rvgp_eigsh: null pointer");
+  RVGP_CHECK_ARG(mode == 0 || (mode == 1 && vals32), "rvgp_eigsh: mode 1 needs FP32 values");
+  RVGP_CHECK_ARG(m >= 1 && m < N - 1, "k must be less than ndim(A)-1, got k=%d", m);
+  RVGP_CHECK_ARG(p > m && p <= N && p % 4 == 0 && p <= 2048, "rvgp_eigsh: block size p=%d invalid", p);
+  RVGP_CHECK_ARG(DB >= 1 && DB <= 4, "rvgp_eigsh: block size %d unsupported", DB);
+  size_t need = rvgp_eigsh_workspace(n, DB, m, p, mode);
+  RVGP_CHECK_ARG(workspace && ws_bytes >= need, "rvgp_eigsh: workspace of %zu bytes needed", need);
+  cudaStream_t st = as_stream(stream);
+  Workspace ws(workspace, ws_bytes);
+  Layout L = carve(ws, N, p, mode);
+  Small& s = L.s;
+  Problem P{n, DB, N, indptr, indices, vals64, vals32, m, p};
+  Stats stt;
+
+  // spectrum upper bound (Gershgorin)
+  const int gb = std::min(kNumSMs * 2, ceil_div(N, 256));
+  rvgp::note_launch(); gershgorin_kernel<<<gb, 256, 0, st>>>(n, DB, indptr, vals64, s.gersh);
+  std::vector<double> gp(gb);
+  cudaMemcpyAsync(gp.data(), s.gersh, sizeof(double) * gb, cudaMemcpyDeviceToHost, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess) return check_launch("rvgp_eigsh");
+  double bup = 0.0;
+  for (double v : gp) bup = std::max(bup, v);
+  bup = bup * (1.0 + 1e-12) + 1e-300;
+
+  std::vector<double> theta, res;
+  int nconv = 0;
+  const int first_deg = 12;
+  if (mode == 1) {
+    rvgp::note_launch(); random_block<float><<<ceil_div(N * p, 256), 256, 0, st>>>(L.f.V, N, p, p, seed);
+    TRY(iterate<float>(P, L.f, s, stt, bup, tol32, max_iter, first_deg, 1e4, theta, res, false, &nconv, st));
+    // FP64 refinement from the FP32 subspace
+    TRY(convert_f32_to_f64(L.f.V, p, L.d.V, p, N, p, st));
+    nconv = 0;
+    for (int j = 0; j < m; ++j)
+      if (res[j] <= tol * bup) ++nconv;
+    if (nconv < m) {
+      const int before = stt.iters;
+      TRY(iterate<double>(P, L.d, s, stt, bup, tol, max_iter, 4, 1e10, theta, res, true, &nconv, st));
+      stt.refine_iters = stt.iters - before;
+    }
+  } else {
+    rvgp::note_launch(); random_block<double><<<ceil_div(N * p, 256), 256, 0, st>>>(L.d.V, N, p, p, seed);
+    TRY(iterate<double>(P, L.d, s, stt, bup, tol, max_iter, first_deg, 1e10, theta, res, false, &nconv, st));
+  }
+  stt.conv = nconv;
+  cudaMemcpyAsync(evals, s.theta, sizeof(double) * m, cudaMemcpyDeviceToDevice, st);
+  rvgp::note_launch(); write_output<double><<<ceil_div(N * m, 256), 256, 0, st>>>(L.d.V, p, N, m, scale, evecs, ld_evecs);
+  if (stats) {
+    stats[0] = stt.iters;
+    stats[1] = stt.spmm;
+    stats[2] = stt.sweeps;
+    stats[3] = stt.conv;
+    stats[4] = stt.refine_iters;
+    stats[5] = stt.chol_rescues;
+  }
+  RVGP_LAUNCH_CHECK("rvgp_eigsh");
+  if (cudaStreamSynchronize(st) != cudaSuccess) return check_launch("rvgp_eigsh");
+  if (nconv < m) {
+    set_error("eigensolver: %d of %d eigenpairs did not converge in %d iterations", m - nconv, m, max_iter);
+    return m - nconv;
+  }
+  return RVGP_OK;
+}

@@ -1,0 +1,394 @@
+// Exact k-nearest-neighbour search (replaces sklearn kneighbors_graph,
+// RVGP/geometry.py:103-110, connectivity mode, include_self=False).
+//
+// Result contract: for every point q, the k indices j != q with the smallest
+// FP64 squared distance  sum_j (x_qj - x_cj)^2  (coordinates summed in order,
+// no fused multiply-add), ties broken by the lower index, listed in ascending
+// (distance, index) order.
+//
+// Pipeline (all on the caller's stream):
+//   1. prep     : bounding-box centre, FP32 centred copy padded to DP columns,
+//                 radius R = max |x - c| (two-stage deterministic reductions).
+//   2. screen   : FP32 brute force.  CTA = 128 queries x one slice of the
+//                 candidates staged through shared memory; every query keeps its
+//                 kc = k + 8 smallest FP32 squared distances.
+//   3. finish   : merge the slices, rescore the kc survivors in exact FP64, sort
+//                 by (d2, index) and certify: with u = 2^-24 the FP32 distance f
+//                 of any pair satisfies  true >= (f/(1+g) - 4.01 u R)/(1+u),
+//                 g = DP u/(1 - DP u).  If that lower bound for the kc-th FP32
+//                 survivor exceeds the exact k-th distance, no non-survivor can
+//                 enter the top k and the row is exact.  Otherwise the row is
+//                 queued.
+//   4. fallback : exact FP64 scan of the queued rows (one CTA per row).
+#include "common.cuh"
+#include <float.h>
+#include <limits.h>
+
+namespace rvgp {
+namespace {
+
+constexpr int kQB = 128;      // queries per CTA in the screen
+constexpr int kTileElems = 8192;  // floats of candidate coordinates per shared-memory tile (32 KB)
+constexpr int kExtra = 8;     // surplus survivors kept by the FP32 screen
+constexpr int kMaxKC = 72;    // k + kExtra upper bound
+constexpr int kFbThreads = 128;
+
+__global__ void prep_minmax(const double* __restrict__ X, int n, int D, double* __restrict__ part) {
+  // part[(block * D + j) * 2 + {0,1}] = min, max of column j over this block's rows
+  extern __shared__ double sh[];
+  for (int j = 0; j < D; ++j) {
+    double lo = DBL_MAX, hi = -DBL_MAX;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+      double v = X[(size_t)i * D + j];
+      lo = fmin(lo, v);
+      hi = fmax(hi, v);
+    }
+    sh[threadIdx.x] = lo;
+    sh[blockDim.x + threadIdx.x] = hi;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+      if (threadIdx.x < s) {
+        sh[threadIdx.x] = fmin(sh[threadIdx.x], sh[threadIdx.x + s]);
+        sh[blockDim.x + threadIdx.x] = fmax(sh[blockDim.x + threadIdx.x], sh[blockDim.x + threadIdx.x + s]);
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      part[((size_t)blockIdx.x * D + j) * 2 + 0] = sh[0];
+      part[((size_t)blockIdx.x * D + j) * 2 + 1] = sh[blockDim.x];
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void prep_centre(const double* __restrict__ part, int nblk, int D, double* __restrict__ centre) {
+  int j = threadIdx.x;
+  if (j >= D) return;
+  double lo = DBL_MAX, hi = -DBL_MAX;
+  for (int b = 0; b < nblk; ++b) {
+    lo = fmin(lo, part[((size_t)b * D + j) * 2 + 0]);
+    hi = fmax(hi, part[((size_t)b * D + j) * 2 + 1]);
+  }
+  centre[j] = 0.5 * (lo + hi);
+}
+
+__global__ void prep_copy(const double* __restrict__ X, int n, int D, int DP, const double* __restrict__ centre,
+                          float* __restrict__ Xf, double* __restrict__ part_r2) {
+  __shared__ double sh[256];
+  double r2max = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double r2 = 0.0;
+    for (int j = 0; j < DP; ++j) {
+      double a = j < D ? X[(size_t)i * D + j] - centre[j] : 0.0;
+      Xf[(size_t)i * DP + j] = (float)a;
+      r2 += a * a;
+    }
+    r2max = fmax(r2max, r2);
+  }
+  sh[threadIdx.x] = r2max;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sh[threadIdx.x] = fmax(sh[threadIdx.x], sh[threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part_r2[blockIdx.x] = sh[0];
+}
+
+__global__ void prep_radius(const double* __restrict__ part_r2, int nblk, double* __restrict__ radius) {
+  if (threadIdx.x != 0) return;
+  double m = 0.0;
+  for (int b = 0; b < nblk; ++b) m = fmax(m, part_r2[b]);
+  // sqrt of an FP64 sum: inflate by a relative 1e-12 so R is an upper bound
+  *radius = sqrt(m) * (1.0 + 1e-12);
+}
+
+// Keeps the kc smallest values seen; "worst" is the largest kept value once full.
+struct TopList {
+  float d[kMaxKC];
+  int i[kMaxKC];
+  int cnt;
+  int kc;
+  float worst;
+  int wpos;
+  __device__ void init(int kc_) { cnt = 0; kc = kc_; worst = FLT_MAX; wpos = 0; }
+  __device__ void refresh() {
+    worst = d[0];
+    wpos = 0;
+    for (int r = 1; r < kc; ++r)
+      if (d[r] > worst) { worst = d[r]; wpos = r; }
+  }
+  __device__ void push(float v, int idx) {
+    if (cnt < kc) {
+      d[cnt] = v;
+      i[cnt] = idx;
+      if (++cnt == kc) refresh();
+    } else if (v < worst) {
+      d[wpos] = v;
+      i[wpos] = idx;
+      refresh();
+    }
+  }
+};
+
+template <int DP>
+__global__ void __launch_bounds__(kQB) knn_screen(const float* __restrict__ Xf, int n, int kc, int nsplit,
+                                                  float* __restrict__ part_d, int* __restrict__ part_i) {
+  constexpr int kTile = kTileElems / DP;
+  __shared__ float tile[kTile * DP];
+  const int q = blockIdx.x * kQB + threadIdx.x;
+  const int split = blockIdx.y;
+  const long long chunk = ((long long)n + nsplit - 1) / nsplit;
+  const int c0 = (int)min((long long)n, split * chunk);
+  const int c1 = (int)min((long long)n, c0 + chunk);
+  float xq[DP];
+#pragma unroll
+  for (int j = 0; j < DP; ++j) xq[j] = q < n ? Xf[(size_t)q * DP + j] : 0.f;
+  TopList L;
+  L.init(kc);
+  for (int t0 = c0; t0 < c1; t0 += kTile) {
+    const int tn = min(kTile, c1 - t0);
+    __syncthreads();
+    for (int e = threadIdx.x; e < tn * DP; e += kQB) tile[e] = Xf[(size_t)t0 * DP + e];
+    __syncthreads();
+    if (q < n) {
+      for (int c = 0; c < tn; ++c) {
+        float acc = 0.f;
+#pragma unroll
+        for (int j = 0; j < DP; ++j) {
+          float df = xq[j] - tile[c * DP + j];
+          acc = fmaf(df, df, acc);
+        }
+        const int ci = t0 + c;
+        if (ci != q && (L.cnt < kc || acc < L.worst)) L.push(acc, ci);
+      }
+    }
+  }
+  if (q < n) {
+    size_t base = ((size_t)q * nsplit + split) * kc;
+    for (int r = 0; r < kc; ++r) {
+      part_d[base + r] = r < L.cnt ? L.d[r] : FLT_MAX;
+      part_i[base + r] = r < L.cnt ? L.i[r] : -1;
+    }
+  }
+}
+
+__device__ __forceinline__ double exact_d2(const double* __restrict__ X, int D, int a, int b) {
+  double acc = 0.0;
+  for (int j = 0; j < D; ++j) {
+    double df = __dsub_rn(X[(size_t)a * D + j], X[(size_t)b * D + j]);
+    acc = __dadd_rn(acc, __dmul_rn(df, df));
+  }
+  return acc;
+}
+
+__device__ __forceinline__ bool lex_less(double da, int ia, double db, int ib) {
+  return da < db || (da == db && ia < ib);
+}
+
+__global__ void knn_finish(const double* __restrict__ X, int n, int D, int DP, int k, int kc, int nsplit,
+                           const float* __restrict__ part_d, const int* __restrict__ part_i,
+                           const double* __restrict__ radius, int* __restrict__ out_idx,
+                           int* __restrict__ nflag, int* __restrict__ flag_list) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  TopList L;
+  L.init(kc);
+  const size_t base = (size_t)q * nsplit * kc;
+  int total = 0;
+  for (int e = 0; e < nsplit * kc; ++e) {
+    int ci = part_i[base + e];
+    if (ci < 0) continue;
+    ++total;
+    float v = part_d[base + e];
+    if (L.cnt < kc || v < L.worst) L.push(v, ci);
+  }
+  const int cnt = L.cnt;
+  double d2[kMaxKC];
+  int id[kMaxKC];
+  for (int r = 0; r < cnt; ++r) {
+    double v = exact_d2(X, D, q, L.i[r]);
+    int ci = L.i[r];
+    int s = r;
+    while (s > 0 && lex_less(v, ci, d2[s - 1], id[s - 1])) {
+      d2[s] = d2[s - 1];
+      id[s] = id[s - 1];
+      --s;
+    }
+    d2[s] = v;
+    id[s] = ci;
+  }
+  bool certified;
+  if (total == n - 1 && cnt == total) {
+    certified = true;  // every other point was rescored exactly
+  } else {
+    // here some slice kept a full list, so total >= kc and cnt == kc
+    const double u = 5.9604644775390625e-08;  // 2^-24
+    const double g = DP * u / (1.0 - DP * u);
+    const double f = sqrt((double)L.worst);
+    double lb = (f / (1.0 + g) - 4.01 * u * radius[0]) / (1.0 + u);
+    lb *= (1.0 - 1e-12);
+    certified = lb > 0.0 && lb * lb > d2[k - 1] * (1.0 + 1e-12);
+  }
+  for (int r = 0; r < k; ++r) out_idx[(size_t)q * k + r] = r < cnt ? id[r] : -1;
+  if (!certified) {
+    int slot = atomicAdd(nflag, 1);
+    flag_list[slot] = q;
+  }
+}
+
+// Exact FP64 scan for the rows the certificate could not settle.
+__global__ void __launch_bounds__(kFbThreads) knn_fallback(const double* __restrict__ X, int n, int D, int k,
+                                                           const int* __restrict__ nflag,
+                                                           const int* __restrict__ flag_list,
+                                                           int* __restrict__ out_idx) {
+  __shared__ double sd[kFbThreads];
+  __shared__ int si[kFbThreads];
+  __shared__ int st[kFbThreads];
+  const int nf = *nflag;
+  for (int f = blockIdx.x; f < nf; f += gridDim.x) {
+    const int q = flag_list[f];
+    double d2[kMaxKC];
+    int id[kMaxKC];
+    int cnt = 0;
+    for (int c = threadIdx.x; c < n; c += blockDim.x) {
+      if (c == q) continue;
+      double v = exact_d2(X, D, q, c);
+      if (cnt == k && !lex_less(v, c, d2[k - 1], id[k - 1])) continue;
+      int s = cnt < k ? cnt++ : k - 1;
+      while (s > 0 && lex_less(v, c, d2[s - 1], id[s - 1])) {
+        d2[s] = d2[s - 1];
+        id[s] = id[s - 1];
+        --s;
+      }
+      d2[s] = v;
+      id[s] = c;
+    }
+    int head = 0;
+    for (int r = 0; r < k; ++r) {
+      sd[threadIdx.x] = head < cnt ? d2[head] : DBL_MAX;
+      si[threadIdx.x] = head < cnt ? id[head] : INT_MAX;
+      st[threadIdx.x] = threadIdx.x;
+      __syncthreads();
+      for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) {
+          int o = threadIdx.x + s;
+          if (lex_less(sd[o], si[o], sd[threadIdx.x], si[threadIdx.x])) {
+            sd[threadIdx.x] = sd[o];
+            si[threadIdx.x] = si[o];
+            st[threadIdx.x] = st[o];
+          }
+        }
+        __syncthreads();
+      }
+      if (threadIdx.x == 0) out_idx[(size_t)q * k + r] = si[0];
+      if (threadIdx.x == st[0]) ++head;
+      __syncthreads();
+    }
+  }
+}
+
+int padded_dim(int D) {
+  if (D <= 4) return 4;
+  if (D <= 8) return 8;
+  if (D <= 16) return 16;
+  if (D <= 32) return 32;
+  if (D <= 64) return 64;
+  if (D <= 128) return 128;
+  return -1;
+}
+
+struct KnnPlan {
+  int DP, kc, nsplit, nblk_prep;
+};
+
+KnnPlan plan(int n, int D, int k) {
+  KnnPlan p;
+  p.DP = padded_dim(D);
+  p.kc = min(k + kExtra, n - 1);
+  int qblocks = ceil_div(n, kQB);
+  p.nsplit = max(1, min(16, ceil_div(4 * kNumSMs, qblocks)));
+  p.nblk_prep = min(kNumSMs * 2, max(1, ceil_div(n, 256)));
+  return p;
+}
+
+struct KnnBufs {
+  double *part_mm, *centre, *part_r2, *radius;
+  float *Xf, *part_d;
+  int *part_i, *nflag, *flag_list;
+};
+
+KnnBufs carve(Workspace& ws, const KnnPlan& p, int n, int D) {
+  KnnBufs b;
+  b.part_mm = ws.take<double>((size_t)p.nblk_prep * D * 2);
+  b.centre = ws.take<double>(D);
+  b.part_r2 = ws.take<double>(p.nblk_prep);
+  b.radius = ws.take<double>(1);
+  b.Xf = ws.take<float>((size_t)n * p.DP);
+  b.part_d = ws.take<float>((size_t)n * p.nsplit * p.kc);
+  b.part_i = ws.take<int>((size_t)n * p.nsplit * p.kc);
+  b.nflag = ws.take<int>(1);
+  b.flag_list = ws.take<int>(n);
+  return b;
+}
+
+size_t workspace_bytes(int n, int D, int k) {
+  Workspace ws(nullptr, 0);
+  carve(ws, plan(n, D, k), n, D);
+  return ws.used;
+}
+
+}  // namespace
+}  // namespace rvgp
+
+using namespace rvgp;
+
+RVGP_API size_t rvgp_knn_workspace(int n, int D, int k) {
+  if (n < 2 || D < 1 || k < 1) return 0;
+  return workspace_bytes(n, D, k);
+}
+
+RVGP_API int rvgp_knn(const double* X, int n, int D, int k, int* idx, void* workspace, size_t ws_bytes,
+                      void* stream) {
+  RVGP_CHECK_ARG(X && idx, "rvgp_knn: null pointer");
+  RVGP_CHECK_ARG(n >= 2, "rvgp_knn: need at least 2 points, got %d", n);
+  RVGP_CHECK_ARG(k >= 1 && k < n, "Expected n_neighbors < n_samples, got %d >= %d", k, n);
+  RVGP_CHECK_ARG(k + kExtra <= kMaxKC, "rvgp_knn: k=%d exceeds the supported maximum %d", k, kMaxKC - kExtra);
+  RVGP_CHECK_ARG(padded_dim(D) > 0, "rvgp_knn: ambient dimension %d > 128 is not supported", D);
+  size_t need = workspace_bytes(n, D, k);
+  RVGP_CHECK_ARG(workspace && ws_bytes >= need, "rvgp_knn: workspace of %zu bytes needed", need);
+  cudaStream_t st = as_stream(stream);
+  KnnPlan p = plan(n, D, k);
+  Workspace ws(workspace, ws_bytes);
+  KnnBufs b = carve(ws, p, n, D);
+  rvgp::note_launch(); prep_minmax<<<p.nblk_prep, 256, 2 * 256 * sizeof(double), st>>>(X, n, D, b.part_mm);
+  rvgp::note_launch(); prep_centre<<<1, 128, 0, st>>>(b.part_mm, p.nblk_prep, D, b.centre);
+  rvgp::note_launch(); prep_copy<<<p.nblk_prep, 256, 0, st>>>(X, n, D, p.DP, b.centre, b.Xf, b.part_r2);
+  rvgp::note_launch(); prep_radius<<<1, 32, 0, st>>>(b.part_r2, p.nblk_prep, b.radius);
+  cudaMemsetAsync(b.nflag, 0, sizeof(int), st);
+  dim3 grid(ceil_div(n, kQB), p.nsplit);
+  switch (p.DP) {
+    case 4: rvgp::note_launch(); knn_screen<4><<<grid, kQB, 0, st>>>(b.Xf, n, p.kc, p.nsplit, b.part_d, b.part_i); break;
+    case 8: rvgp::note_launch(); knn_screen<8><<<grid, kQB, 0, st>>>(b.Xf, n, p.kc, p.nsplit, b.part_d, b.part_i); break;
+    case 16: rvgp::note_launch(); knn_screen<16><<<grid, kQB, 0, st>>>(b.Xf, n, p.kc, p.nsplit, b.part_d, b.part_i); break;
+    case 32: rvgp::note_launch(); knn_screen<32><<<grid, kQB, 0, st>>>(b.Xf, n, p.kc, p.nsplit, b.part_d, b.part_i); break;
+    case 64: rvgp::note_launch(); knn_screen<64><<<grid, kQB, 0, st>>>(b.Xf, n, p.kc, p.nsplit, b.part_d, b.part_i); break;
+    rvgp::note_launch(); default: knn_screen<128><<<grid, kQB, 0, st>>>(b.Xf, n, p.kc, p.nsplit, b.part_d, b.part_i); break;
+  }
+  rvgp::note_launch(); knn_finish<<<ceil_div(n, 128), 128, 0, st>>>(X, n, D, p.DP, k, p.kc, p.nsplit, b.part_d, b.part_i, b.radius,
+                                               idx, b.nflag, b.flag_list);
+  rvgp::note_launch(); knn_fallback<<<kNumSMs, kFbThreads, 0, st>>>(X, n, D, k, b.nflag, b.flag_list, idx);
+  RVGP_LAUNCH_CHECK("rvgp_knn");
+  return RVGP_OK;
+}
+
+// Number of rows the last rvgp_knn call on this workspace sent to the exact
+// fallback (reads one int from the workspace; synchronises the stream).
+RVGP_API int rvgp_knn_fallback_rows(int n, int D, int k, void* workspace, void* stream) {
+  if (padded_dim(D) < 0 || k < 1 || k >= n) return -1;
+  Workspace ws(workspace, SIZE_MAX);
+  KnnBufs b = carve(ws, plan(n, D, k), n, D);
+  int h = -1;
+  if (cudaMemcpyAsync(&h, b.nflag, sizeof(int), cudaMemcpyDeviceToHost, as_stream(stream)) != cudaSuccess) return -1;
+  if (cudaStreamSynchronize(as_stream(stream)) != cudaSuccess) return -1;
+  return h;
+}

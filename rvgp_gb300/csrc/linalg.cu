@@ -1,0 +1,693 @@
+// Dense linear algebra kernels (see linalg.cuh).
+#include "linalg.cuh"
+#include <math.h>
+#include <limits.h>
+#include <vector>
+#include <mutex>
+#include <map>
+#include <algorithm>
+
+namespace rvgp {
+namespace {
+
+constexpr int TB = 64;   // output tile edge
+constexpr int BK = 16;   // reduction slab
+
+// ------------------------------------------------------------------ C = Aᵀ B (split over N)
+template <typename T>
+__global__ void __launch_bounds__(256) gram_partial(const T* __restrict__ A, int lda, const T* __restrict__ B, int ldb,
+                                                    long long N, int p, int q, long long chunk, T* __restrict__ part) {
+  __shared__ T As[BK][TB];
+  __shared__ T Bs[BK][TB];
+  const int i0 = blockIdx.x * TB, j0 = blockIdx.y * TB;
+  const long long n0 = blockIdx.z * chunk;
+  const long long n1 = min(N, n0 + chunk);
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  T acc[4][4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) acc[u][v] = T(0);
+  for (long long nb = n0; nb < n1; nb += BK) {
+    for (int e = threadIdx.x; e < BK * TB; e += 256) {
+      const int r = e / TB, c = e % TB;
+      const long long n = nb + r;
+      As[r][c] = (n < n1 && i0 + c < p) ? A[n * lda + i0 + c] : T(0);
+      Bs[r][c] = (n < n1 && j0 + c < q) ? B[n * ldb + j0 + c] : T(0);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < BK; ++r) {
+      T a[4], b[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) a[u] = As[r][ty * 4 + u];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) b[v] = Bs[r][tx * 4 + v];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) acc[u][v] = fma(a[u], b[v], acc[u][v]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const int i = i0 + ty * 4 + u, j = j0 + tx * 4 + v;
+      if (i < p && j < q) part[((size_t)blockIdx.z * p + i) * q + j] = acc[u][v];
+    }
+}
+
+template <typename T>
+__global__ void reduce_splits(const T* __restrict__ part, int splits, int p, int q, T* __restrict__ C, int ldc,
+                              T alpha, T beta) {
+  const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e >= (long long)p * q) return;
+  const int i = (int)(e / q), j = (int)(e % q);
+  T s = T(0);
+  for (int t = 0; t < splits; ++t) s += part[((size_t)t * p + i) * q + j];
+  T* c = C + (size_t)i * ldc + j;
+  *c = beta == T(0) ? alpha * s : alpha * s + beta * (*c);
+}
+
+__global__ void reduce_splits_f32_to_f64(const float* __restrict__ part, int splits, int p, int q,
+                                         double* __restrict__ C, int ldc, double alpha, double beta) {
+  const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e >= (long long)p * q) return;
+  const int i = (int)(e / q), j = (int)(e % q);
+  double s = 0.0;
+  for (int t = 0; t < splits; ++t) s += (double)part[((size_t)t * p + i) * q + j];
+  double* c = C + (size_t)i * ldc + j;
+  *c = beta == 0.0 ? alpha * s : alpha * s + beta * (*c);
+}
+
+template <typename T>
+int gram_splits(long long N, int p, int q) {
+  const int tiles = ceil_div(p, TB) * ceil_div(q, TB);
+  int s = ceil_div(4 * kNumSMs, tiles);
+  s = (int)std::min<long long>(s, std::max<long long>(1, N / 512));
+  return std::max(1, std::min(s, 1024));
+}
+
+// ------------------------------------------------------------------ C = A B
+template <typename T>
+__global__ void __launch_bounds__(256) gemm_nn_kernel(const T* __restrict__ A, int lda, const T* __restrict__ B,
+                                                      int ldb, long long N, int p, int q, T* __restrict__ C, int ldc,
+                                                      T alpha, T beta) {
+  __shared__ T As[TB][BK + 1];
+  __shared__ T Bs[BK][TB];
+  const long long r0 = (long long)blockIdx.x * TB;
+  const int j0 = blockIdx.y * TB;
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  T acc[4][4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) acc[u][v] = T(0);
+  for (int k0 = 0; k0 < p; k0 += BK) {
+    for (int e = threadIdx.x; e < TB * BK; e += 256) {
+      const int r = e / BK, c = e % BK;
+      As[r][c] = (r0 + r < N && k0 + c < p) ? A[(r0 + r) * lda + k0 + c] : T(0);
+      const int rb = e / TB, cb = e % TB;
+      Bs[rb][cb] = (k0 + rb < p && j0 + cb < q) ? B[(size_t)(k0 + rb) * ldb + j0 + cb] : T(0);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < BK; ++kk) {
+      T a[4], b[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) a[u] = As[ty * 4 + u][kk];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) b[v] = Bs[kk][tx * 4 + v];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) acc[u][v] = fma(a[u], b[v], acc[u][v]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const long long r = r0 + ty * 4 + u;
+      const int j = j0 + tx * 4 + v;
+      if (r < N && j < q) {
+        T* c = C + r * ldc + j;
+        *c = beta == T(0) ? alpha * acc[u][v] : alpha * acc[u][v] + beta * (*c);
+      }
+    }
+}
+
+// ------------------------------------------------------------------ Cholesky (one CTA)
+template <typename T>
+__global__ void __launch_bounds__(1024) chol_kernel(T* __restrict__ A, int lda, int p, int* __restrict__ info) {
+  __shared__ int bad;
+  if (threadIdx.x == 0) {
+    bad = 0;
+    *info = 0;
+  }
+  for (int j = 0; j < p; ++j) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      T d = A[(size_t)j * lda + j];
+      if (!(d > T(0))) {
+        bad = j + 1;
+        *info = j + 1;
+      } else {
+        A[(size_t)j * lda + j] = sqrt(d);
+      }
+    }
+    __syncthreads();
+    if (bad) return;
+    const T djj = A[(size_t)j * lda + j];
+    for (int i = j + 1 + threadIdx.x; i < p; i += blockDim.x) A[(size_t)i * lda + j] /= djj;
+    __syncthreads();
+    const int m = p - j - 1;
+    for (long long e = threadIdx.x; e < (long long)m * m; e += blockDim.x) {
+      const int ii = (int)(e / m), kk = (int)(e % m);
+      if (kk <= ii) {
+        const int i = j + 1 + ii, k = j + 1 + kk;
+        A[(size_t)i * lda + k] -= A[(size_t)i * lda + j] * A[(size_t)k * lda + j];
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------------ blocked Cholesky (many CTAs)
+constexpr int NB = 32;
+
+// factor the diagonal block [k0, k0+nb) in shared memory (one CTA)
+template <typename T>
+__global__ void __launch_bounds__(256) potrf_diag(T* __restrict__ A, int lda, int k0, int nb, int* __restrict__ info) {
+  __shared__ T L[NB][NB + 1];
+  __shared__ int bad;
+  if (*info) return;  // an earlier block already failed
+  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) L[e / nb][e % nb] = A[(size_t)(k0 + e / nb) * lda + k0 + e % nb];
+  if (threadIdx.x == 0) bad = 0;
+  __syncthreads();
+  for (int j = 0; j < nb; ++j) {
+    if (threadIdx.x == 0) {
+      T d = L[j][j];
+      if (!(d > T(0))) {
+        bad = 1;
+        if (*info == 0) *info = k0 + j + 1;
+      } else {
+        L[j][j] = sqrt(d);
+      }
+    }
+    __syncthreads();
+    if (bad) return;
+    for (int i = j + 1 + threadIdx.x; i < nb; i += blockDim.x) L[i][j] /= L[j][j];
+    __syncthreads();
+    const int m = nb - j - 1;
+    for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
+      const int ii = e / m, kk = e % m;
+      if (kk <= ii) L[j + 1 + ii][j + 1 + kk] -= L[j + 1 + ii][j] * L[j + 1 + kk][j];
+    }
+    __syncthreads();
+  }
+  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
+    const int i = e / nb, c = e % nb;
+    if (c <= i) A[(size_t)(k0 + i) * lda + k0 + c] = L[i][c];
+  }
+}
+
+// panel: rows [k0+nb, p) of columns [k0, k0+nb) <- A L_kkᵀ⁻¹ (one CTA per NB rows)
+template <typename T>
+__global__ void __launch_bounds__(NB) trsm_panel(T* __restrict__ A, int lda, int k0, int nb, int p,
+                                                 const int* __restrict__ info) {
+  __shared__ T L[NB][NB + 1];
+  if (*info) return;
+  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) L[e / nb][e % nb] = A[(size_t)(k0 + e / nb) * lda + k0 + e % nb];
+  __syncthreads();
+  const int r = k0 + nb + blockIdx.x * NB + threadIdx.x;
+  if (r >= p) return;
+  T x[NB];
+  for (int c = 0; c < nb; ++c) {
+    T v = A[(size_t)r * lda + k0 + c];
+    for (int t = 0; t < c; ++t) v -= x[t] * L[c][t];
+    x[c] = v / L[c][c];
+  }
+  for (int c = 0; c < nb; ++c) A[(size_t)r * lda + k0 + c] = x[c];
+}
+
+// trailing update of the lower part: A_ij -= A_ik A_jkᵀ for blocks (i, j), j <= i, both > k
+template <typename T>
+__global__ void __launch_bounds__(256) syrk_update(T* __restrict__ A, int lda, int k0, int nb, int p,
+                                                   const int* __restrict__ info) {
+  __shared__ T Ai[NB][NB + 1], Aj[NB][NB + 1];
+  if (*info) return;
+  const int bi = blockIdx.y, bj = blockIdx.x;
+  if (bj > bi) return;
+  const int r0 = k0 + nb + bi * NB, c0 = k0 + nb + bj * NB;
+  for (int e = threadIdx.x; e < NB * nb; e += blockDim.x) {
+    const int rr = e / nb, cc = e % nb;
+    Ai[rr][cc] = r0 + rr < p ? A[(size_t)(r0 + rr) * lda + k0 + cc] : T(0);
+    Aj[rr][cc] = c0 + rr < p ? A[(size_t)(c0 + rr) * lda + k0 + cc] : T(0);
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < NB * NB; e += blockDim.x) {
+    const int rr = e / NB, cc = e % NB;
+    const int i = r0 + rr, j = c0 + cc;
+    if (i >= p || j >= p || j > i) continue;
+    T s = T(0);
+    for (int t = 0; t < nb; ++t) s += Ai[rr][t] * Aj[cc][t];
+    A[(size_t)i * lda + j] -= s;
+  }
+}
+
+// ------------------------------------------------------------------ triangular inverse (warp per column)
+template <typename T>
+__global__ void trinv_kernel(const T* __restrict__ L, int ldl, int p, T* __restrict__ X, int ldx) {
+  const int lane = threadIdx.x & 31;
+  const int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (j >= p) return;
+  for (int i = lane; i < j; i += 32) X[(size_t)i * ldx + j] = T(0);
+  if (lane == 0) X[(size_t)j * ldx + j] = T(1) / L[(size_t)j * ldl + j];
+  __syncwarp();
+  for (int i = j + 1; i < p; ++i) {
+    T s = T(0);
+    for (int k = j + lane; k < i; k += 32) s += L[(size_t)i * ldl + k] * X[(size_t)k * ldx + j];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) X[(size_t)i * ldx + j] = -s / L[(size_t)i * ldl + i];
+    __syncwarp();
+  }
+}
+
+// ------------------------------------------------------------------ Jacobi eigensolver
+template <typename T>
+struct Eps;
+template <> struct Eps<float> { static constexpr double v = 5.96e-8; };
+template <> struct Eps<double> { static constexpr double v = 1.12e-16; };
+
+// (c1, c2, P, Q) of index i for this round: new basis e'_i = c1 e_P + c2 e_Q
+template <typename T>
+__device__ __forceinline__ void rot_of(const T* __restrict__ H, int p, const int* __restrict__ partner, int i, T& c1,
+                                       T& c2, int& P, int& Q) {
+  const int m = partner[i];
+  if (m == i || m >= p) {
+    c1 = T(1);
+    c2 = T(0);
+    P = Q = i;
+    return;
+  }
+  P = min(i, m);
+  Q = max(i, m);
+  const T a = H[(size_t)P * p + P], b = H[(size_t)Q * p + Q], c = H[(size_t)P * p + Q];
+  T cs = T(1), sn = T(0);
+  if (c != T(0) && fabs((double)c) > Eps<T>::v * 1e-3 * sqrt(fabs((double)a) * fabs((double)b))) {
+    const T theta = (b - a) / (T(2) * c);
+    const T t = (theta >= T(0) ? T(1) : T(-1)) / (fabs(theta) + sqrt(theta * theta + T(1)));
+    cs = T(1) / sqrt(t * t + T(1));
+    sn = t * cs;
+  }
+  if (i == P) {
+    c1 = cs;
+    c2 = -sn;
+  } else {
+    c1 = sn;
+    c2 = cs;
+  }
+}
+
+// per-index rotation coefficients of this round: coef[i] = (c1, c2), pq[i] = (P, Q)
+template <typename T>
+__global__ void jacobi_params(const T* __restrict__ H, int p, const int* __restrict__ partner, T* __restrict__ coef,
+                              int2* __restrict__ pq) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p) return;
+  T c1, c2;
+  int P, Q;
+  rot_of(H, p, partner, i, c1, c2, P, Q);
+  coef[2 * i] = c1;
+  coef[2 * i + 1] = c2;
+  pq[i] = make_int2(P, Q);
+}
+
+template <typename T>
+__global__ void jacobi_round(const T* __restrict__ H, T* __restrict__ Hn, const T* __restrict__ V,
+                             T* __restrict__ Vn, int p, const int* __restrict__ partner, const T* __restrict__ coef,
+                             const int2* __restrict__ pq) {
+  const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long pp = (long long)p * p;
+  if (e < pp) {
+    const int i = (int)(e / p), j = (int)(e % p);
+    const T ci1 = coef[2 * i], ci2 = coef[2 * i + 1], cj1 = coef[2 * j], cj2 = coef[2 * j + 1];
+    const int2 a = pq[i], b = pq[j];
+    T v;
+    if (i != j && partner[i] == j) {
+      v = T(0);
+    } else {
+      v = ci1 * (cj1 * H[(size_t)a.x * p + b.x] + cj2 * H[(size_t)a.x * p + b.y]);
+      if (ci2 != T(0)) v += ci2 * (cj1 * H[(size_t)a.y * p + b.x] + cj2 * H[(size_t)a.y * p + b.y]);
+    }
+    Hn[e] = v;
+  } else if (e < 2 * pp) {
+    const long long f = e - pp;
+    const int r = (int)(f / p), i = (int)(f % p);
+    const T c1 = coef[2 * i], c2 = coef[2 * i + 1];
+    const int2 a = pq[i];
+    T v = c1 * V[(size_t)r * p + a.x];
+    if (c2 != T(0)) v += c2 * V[(size_t)r * p + a.y];
+    Vn[f] = v;
+  }
+}
+
+// H <- (H + Hᵀ)/2: rotations leave the antisymmetric part's norm unchanged, so
+// rounding asymmetry must go before the off-norm test.
+template <typename T>
+__global__ void symmetrise(T* __restrict__ H, int p) {
+  const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e >= (long long)p * p) return;
+  const int i = (int)(e / p), j = (int)(e % p);
+  if (j <= i) return;
+  const T v = (H[(size_t)i * p + j] + H[(size_t)j * p + i]) * T(0.5);
+  H[(size_t)i * p + j] = v;
+  H[(size_t)j * p + i] = v;
+}
+
+template <typename T>
+__global__ void set_identity(T* __restrict__ V, int p) {
+  const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e < (long long)p * p) V[e] = (e / p == e % p) ? T(1) : T(0);
+}
+
+// off-diagonal and total squared Frobenius norms (one CTA, fixed order)
+template <typename T>
+__global__ void __launch_bounds__(1024) offnorm_kernel(const T* __restrict__ H, int p, double* __restrict__ out) {
+  __shared__ double so[1024], st[1024];
+  double off = 0.0, tot = 0.0;
+  for (long long e = threadIdx.x; e < (long long)p * p; e += blockDim.x) {
+    double v = (double)H[e];
+    tot += v * v;
+    if (e / p != e % p) off += v * v;
+  }
+  so[threadIdx.x] = off;
+  st[threadIdx.x] = tot;
+  __syncthreads();
+  for (int s = 512; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      so[threadIdx.x] += so[threadIdx.x + s];
+      st[threadIdx.x] += st[threadIdx.x + s];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    out[0] = so[0];
+    out[1] = st[0];
+  }
+}
+
+// sort the diagonal ascending (ties by index) and permute the columns of V
+template <typename T>
+__global__ void __launch_bounds__(1024) sort_eig(const T* __restrict__ H, const T* __restrict__ V, int p,
+                                                 T* __restrict__ w, T* __restrict__ Vout) {
+  extern __shared__ unsigned char smem[];
+  T* key = reinterpret_cast<T*>(smem);
+  int* idx = reinterpret_cast<int*>(key + 2048);
+  int P2 = 1;
+  while (P2 < p) P2 <<= 1;
+  for (int t = threadIdx.x; t < P2; t += blockDim.x) {
+    key[t] = t < p ? H[(size_t)t * p + t] : T(0);
+    idx[t] = t < p ? t : INT_MAX;
+  }
+  __syncthreads();
+  auto less = [&](int a, int b) {
+    if (idx[a] == INT_MAX) return false;
+    if (idx[b] == INT_MAX) return true;
+    return key[a] < key[b] || (key[a] == key[b] && idx[a] < idx[b]);
+  };
+  for (int size = 2; size <= P2; size <<= 1)
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int t = threadIdx.x; t < P2; t += blockDim.x) {
+        const int o = t ^ stride;
+        if (o > t) {
+          const bool up = (t & size) == 0;
+          if (up ? less(o, t) : less(t, o)) {
+            T k = key[t];
+            key[t] = key[o];
+            key[o] = k;
+            int x = idx[t];
+            idx[t] = idx[o];
+            idx[o] = x;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  for (int t = threadIdx.x; t < p; t += blockDim.x) w[t] = key[t];
+  for (long long e = threadIdx.x; e < (long long)p * p; e += blockDim.x) {
+    const int r = (int)(e / p), c = (int)(e % p);
+    Vout[e] = V[(size_t)r * p + idx[c]];
+  }
+}
+
+// round-robin (circle method) partner tables, cached per size
+std::mutex g_sched_mu;
+std::map<int, std::vector<int>> g_sched;
+
+const std::vector<int>& schedule(int p) {
+  std::lock_guard<std::mutex> lk(g_sched_mu);
+  auto it = g_sched.find(p);
+  if (it != g_sched.end()) return it->second;
+  const int P = p + (p & 1);
+  const int rounds = P - 1;
+  std::vector<int> tab((size_t)rounds * p);
+  for (int r = 0; r < rounds; ++r) {
+    std::vector<int> part(P);
+    part[P - 1] = r;
+    part[r] = P - 1;
+    for (int k = 1; k < P / 2; ++k) {
+      int a = (r + k) % (P - 1), b = (r - k + (P - 1)) % (P - 1);
+      part[a] = b;
+      part[b] = a;
+    }
+    for (int i = 0; i < p; ++i) tab[(size_t)r * p + i] = part[i] >= p ? i : part[i];
+  }
+  return g_sched.emplace(p, std::move(tab)).first->second;
+}
+
+// ------------------------------------------------------------------ column utilities
+template <typename T>
+__global__ void colsq_partial(const T* __restrict__ X, int ld, long long N, int b, long long chunk, T* __restrict__ part) {
+  const long long r0 = blockIdx.x * chunk, r1 = min(N, r0 + chunk);
+  for (int j = threadIdx.x; j < b; j += blockDim.x) {
+    T s = T(0);
+    for (long long r = r0; r < r1; ++r) {
+      T v = X[r * ld + j];
+      s = fma(v, v, s);
+    }
+    part[(size_t)blockIdx.x * b + j] = s;
+  }
+}
+
+template <typename T>
+__global__ void colsq_final(const T* __restrict__ part, int nchunk, int b, T* __restrict__ out) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= b) return;
+  T s = T(0);
+  for (int c = 0; c < nchunk; ++c) s += part[(size_t)c * b + j];
+  out[j] = sqrt(s);
+}
+
+template <typename T>
+__global__ void scale_cols_kernel(T* __restrict__ X, int ld, long long N, int b, const T* __restrict__ s, bool inv) {
+  const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e >= N * b) return;
+  const long long r = e / b;
+  const int j = (int)(e % b);
+  const T f = s[j];
+  X[r * ld + j] = inv ? (f != T(0) ? X[r * ld + j] / f : T(0)) : X[r * ld + j] * f;
+}
+
+template <typename A, typename B>
+__global__ void convert_kernel(const A* __restrict__ in, int ldi, B* __restrict__ out, int ldo, long long N, int b) {
+  const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e >= N * b) return;
+  const long long r = e / b;
+  const int j = (int)(e % b);
+  out[r * ldo + j] = (B)in[r * ldi + j];
+}
+
+int col_chunks(long long N) { return (int)std::max<long long>(1, std::min<long long>(1024, N / 64)); }
+
+}  // namespace
+
+// ------------------------------------------------------------------ host launchers
+template <typename T>
+size_t gram_workspace(long long N, int p, int q) {
+  return sizeof(T) * (size_t)gram_splits<T>(N, p, q) * p * q + 256;
+}
+
+template <typename T>
+int gram(const T* A, int lda, const T* B, int ldb, long long N, int p, int q, T* C, int ldc, T alpha, T beta,
+         void* ws, size_t ws_bytes, cudaStream_t st) {
+  const int splits = gram_splits<T>(N, p, q);
+  if (ws_bytes < gram_workspace<T>(N, p, q)) {
+    set_error("gram: workspace too small");
+    return RVGP_EWORKSPACE;
+  }
+  const long long chunk = (N + splits - 1) / splits;
+  dim3 grid(ceil_div(p, TB), ceil_div(q, TB), splits);
+  T* part = static_cast<T*>(ws);
+  rvgp::note_launch(); gram_partial<T><<<grid, 256, 0, st>>>(A, lda, B, ldb, N, p, q, chunk, part);
+  rvgp::note_launch(); reduce_splits<T><<<ceil_div((long long)p * q, 256), 256, 0, st>>>(part, splits, p, q, C, ldc, alpha, beta);
+  return check_launch("gram");
+}
+
+int gram_f32_out64(const float* A, int lda, const float* B, int ldb, long long N, int p, int q, double* C, int ldc,
+                   double alpha, double beta, void* ws, size_t ws_bytes, cudaStream_t st) {
+  const int splits = gram_splits<float>(N, p, q);
+  if (ws_bytes < gram_workspace<float>(N, p, q)) {
+    set_error("gram: workspace too small");
+    return RVGP_EWORKSPACE;
+  }
+  const long long chunk = (N + splits - 1) / splits;
+  dim3 grid(ceil_div(p, TB), ceil_div(q, TB), splits);
+  float* part = static_cast<float*>(ws);
+  rvgp::note_launch(); gram_partial<float><<<grid, 256, 0, st>>>(A, lda, B, ldb, N, p, q, chunk, part);
+  rvgp::note_launch(); reduce_splits_f32_to_f64<<<ceil_div((long long)p * q, 256), 256, 0, st>>>(part, splits, p, q, C, ldc, alpha, beta);
+  return check_launch("gram_f32_out64");
+}
+
+template <typename T>
+int gemm_nn(const T* A, int lda, const T* B, int ldb, long long N, int p, int q, T* C, int ldc, T alpha, T beta,
+            cudaStream_t st) {
+  dim3 grid(ceil_div(N, TB), ceil_div(q, TB));
+  rvgp::note_launch(); gemm_nn_kernel<T><<<grid, 256, 0, st>>>(A, lda, B, ldb, N, p, q, C, ldc, alpha, beta);
+  return check_launch("gemm_nn");
+}
+
+template <typename T>
+int cholesky(T* A, int lda, int p, int* info, cudaStream_t st) {
+  if (p <= 64) {
+    rvgp::note_launch(); chol_kernel<T><<<1, 1024, 0, st>>>(A, lda, p, info);
+    return check_launch("cholesky");
+  }
+  cudaMemsetAsync(info, 0, sizeof(int), st);
+  for (int k0 = 0; k0 < p; k0 += NB) {
+    const int nb = std::min(NB, p - k0);
+    rvgp::note_launch(); potrf_diag<T><<<1, 256, 0, st>>>(A, lda, k0, nb, info);
+    const int rest = p - k0 - nb;
+    if (rest <= 0) break;
+    const int rb = ceil_div(rest, NB);
+    rvgp::note_launch(); trsm_panel<T><<<rb, NB, 0, st>>>(A, lda, k0, nb, p, info);
+    rvgp::note_launch(); syrk_update<T><<<dim3(rb, rb), 256, 0, st>>>(A, lda, k0, nb, p, info);
+  }
+  return check_launch("cholesky");
+}
+
+template <typename T>
+int tri_inv_lower(const T* L, int ldl, int p, T* Linv, int ldi, cudaStream_t st) {
+  rvgp::note_launch(); trinv_kernel<T><<<ceil_div((long long)p * 32, 128), 128, 0, st>>>(L, ldl, p, Linv, ldi);
+  return check_launch("tri_inv_lower");
+}
+
+template <typename T>
+size_t jacobi_workspace(int p) {
+  const int P = p + (p & 1);
+  return sizeof(T) * (size_t)p * p * 3 + sizeof(int) * (size_t)(P - 1) * p + 2 * sizeof(double) +
+         sizeof(T) * 2 * (size_t)p + sizeof(int2) * (size_t)p + 8192;
+}
+
+template <typename T>
+int jacobi_eigh(T* H, int p, T* w, T* V, int max_sweeps, double tol, int* sweeps_used, void* ws, size_t ws_bytes,
+                cudaStream_t st) {
+  if (p < 1 || p > 2048) {
+    set_error("jacobi_eigh: p=%d out of range", p);
+    return RVGP_ENOTSUP;
+  }
+  if (ws_bytes < jacobi_workspace<T>(p)) {
+    set_error("jacobi_eigh: workspace too small");
+    return RVGP_EWORKSPACE;
+  }
+  Workspace W(ws, ws_bytes);
+  T* Hb = W.take<T>((size_t)p * p);
+  T* Va = W.take<T>((size_t)p * p);
+  T* Vb = W.take<T>((size_t)p * p);
+  const int P = p + (p & 1);
+  const int rounds = P - 1;
+  int* part = W.take<int>((size_t)rounds * p);
+  double* nrm = W.take<double>(2);
+  T* coef = W.take<T>(2 * (size_t)p);
+  int2* pq = W.take<int2>(p);
+  const std::vector<int>& tab = schedule(p);
+  cudaMemcpyAsync(part, tab.data(), sizeof(int) * tab.size(), cudaMemcpyHostToDevice, st);
+  const long long pp = (long long)p * p;
+  rvgp::note_launch(); set_identity<T><<<ceil_div(pp, 256), 256, 0, st>>>(Va, p);
+  rvgp::note_launch(); symmetrise<T><<<ceil_div(pp, 256), 256, 0, st>>>(H, p);
+  T *h0 = H, *h1 = Hb, *v0 = Va, *v1 = Vb;
+  int used = 0;
+  for (int sweep = 0; sweep < max_sweeps && p > 1; ++sweep) {
+    rvgp::note_launch(); offnorm_kernel<T><<<1, 1024, 0, st>>>(h0, p, nrm);
+    double hn[2];
+    cudaMemcpyAsync(hn, nrm, sizeof(hn), cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return check_launch("jacobi_eigh");
+    if (!(hn[0] > tol * tol * hn[1])) break;
+    for (int r = 0; r < rounds; ++r) {
+      rvgp::note_launch(); jacobi_params<T><<<ceil_div(p, 128), 128, 0, st>>>(h0, p, part + (size_t)r * p, coef, pq);
+      rvgp::note_launch(); jacobi_round<T><<<ceil_div(2 * pp, 256), 256, 0, st>>>(h0, h1, v0, v1, p, part + (size_t)r * p, coef, pq);
+      T* t = h0; h0 = h1; h1 = t;
+      t = v0; v0 = v1; v1 = t;
+    }
+    ++used;
+  }
+  if (sweeps_used) *sweeps_used = used;
+  const size_t smem = 2048 * sizeof(T) + 2048 * sizeof(int);
+  rvgp::note_launch(); sort_eig<T><<<1, 1024, smem, st>>>(h0, v0, p, w, V);
+  return check_launch("jacobi_eigh");
+}
+
+template <typename T>
+size_t col_norms_workspace(long long N, int b) {
+  return sizeof(T) * (size_t)col_chunks(N) * b + 256;
+}
+
+template <typename T>
+int col_norms(const T* X, int ld, long long N, int b, T* out, void* ws, size_t ws_bytes, cudaStream_t st) {
+  const int nc = col_chunks(N);
+  if (ws_bytes < col_norms_workspace<T>(N, b)) {
+    set_error("col_norms: workspace too small");
+    return RVGP_EWORKSPACE;
+  }
+  const long long chunk = (N + nc - 1) / nc;
+  T* part = static_cast<T*>(ws);
+  rvgp::note_launch(); colsq_partial<T><<<nc, 256, 0, st>>>(X, ld, N, b, chunk, part);
+  rvgp::note_launch(); colsq_final<T><<<ceil_div(b, 256), 256, 0, st>>>(part, nc, b, out);
+  return check_launch("col_norms");
+}
+
+template <typename T>
+int scale_cols(T* X, int ld, long long N, int b, const T* s, bool inverse, cudaStream_t st) {
+  rvgp::note_launch(); scale_cols_kernel<T><<<ceil_div(N * b, 256), 256, 0, st>>>(X, ld, N, b, s, inverse);
+  return check_launch("scale_cols");
+}
+
+int convert_f32_to_f64(const float* in, int ldi, double* out, int ldo, long long N, int b, cudaStream_t st) {
+  rvgp::note_launch(); convert_kernel<float, double><<<ceil_div(N * b, 256), 256, 0, st>>>(in, ldi, out, ldo, N, b);
+  return check_launch("convert");
+}
+int convert_f64_to_f32(const double* in, int ldi, float* out, int ldo, long long N, int b, cudaStream_t st) {
+  rvgp::note_launch(); convert_kernel<double, float><<<ceil_div(N * b, 256), 256, 0, st>>>(in, ldi, out, ldo, N, b);
+  return check_launch("convert");
+}
+
+#define INST(T)                                                                                                     \
+  template size_t gram_workspace<T>(long long, int, int);                                                           \
+  template int gram<T>(const T*, int, const T*, int, long long, int, int, T*, int, T, T, void*, size_t, cudaStream_t); \
+  template int gemm_nn<T>(const T*, int, const T*, int, long long, int, int, T*, int, T, T, cudaStream_t);           \
+  template int cholesky<T>(T*, int, int, int*, cudaStream_t);                                                       \
+  template int tri_inv_lower<T>(const T*, int, int, T*, int, cudaStream_t);                                         \
+  template size_t jacobi_workspace<T>(int);                                                                         \
+  template int jacobi_eigh<T>(T*, int, T*, T*, int, double, int*, void*, size_t, cudaStream_t);                     \
+  template size_t col_norms_workspace<T>(long long, int);                                                           \
+  template int col_norms<T>(const T*, int, long long, int, T*, void*, size_t, cudaStream_t);                        \
+  template int scale_cols<T>(T*, int, long long, int, const T*, bool, cudaStream_t);
+INST(float)
+INST(double)
+#undef INST
+
+}  // namespace rvgp

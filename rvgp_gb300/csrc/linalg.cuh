@@ -1,0 +1,62 @@
+// Dense linear algebra used by the eigensolver and the GP (internal API).
+//
+// Shapes are row-major with explicit leading dimensions.  The tall-skinny
+// products (N up to millions, p, q up to ~1024) are the GEMM-shaped part of
+// block subspace iteration and of the low-rank GP algebra; the p x p kernels
+// (Cholesky, triangular inverse, symmetric Jacobi eigensolver) are the small
+// dense steps.  Every reduction is in a fixed order (deterministic).
+#pragma once
+#include "common.cuh"
+
+namespace rvgp {
+
+// C (p x q, ldc) = alpha * Aᵀ B + beta * C,  A: N x p (lda), B: N x q (ldb).
+template <typename T>
+size_t gram_workspace(long long N, int p, int q);
+template <typename T>
+int gram(const T* A, int lda, const T* B, int ldb, long long N, int p, int q, T* C, int ldc, T alpha, T beta,
+         void* ws, size_t ws_bytes, cudaStream_t st);
+
+// Same product for FP32 inputs with FP32 partial sums reduced in FP64 into an FP64 C.
+int gram_f32_out64(const float* A, int lda, const float* B, int ldb, long long N, int p, int q, double* C, int ldc,
+                   double alpha, double beta, void* ws, size_t ws_bytes, cudaStream_t st);
+
+// C (N x q, ldc) = alpha * A (N x p, lda) * B (p x q, ldb) + beta * C.  C must not alias A or B.
+template <typename T>
+int gemm_nn(const T* A, int lda, const T* B, int ldb, long long N, int p, int q, T* C, int ldc, T alpha, T beta,
+            cudaStream_t st);
+
+// In-place lower Cholesky of the p x p matrix A (lda).  *info (device) = 0 or
+// j+1 when the leading (j+1) x (j+1) minor is not positive definite.  The
+// strict upper triangle is not referenced.
+template <typename T>
+int cholesky(T* A, int lda, int p, int* info, cudaStream_t st);
+
+// Linv (p x p, ld) = inverse of the lower-triangular L (lower part used); the
+// strict upper part of Linv is set to zero.
+template <typename T>
+int tri_inv_lower(const T* L, int ldl, int p, T* Linv, int ldi, cudaStream_t st);
+
+// Symmetric eigendecomposition by parallel cyclic Jacobi: H (p x p, symmetric,
+// destroyed) -> eigenvalues w (ascending) and eigenvectors V (p x p, columns).
+// max_sweeps bounds the work; *sweeps_used (host) reports it.  tol: stop when
+// off(H) <= tol * ||H||_F.
+template <typename T>
+size_t jacobi_workspace(int p);
+template <typename T>
+int jacobi_eigh(T* H, int p, T* w, T* V, int max_sweeps, double tol, int* sweeps_used, void* ws, size_t ws_bytes,
+                cudaStream_t st);
+
+// Column utilities on X (N x b, ld).
+template <typename T>
+int col_norms(const T* X, int ld, long long N, int b, T* out, void* ws, size_t ws_bytes, cudaStream_t st);
+template <typename T>
+size_t col_norms_workspace(long long N, int b);
+template <typename T>
+int scale_cols(T* X, int ld, long long N, int b, const T* s, bool inverse, cudaStream_t st);
+
+// Dtype conversion of an N x b block (ld in/out).
+int convert_f32_to_f64(const float* in, int ldi, double* out, int ldo, long long N, int b, cudaStream_t st);
+int convert_f64_to_f32(const double* in, int ldi, float* out, int ldo, long long N, int b, cudaStream_t st);
+
+}  // namespace rvgp

@@ -1,0 +1,223 @@
+"""The RVGP data object (RVGP/dataclass.py:21-120) on the GPU.
+
+``data(vertices, vectors=None, dim_man=2, n_neighbors=10,
+frac_geodesic_neighbours=1.5, explained_variance=0.8, n_eigenpairs=None)``
+runs kNN graph -> geodesic-neighbourhood gauges -> manifold dimension ->
+connections -> Laplacians -> eigenpairs of L and Lc -> gauge lift, all as
+CUDA kernels.  The reference's attributes (``vertices, n, dim_man, G, gauges,
+R, L, Lc, evals_L, evecs_L, evals_Lc, evecs_Lc, vectors``) are available as
+host objects (numpy / scipy.sparse, ``G`` as networkx when installed); they are
+copied off the device on first access.  The device tensors live in
+``self._dev``.
+
+Differences from the reference, each deliberate:
+* the gauges keep min(D, K+1) singular values (the reference asks for D and
+  therefore rejects K < D, RVGP/lib/ptu_dijkstra.pyx:73-77, e.g. every
+  64-dimensional cloud with n_neighbors=15);
+* ``n_eigenpairs=None`` raises the error ARPACK would raise (k must be < N - 1)
+  instead of attempting a full decomposition;
+* ``estimate_dim=False`` uses ``dim_man`` instead of the estimate (the reference
+  always estimates and ignores ``dim_man``, RVGP/dataclass.py:37).
+"""
+from __future__ import annotations
+
+import math
+from types import SimpleNamespace
+
+import numpy as np
+import torch
+
+from rvgp_gb300 import _core
+
+
+def _log(verbose, *a):
+    if verbose:
+        print(*a)
+
+
+class data:
+    def __init__(self, vertices, vectors=None, dim_man=2, n_neighbors=10, frac_geodesic_neighbours=1.5,
+                 explained_variance=0.8, n_eigenpairs=None, *, precision="mixed", estimate_dim=True,
+                 strict_rank=True, eig_tol=1e-11, seed=0, verbose=True):
+        _core.require_cuda()
+        device = torch.device("cuda", torch.cuda.current_device())
+        if isinstance(vertices, torch.Tensor):
+            X = vertices.to(device=device, dtype=torch.float64).contiguous()
+            self._vertices_host = None
+        else:
+            self._vertices_host = np.asarray(vertices)
+            X = torch.as_tensor(np.ascontiguousarray(vertices, dtype=np.float64), device=device)
+        n, D = X.shape
+        self.precision = precision
+        dev = SimpleNamespace(X=X)
+
+        _log(verbose, "Fit graph")
+        knn = _core.knn(X, n_neighbors)
+        indptr, indices, maxdeg = _core.graph_build(knn)
+        dev.indptr, dev.indices, dev.maxdeg = indptr, indices, maxdeg
+
+        _log(verbose, "Fit tangent spaces")
+        K = int(n_neighbors * frac_geodesic_neighbours)
+        if K >= n:
+            raise ValueError("Geodesic neighborhood size must be less than the total number of samples")
+        c = min(D, K + 1)
+        d_out = min(c, 8)
+        T, Sigma, _ = _core.gauges(X, indptr, indices, K, maxdeg, d_out)
+        if estimate_dim:
+            if explained_variance == 1.0:
+                dim = c
+            else:
+                dim, var_exp = _core.manifold_dimension(Sigma, explained_variance)
+                _log(verbose, "Fraction of variance explained: ", var_exp.cpu().numpy())
+                if dim < 0:
+                    raise IndexError("no number of dimensions explains the requested fraction of variance")
+        else:
+            dim = int(dim_man)
+        if dim > d_out:
+            T, Sigma, _ = _core.gauges(X, indptr, indices, K, maxdeg, dim)
+        check = c if (strict_rank and D <= K) else dim
+        if bool((Sigma[:, :check] < 1e-10).any()):
+            raise RuntimeError("Local tangent space approximation failed, at least one geodesic neighborhood does "
+                               "not span d-dimensional space")
+        dev.T, dev.Sigma = T, Sigma
+        _log(verbose, "Predicted manifold dimension is {}".format(dim))
+
+        R, lc64, lc32 = _core.connections(T, dim, indptr, indices, want32=(precision == "mixed"))
+        dev.R, dev.Lc_vals, dev.Lc_vals32 = R, lc64, lc32
+        _log(verbose, "Fit connections")
+
+        _log(verbose, "Compute Laplacians")
+        dev.L_vals = _core.laplacian_values(indptr, indices)
+        dev.bound = 2.0 * maxdeg * (1.0 + 1e-12)  # spectral bound of L and Lc (|D| + |A|)
+
+        _log(verbose, "Compute eigendecompositions")
+        m = n if n_eigenpairs is None else min(int(n_eigenpairs), n)
+        mode = "mixed" if precision == "mixed" else "fp64"
+        dev.evals_L, dev.evecs_L, dev.eig_info_L = _core.eigsh(indptr, indices, dev.L_vals, None, m=m, mode=mode,
+                                                               tol=eig_tol, seed=seed, scale=math.sqrt(n))
+        dev.evals_Lc, U, dev.eig_info_Lc = _core.eigsh(indptr, indices, lc64, lc32, m=m, mode=mode, tol=eig_tol,
+                                                       seed=seed + 1, scale=math.sqrt(n * dim))
+        dev.evecs_Lc_local = U
+        dev.evecs_Lc = _core.lift(T, dim, U)
+        dev.vectors = None
+        self._dev = dev
+        self.n = n
+        self.dim_man = dim
+        self.n_eigenpairs = m
+        self._host = {}
+        self.vectors = vectors
+
+    # ------------------------------------------------------------------ host views
+    def _cached(self, key, fn):
+        if key not in self._host:
+            self._host[key] = fn()
+        return self._host[key]
+
+    @property
+    def vertices(self):
+        if self._vertices_host is None:
+            self._vertices_host = self._dev.X.cpu().numpy()
+        return self._vertices_host
+
+    @property
+    def vectors(self):
+        if self._dev.vectors is None:
+            return None
+        return self._cached("vectors", lambda: self._dev.vectors.cpu().numpy())
+
+    @vectors.setter
+    def vectors(self, v):
+        self._host.pop("vectors", None)
+        if v is None:
+            self._dev.vectors = None
+        elif isinstance(v, torch.Tensor):
+            self._dev.vectors = v.to(device=self._dev.X.device, dtype=torch.float64).contiguous()
+        else:
+            self._host["vectors"] = np.asarray(v)
+            self._dev.vectors = torch.as_tensor(np.ascontiguousarray(v, dtype=np.float64), device=self._dev.X.device)
+
+    @property
+    def gauges(self):
+        return self._cached("gauges", lambda: np.ascontiguousarray(
+            self._dev.T[:, :, :self.dim_man].cpu().numpy()))
+
+    @property
+    def L(self):
+        import scipy.sparse as sp
+        d = self._dev
+        return self._cached("L", lambda: sp.csr_matrix(
+            (d.L_vals.cpu().numpy(), d.indices.cpu().numpy(), d.indptr.cpu().numpy()), shape=(self.n, self.n)))
+
+    @property
+    def Lc(self):
+        import scipy.sparse as sp
+        d, k = self._dev, self.dim_man
+        return self._cached("Lc", lambda: sp.bsr_matrix(
+            (d.Lc_vals.cpu().numpy(), d.indices.cpu().numpy(), d.indptr.cpu().numpy()),
+            shape=(self.n * k, self.n * k)))
+
+    @property
+    def R(self):
+        """Transports as the reference's COO nd x nd (RVGP/lib/ptu_dijkstra.pyx:194-197)."""
+        import scipy.sparse as sp
+
+        def build():
+            d, k = self._dev, self.dim_man
+            ip, ix = d.indptr.cpu().numpy(), d.indices.cpu().numpy()
+            rows = np.repeat(np.arange(self.n), np.diff(ip))
+            p, q = np.meshgrid(np.arange(k), np.arange(k), indexing="ij")
+            r = (rows[:, None] * k + p.ravel()[None, :]).ravel()
+            c = (ix[:, None] * k + q.ravel()[None, :]).ravel()
+            return sp.coo_matrix((d.R.cpu().numpy().ravel(), (r, c)))
+        return self._cached("R", build)
+
+    @property
+    def evals_L(self):
+        return self._cached("evals_L", lambda: self._dev.evals_L.cpu().numpy())
+
+    @property
+    def evecs_L(self):
+        return self._cached("evecs_L", lambda: self._dev.evecs_L.cpu().numpy())
+
+    @property
+    def evals_Lc(self):
+        return self._cached("evals_Lc", lambda: self._dev.evals_Lc.cpu().numpy())
+
+    @property
+    def evecs_Lc(self):
+        return self._cached("evecs_Lc", lambda: self._dev.evecs_Lc.cpu().numpy())
+
+    @property
+    def G(self):
+        """The kNN graph as a networkx Graph with 'pos' node attributes (needs networkx)."""
+        def build():
+            import networkx as nx
+            A = self.L.copy()
+            A.data[:] = 1.0
+            G = nx.from_scipy_sparse_array(A)
+            nx.set_node_attributes(G, {i: self.vertices[i] for i in G.nodes}, "pos")
+            return G
+        return self._cached("G", build)
+
+    # ------------------------------------------------------------------ fields
+    def random_vector_field(self, seed=0):
+        """Generate random vector field over manifold (RVGP/dataclass.py:91-103).
+
+        The random numbers come from numpy's legacy global generator exactly as
+        in the reference; projection and normalisation run on the GPU."""
+        np.random.seed(seed)
+        v = np.random.uniform(low=-0.5, high=0.5, size=(self.n, self._dev.X.shape[1]))
+        vd = torch.as_tensor(v, device=self._dev.X.device)
+        vd = _core.frame_map(self._dev.T, self.dim_man, vd, "project")
+        self.vectors = _core.normalise_rows(vd)
+
+    def smooth_vector_field(self, t=100):
+        """Vector diffusion of the field (RVGP/dataclass.py:105-120) with the exact
+        action of exp(-t Lc) (and exp(-t L) for the magnitude renormalisation)."""
+        if self._dev.vectors is None:
+            print("No vectors found. Nothing to smooth.")
+            return
+        d = self._dev
+        loc = _core.frame_map(d.T, self.dim_man, d.vectors, "to_local")
+        loc = _core.vector_diffusion(d.indptr, d.indices, d.L_vals, d.Lc_vals, loc, t, d.bound, d.bound)
+        self.vectors = _core.frame_map(d.T, self.dim_man, loc, "from_local")

@@ -1,0 +1,248 @@
+"""GP fit / predict with the surface of RVGP/main.py.
+
+``train_gp`` (exported as ``fit``) keeps the reference's signature and flow
+(RVGP/main.py:11-84): default ``ManifoldKernel(nu=3/2, kappa=5, sigma_f=1)``,
+rows = (training point, ambient coordinate), sklearn's seeded 80/20
+``train_test_split`` of ``train_ind``, L-BFGS-B on the negative log marginal
+likelihood for at most ``epochs`` iterations, then the "Relative l2 error"
+print on the held-out 20 %.  Every likelihood evaluation, gradient and
+prediction is a CUDA computation (rvgp_gp_lml / rvgp_gp_predict); the
+optimiser loop itself runs on the host, as GPflow's Scipy optimiser does.
+
+Reference behaviours kept by default (``reference_quirks=True``): the
+likelihood variance starts at 1.0 because ``noise_variance`` never reaches
+GPflow (RVGP/main.py:99-100); the positive-parameter lower bound of the default
+kernel is the one in force when it was created (RVGP/main.py:30,52).
+``reference_quirks=False`` starts the noise at ``noise_variance``.
+
+Extensions: ``optimizer="adam"`` (``epochs`` Adam steps at ``lr``, gradients
+from the hand-written adjoint behind ``torch.autograd``), ``precision``
+("mixed" or "fp64", default the data object's), and ``transform`` accepting
+numpy integer arrays and boolean masks.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+import scipy.optimize
+import torch
+
+from rvgp_gb300 import _core
+from rvgp_gb300.kernels import ManifoldKernel, Parameter, set_default_positive_minimum
+
+
+def train_test_split_indices(n_samples, test_size=0.2, seed=0):
+    """Index split of sklearn ``train_test_split(..., test_size, random_state=seed)``
+    (ShuffleSplit: RandomState(seed).permutation, first ceil(test_size*n) are test)."""
+    n_test = int(math.ceil(test_size * n_samples))
+    n_train = n_samples - n_test
+    perm = np.random.RandomState(seed).permutation(n_samples)
+    return perm[n_test:n_test + n_train], perm[:n_test]
+
+
+class _LML(torch.autograd.Function):
+    """Log marginal likelihood with its hand-written adjoint (see rvgp_gp_lml)."""
+
+    @staticmethod
+    def forward(ctx, theta, model):
+        out, _ = _core.gp_lml(model.C, model.b, model.yy, model.N, model.kernel.eigenvalues,
+                              model.kernel.num_verticies, theta.detach().contiguous(), model.kernel.typ, model.work)
+        ctx.save_for_backward(out[1:5].clone())
+        return out[0].clone()
+
+    @staticmethod
+    def backward(ctx, g):
+        (grad,) = ctx.saved_tensors
+        return g * grad, None
+
+
+def log_marginal_likelihood(theta, model):
+    """Differentiable LML: theta = CUDA f64 tensor [nu, kappa, sigma_f, noise]."""
+    return _LML.apply(theta, model)
+
+
+class manifold_GPR:
+    """GPflow-GPR-like model on the manifold kernel (RVGP/main.py:99-116)."""
+
+    def __init__(self, data, kernel, train_points, noise_variance=1.0, precision="mixed"):
+        self.data_obj = data
+        self.kernel = kernel
+        self.precision = precision
+        self.likelihood = type("Gaussian", (), {})()
+        self.likelihood.variance = Parameter(noise_variance, lower=1e-6, name="noise_variance")
+        dev = data._dev
+        if dev.vectors is None:
+            raise ValueError("the data object has no vectors to fit")
+        self.D = dev.X.shape[1]
+        idx = torch.as_tensor(np.asarray(train_points, dtype=np.int32), device=dev.X.device)
+        Phi, Phi32, y = _core.gather_rows(kernel.eigenvectors, self.D, idx, vec=dev.vectors,
+                                          want32=(precision == "mixed"))
+        self.C, self.b, self.yy = _core.gp_prepare(Phi, y, Phi32, precision)
+        self.N = Phi.shape[0]
+        self.m = kernel.eigenvalues.numel()
+        self.work = _core.LMLWorkspace(self.m, dev.X.device)
+        self.n_evals = 0
+
+    # ------------------------------------------------------------------ parameters
+    @property
+    def trainable_parameters(self):
+        ps = self.kernel.parameters + [self.likelihood.variance]
+        return [p for p in ps if p.trainable]
+
+    def theta(self):
+        return self.kernel.theta(float(self.likelihood.variance))
+
+    def _evaluate(self):
+        out, _ = _core.gp_lml(self.C, self.b, self.yy, self.N, self.kernel.eigenvalues, self.kernel.num_verticies,
+                              self.theta(), self.kernel.typ, self.work)
+        self.n_evals += 1
+        return out.cpu().numpy()
+
+    def log_marginal_likelihood(self):
+        return float(self._evaluate()[0])
+
+    def training_loss(self):
+        return -self.log_marginal_likelihood()
+
+    def _loss_and_grad_u(self, params):
+        out = self._evaluate()
+        grads = {"nu": out[1], "kappa": out[2], "sigma_f": out[3], "noise_variance": out[4]}
+        g = np.array([-grads[p.name] * p.dvalue_du() for p in params])
+        return -out[0], g
+
+    # ------------------------------------------------------------------ optimisation
+    def optimize(self, epochs=1000, method="l-bfgs-b", lr=0.05, disp=True):
+        params = self.trainable_parameters
+        if not params or epochs <= 0:
+            return None
+        if method.lower() in ("l-bfgs-b", "lbfgs", "scipy"):
+            def fun(x):
+                for p, u in zip(params, x):
+                    p.unconstrained = float(u)
+                f, g = self._loss_and_grad_u(params)
+                if not np.isfinite(f):
+                    return np.inf, np.zeros_like(g)
+                return f, g
+            x0 = np.array([p.unconstrained for p in params])
+            res = scipy.optimize.minimize(fun, x0, jac=True, method="L-BFGS-B",
+                                          options={"disp": disp, "maxiter": epochs})
+            for p, u in zip(params, res.x):
+                p.unconstrained = float(u)
+            return res
+        if method.lower() == "adam":
+            return self._adam(params, epochs, lr)
+        raise ValueError(f"unknown optimiser {method!r}")
+
+    def _adam(self, params, steps, lr):
+        u = torch.tensor([p.unconstrained for p in params], dtype=torch.float64, requires_grad=True)
+        opt = torch.optim.Adam([u], lr=lr)
+        names = [p.name for p in params]
+        fixed = {p.name: float(p) for p in self.kernel.parameters + [self.likelihood.variance] if not p.trainable}
+        lowers = torch.tensor([p.lower for p in params], dtype=torch.float64)
+        dev = self.kernel.device
+        for _ in range(steps):
+            opt.zero_grad()
+            vals = torch.nn.functional.softplus(u) + lowers
+            v = dict(zip(names, vals))
+            theta = torch.stack([
+                v.get("nu", torch.tensor(fixed.get("nu", 0.0), dtype=torch.float64)),
+                v.get("kappa", torch.tensor(fixed.get("kappa", 0.0), dtype=torch.float64)),
+                v.get("sigma_f", torch.tensor(fixed.get("sigma_f", 0.0), dtype=torch.float64)),
+                v.get("noise_variance", torch.tensor(fixed.get("noise_variance", 0.0), dtype=torch.float64)),
+            ]).to(dev)
+            loss = -log_marginal_likelihood(theta, self)
+            loss.backward()
+            opt.step()
+            self.n_evals += 1
+        with torch.no_grad():
+            for p, x in zip(params, u.tolist()):
+                p.unconstrained = float(x)
+        return u.detach()
+
+    # ------------------------------------------------------------------ prediction
+    def _predict_rows(self, Phi_star):
+        self._evaluate()  # posterior state at the current parameters
+        mode = self.precision
+        mean, var = _core.gp_predict(Phi_star, self.work.state, self.m, None, mode)
+        return mean, var
+
+    def predict_f(self, Xnew):
+        """Posterior mean and marginal variance, each (rows, 1), at rows of the spectral input."""
+        dev = self.kernel.device
+        Xd = Xnew.to(dev, torch.float64) if isinstance(Xnew, torch.Tensor) else torch.as_tensor(
+            np.ascontiguousarray(Xnew, dtype=np.float64), device=dev)
+        mean, var = self._predict_rows(Xd.reshape(-1, self.m).contiguous())
+        return mean.reshape(-1, 1).cpu(), var.reshape(-1, 1).cpu()
+
+    def predict_points(self, points):
+        """Posterior mean and variance at manifold points (indices), each (len, D), on the device."""
+        idx = torch.as_tensor(np.asarray(points, dtype=np.int32), device=self.kernel.device)
+        Phi, _, _ = _core.gather_rows(self.kernel.eigenvectors, self.D, idx)
+        mean, var = self._predict_rows(Phi)
+        return mean.reshape(-1, self.D), var.reshape(-1, self.D)
+
+    def transform(self, data, test_ind):
+        """Posterior mean and variance (the reference names it f_pred_std, but it
+        is the variance) at test points, as in RVGP/main.py:102-116.  Integer
+        indices select manifold points; floats are spectral inputs."""
+        first = test_ind[0] if len(test_ind) else 0
+        arr = np.asarray(test_ind)
+        if arr.dtype == bool:
+            arr = np.nonzero(arr)[0]
+        if np.issubdtype(np.asarray(first).dtype, np.integer) or arr.dtype == bool or np.issubdtype(arr.dtype,
+                                                                                                   np.integer):
+            mean, var = self.predict_points(arr)
+            return mean.cpu().numpy(), var.cpu().numpy()
+        mean, var = self.predict_f(np.asarray(test_ind, dtype=np.float64))
+        n = len(test_ind)
+        return mean.numpy().reshape(n, -1), var.numpy().reshape(n, -1)
+
+
+class manifold_SGPR:
+    """Sparse variational GP with inducing points (RVGP/main.py:119-137) is not part of this build."""
+
+    def __init__(self, *a, **k):
+        raise NotImplementedError("manifold_SGPR (n_inducing_points) is not implemented in rvgp_gb300 yet")
+
+
+def optimize_model_with_scipy(model, epochs):
+    """RVGP/main.py:87-95: L-BFGS-B with maxiter=epochs."""
+    model.optimize(epochs=epochs, method="l-bfgs-b")
+    return model
+
+
+def train_gp(data, train_ind=None, n_inducing_points=None, test_size=0.2, kernel=None, noise_variance=0.001,
+             kernel_lengthscale=None, kernel_variance=None, epochs=1000, positivity_constraint=1e-2, seed=0, *,
+             optimizer="l-bfgs-b", lr=0.05, precision=None, reference_quirks=True, verbose=True):
+    """Fit a vector-field GP on the manifold (RVGP/main.py:11-84)."""
+    if train_ind is None:
+        train_ind = np.arange(data.n)
+    train_ind = np.asarray(train_ind)
+    if kernel is None:
+        kernel = ManifoldKernel(data, nu=3 / 2, kappa=5, typ="matern", sigma_f=1.0)
+    elif isinstance(kernel, str):
+        raise NotImplementedError(f"kernel={kernel!r}: only the manifold kernel is implemented in rvgp_gb300")
+    tr, te = train_test_split_indices(len(train_ind), test_size, seed)
+    pts_train, pts_test = train_ind[tr], train_ind[te]
+    set_default_positive_minimum(positivity_constraint)
+    if n_inducing_points is not None:
+        return manifold_SGPR()
+    precision = precision or getattr(data, "precision", "mixed")
+    GP = manifold_GPR(data, kernel, pts_train, noise_variance=1.0 if reference_quirks else noise_variance,
+                      precision=precision)
+    if kernel_variance is not None:
+        kernel.sigma_f.assign(kernel_variance)
+        kernel.sigma_f.trainable = False
+    if kernel_lengthscale is not None:
+        kernel.kappa.assign(kernel_lengthscale)
+        kernel.kappa.trainable = False
+    GP.optimize(epochs=epochs, method=optimizer, lr=lr, disp=verbose)
+    if len(pts_test):
+        mean, _ = GP.predict_points(pts_test)
+        out_test = data._dev.vectors[torch.as_tensor(pts_test, device=mean.device, dtype=torch.long)]
+        l2_error = float(torch.linalg.vector_norm(out_test - mean, dim=1).mean())
+        if verbose:
+            print("Relative l2 error is {}".format(l2_error))
+        GP.l2_error = l2_error
+    return GP

@@ -1,0 +1,135 @@
+"""GPU parity: graph, gauges, connections and the sparse products against the
+oracle and the reference's golden fixtures (all through the C ABI)."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+import torch
+
+from conftest import load_golden, projector_distance
+from oracle import rvgp_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def core():
+    from rvgp_gb300 import _core
+    _core.require_cuda()
+    return _core
+
+
+def cu(a, dtype=torch.float64):
+    return torch.as_tensor(np.ascontiguousarray(a)).to("cuda", dtype)
+
+
+@pytest.mark.parametrize("name", ["sphere", "torus", "ellipsoid", "swissroll64"])
+def test_knn_and_graph_match_reference(core, name):
+    g = load_golden(name)
+    X, k = g["X"], int(g["k"])
+    idx = core.knn(cu(X), k).cpu().numpy()
+    assert np.array_equal(idx, O.knn(X, k))
+    indptr, indices, maxdeg = core.graph_build(torch.as_tensor(idx).cuda())
+    assert np.array_equal(indptr.cpu().numpy(), g["indptr"])
+    assert np.array_equal(indices.cpu().numpy(), g["indices"])
+    assert maxdeg == int(np.diff(g["indptr"]).max() - 1)
+    vals = core.laplacian_values(indptr, indices).cpu().numpy()
+    assert np.array_equal(vals, g["L_data"])
+
+
+@pytest.mark.parametrize("kind,n,k", [("sphere", 5000, 10), ("torus", 6000, 20), ("swissroll64", 3000, 15),
+                                      ("bumpy_sphere", 4000, 20)])
+def test_knn_random_clouds(core, kind, n, k):
+    from rvgp_gb300.workloads import make_points
+    X = make_points(kind, n, seed=3)
+    idx = core.knn(cu(X), k).cpu().numpy()
+    assert np.array_equal(idx, O.knn(X, k))
+
+
+def test_knn_exact_ties_and_fallback(core):
+    """A lattice: FP32 cannot separate the many exactly tied distances, so rows
+    go to the exact FP64 scan; ties resolve to the lower index."""
+    g = np.stack(np.meshgrid(np.arange(9), np.arange(9), np.arange(9), indexing="ij"), -1)
+    X = g.reshape(-1, 3).astype(float) * 0.37 + 5.0
+    for k in (6, 18, 7):
+        idx = core.knn(cu(X), k).cpu().numpy()
+        assert np.array_equal(idx, O.knn(X, k))
+    # k = 7 cuts the 12-point shell at distance sqrt(2) spacing: FP32 cannot certify it
+    assert core.lib().rvgp_knn_fallback_rows(len(X), 3, 7, core.ptr(core.knn.last_ws), core.stream()) > 0
+
+
+def test_knn_duplicates_and_small(core):
+    rng = np.random.default_rng(5)
+    X = rng.standard_normal((40, 3))
+    X[10] = X[3]
+    X[11] = X[3]
+    for k in (1, 5, 39):
+        idx = core.knn(cu(X), k).cpu().numpy()
+        assert np.array_equal(idx, O.knn(X, k))
+    with pytest.raises(ValueError):
+        core.knn(cu(X), 40)
+
+
+@pytest.mark.parametrize("name", ["sphere", "torus", "ellipsoid", "swissroll64"])
+def test_gauges_match_reference(core, name):
+    g = load_golden(name)
+    X, K, d = g["X"], int(g["K"]), int(g["dim_man"])
+    n, D = X.shape
+    ip, ix = cu(g["indptr"], torch.int32), cu(g["indices"], torch.int32)
+    maxdeg = int(np.diff(g["indptr"]).max() - 1)
+    c = min(D, K + 1)
+    T, S, nbh = core.gauges(cu(X), ip, ix, K, maxdeg, d_out=min(c, 4), return_nbh=True)
+    nbh = nbh.cpu().numpy()
+    # exact neighbourhood sets and scan order of the reference's heap
+    assert np.array_equal(nbh, O.geodesic_neighbourhoods(g["indptr"], g["indices"], K))
+    Sg = g["Sigma"]
+    np.testing.assert_allclose(S.cpu().numpy()[:, :Sg.shape[1]], Sg, rtol=1e-11, atol=1e-13)
+    T = T.cpu().numpy()
+    assert projector_distance(T[:, :, :d], g["gauges"]) < 1e-11
+    # orthonormal columns
+    G = np.einsum("nki,nkj->nij", T, T)
+    assert np.abs(G - np.eye(T.shape[2])).max() < 1e-12
+
+
+def test_gauges_component_too_small(core):
+    # two far-apart clusters of 5 points each: K=6 cannot be met inside a component
+    rng = np.random.default_rng(0)
+    X = np.concatenate([rng.standard_normal((5, 3)), 100 + rng.standard_normal((5, 3))])
+    idx = core.knn(cu(X), 3)
+    ip, ix, maxdeg = core.graph_build(idx)
+    with pytest.raises(RuntimeError):
+        core.gauges(cu(X), ip, ix, 6, maxdeg, 2)
+
+
+@pytest.mark.parametrize("name", ["sphere", "torus", "swissroll64"])
+def test_connections_and_lc(core, name):
+    g = load_golden(name)
+    d = int(g["dim_man"])
+    ip, ix = cu(g["indptr"], torch.int32), cu(g["indices"], torch.int32)
+    # with the reference's own gauges the transports must equal the reference's R
+    R, v64, v32 = core.connections(cu(g["gauges"]), d, ip, ix)
+    np.testing.assert_allclose(R.cpu().numpy(), g["R"], atol=1e-13)
+    n = len(g["X"])
+    L = O.laplacian(g["indptr"], g["indices"], n)
+    Lc = O.connection_laplacian(L, g["R"], g["indptr"], g["indices"], d)
+    Lc_gpu = sp.bsr_matrix((v64.cpu().numpy(), g["indices"], g["indptr"]), shape=Lc.shape).tocsr()
+    assert abs(Lc_gpu - Lc).max() < 1e-12
+    np.testing.assert_allclose(v32.cpu().numpy(), v64.cpu().numpy().astype(np.float32), rtol=0, atol=0)
+
+
+@pytest.mark.parametrize("d,dtype,b", [(1, torch.float64, 6), (2, torch.float64, 40), (2, torch.float32, 64),
+                                       (3, torch.float32, 8), (1, torch.float32, 12)])
+def test_bspmm(core, d, dtype, b):
+    rng = np.random.default_rng(d * 100 + b)
+    n = 700
+    A = sp.random(n, n, density=0.02, random_state=1, format="csr") + sp.eye(n)
+    A.sort_indices()
+    blocks = rng.standard_normal((A.nnz, d, d))
+    M = sp.bsr_matrix((blocks, A.indices, A.indptr), shape=(n * d, n * d))
+    X = rng.standard_normal((n * d, b))
+    Z = rng.standard_normal((n * d, b))
+    ref = 0.7 * (M @ X) - 0.3 * X + 1.9 * Z
+    vals = cu(blocks if d > 1 else blocks[:, 0, 0], dtype)
+    Y = core.bspmm(cu(A.indptr, torch.int32), cu(A.indices, torch.int32), vals, cu(X, dtype), Z=cu(Z, dtype),
+                   alpha=0.7, beta=-0.3, gamma=1.9)
+    tol = 1e-12 if dtype == torch.float64 else 2e-5
+    np.testing.assert_allclose(Y.cpu().double().numpy(), ref, atol=tol * np.abs(ref).max())
