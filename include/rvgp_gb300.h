@@ -94,8 +94,10 @@ int rvgp_bspmm_f64(int n, int DB, const int* indptr, const int* indices, const d
  * Cholesky and Rayleigh-Ritz, then FP64 refinement.  p: block size
  * (m < p <= n*DB, multiple of 4).  tol / tol32: residual tolerances relative to
  * the Gershgorin bound.  evals ascending (m); evecs N x m (ld_evecs) times
- * `scale` (the reference scales by sqrt(N)).  stats: 8 host ints (iterations,
- * SpMMs, Jacobi sweeps, converged, refinement iterations, Cholesky rescues).
+ * `scale` (the reference scales by sqrt(N)).  stats: 16 host ints (iterations,
+ * SpMMs, Jacobi sweeps, converged, refinement iterations, Cholesky rescues, -,
+ * -, then microseconds spent in filter / orthonormalisation / Rayleigh-Ritz
+ * tall products / Jacobi).  When tol >= tol32 (mode 1) no FP64 iteration runs.
  * Returns 0, or the number of unconverged pairs.  Synchronises the stream. */
 size_t rvgp_eigsh_workspace(int n, int DB, int m, int p, int mode);
 int rvgp_eigsh(const int* indptr, const int* indices, const double* vals64, const float* vals32, int n, int DB, int m,
@@ -130,6 +132,16 @@ size_t rvgp_gp_state_size(int m);
 int rvgp_gp_lml(const double* C, const double* b, const double* yy, long long N, int m, const double* evals,
                 double n_rows, int typ, const double* theta, double* out, double* state, void* workspace,
                 size_t ws_bytes, void* stream);
+/* Hyperparameter learning on the device: `steps` Adam steps on the
+ * softplus-unconstrained parameters minimising -LML (the optimisation of
+ * RVGP/main.py:77,87-95 with Adam in place of L-BFGS-B), no host
+ * synchronisation.  theta0 (device, 4); lower, mask (host, 4 each); theta_out
+ * (device, 4); hist (device, steps, optional): LML before each step; out/state
+ * as rvgp_gp_lml at theta_out. */
+int rvgp_gp_fit_adam(const double* C, const double* b, const double* yy, long long N, int m, const double* evals,
+                     double n_rows, int typ, const double* theta0, const double* lower, const int* mask, int steps,
+                     double lr, double beta1, double beta2, double eps, double* theta_out, double* hist, double* out,
+                     double* state, void* workspace, size_t ws_bytes, void* stream);
 /* predict_f(full_cov=False) mean and variance at Nte rows (RVGP/main.py:102-116). */
 size_t rvgp_gp_predict_workspace(long long Nte, int m, int mode);
 int rvgp_gp_predict(const double* Phi_star, const float* Phi_star32, long long Nte, int m, int mode,
@@ -149,16 +161,18 @@ int rvgp_manifold_dimension(const double* sigma, int n, int c, double frac, doub
 int rvgp_frame_map(const double* T, int n, int D, int ld, int d, const double* v, int mode, double* out, void* stream);
 int rvgp_normalise_rows(double* v, int n, int D, void* stream);
 /* exp(-tA) X without forming the exponential (scipy.linalg.expm(-t A) @ x at
- * RVGP/smoothing.py:13-15); A block-CSR with spectrum in [0, bound], b <= 4. */
+ * RVGP/smoothing.py:13-15); A block-CSR with spectrum in [shift, bound]
+ * (shift = a lower bound, e.g. λ_min, for accuracy at large t), b <= 4. */
 size_t rvgp_expm_action_workspace(int n, int DB, int b);
 int rvgp_expm_action(const int* indptr, const int* indices, const double* vals, int n, int DB, const double* X, int b,
-                     double t, double bound, double* Y, void* workspace, size_t ws_bytes, void* stream);
+                     double t, double bound, double shift, double* Y, void* workspace, size_t ws_bytes, void* stream);
 /* vector_diffusion(x, t, Lc, L, method="matrix_exp", normalise=True)
- * (RVGP/smoothing.py:37-63) on the local-frame field x_loc (n, d). */
+ * (RVGP/smoothing.py:37-63) on the local-frame field x_loc (n, d); shift_Lc
+ * a lower bound of Lc's spectrum. */
 size_t rvgp_vector_diffusion_workspace(int n, int d);
 int rvgp_vector_diffusion(const int* indptr, const int* indices, const double* L_vals, const double* Lc_vals, int n,
-                          int d, const double* x_loc, double t, double bound_L, double bound_Lc, double* out,
-                          void* workspace, size_t ws_bytes, void* stream);
+                          int d, const double* x_loc, double t, double bound_L, double bound_Lc, double shift_Lc,
+                          double* out, void* workspace, size_t ws_bytes, void* stream);
 /* Y = Φ diag(exp(-tλ)) Φᵀ X with orthonormal Φ (the spectral branch of
  * RVGP/smoothing.py:17-32). */
 size_t rvgp_spectral_diffusion_workspace(long long N, int m, int b);

@@ -43,6 +43,8 @@ SIGNATURES = {
     "rvgp_gp_lml_workspace": (c_size_t, [c_int]),
     "rvgp_gp_state_size": (c_size_t, [c_int]),
     "rvgp_gp_lml": (c_int, [P, P, P, ctypes.c_longlong, c_int, P, c_double, c_int, P, P, P, P, c_size_t, P]),
+    "rvgp_gp_fit_adam": (c_int, [P, P, P, ctypes.c_longlong, c_int, P, c_double, c_int, P, P, P, c_int, c_double,
+                                 c_double, c_double, c_double, P, P, P, P, P, c_size_t, P]),
     "rvgp_gp_predict_workspace": (c_size_t, [ctypes.c_longlong, c_int, c_int]),
     "rvgp_gp_predict": (c_int, [P, P, ctypes.c_longlong, c_int, c_int, P, P, P, P, c_size_t, P]),
     "rvgp_kernel_matrix": (c_int, [P, ctypes.c_longlong, P, ctypes.c_longlong, c_int, P, P, P]),
@@ -51,9 +53,10 @@ SIGNATURES = {
     "rvgp_frame_map": (c_int, [P, c_int, c_int, c_int, c_int, P, c_int, P, P]),
     "rvgp_normalise_rows": (c_int, [P, c_int, c_int, P]),
     "rvgp_expm_action_workspace": (c_size_t, [c_int, c_int, c_int]),
-    "rvgp_expm_action": (c_int, [P, P, P, c_int, c_int, P, c_int, c_double, c_double, P, P, c_size_t, P]),
+    "rvgp_expm_action": (c_int, [P, P, P, c_int, c_int, P, c_int, c_double, c_double, c_double, P, P, c_size_t, P]),
     "rvgp_vector_diffusion_workspace": (c_size_t, [c_int, c_int]),
-    "rvgp_vector_diffusion": (c_int, [P, P, P, P, c_int, c_int, P, c_double, c_double, c_double, P, P, c_size_t, P]),
+    "rvgp_vector_diffusion": (c_int, [P, P, P, P, c_int, c_int, P, c_double, c_double, c_double, c_double, P, P,
+                                      c_size_t, P]),
     "rvgp_spectral_diffusion_workspace": (c_size_t, [ctypes.c_longlong, c_int, c_int]),
     "rvgp_spectral_diffusion": (c_int, [P, ctypes.c_longlong, c_int, P, P, c_int, c_double, P, P, c_size_t, P]),
     "rvgp_fps_workspace": (c_size_t, [c_int]),
@@ -218,7 +221,7 @@ def block_size(m, N):
     return min(p, N - N % 4)
 
 
-def eigsh(indptr, indices, vals64, vals32=None, m=10, mode="mixed", tol=1e-11, tol32=2e-5, max_iter=60, seed=0,
+def eigsh(indptr, indices, vals64, vals32=None, m=10, mode="mixed", tol=None, tol32=2e-5, max_iter=60, seed=0,
           scale=None, p=None):
     """m smallest eigenpairs of the block-CSR matrix: (evals (m,), evecs (N, m), stats dict).
 
@@ -237,14 +240,17 @@ def eigsh(indptr, indices, vals64, vals32=None, m=10, mode="mixed", tol=1e-11, t
     dev = vals64.device
     evals = torch.empty(m, dtype=torch.float64, device=dev)
     evecs = torch.empty((N, m), dtype=torch.float64, device=dev)
-    stats = (ctypes.c_int * 8)()
+    stats = (ctypes.c_int * 16)()
+    if tol is None:  # mixed: stop at the FP32 stage's accuracy; fp64: ARPACK-level residuals
+        tol = tol32 if imode == 1 else 1e-11
     L = lib()
     ws = workspace(L.rvgp_eigsh_workspace(n, DB, m, p, imode), dev)
     st = L.rvgp_eigsh(ptr(indptr), ptr(indices), ptr(vals64), ptr(vals32), n, DB, m, p, imode, tol, tol32, max_iter,
                       seed, ptr(evals), ptr(evecs), m, 1.0 if scale is None else float(scale), stats, ptr(ws),
                       ws.numel(), stream())
     info = dict(iters=stats[0], spmm=stats[1], sweeps=stats[2], converged=stats[3], refine_iters=stats[4],
-                chol_rescues=stats[5], p=p)
+                chol_rescues=stats[5], p=p, filter_ms=stats[8] / 1e3, orth_ms=stats[9] / 1e3,
+                rr_ms=stats[10] / 1e3, jacobi_ms=stats[11] / 1e3)
     if st < 0:
         check(st, "rvgp_eigsh")
     if st > 0:
@@ -324,6 +330,23 @@ def gp_lml(C, b, yy, N, evals, n_rows, theta, typ="matern", work=None):
     return work.out, work
 
 
+def gp_fit_adam(C, b, yy, N, evals, n_rows, theta0, lower, mask, steps, lr=0.05, betas=(0.9, 0.999), eps=1e-8,
+                typ="matern", work=None, history=False):
+    """Device-resident Adam on the LML: returns (theta (4,), out (5,), history or None, work)."""
+    m = evals.numel()
+    dev = evals.device
+    work = work or LMLWorkspace(m, dev)
+    theta = torch.empty(4, dtype=torch.float64, device=dev)
+    hist = torch.empty(max(steps, 1), dtype=torch.float64, device=dev) if history else None
+    lo = (ctypes.c_double * 4)(*[float(v) for v in lower])
+    mk = (ctypes.c_int * 4)(*[int(bool(v)) for v in mask])
+    check(lib().rvgp_gp_fit_adam(ptr(C), ptr(b), ptr(yy), int(N), m, ptr(evals), float(n_rows), KERNEL_TYPES[typ],
+                                 ptr(theta0.contiguous()), lo, mk, int(steps), float(lr), float(betas[0]),
+                                 float(betas[1]), float(eps), ptr(theta), ptr(hist), ptr(work.out), ptr(work.state),
+                                 ptr(work.ws), work.ws.numel(), stream()), "rvgp_gp_fit_adam")
+    return theta, work.out, hist, work
+
+
 def gp_predict(Phi_star, state, m, Phi_star32=None, mode="fp64"):
     Nte = Phi_star.shape[0]
     dev = Phi_star.device
@@ -384,8 +407,8 @@ def normalise_rows(v):
     return v
 
 
-def expm_action(indptr, indices, vals, X, t, bound):
-    """exp(-t A) X for block-CSR A (spectrum in [0, bound]); X: (N, b <= 4)."""
+def expm_action(indptr, indices, vals, X, t, bound, shift=0.0):
+    """exp(-t A) X for block-CSR A (spectrum in [shift, bound]); X: (N, b <= 4)."""
     n = indptr.numel() - 1
     DB = 1 if vals.dim() == 1 else vals.shape[-1]
     X = X.contiguous()
@@ -393,19 +416,19 @@ def expm_action(indptr, indices, vals, X, t, bound):
     Y = torch.empty_like(X)
     L = lib()
     ws = workspace(L.rvgp_expm_action_workspace(n, DB, b), X.device)
-    check(L.rvgp_expm_action(ptr(indptr), ptr(indices), ptr(vals), n, DB, ptr(X), b, float(t), float(bound), ptr(Y),
-                             ptr(ws), ws.numel(), stream()), "rvgp_expm_action")
+    check(L.rvgp_expm_action(ptr(indptr), ptr(indices), ptr(vals), n, DB, ptr(X), b, float(t), float(bound),
+                             float(shift), ptr(Y), ptr(ws), ws.numel(), stream()), "rvgp_expm_action")
     return Y
 
 
-def vector_diffusion(indptr, indices, L_vals, Lc_vals, x_loc, t, bound_L, bound_Lc):
+def vector_diffusion(indptr, indices, L_vals, Lc_vals, x_loc, t, bound_L, bound_Lc, shift_Lc=0.0):
     n, d = x_loc.shape
     out = torch.empty_like(x_loc)
     L = lib()
     ws = workspace(L.rvgp_vector_diffusion_workspace(n, d), x_loc.device)
     check(L.rvgp_vector_diffusion(ptr(indptr), ptr(indices), ptr(L_vals), ptr(Lc_vals), n, d, ptr(x_loc.contiguous()),
-                                  float(t), float(bound_L), float(bound_Lc), ptr(out), ptr(ws), ws.numel(), stream()),
-          "rvgp_vector_diffusion")
+                                  float(t), float(bound_L), float(bound_Lc), float(shift_Lc), ptr(out), ptr(ws),
+                                  ws.numel(), stream()), "rvgp_vector_diffusion")
     return out
 
 

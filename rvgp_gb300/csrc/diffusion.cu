@@ -121,25 +121,33 @@ __global__ void pack_columns(const double* __restrict__ x_loc, int n, int d, dou
   Xs[(size_t)i * 2 + 1] = 1.0;
 }
 
+// exp(-t A) X = e^{-t mu} exp(-t (A - mu I)) X.  Shifting by mu <= λ_min keeps
+// the slowest component O(1) through the sum: without it the terms (size
+// ~1/sqrt(2πα)) cancel down to e^{-t λ_min} and the relative error grows like
+// ε e^{t λ_min}.  The spectrum of A - mu I lies in [0, bound - mu].
 template <int DB>
 int run_expm(int n, const int* indptr, const int* indices, const double* vals, const double* X, int b, double t,
-             double bound, double* Y, double* ws3, cudaStream_t st) {
+             double bound, double mu, bool rescale, double* Y, double* ws3, cudaStream_t st) {
   const long long cnt = (long long)n * DB * b;
-  const double alpha = 0.5 * t * bound;
+  const double bp = bound - mu;
+  const double alpha = 0.5 * t * bp;
   const int K = terms_for(alpha);
   std::vector<double> c = scaled_bessel(alpha, K);
+  const double scale = rescale ? exp(-t * mu) : 1.0;
+  for (double& v : c) v *= scale;
   double* T0 = ws3;
   double* T1 = ws3 + cnt;
   double* T2 = ws3 + 2 * cnt;
   const int grid = ceil_div(cnt / DB, 256);
   rvgp::note_launch(); axpby_init<<<ceil_div(cnt, 256), 256, 0, st>>>(X, T0, Y, cnt, c[0]);
-  // T1 = s x = (2/b) A x - x ; Y += -2 I_1 T1
-  rvgp::note_launch(); cheb_step<DB><<<grid, 256, 0, st>>>(n, indptr, indices, vals, T0, nullptr, T1, Y, b, 2.0 / bound, -1.0, 0.0,
-                                      -2.0 * c[1]);
+  // T1 = s x = (2/b')(A - mu) x - x ; Y += -2 I_1 T1
+  rvgp::note_launch(); cheb_step<DB><<<grid, 256, 0, st>>>(n, indptr, indices, vals, T0, nullptr, T1, Y, b, 2.0 / bp,
+                                                           -(2.0 * mu / bp + 1.0), 0.0, -2.0 * c[1]);
   double *tp = T0, *tc = T1, *tn = T2;
   for (int k = 1; k < K; ++k) {
     const double ck = ((k + 1) % 2 ? -2.0 : 2.0) * c[k + 1];
-    rvgp::note_launch(); cheb_step<DB><<<grid, 256, 0, st>>>(n, indptr, indices, vals, tc, tp, tn, Y, b, 4.0 / bound, -2.0, -1.0, ck);
+    rvgp::note_launch(); cheb_step<DB><<<grid, 256, 0, st>>>(n, indptr, indices, vals, tc, tp, tn, Y, b, 4.0 / bp,
+                                                             -(4.0 * mu / bp + 2.0), -1.0, ck);
     double* tmp = tp;
     tp = tc;
     tc = tn;
@@ -156,20 +164,23 @@ using namespace rvgp;
 RVGP_API size_t rvgp_expm_action_workspace(int n, int DB, int b) { return sizeof(double) * 3 * (size_t)n * DB * b + 256; }
 
 // Y = exp(-t A) X for the block-CSR A (n block rows, DB x DB blocks, spectrum
-// in [0, bound]); X, Y: (n*DB) x b row-major with ld = b, b <= 4.
+// in [shift, bound]); X, Y: (n*DB) x b row-major with ld = b, b <= 4.  shift:
+// a lower bound of the spectrum (0 when unknown; λ_min gives full accuracy
+// at large t).
 RVGP_API int rvgp_expm_action(const int* indptr, const int* indices, const double* vals, int n, int DB, const double* X,
-                              int b, double t, double bound, double* Y, void* workspace, size_t ws_bytes,
-                              void* stream) {
+                              int b, double t, double bound, double shift, double* Y, void* workspace,
+                              size_t ws_bytes, void* stream) {
   RVGP_CHECK_ARG(indptr && indices && vals && X && Y && b >= 1 && b <= 4, "rvgp_expm_action: bad arguments");
-  RVGP_CHECK_ARG(t >= 0 && bound > 0, "rvgp_expm_action: need t >= 0 and a positive spectral bound");
+  RVGP_CHECK_ARG(t >= 0 && bound > 0 && shift >= 0 && shift < bound,
+                 "rvgp_expm_action: need t >= 0 and 0 <= shift < bound");
   RVGP_CHECK_ARG(ws_bytes >= rvgp_expm_action_workspace(n, DB, b), "rvgp_expm_action: workspace too small");
   cudaStream_t st = as_stream(stream);
   double* ws3 = static_cast<double*>(workspace);
   switch (DB) {
-    case 1: return run_expm<1>(n, indptr, indices, vals, X, b, t, bound, Y, ws3, st);
-    case 2: return run_expm<2>(n, indptr, indices, vals, X, b, t, bound, Y, ws3, st);
-    case 3: return run_expm<3>(n, indptr, indices, vals, X, b, t, bound, Y, ws3, st);
-    case 4: return run_expm<4>(n, indptr, indices, vals, X, b, t, bound, Y, ws3, st);
+    case 1: return run_expm<1>(n, indptr, indices, vals, X, b, t, bound, shift, true, Y, ws3, st);
+    case 2: return run_expm<2>(n, indptr, indices, vals, X, b, t, bound, shift, true, Y, ws3, st);
+    case 3: return run_expm<3>(n, indptr, indices, vals, X, b, t, bound, shift, true, Y, ws3, st);
+    case 4: return run_expm<4>(n, indptr, indices, vals, X, b, t, bound, shift, true, Y, ws3, st);
   }
   set_error("rvgp_expm_action: block size %d unsupported", DB);
   return RVGP_ENOTSUP;
@@ -182,11 +193,14 @@ RVGP_API size_t rvgp_vector_diffusion_workspace(int n, int d) {
 }
 
 // vector_diffusion(x, t, Lc, L, normalise=True) with the exact exponential
-// action: x_loc (n, d) -> out (n, d).  bound_L / bound_Lc: spectral upper bounds.
+// action: x_loc (n, d) -> out (n, d).  bound_L / bound_Lc: spectral upper
+// bounds; shift_Lc: a lower bound of Lc's spectrum (its smallest eigenvalue).
+// The factor e^{-t shift_Lc} cancels in the normalisation and is not applied.
 RVGP_API int rvgp_vector_diffusion(const int* indptr, const int* indices, const double* L_vals, const double* Lc_vals,
                                    int n, int d, const double* x_loc, double t, double bound_L, double bound_Lc,
-                                   double* out, void* workspace, size_t ws_bytes, void* stream) {
+                                   double shift_Lc, double* out, void* workspace, size_t ws_bytes, void* stream) {
   RVGP_CHECK_ARG(ws_bytes >= rvgp_vector_diffusion_workspace(n, d), "rvgp_vector_diffusion: workspace too small");
+  RVGP_CHECK_ARG(d >= 1 && d <= 4 && shift_Lc >= 0 && shift_Lc < bound_Lc, "rvgp_vector_diffusion: bad d or shift");
   cudaStream_t st = as_stream(stream);
   Workspace ws(workspace, ws_bytes);
   double* Xc = ws.take<double>((size_t)n * d * 2);
@@ -197,9 +211,16 @@ RVGP_API int rvgp_vector_diffusion(const int* indptr, const int* indices, const 
   void* w1 = ws.take<char>(wc);
   void* w2 = ws.take<char>(wsz);
   rvgp::note_launch(); pack_columns<<<ceil_div(n, 128), 128, 0, st>>>(x_loc, n, d, Xc, Xs);
-  int rc = rvgp_expm_action(indptr, indices, Lc_vals, n, d, Xc, 2, t, bound_Lc, Yc, w1, wc, stream);
+  double* w1d = static_cast<double*>(w1);
+  int rc;
+  switch (d) {
+    case 1: rc = run_expm<1>(n, indptr, indices, Lc_vals, Xc, 2, t, bound_Lc, shift_Lc, false, Yc, w1d, st); break;
+    case 2: rc = run_expm<2>(n, indptr, indices, Lc_vals, Xc, 2, t, bound_Lc, shift_Lc, false, Yc, w1d, st); break;
+    case 3: rc = run_expm<3>(n, indptr, indices, Lc_vals, Xc, 2, t, bound_Lc, shift_Lc, false, Yc, w1d, st); break;
+    default: rc = run_expm<4>(n, indptr, indices, Lc_vals, Xc, 2, t, bound_Lc, shift_Lc, false, Yc, w1d, st); break;
+  }
   if (rc) return rc;
-  rc = rvgp_expm_action(indptr, indices, L_vals, n, 1, Xs, 2, t, bound_L, Ys, w2, wsz, stream);
+  rc = rvgp_expm_action(indptr, indices, L_vals, n, 1, Xs, 2, t, bound_L, 0.0, Ys, w2, wsz, stream);
   if (rc) return rc;
   rvgp::note_launch(); combine_vector_diffusion<<<ceil_div(n, 128), 128, 0, st>>>(Yc, Ys, n, d, out);
   RVGP_LAUNCH_CHECK("rvgp_vector_diffusion");

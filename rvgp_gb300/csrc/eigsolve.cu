@@ -211,6 +211,26 @@ inline int gram_any(const double* A, const double* B, long long N, int p, double
 
 struct Stats {
   int iters = 0, spmm = 0, sweeps = 0, conv = 0, refine_iters = 0, chol_rescues = 0;
+  float ms[4] = {0, 0, 0, 0};  // filter, orthonormalise, Rayleigh-Ritz tall products, Jacobi
+};
+
+// CUDA events at phase boundaries; elapsed times are collected after the
+// synchronisation that ends every Rayleigh-Ritz step.
+struct PhaseEvents {
+  cudaEvent_t e[6];
+  PhaseEvents() {
+    for (auto& x : e) cudaEventCreate(&x);
+  }
+  ~PhaseEvents() {
+    for (auto& x : e) cudaEventDestroy(x);
+  }
+  void collect(Stats& s) {
+    float t;
+    const int pairs[4][2] = {{0, 1}, {1, 2}, {2, 5}, {3, 4}};
+    for (int q = 0; q < 4; ++q)
+      if (cudaEventElapsedTime(&t, e[pairs[q][0]], e[pairs[q][1]]) == cudaSuccess) s.ms[q] += t;
+    s.ms[2] -= (cudaEventElapsedTime(&t, e[3], e[4]) == cudaSuccess) ? t : 0.f;  // RR time excludes Jacobi
+  }
 };
 
 // Chebyshev filter of degree deg on [a, b] with lower bound a0; result pointer returned in *out.
@@ -283,14 +303,18 @@ int orthonormalise(const Problem& P, Block<T>& B, Small& s, Stats& stt, cudaStre
 // Rayleigh-Ritz: V, W = A V rotated to Ritz vectors; theta, residuals to host.
 template <typename T>
 int rayleigh_ritz(const Problem& P, Block<T>& B, Small& s, Stats& stt, int max_sweeps, std::vector<double>& theta,
-                  std::vector<double>& res, cudaStream_t st) {
+                  std::vector<double>& res, PhaseEvents& ev, cudaStream_t st) {
   const long long N = P.N;
   const int p = P.p;
   TRY(spmm(P.n, P.DB, P.indptr, P.indices, vals_of<T>(P), B.V, B.W, (const T*)nullptr, p, p, 1.0, 0.0, 0.0, st));
   ++stt.spmm;
   TRY(gram_any(B.V, B.W, N, p, s.H, s, st));
   int used = 0;
-  TRY(jacobi_eigh<double>(s.H, p, s.theta, s.Q, max_sweeps, 1e-15, &used, s.jac_ws, s.jac_bytes, st));
+  // off(H) tolerance: the Ritz vectors of an FP32 block are accurate to ~1e-7 anyway
+  const double jtol = sizeof(T) == 4 ? 1e-10 : 1e-13;
+  cudaEventRecord(ev.e[3], st);
+  TRY(jacobi_eigh<double>(s.H, p, s.theta, s.Q, max_sweeps, jtol, &used, s.jac_ws, s.jac_bytes, st));
+  cudaEventRecord(ev.e[4], st);
   stt.sweeps += used;
   rvgp::note_launch(); copy_to<T><<<ceil_div((long long)p * p, 256), 256, 0, st>>>(s.Q, (long long)p * p, Bmat<T>(s));
   TRY(gemm_nn<T>(B.V, p, Bmat<T>(s), p, N, p, p, B.T1, p, T(1), T(0), st));
@@ -301,11 +325,13 @@ int rayleigh_ritz(const Problem& P, Block<T>& B, Small& s, Stats& stt, int max_s
   const long long chunk = (N + nc - 1) / nc;
   rvgp::note_launch(); resid_partial<T><<<nc, 256, 0, st>>>(B.W, B.V, s.theta, p, N, p, chunk, s.resid_part);
   rvgp::note_launch(); resid_final<<<ceil_div(p, 256), 256, 0, st>>>(s.resid_part, nc, p, s.res);
+  cudaEventRecord(ev.e[5], st);
   theta.resize(p);
   res.resize(p);
   cudaMemcpyAsync(theta.data(), s.theta, sizeof(double) * p, cudaMemcpyDeviceToHost, st);
   cudaMemcpyAsync(res.data(), s.res, sizeof(double) * p, cudaMemcpyDeviceToHost, st);
   if (cudaStreamSynchronize(st) != cudaSuccess) return check_launch("rayleigh_ritz");
+  ev.collect(stt);
   return check_launch("rayleigh_ritz");
 }
 
@@ -336,11 +362,15 @@ int iterate(const Problem& P, Block<T>& B, Small& s, Stats& stt, double bup, dou
     a = bup * std::min(0.5, std::max(4.0 * p / (double)P.N, 0.01));
     a0 = -1e-3 * bup;
   }
+  PhaseEvents ev;
   for (int it = 0; it < max_iter; ++it) {
     if (a >= bup * 0.999) a = bup * 0.5;
+    cudaEventRecord(ev.e[0], st);
     TRY(filter<T>(P, B, deg, a, bup, a0, stt, st));
+    cudaEventRecord(ev.e[1], st);
     TRY(orthonormalise<T>(P, B, s, stt, st));
-    TRY(rayleigh_ritz<T>(P, B, s, stt, 60, theta, res, st));
+    cudaEventRecord(ev.e[2], st);
+    TRY(rayleigh_ritz<T>(P, B, s, stt, 60, theta, res, ev, st));
     ++stt.iters;
     nconv = 0;
     for (int j = 0; j < m; ++j)
@@ -476,6 +506,7 @@ RVGP_API int rvgp_eigsh(const int* indptr, const int* indices, const double* val
     stats[3] = stt.conv;
     stats[4] = stt.refine_iters;
     stats[5] = stt.chol_rescues;
+    for (int q = 0; q < 4; ++q) stats[8 + q] = (int)(stt.ms[q] * 1000.f);  // microseconds per phase
   }
   RVGP_LAUNCH_CHECK("rvgp_eigsh");
   if (cudaStreamSynchronize(st) != cudaSuccess) return check_launch("rvgp_eigsh");

@@ -9,14 +9,15 @@
 // Because K has rank m, every quantity is computed exactly in the m-space
 // (Woodbury identity and matrix determinant lemma) from C = ΦᵀΦ, b = Φᵀy and
 // yᵀy, which are formed once:
-//   R = diag(√S),  A = I + R C R / σ² = L_A L_Aᵀ
+//   R = diag(√S),  A = I + R C R / σ² = L_A L_Aᵀ,  z = L_A⁻¹ R b,  w = A⁻¹ R b
 //   log|K_y| = N log σ² + 2 Σ log diag L_A
-//   yᵀK_y⁻¹y = (yᵀy − |L_A⁻¹ R b|² / σ²) / σ²
-//   Φᵀα = (b − C R A⁻¹ R b / σ²) / σ²                       (α = K_y⁻¹ y)
-//   diag(ΦᵀK_y⁻¹Φ) = (diag C − diag(EᵀE) / σ²) / σ²,   E = L_A⁻¹ R C
-//   ∂LML/∂S_l = ½[(Φᵀα)_l² − diag(ΦᵀK_y⁻¹Φ)_l]
-//   ∂LML/∂σ²  = ½[αᵀα − tr K_y⁻¹],  tr K_y⁻¹ = (N − m + |L_A⁻¹|_F²)/σ²
-// and the chain rule through S(ν, κ, σ_f) including the Σs normalisation.
+//   yᵀK_y⁻¹y = (yᵀy − zᵀz / σ²) / σ²
+//   Φᵀα = w / (r σ²)  (α = K_y⁻¹ y),   S_l (ΦᵀK_y⁻¹Φ)_ll = 1 − (A⁻¹)_ll
+//   ∂LML/∂S_l = ½[(Φᵀα)_l² − (ΦᵀK_y⁻¹Φ)_ll]
+//   ∂LML/∂σ²  = ½[αᵀα − tr K_y⁻¹],  αᵀα = (yᵀy − zᵀz/σ² − wᵀw/σ²)/σ⁴,
+//                                    tr K_y⁻¹ = (N − m + tr A⁻¹)/σ²
+// (the identities follow from A w = R b and R C R = σ²(A − I)), and the chain
+// rule through S(ν, κ, σ_f) including the Σs normalisation.
 // Posterior (predict_f, full_cov=False): mean = Φ* (S ∘ Φᵀα),
 // var = diag(Φ* R A⁻¹ R Φ*ᵀ) = |L_A⁻¹ R φ*_i|² per test row.
 // The m x m factorisation is FP64 in both forms (cond(A) grows like
@@ -117,22 +118,58 @@ __global__ void build_A(const double* __restrict__ C, int m, const double* __res
   A[e] = (i == j ? 1.0 : 0.0) + sqrt(S[i]) * C[e] * sqrt(S[j]) / s2;
 }
 
-// B (m x m) = diag(r) C with r = sqrt(S)
-__global__ void scale_rows_sqrtS(const double* __restrict__ C, int m, const double* __restrict__ S,
-                                 double* __restrict__ B) {
-  const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (e >= (long long)m * m) return;
-  B[e] = sqrt(S[e / m]) * C[e];
+// state layout (doubles): [0, m²) L_A⁻¹, then sp = S ∘ Φᵀα = r ∘ w / σ² (m), S (m),
+// r (m), w = A⁻¹ R b (m).
+//
+// With w = A⁻¹ R b the Woodbury algebra collapses (A w = R b and
+// R C R = σ²(A − I)):  Φᵀα = w / (r σ²),  diag(ΦᵀK⁻¹Φ)_l S_l = 1 − (A⁻¹)_ll,
+// αᵀα = (yᵀy − zᵀz/σ² − wᵀw/σ²)/σ⁴ with z = L_A⁻¹ R b.  Every gradient term is
+// then O(m) given L_A⁻¹ and is free of cancellation:
+//   ∂LML/∂θ = ½ Σ_l [(w_l/σ²)² − (1 − (A⁻¹)_ll)] ∂log S_l/∂θ.
+
+// z = L_A⁻¹ (r ∘ b): one warp per row k of L_A⁻¹
+__global__ void lml_z(const double* __restrict__ Li, int m, const double* __restrict__ S,
+                      const double* __restrict__ b, double* __restrict__ z, const int* __restrict__ info) {
+  const int lane = threadIdx.x & 31;
+  const int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (k >= m || *info) return;
+  double s = 0.0;
+  for (int l = lane; l <= k; l += 32) s += Li[(size_t)k * m + l] * sqrt(S[l]) * b[l];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) z[k] = s;
 }
 
-// state layout (doubles): [0, m²) L_A⁻¹, then pa = Φᵀα (m), S (m), r (m), w (m)
-__global__ void __launch_bounds__(kCTA) lml_epilogue(const double* __restrict__ C, const double* __restrict__ b,
-                                                     const double* __restrict__ yy, long long N, int m,
-                                                     const double* __restrict__ LA, const double* __restrict__ E,
-                                                     const double* __restrict__ S, const double* __restrict__ dS,
-                                                     const double* __restrict__ theta, const int* __restrict__ info,
-                                                     double* __restrict__ state, double* __restrict__ tmp,
-                                                     double* __restrict__ out) {
+// w = L_A⁻ᵀ z and (A⁻¹)_ll = Σ_k (L_A⁻¹)_kl²: one warp per column l
+__global__ void lml_w_diag(const double* __restrict__ Li, int m, const double* __restrict__ z,
+                           double* __restrict__ w, double* __restrict__ ainv_diag, const int* __restrict__ info) {
+  const int lane = threadIdx.x & 31;
+  const int l = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (l >= m || *info) return;
+  double s = 0.0, q = 0.0;
+  for (int k = l + lane; k < m; k += 32) {
+    const double v = Li[(size_t)k * m + l];
+    s += v * z[k];
+    q += v * v;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    s += __shfl_xor_sync(0xffffffffu, s, o);
+    q += __shfl_xor_sync(0xffffffffu, q, o);
+  }
+  if (lane == 0) {
+    w[l] = s;
+    ainv_diag[l] = q;
+  }
+}
+
+// LML, its gradient w.r.t. [nu, kappa, sigma_f, noise] and the predict state (one CTA)
+__global__ void __launch_bounds__(kCTA) lml_final(const double* __restrict__ yy, long long N, int m,
+                                                  const double* __restrict__ LA, const double* __restrict__ S,
+                                                  const double* __restrict__ dS, const double* __restrict__ z,
+                                                  const double* __restrict__ w, const double* __restrict__ ainv_diag,
+                                                  const double* __restrict__ theta, const int* __restrict__ info,
+                                                  double* __restrict__ state, double* __restrict__ out) {
   __shared__ double sh[kCTA];
   const double s2 = theta[3];
   if (*info != 0) {
@@ -140,65 +177,31 @@ __global__ void __launch_bounds__(kCTA) lml_epilogue(const double* __restrict__ 
       for (int t = 0; t < 5; ++t) out[t] = nan("");
     return;
   }
-  const double* Li = state;  // L_A⁻¹ (lower)
-  double* pa = state + (size_t)m * m;
-  double* Sst = pa + m;
+  double* sp = state + (size_t)m * m;
+  double* Sst = sp + m;
   double* r = Sst + m;
-  double* w = r + m;
-  double* z = tmp;
-  double* rw = tmp + m;
-  double* Crw = tmp + 2 * m;
+  double* wst = r + m;
+  double zz = 0.0, ww = 0.0, logd = 0.0, tr = 0.0, g0 = 0.0, g1 = 0.0, g2 = 0.0;
   for (int l = threadIdx.x; l < m; l += blockDim.x) {
-    r[l] = sqrt(S[l]);
-    Sst[l] = S[l];
-  }
-  __syncthreads();
-  // z = L_A⁻¹ (r ∘ b)
-  for (int k = threadIdx.x; k < m; k += blockDim.x) {
-    double s = 0.0;
-    for (int l = 0; l <= k; ++l) s += Li[(size_t)k * m + l] * r[l] * b[l];
-    z[k] = s;
-  }
-  __syncthreads();
-  // w = L_A⁻ᵀ z = A⁻¹ R b ;  rw = r ∘ w
-  for (int l = threadIdx.x; l < m; l += blockDim.x) {
-    double s = 0.0;
-    for (int k = l; k < m; ++k) s += Li[(size_t)k * m + l] * z[k];
-    w[l] = s;
-    rw[l] = r[l] * s;
-  }
-  __syncthreads();
-  for (int l = threadIdx.x; l < m; l += blockDim.x) {
-    double s = 0.0;
-    for (int j = 0; j < m; ++j) s += C[(size_t)l * m + j] * rw[j];
-    Crw[l] = s;
-  }
-  __syncthreads();
-  double zz = 0.0, logd = 0.0, rwb = 0.0, rwCrw = 0.0, fro = 0.0;
-  double g0 = 0.0, g1 = 0.0, g2 = 0.0;
-  for (int l = threadIdx.x; l < m; l += blockDim.x) {
+    const double Sl = S[l], rl = sqrt(Sl), wl = w[l];
     zz += z[l] * z[l];
+    ww += wl * wl;
     logd += log(LA[(size_t)l * m + l]);
-    rwb += rw[l] * b[l];
-    rwCrw += rw[l] * Crw[l];
-    const double p_l = (b[l] - Crw[l] / s2) / s2;
-    pa[l] = p_l;
-    double dm = 0.0;
-    for (int k = 0; k < m; ++k) dm += E[(size_t)k * m + l] * E[(size_t)k * m + l];
-    const double gl = 0.5 * (p_l * p_l - (C[(size_t)l * m + l] - dm / s2) / s2);
-    g0 += gl * dS[l];
-    g1 += gl * dS[m + l];
-    g2 += gl * dS[2 * m + l];
-  }
-  for (long long e = threadIdx.x; e < (long long)m * m; e += blockDim.x) {
-    const int i = (int)(e / m), j = (int)(e % m);
-    if (j <= i) fro += Li[e] * Li[e];
+    tr += ainv_diag[l];
+    sp[l] = rl * wl / s2;
+    Sst[l] = Sl;
+    r[l] = rl;
+    wst[l] = wl;
+    // ½[(w_l/σ²)² − (1 − (A⁻¹)_ll)] · ∂S_l/∂θ / S_l
+    const double q = 0.5 * ((wl / s2) * (wl / s2) - (1.0 - ainv_diag[l])) / Sl;
+    g0 += q * dS[l];
+    g1 += q * dS[m + l];
+    g2 += q * dS[2 * m + l];
   }
   zz = block_sum(zz, sh);
+  ww = block_sum(ww, sh);
   logd = block_sum(logd, sh);
-  rwb = block_sum(rwb, sh);
-  rwCrw = block_sum(rwCrw, sh);
-  fro = block_sum(fro, sh);
+  tr = block_sum(tr, sh);
   g0 = block_sum(g0, sh);
   g1 = block_sum(g1, sh);
   g2 = block_sum(g2, sh);
@@ -206,14 +209,53 @@ __global__ void __launch_bounds__(kCTA) lml_epilogue(const double* __restrict__ 
     const double Nd = (double)N;
     const double quad = (yy[0] - zz / s2) / s2;
     const double logdet = Nd * log(s2) + 2.0 * logd;
-    const double lml = -0.5 * quad - 0.5 * logdet - 0.5 * Nd * log(2.0 * M_PI);
-    const double a2 = (yy[0] - 2.0 * rwb / s2 + rwCrw / (s2 * s2)) / (s2 * s2);
-    const double trk = (Nd - m + fro) / s2;
-    out[0] = lml;
+    out[0] = -0.5 * quad - 0.5 * logdet - 0.5 * Nd * log(2.0 * M_PI);
     out[1] = g0;
     out[2] = g1;
     out[3] = g2;
-    out[4] = 0.5 * (a2 - trk);
+    const double a2 = (yy[0] - zz / s2 - ww / s2) / (s2 * s2);
+    out[4] = 0.5 * (a2 - (Nd - m + tr) / s2);
+  }
+}
+
+__device__ __forceinline__ double softplus_d(double u) { return u > 0.0 ? u + log1p(exp(-u)) : log1p(exp(u)); }
+__device__ __forceinline__ double sigmoid_d(double u) {
+  return u >= 0.0 ? 1.0 / (1.0 + exp(-u)) : exp(u) / (1.0 + exp(u));
+}
+
+// Adam on the unconstrained parameters u (value = softplus(u) + lower) minimising −LML.
+// adam = [u(4), m(4), v(4)]; hyper = [lr, beta1, beta2, eps]; mask = trainable flags.
+__global__ void adam_step(double* __restrict__ theta, double* __restrict__ adam, const double* __restrict__ lower,
+                          const int* __restrict__ mask, const double* __restrict__ out, int step, double lr,
+                          double beta1, double beta2, double eps, double* __restrict__ hist) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (hist) hist[step] = out[0];
+  bool finite = true;
+  for (int q = 0; q < 5; ++q) finite = finite && isfinite(out[q]);
+  if (!finite) return;  // keep the parameters; the history records the failure
+  const double b1t = 1.0 - pow(beta1, (double)(step + 1)), b2t = 1.0 - pow(beta2, (double)(step + 1));
+  for (int q = 0; q < 4; ++q) {
+    if (!mask[q]) continue;
+    double* u = adam + q;
+    double* m1 = adam + 4 + q;
+    double* v1 = adam + 8 + q;
+    const double g = -out[1 + q] * sigmoid_d(*u);  // d(−LML)/du
+    *m1 = beta1 * *m1 + (1.0 - beta1) * g;
+    *v1 = beta2 * *v1 + (1.0 - beta2) * g * g;
+    *u -= lr * (*m1 / b1t) / (sqrt(*v1 / b2t) + eps);
+    theta[q] = softplus_d(*u) + lower[q];
+  }
+}
+
+__global__ void adam_init(const double* __restrict__ theta0, const double* __restrict__ lower,
+                          double* __restrict__ theta, double* __restrict__ adam) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  for (int q = 0; q < 4; ++q) {
+    theta[q] = theta0[q];
+    const double v = theta0[q] - lower[q];
+    adam[q] = v > 30.0 ? v : log(expm1(fmax(v, 1e-300)));  // inverse softplus
+    adam[4 + q] = 0.0;
+    adam[8 + q] = 0.0;
   }
 }
 
@@ -253,22 +295,21 @@ __global__ void make_Bt(const double* __restrict__ state, int m, T* __restrict__
   const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (e >= (long long)m * m) return;
   const int l = (int)(e / m), k = (int)(e % m);
-  const double* r = state + (size_t)m * m + 2 * m;  // after L_A⁻¹, pa, S
+  const double* r = state + (size_t)m * m + 2 * m;  // after L_A⁻¹, sp, S
   Bt[e] = (T)(k >= l ? r[l] * state[(size_t)k * m + l] : 0.0);
 }
 
-// mean_i = Σ_l Φ*_il S_l pa_l ; var_i = Σ_k P_ik²  (warp per row)
+// mean_i = Σ_l Φ*_il sp_l  (sp = S ∘ Φᵀα) ; var_i = Σ_k P_ik²  (warp per row)
 template <typename T>
 __global__ void predict_rows(const double* __restrict__ Phi, long long Nte, int m, const double* __restrict__ state,
                              const T* __restrict__ P, double* __restrict__ mean, double* __restrict__ var) {
   const int lane = threadIdx.x & 31;
   const long long i = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
   if (i >= Nte) return;
-  const double* pa = state + (size_t)m * m;
-  const double* S = pa + m;
+  const double* sp = state + (size_t)m * m;
   double sm = 0.0, sv = 0.0;
   for (int l = lane; l < m; l += 32) {
-    sm += Phi[i * m + l] * S[l] * pa[l];
+    sm += Phi[i * m + l] * sp[l];
     const double p = (double)P[i * m + l];
     sv += p * p;
   }
@@ -323,8 +364,8 @@ __global__ void kernel_diag(const double* __restrict__ A, long long N, int m, co
 }
 
 struct LmlBufs {
-  double *S, *dS, *stmp, *A, *B, *E, *etmp;
-  int* info;
+  double *S, *dS, *stmp, *A, *z, *w, *ainv, *theta, *adam, *lower;
+  int *info, *mask;
 };
 
 LmlBufs carve_lml(Workspace& ws, int m) {
@@ -333,11 +374,34 @@ LmlBufs carve_lml(Workspace& ws, int m) {
   b.dS = ws.take<double>(3 * (size_t)m);
   b.stmp = ws.take<double>(3 * (size_t)m);
   b.A = ws.take<double>((size_t)m * m);
-  b.B = ws.take<double>((size_t)m * m);
-  b.E = ws.take<double>((size_t)m * m);
-  b.etmp = ws.take<double>(3 * (size_t)m);
+  b.z = ws.take<double>(m);
+  b.w = ws.take<double>(m);
+  b.ainv = ws.take<double>(m);
+  b.theta = ws.take<double>(4);
+  b.adam = ws.take<double>(12);
+  b.lower = ws.take<double>(4);
   b.info = ws.take<int>(4);
+  b.mask = ws.take<int>(4);
   return b;
+}
+
+// One likelihood + gradient evaluation at theta (device), all stream-ordered.
+int lml_chain(const LmlBufs& B, const double* C, const double* b, const double* yy, long long N, int m,
+              const double* evals, double n_rows, int typ, const double* theta, double* out, double* state,
+              cudaStream_t st) {
+  const long long mm = (long long)m * m;
+  rvgp::note_launch(); spectral_S_kernel<<<1, kCTA, 0, st>>>(evals, m, theta, n_rows, typ, B.S, B.dS, B.stmp);
+  rvgp::note_launch(); build_A<<<ceil_div(mm, 256), 256, 0, st>>>(C, m, B.S, theta, B.A);
+  int rc = cholesky<double>(B.A, m, m, B.info, st);
+  if (rc) return rc;
+  rc = tri_inv_lower<double>(B.A, m, m, state, m, st);
+  if (rc) return rc;
+  const int wb = ceil_div((long long)m * 32, 256);
+  rvgp::note_launch(); lml_z<<<wb, 256, 0, st>>>(state, m, B.S, b, B.z, B.info);
+  rvgp::note_launch(); lml_w_diag<<<wb, 256, 0, st>>>(state, m, B.z, B.w, B.ainv, B.info);
+  rvgp::note_launch(); lml_final<<<1, kCTA, 0, st>>>(yy, N, m, B.A, B.S, B.dS, B.z, B.w, B.ainv, theta, B.info, state,
+                                                    out);
+  return check_launch("lml_chain");
 }
 
 }  // namespace
@@ -418,18 +482,40 @@ RVGP_API int rvgp_gp_lml(const double* C, const double* b, const double* yy, lon
   cudaStream_t st = as_stream(stream);
   Workspace ws(workspace, ws_bytes);
   LmlBufs B = carve_lml(ws, m);
-  const long long mm = (long long)m * m;
-  rvgp::note_launch(); spectral_S_kernel<<<1, kCTA, 0, st>>>(evals, m, theta, n_rows, typ, B.S, B.dS, B.stmp);
-  rvgp::note_launch(); build_A<<<ceil_div(mm, 256), 256, 0, st>>>(C, m, B.S, theta, B.A);
-  int rc = cholesky<double>(B.A, m, m, B.info, st);
+  return lml_chain(B, C, b, yy, N, m, evals, n_rows, typ, theta, out, state, st);
+}
+
+// Hyperparameter learning on the device: `steps` Adam steps (Kingma & Ba, with
+// bias correction) on the unconstrained parameters u, value = softplus(u) +
+// lower, minimising −LML with the gradient above; no host synchronisation.
+// theta0 (device, 4): start values [nu, kappa, sigma_f, noise]; lower / mask
+// (host, 4 each): lower bounds and trainable flags; hyper = lr, beta1, beta2,
+// eps.  theta_out (device, 4) = final values; hist (device, steps, optional) =
+// LML before each step; out / state as for rvgp_gp_lml, evaluated at theta_out.
+RVGP_API int rvgp_gp_fit_adam(const double* C, const double* b, const double* yy, long long N, int m,
+                              const double* evals, double n_rows, int typ, const double* theta0, const double* lower,
+                              const int* mask, int steps, double lr, double beta1, double beta2, double eps,
+                              double* theta_out, double* hist, double* out, double* state, void* workspace,
+                              size_t ws_bytes, void* stream) {
+  RVGP_CHECK_ARG(C && b && yy && evals && theta0 && lower && mask && theta_out && out && state,
+                 "rvgp_gp_fit_adam: null pointer");
+  RVGP_CHECK_ARG(steps >= 0 && ws_bytes >= rvgp_gp_lml_workspace(m), "rvgp_gp_fit_adam: bad steps or workspace");
+  cudaStream_t st = as_stream(stream);
+  Workspace ws(workspace, ws_bytes);
+  LmlBufs B = carve_lml(ws, m);
+  cudaMemcpyAsync(B.lower, lower, 4 * sizeof(double), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(B.mask, mask, 4 * sizeof(int), cudaMemcpyHostToDevice, st);
+  rvgp::note_launch(); adam_init<<<1, 32, 0, st>>>(theta0, B.lower, B.theta, B.adam);
+  for (int s = 0; s < steps; ++s) {
+    int rc = lml_chain(B, C, b, yy, N, m, evals, n_rows, typ, B.theta, out, state, st);
+    if (rc) return rc;
+    rvgp::note_launch(); adam_step<<<1, 32, 0, st>>>(B.theta, B.adam, B.lower, B.mask, out, s, lr, beta1, beta2, eps,
+                                                     hist);
+  }
+  int rc = lml_chain(B, C, b, yy, N, m, evals, n_rows, typ, B.theta, out, state, st);
   if (rc) return rc;
-  rc = tri_inv_lower<double>(B.A, m, m, state, m, st);
-  if (rc) return rc;
-  rvgp::note_launch(); scale_rows_sqrtS<<<ceil_div(mm, 256), 256, 0, st>>>(C, m, B.S, B.B);
-  rc = gemm_nn<double>(state, m, B.B, m, m, m, m, B.E, m, 1.0, 0.0, st);
-  if (rc) return rc;
-  rvgp::note_launch(); lml_epilogue<<<1, kCTA, 0, st>>>(C, b, yy, N, m, B.A, B.E, B.S, B.dS, theta, B.info, state, B.etmp, out);
-  RVGP_LAUNCH_CHECK("rvgp_gp_lml");
+  cudaMemcpyAsync(theta_out, B.theta, 4 * sizeof(double), cudaMemcpyDeviceToDevice, st);
+  RVGP_LAUNCH_CHECK("rvgp_gp_fit_adam");
   return RVGP_OK;
 }
 

@@ -38,9 +38,17 @@ def _log(verbose, *a):
 class data:
     def __init__(self, vertices, vectors=None, dim_man=2, n_neighbors=10, frac_geodesic_neighbours=1.5,
                  explained_variance=0.8, n_eigenpairs=None, *, precision="mixed", estimate_dim=True,
-                 strict_rank=True, eig_tol=1e-11, seed=0, verbose=True):
+                 strict_rank=True, eig_tol=None, seed=0, verbose=True, timings=None):
         _core.require_cuda()
         device = torch.device("cuda", torch.cuda.current_device())
+        marks = []
+
+        def mark(name):  # CUDA events between stages when a timings dict is given
+            if timings is not None:
+                ev = torch.cuda.Event(enable_timing=True)
+                ev.record()
+                marks.append((name, ev))
+        mark("start")
         if isinstance(vertices, torch.Tensor):
             X = vertices.to(device=device, dtype=torch.float64).contiguous()
             self._vertices_host = None
@@ -55,6 +63,7 @@ class data:
         knn = _core.knn(X, n_neighbors)
         indptr, indices, maxdeg = _core.graph_build(knn)
         dev.indptr, dev.indices, dev.maxdeg = indptr, indices, maxdeg
+        mark("graph")
 
         _log(verbose, "Fit tangent spaces")
         K = int(n_neighbors * frac_geodesic_neighbours)
@@ -80,6 +89,7 @@ class data:
             raise RuntimeError("Local tangent space approximation failed, at least one geodesic neighborhood does "
                                "not span d-dimensional space")
         dev.T, dev.Sigma = T, Sigma
+        mark("gauges")
         _log(verbose, "Predicted manifold dimension is {}".format(dim))
 
         R, lc64, lc32 = _core.connections(T, dim, indptr, indices, want32=(precision == "mixed"))
@@ -89,16 +99,23 @@ class data:
         _log(verbose, "Compute Laplacians")
         dev.L_vals = _core.laplacian_values(indptr, indices)
         dev.bound = 2.0 * maxdeg * (1.0 + 1e-12)  # spectral bound of L and Lc (|D| + |A|)
+        mark("connections")
 
         _log(verbose, "Compute eigendecompositions")
         m = n if n_eigenpairs is None else min(int(n_eigenpairs), n)
         mode = "mixed" if precision == "mixed" else "fp64"
         dev.evals_L, dev.evecs_L, dev.eig_info_L = _core.eigsh(indptr, indices, dev.L_vals, None, m=m, mode=mode,
                                                                tol=eig_tol, seed=seed, scale=math.sqrt(n))
+        mark("eigsh_L")
         dev.evals_Lc, U, dev.eig_info_Lc = _core.eigsh(indptr, indices, lc64, lc32, m=m, mode=mode, tol=eig_tol,
                                                        seed=seed + 1, scale=math.sqrt(n * dim))
         dev.evecs_Lc_local = U
         dev.evecs_Lc = _core.lift(T, dim, U)
+        mark("eigsh_Lc")
+        if timings is not None:
+            torch.cuda.synchronize()
+            for (a, ea), (b, eb) in zip(marks[:-1], marks[1:]):
+                timings[b] = timings.get(b, 0.0) + ea.elapsed_time(eb) / 1e3
         dev.vectors = None
         self._dev = dev
         self.n = n
@@ -219,5 +236,8 @@ class data:
             return
         d = self._dev
         loc = _core.frame_map(d.T, self.dim_man, d.vectors, "to_local")
-        loc = _core.vector_diffusion(d.indptr, d.indices, d.L_vals, d.Lc_vals, loc, t, d.bound, d.bound)
+        # the smallest eigenvalue of Lc (known from the eigensolver) keeps the
+        # Chebyshev sum free of cancellation at large t
+        shift = max(0.0, float(d.evals_Lc[0]) * (1.0 - 1e-9) - 1e-12)
+        loc = _core.vector_diffusion(d.indptr, d.indices, d.L_vals, d.Lc_vals, loc, t, d.bound, d.bound, shift)
         self.vectors = _core.frame_map(d.T, self.dim_man, loc, "from_local")

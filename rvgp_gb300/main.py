@@ -134,31 +134,25 @@ class manifold_GPR:
             return self._adam(params, epochs, lr)
         raise ValueError(f"unknown optimiser {method!r}")
 
+    def _slots(self):
+        """The four hyperparameters in theta order [nu, kappa, sigma_f, noise] (nu None for SE)."""
+        return [self.kernel.nu, self.kernel.kappa, self.kernel.sigma_f, self.likelihood.variance]
+
     def _adam(self, params, steps, lr):
-        u = torch.tensor([p.unconstrained for p in params], dtype=torch.float64, requires_grad=True)
-        opt = torch.optim.Adam([u], lr=lr)
-        names = [p.name for p in params]
-        fixed = {p.name: float(p) for p in self.kernel.parameters + [self.likelihood.variance] if not p.trainable}
-        lowers = torch.tensor([p.lower for p in params], dtype=torch.float64)
-        dev = self.kernel.device
-        for _ in range(steps):
-            opt.zero_grad()
-            vals = torch.nn.functional.softplus(u) + lowers
-            v = dict(zip(names, vals))
-            theta = torch.stack([
-                v.get("nu", torch.tensor(fixed.get("nu", 0.0), dtype=torch.float64)),
-                v.get("kappa", torch.tensor(fixed.get("kappa", 0.0), dtype=torch.float64)),
-                v.get("sigma_f", torch.tensor(fixed.get("sigma_f", 0.0), dtype=torch.float64)),
-                v.get("noise_variance", torch.tensor(fixed.get("noise_variance", 0.0), dtype=torch.float64)),
-            ]).to(dev)
-            loss = -log_marginal_likelihood(theta, self)
-            loss.backward()
-            opt.step()
-            self.n_evals += 1
-        with torch.no_grad():
-            for p, x in zip(params, u.tolist()):
-                p.unconstrained = float(x)
-        return u.detach()
+        """``steps`` Adam steps on the device (rvgp_gp_fit_adam): no host round trip per step."""
+        slots = self._slots()
+        lower = [p.lower if p is not None else 0.0 for p in slots]
+        mask = [p is not None and p.trainable for p in slots]
+        theta, out, hist, _ = _core.gp_fit_adam(self.C, self.b, self.yy, self.N, self.kernel.eigenvalues,
+                                                self.kernel.num_verticies, self.theta(), lower, mask, steps, lr=lr,
+                                                typ=self.kernel.typ, work=self.work, history=True)
+        vals = theta.cpu().numpy()
+        for p, v in zip(slots, vals):
+            if p is not None and p.trainable:
+                p.assign(float(v))
+        self.n_evals += steps + 1
+        self.lml_history = hist
+        return vals
 
     # ------------------------------------------------------------------ prediction
     def _predict_rows(self, Phi_star):

@@ -37,14 +37,29 @@ def test_eigsh_matches_reference(core, name, mode):
     n, d, m = len(g["X"]), int(g["dim_man"]), int(g["m"])
     ip, ix = cu(g["indptr"], torch.int32), cu(g["indices"], torch.int32)
     # scalar Laplacian (evecs scaled by sqrt(n) as compute_spectrum does)
-    ev, V, info = core.eigsh(ip, ix, cu(g["L_data"]), m=m, mode=mode, scale=np.sqrt(n))
+    ev, V, info = core.eigsh(ip, ix, cu(g["L_data"]), m=m, mode=mode, tol=1e-11, scale=np.sqrt(n))
     check_pairs(ev.cpu().numpy(), V.cpu().numpy(), g["evals_L"], g["evecs_L"], m, 1e-9, 1e-6)
     np.testing.assert_allclose(np.linalg.norm(V.cpu().numpy(), axis=0), np.sqrt(n), rtol=1e-10)
     # connection Laplacian from the reference's own transports
     L = O.laplacian(g["indptr"], g["indices"], n)
     blocks = L.data[:, None, None] * g["R"]
-    ev, V, info = core.eigsh(ip, ix, cu(blocks), m=m, mode=mode, scale=np.sqrt(n * d))
+    ev, V, info = core.eigsh(ip, ix, cu(blocks), m=m, mode=mode, tol=1e-11, scale=np.sqrt(n * d))
     check_pairs(ev.cpu().numpy(), V.cpu().numpy(), g["evals_Lc"], g["evecs_Lc_local"], m, 1e-9, 1e-6)
+
+
+@pytest.mark.parametrize("name", ["sphere", "torus"])
+def test_eigsh_mixed_default_accuracy(core, name):
+    """The mixed form's default stops at FP32-level residuals (no FP64 tall
+    iterations): eigenvalues to 1e-5 relative of the reference's ARPACK values."""
+    g = load_golden(name)
+    n, d, m = len(g["X"]), int(g["dim_man"]), int(g["m"])
+    ip, ix = cu(g["indptr"], torch.int32), cu(g["indices"], torch.int32)
+    L = O.laplacian(g["indptr"], g["indices"], n)
+    blocks = L.data[:, None, None] * g["R"]
+    ev, V, info = core.eigsh(ip, ix, cu(blocks), m=m, mode="mixed", scale=np.sqrt(n * d))
+    assert info["refine_iters"] == 0
+    ref = g["evals_Lc"]
+    assert np.abs(ev.cpu().numpy() - ref).max() <= 1e-5 * ref.max()
 
 
 @pytest.mark.parametrize("kind,n,k,m", [("torus", 4000, 20, 60), ("sphere", 3000, 10, 40)])
@@ -62,7 +77,7 @@ def test_eigsh_midsize(core, kind, n, k, m):
     blocks = L.data[:, None, None] * R
     for mode in ("mixed", "fp64"):
         ev, V, info = core.eigsh(cu(ip, torch.int32), cu(ix, torch.int32), cu(blocks), m=m, mode=mode,
-                                 scale=np.sqrt(2 * n))
+                                 tol=1e-11, scale=np.sqrt(2 * n))
         check_pairs(ev.cpu().numpy(), V.cpu().numpy(), ev_ref, V_ref, m, 1e-9, 1e-6)
         assert info["converged"] == m
 

@@ -27,7 +27,7 @@ def test_data_object_matches_reference(RVGP, name, precision):
     g = load_golden(name)
     m = int(g["m"])
     d = RVGP.create_data_object(g["X"], n_neighbors=int(g["k"]), n_eigenpairs=m, precision=precision,
-                                verbose=False)
+                                eig_tol=1e-11, verbose=False)
     assert d.dim_man == int(g["dim_man"]) and d.n == len(g["X"])
     L = d.L
     assert np.array_equal(L.indptr, g["L_indptr"]) and np.array_equal(L.indices, g["L_indices"])
@@ -143,9 +143,10 @@ def test_fit_transform_against_dense_oracle(RVGP, precision):
     m_ref, v_ref = O.predict_f(Phi, y, S, 1.0, Phi_te)
     tol = 1e-7 if precision == "fp64" else 1e-4
     assert np.linalg.norm(mean.ravel() - m_ref) <= tol * np.linalg.norm(m_ref)
-    np.testing.assert_allclose(var.ravel(), v_ref, rtol=1e-5, atol=1e-8)
+    np.testing.assert_allclose(var.ravel(), v_ref, rtol=(1e-5 if precision == "fp64" else 1e-3), atol=1e-8)
     lml_ref = O.lml_dense(Phi, y, S, 1.0)
-    assert abs(gp.log_marginal_likelihood() - lml_ref) <= 1e-6 * abs(lml_ref)
+    ltol = 1e-8 if precision == "fp64" else 1e-5
+    assert abs(gp.log_marginal_likelihood() - lml_ref) <= ltol * abs(lml_ref)
 
 
 def test_fit_optimises_likelihood(RVGP):
