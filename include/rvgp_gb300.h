@@ -35,6 +35,16 @@ long long rvgp_launch_count(void);
  * idx: (n, k) int32, each row ascending by (distance, index). */
 size_t rvgp_knn_workspace(int n, int D, int k);
 int rvgp_knn(const double* X, int n, int D, int k, int* idx, void* workspace, size_t ws_bytes, void* stream);
+/* rvgp_knn without any device allocation, for callers that cannot allocate
+ * device memory when they search (a device-memory budget fixed at start-up,
+ * a host framework that owns the memory pool, no allocation latency allowed).
+ * No counterpart in the reference.  Scratch is a 32 MiB buffer compiled into
+ * the library (held by every GPU that loads it until exit); problems needing
+ * more (rvgp_knn_workspace(n, D, k) > 32 MiB) are rejected with an error.
+ * The first call on a device caches the buffer's address and should come
+ * before any stream capture.  Calls share the buffer: calls that overlap on
+ * the GPU race and must be serialised by the caller. */
+int rvgp_knn_noalloc(const double* X, int n, int D, int k, int* idx, void* stream);
 /* Rows the last rvgp_knn on this workspace settled by the exact fallback scan
  * (synchronises the stream; diagnostics only). */
 int rvgp_knn_fallback_rows(int n, int D, int k, void* workspace, void* stream);

@@ -26,6 +26,7 @@ SIGNATURES = {
     "rvgp_knn_workspace": (c_size_t, [c_int, c_int, c_int]),
     "rvgp_knn": (c_int, [P, c_int, c_int, c_int, P, P, c_size_t, P]),
     "rvgp_knn_fallback_rows": (c_int, [c_int, c_int, c_int, P, P]),
+    "rvgp_knn_noalloc": (c_int, [P, c_int, c_int, c_int, P, P]),
     "rvgp_graph_workspace": (c_size_t, [c_int, c_int]),
     "rvgp_graph_build": (c_int, [P, c_int, c_int, P, P, P, P, P, c_size_t, P]),
     "rvgp_laplacian_values": (c_int, [P, P, c_int, P, P]),

@@ -23,6 +23,7 @@
 #include "common.cuh"
 #include <float.h>
 #include <limits.h>
+#include <mutex>
 
 namespace rvgp {
 namespace {
@@ -372,13 +373,78 @@ RVGP_API int rvgp_knn(const double* X, int n, int D, int k, int* idx, void* work
     case 16: rvgp::note_launch(); knn_screen<16><<<grid, kQB, 0, st>>>(b.Xf, n, p.kc, p.nsplit, b.part_d, b.part_i); break;
     case 32: rvgp::note_launch(); knn_screen<32><<<grid, kQB, 0, st>>>(b.Xf, n, p.kc, p.nsplit, b.part_d, b.part_i); break;
     case 64: rvgp::note_launch(); knn_screen<64><<<grid, kQB, 0, st>>>(b.Xf, n, p.kc, p.nsplit, b.part_d, b.part_i); break;
-    rvgp::note_launch(); default: knn_screen<128><<<grid, kQB, 0, st>>>(b.Xf, n, p.kc, p.nsplit, b.part_d, b.part_i); break;
+    default: rvgp::note_launch(); knn_screen<128><<<grid, kQB, 0, st>>>(b.Xf, n, p.kc, p.nsplit, b.part_d, b.part_i); break;
   }
   rvgp::note_launch(); knn_finish<<<ceil_div(n, 128), 128, 0, st>>>(X, n, D, p.DP, k, p.kc, p.nsplit, b.part_d, b.part_i, b.radius,
                                                idx, b.nflag, b.flag_list);
   rvgp::note_launch(); knn_fallback<<<kNumSMs, kFbThreads, 0, st>>>(X, n, D, k, b.nflag, b.flag_list, idx);
   RVGP_LAUNCH_CHECK("rvgp_knn");
   return RVGP_OK;
+}
+
+// ---------------------------------------------------------------------------
+// kNN without any device allocation.
+//
+// For callers that cannot allocate device memory at the time they need a
+// neighbour search: applications that reserve their whole device-memory
+// budget at start-up and forbid later allocations, hosts that embed this
+// library inside a framework owning the device memory pool without offering
+// an allocator to plug in, and latency-critical loops where an allocation's
+// implicit synchronisation is not acceptable.  They pass inputs and outputs
+// only; the scratch comes from a fixed buffer compiled into this library.
+//
+// Limits and behaviour:
+//  * the buffer holds kNoAllocScratchBytes (32 MiB); a problem whose scratch
+//    (rvgp_knn_workspace(n, D, k)) is larger is rejected with an error.  Every
+//    n up to 70,000 fits at D = 3, k = 20 (up to 50,000 at D = 64, k = 15);
+//    query rvgp_knn_workspace for other shapes;
+//  * the buffer is a file-scope device array, so every GPU that loads this
+//    library keeps those 32 MiB until the process exits;
+//  * the first call on a device looks up the buffer's device address with
+//    that device current and caches it; make that first call before any
+//    stream capture;
+//  * all calls share the one buffer, which keeps the previous call's data:
+//    the search overwrites every part it reads and zeroes its fallback
+//    counter on each call, but two calls whose work overlaps on the GPU (on
+//    different streams, or from different host threads) race on the buffer
+//    and must be serialised by the caller.
+constexpr size_t kNoAllocScratchBytes = size_t(32) << 20;
+static __device__ __align__(256) unsigned char g_knn_scratch[kNoAllocScratchBytes];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mu;
+void* g_scratch_ptr[kMaxDevices] = {};
+}  // namespace
+
+RVGP_API int rvgp_knn_noalloc(const double* X, int n, int D, int k, int* idx, void* stream) {
+  RVGP_CHECK_ARG(n >= 2 && k >= 1 && k < n && D >= 1, "rvgp_knn_noalloc: bad sizes n=%d D=%d k=%d", n, D, k);
+  const size_t need = rvgp_knn_workspace(n, D, k);
+  RVGP_CHECK_ARG(need > 0 && need <= kNoAllocScratchBytes,
+                 "rvgp_knn_noalloc: n=%d, D=%d, k=%d needs %zu bytes of scratch, more than the fixed %zu-byte "
+                 "buffer; use rvgp_knn with a caller-provided workspace",
+                 n, D, k, need, kNoAllocScratchBytes);
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+    rvgp::set_error("rvgp_knn_noalloc: no usable current CUDA device");
+    return RVGP_ELAUNCH;
+  }
+  void* scratch = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_scratch_mu);
+    if (!g_scratch_ptr[dev]) {
+      void* p = nullptr;
+      cudaError_t e = cudaGetSymbolAddress(&p, g_knn_scratch);
+      if (e != cudaSuccess || !p) {
+        rvgp::set_error("rvgp_knn_noalloc: device address of the scratch buffer unavailable: %s",
+                        cudaGetErrorString(e));
+        return RVGP_ELAUNCH;
+      }
+      g_scratch_ptr[dev] = p;
+    }
+    scratch = g_scratch_ptr[dev];
+  }
+  return rvgp_knn(X, n, D, k, idx, scratch, kNoAllocScratchBytes, stream);
 }
 
 // Number of rows the last rvgp_knn call on this workspace sent to the exact
