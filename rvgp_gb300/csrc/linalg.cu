@@ -1,5 +1,6 @@
 // Dense linear algebra kernels (see linalg.cuh).
 #include "linalg.cuh"
+#include "gridsync.cuh"
 #include <math.h>
 #include <limits.h>
 #include <vector>
@@ -178,59 +179,78 @@ __global__ void __launch_bounds__(1024) chol_kernel(T* __restrict__ A, int lda, 
 // ------------------------------------------------------------------ blocked Cholesky (many CTAs)
 constexpr int NB = 32;
 
-// factor the diagonal block [k0, k0+nb) in shared memory (one CTA)
+// Factor the diagonal block [k0, k0+nb) with one warp: lane i keeps row i of
+// the block in registers, L_kj comes by shuffle, so no step waits on memory or
+// a CTA barrier (FP64 latency, not throughput, bounds these small blocks).
 template <typename T>
-__global__ void __launch_bounds__(256) potrf_diag(T* __restrict__ A, int lda, int k0, int nb, int* __restrict__ info) {
-  __shared__ T L[NB][NB + 1];
-  __shared__ int bad;
+__global__ void __launch_bounds__(32) potrf_diag(T* __restrict__ A, int lda, int k0, int nb, int* __restrict__ info) {
   if (*info) return;  // an earlier block already failed
-  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) L[e / nb][e % nb] = A[(size_t)(k0 + e / nb) * lda + k0 + e % nb];
-  if (threadIdx.x == 0) bad = 0;
-  __syncthreads();
-  for (int j = 0; j < nb; ++j) {
-    if (threadIdx.x == 0) {
-      T d = L[j][j];
+  const int lane = threadIdx.x;
+  T a[NB];
+#pragma unroll
+  for (int c = 0; c < NB; ++c)
+    a[c] = (lane < nb && c <= lane) ? A[(size_t)(k0 + lane) * lda + k0 + c] : T(0);
+  int fail = -1;
+#pragma unroll
+  for (int j = 0; j < NB; ++j) {
+    if (j < nb && fail < 0) {
+      const T d = __shfl_sync(0xffffffffu, a[j], j);
       if (!(d > T(0))) {
-        bad = 1;
-        if (*info == 0) *info = k0 + j + 1;
+        fail = j;
       } else {
-        L[j][j] = sqrt(d);
+        const T inv = rsqrt_nr(d), ljj = d * inv;
+        if (lane == j) a[j] = ljj;
+        else if (lane > j) a[j] *= inv;
+#pragma unroll
+        for (int k = j + 1; k < NB; ++k) {
+          const T lkj = __shfl_sync(0xffffffffu, a[j], k);
+          if (lane >= k) a[k] -= a[j] * lkj;
+        }
       }
     }
-    __syncthreads();
-    if (bad) return;
-    for (int i = j + 1 + threadIdx.x; i < nb; i += blockDim.x) L[i][j] /= L[j][j];
-    __syncthreads();
-    const int m = nb - j - 1;
-    for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
-      const int ii = e / m, kk = e % m;
-      if (kk <= ii) L[j + 1 + ii][j + 1 + kk] -= L[j + 1 + ii][j] * L[j + 1 + kk][j];
-    }
-    __syncthreads();
   }
-  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
-    const int i = e / nb, c = e % nb;
-    if (c <= i) A[(size_t)(k0 + i) * lda + k0 + c] = L[i][c];
+  if (fail >= 0) {
+    if (lane == 0) atomicCAS(info, 0, k0 + fail + 1);
+    return;
   }
+#pragma unroll
+  for (int c = 0; c < NB; ++c)
+    if (lane < nb && c <= lane) A[(size_t)(k0 + lane) * lda + k0 + c] = a[c];
 }
 
-// panel: rows [k0+nb, p) of columns [k0, k0+nb) <- A L_kkᵀ⁻¹ (one CTA per NB rows)
+// panel: rows [k0+nb, p) of columns [k0, k0+nb) <- A L_kkᵀ⁻¹, one row per
+// thread with the row in registers and the pivots' reciprocals in shared memory
 template <typename T>
-__global__ void __launch_bounds__(NB) trsm_panel(T* __restrict__ A, int lda, int k0, int nb, int p,
+__global__ void __launch_bounds__(64) trsm_panel(T* __restrict__ A, int lda, int k0, int nb, int p,
                                                  const int* __restrict__ info) {
   __shared__ T L[NB][NB + 1];
+  __shared__ T inv[NB];
   if (*info) return;
   for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) L[e / nb][e % nb] = A[(size_t)(k0 + e / nb) * lda + k0 + e % nb];
   __syncthreads();
-  const int r = k0 + nb + blockIdx.x * NB + threadIdx.x;
+  for (int c = threadIdx.x; c < nb; c += blockDim.x) inv[c] = rcp_nr(L[c][c]);
+  __syncthreads();
+  const int r = k0 + nb + blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= p) return;
   T x[NB];
-  for (int c = 0; c < nb; ++c) {
-    T v = A[(size_t)r * lda + k0 + c];
-    for (int t = 0; t < c; ++t) v -= x[t] * L[c][t];
-    x[c] = v / L[c][c];
+#pragma unroll
+  for (int c = 0; c < NB; ++c) {
+    if (c < nb) {
+      // four independent partial sums keep the dependent FP64 chain short
+      T v0 = A[(size_t)r * lda + k0 + c], v1 = T(0), v2 = T(0), v3 = T(0);
+#pragma unroll
+      for (int t = 0; t < c; t += 4) {
+        v0 -= x[t] * L[c][t];
+        if (t + 1 < c) v1 -= x[t + 1] * L[c][t + 1];
+        if (t + 2 < c) v2 -= x[t + 2] * L[c][t + 2];
+        if (t + 3 < c) v3 -= x[t + 3] * L[c][t + 3];
+      }
+      x[c] = ((v0 + v1) + (v2 + v3)) * inv[c];
+    }
   }
-  for (int c = 0; c < nb; ++c) A[(size_t)r * lda + k0 + c] = x[c];
+#pragma unroll
+  for (int c = 0; c < NB; ++c)
+    if (c < nb) A[(size_t)r * lda + k0 + c] = x[c];
 }
 
 // trailing update of the lower part: A_ij -= A_ik A_jkᵀ for blocks (i, j), j <= i, both > k
@@ -259,21 +279,33 @@ __global__ void __launch_bounds__(256) syrk_update(T* __restrict__ A, int lda, i
 }
 
 // ------------------------------------------------------------------ triangular inverse (warp per column)
+// Column j of L⁻¹ by column-oriented forward substitution: lane l owns the rows
+// k ≡ l (mod 32) of the running right-hand side y (shared memory) and their
+// reciprocal pivots.  Step i: the owner of row i forms x_i = y_i / L_ii, one
+// shuffle broadcasts it, every lane updates its own rows y_k -= L_ki x_i.  No
+// lane reads another lane's rows, so the dependent chain per step is a
+// multiply, a shuffle and one multiply-add.
 template <typename T>
-__global__ void trinv_kernel(const T* __restrict__ L, int ldl, int p, T* __restrict__ X, int ldx) {
+__global__ void trinv_kernel(const T* __restrict__ L, int ldl, int p, T* __restrict__ X, int ldx, int warps) {
+  extern __shared__ unsigned char smem_raw[];
+  T* y = reinterpret_cast<T*>(smem_raw) + (size_t)(threadIdx.x >> 5) * 2 * p;
+  T* rinv = y + p;
   const int lane = threadIdx.x & 31;
-  const int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int j = blockIdx.x * warps + (threadIdx.x >> 5);
   if (j >= p) return;
   for (int i = lane; i < j; i += 32) X[(size_t)i * ldx + j] = T(0);
-  if (lane == 0) X[(size_t)j * ldx + j] = T(1) / L[(size_t)j * ldl + j];
-  __syncwarp();
-  for (int i = j + 1; i < p; ++i) {
-    T s = T(0);
-    for (int k = j + lane; k < i; k += 32) s += L[(size_t)i * ldl + k] * X[(size_t)k * ldx + j];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0) X[(size_t)i * ldx + j] = -s / L[(size_t)i * ldl + i];
-    __syncwarp();
+  for (int k = j + ((lane - j) & 31); k < p; k += 32) {
+    y[k] = k == j ? T(1) : T(0);
+    rinv[k] = rcp_nr(L[(size_t)k * ldl + k]);
+  }
+  for (int i = j; i < p; ++i) {
+    T xi = T(0);
+    if (lane == (i & 31)) {
+      xi = y[i] * rinv[i];
+      X[(size_t)i * ldx + j] = xi;
+    }
+    xi = __shfl_sync(0xffffffffu, xi, i & 31);
+    for (int k = i + 1 + ((lane - i - 1) & 31); k < p; k += 32) y[k] -= L[(size_t)k * ldl + i] * xi;
   }
 }
 
@@ -298,10 +330,20 @@ __device__ __forceinline__ void rot_of(const T* __restrict__ H, int p, const int
   Q = max(i, m);
   const T a = H[(size_t)P * p + P], b = H[(size_t)Q * p + Q], c = H[(size_t)P * p + Q];
   T cs = T(1), sn = T(0);
-  if (c != T(0) && fabs((double)c) > Eps<T>::v * 1e-3 * sqrt(fabs((double)a) * fabs((double)b))) {
-    const T theta = (b - a) / (T(2) * c);
-    const T t = (theta >= T(0) ? T(1) : T(-1)) / (fabs(theta) + sqrt(theta * theta + T(1)));
-    cs = T(1) / sqrt(t * t + T(1));
+  const double tiny = Eps<T>::v * 1e-3;
+  if (c != T(0) && (double)c * (double)c > tiny * tiny * fabs((double)a) * fabs((double)b)) {
+    // Rutishauser's stable rotation, with reciprocals / square roots from
+    // short-chain Newton refinements: t = sign(θ)/(|θ| + sqrt(θ² + 1)).
+    const T theta = (b - a) * rcp_nr(T(2) * c);
+    T t;
+    if (fabs((double)theta) > 1e15) {
+      t = T(0.5) * rcp_nr(theta);  // sqrt(θ² + 1) = |θ| to working precision
+    } else {
+      const T q = fma(theta, theta, T(1));
+      const T root = q * rsqrt_nr(q);
+      t = (theta >= T(0) ? T(1) : T(-1)) * rcp_nr(fabs(theta) + root);
+    }
+    cs = rsqrt_nr(fma(t, t, T(1)));
     sn = t * cs;
   }
   if (i == P) {
@@ -401,11 +443,21 @@ __global__ void __launch_bounds__(1024) offnorm_kernel(const T* __restrict__ H, 
   }
 }
 
-// sort the diagonal ascending (ties by index) and permute the columns of V
+// sort the diagonal ascending (ties by index) and permute the columns of V (one CTA)
+template <typename T>
+__device__ void sort_eig_block(const T* __restrict__ H, const T* __restrict__ V, int p, T* __restrict__ w,
+                               T* __restrict__ Vout, unsigned char* smem);
+
 template <typename T>
 __global__ void __launch_bounds__(1024) sort_eig(const T* __restrict__ H, const T* __restrict__ V, int p,
                                                  T* __restrict__ w, T* __restrict__ Vout) {
   extern __shared__ unsigned char smem[];
+  sort_eig_block<T>(H, V, p, w, Vout, smem);
+}
+
+template <typename T>
+__device__ void sort_eig_block(const T* __restrict__ H, const T* __restrict__ V, int p, T* __restrict__ w,
+                               T* __restrict__ Vout, unsigned char* smem) {
   T* key = reinterpret_cast<T*>(smem);
   int* idx = reinterpret_cast<int*>(key + 2048);
   int P2 = 1;
@@ -442,6 +494,121 @@ __global__ void __launch_bounds__(1024) sort_eig(const T* __restrict__ H, const 
   for (long long e = threadIdx.x; e < (long long)p * p; e += blockDim.x) {
     const int r = (int)(e / p), c = (int)(e % p);
     Vout[e] = V[(size_t)r * p + idx[c]];
+  }
+}
+
+// The whole Jacobi eigensolve in one cooperative launch: symmetrise, then up to
+// max_sweeps sweeps of p-1 rounds (rotation parameters, barrier, rotate H and
+// V, barrier), with the off-norm test of each sweep reduced in a fixed order so
+// every CTA takes the same decision; CTA 0 finally sorts.  Any barrier timeout
+// makes every CTA leave early with *err set.
+template <typename T>
+__global__ void __launch_bounds__(256) jacobi_persistent(T* H, T* Hb, T* Va, T* Vb, int p,
+                                                         const int* __restrict__ partner, int rounds, double* part,
+                                                         int max_sweeps, double tol2, unsigned int* bar, int* err,
+                                                         int* sweeps_out, T* w, T* Vout) {
+  extern __shared__ unsigned char smem[];
+  __shared__ double red[2][256];
+  __shared__ double s_off, s_tot;
+  T* coef = reinterpret_cast<T*>(smem);                      // 2p rotation coefficients
+  int2* pq = reinterpret_cast<int2*>(coef + 2 * (size_t)p);  // p index pairs
+  const unsigned G = gridDim.x;
+  const long long pp = (long long)p * p;
+  const long long gtid = blockIdx.x * (long long)blockDim.x + threadIdx.x, gsz = (long long)G * blockDim.x;
+  for (long long e = gtid; e < pp; e += gsz) {
+    const int i = (int)(e / p), j = (int)(e % p);
+    if (j > i) {
+      const T v = (H[(size_t)i * p + j] + H[(size_t)j * p + i]) * T(0.5);
+      H[(size_t)i * p + j] = v;
+      H[(size_t)j * p + i] = v;
+    }
+    Va[e] = i == j ? T(1) : T(0);
+  }
+  if (!grid_barrier(bar, err, G)) return;
+  T *h0 = H, *h1 = Hb, *v0 = Va, *v1 = Vb;
+  int used = 0;
+  for (int sweep = 0; sweep < max_sweeps; ++sweep) {
+    double off = 0.0, tot = 0.0;
+    for (long long e = gtid; e < pp; e += gsz) {
+      const double v = (double)h0[e];
+      tot += v * v;
+      if (e / p != e % p) off += v * v;
+    }
+    red[0][threadIdx.x] = off;
+    red[1][threadIdx.x] = tot;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+      if (threadIdx.x < s) {
+        red[0][threadIdx.x] += red[0][threadIdx.x + s];
+        red[1][threadIdx.x] += red[1][threadIdx.x + s];
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      part[2 * blockIdx.x] = red[0][0];
+      part[2 * blockIdx.x + 1] = red[1][0];
+    }
+    if (!grid_barrier(bar, err, G)) return;
+    if (threadIdx.x == 0) {
+      double a = 0.0, b = 0.0;
+      for (unsigned q = 0; q < G; ++q) {
+        a += part[2 * q];
+        b += part[2 * q + 1];
+      }
+      s_off = a;
+      s_tot = b;
+    }
+    __syncthreads();
+    if (!(s_off > tol2 * s_tot)) break;
+    for (int r = 0; r < rounds; ++r) {
+      const int* prt = partner + (size_t)r * p;
+      // every CTA derives the round's p rotation coefficients itself (shared
+      // memory): one grid barrier per round instead of two
+      for (int i = threadIdx.x; i < p; i += blockDim.x) {
+        T c1, c2;
+        int P, Q;
+        rot_of(h0, p, prt, i, c1, c2, P, Q);
+        coef[2 * i] = c1;
+        coef[2 * i + 1] = c2;
+        pq[i] = make_int2(P, Q);
+      }
+      __syncthreads();
+      for (long long e = gtid; e < 2 * pp; e += gsz) {
+        if (e < pp) {
+          const int i = (int)(e / p), j = (int)(e % p);
+          const T ci1 = coef[2 * i], ci2 = coef[2 * i + 1], cj1 = coef[2 * j], cj2 = coef[2 * j + 1];
+          const int2 a = pq[i], b = pq[j];
+          T v;
+          if (i != j && prt[i] == j) {
+            v = T(0);
+          } else {
+            v = ci1 * (cj1 * h0[(size_t)a.x * p + b.x] + cj2 * h0[(size_t)a.x * p + b.y]);
+            if (ci2 != T(0)) v += ci2 * (cj1 * h0[(size_t)a.y * p + b.x] + cj2 * h0[(size_t)a.y * p + b.y]);
+          }
+          h1[e] = v;
+        } else {
+          const long long f = e - pp;
+          const int rr = (int)(f / p), i = (int)(f % p);
+          const T c1 = coef[2 * i], c2 = coef[2 * i + 1];
+          const int2 a = pq[i];
+          T v = c1 * v0[(size_t)rr * p + a.x];
+          if (c2 != T(0)) v += c2 * v0[(size_t)rr * p + a.y];
+          v1[f] = v;
+        }
+      }
+      if (!grid_barrier(bar, err, G)) return;
+      T* t = h0;
+      h0 = h1;
+      h1 = t;
+      t = v0;
+      v0 = v1;
+      v1 = t;
+    }
+    ++used;
+  }
+  if (blockIdx.x == 0) {
+    sort_eig_block<T>(h0, v0, p, w, Vout, smem);
+    if (threadIdx.x == 0) *sweeps_out = used;
   }
 }
 
@@ -563,18 +730,14 @@ int gemm_nn(const T* A, int lda, const T* B, int ldb, long long N, int p, int q,
 
 template <typename T>
 int cholesky(T* A, int lda, int p, int* info, cudaStream_t st) {
-  if (p <= 64) {
-    rvgp::note_launch(); chol_kernel<T><<<1, 1024, 0, st>>>(A, lda, p, info);
-    return check_launch("cholesky");
-  }
   cudaMemsetAsync(info, 0, sizeof(int), st);
   for (int k0 = 0; k0 < p; k0 += NB) {
     const int nb = std::min(NB, p - k0);
-    rvgp::note_launch(); potrf_diag<T><<<1, 256, 0, st>>>(A, lda, k0, nb, info);
+    rvgp::note_launch(); potrf_diag<T><<<1, 32, 0, st>>>(A, lda, k0, nb, info);
     const int rest = p - k0 - nb;
     if (rest <= 0) break;
     const int rb = ceil_div(rest, NB);
-    rvgp::note_launch(); trsm_panel<T><<<rb, NB, 0, st>>>(A, lda, k0, nb, p, info);
+    rvgp::note_launch(); trsm_panel<T><<<ceil_div(rest, 64), 64, 0, st>>>(A, lda, k0, nb, p, info);
     rvgp::note_launch(); syrk_update<T><<<dim3(rb, rb), 256, 0, st>>>(A, lda, k0, nb, p, info);
   }
   return check_launch("cholesky");
@@ -582,15 +745,20 @@ int cholesky(T* A, int lda, int p, int* info, cudaStream_t st) {
 
 template <typename T>
 int tri_inv_lower(const T* L, int ldl, int p, T* Linv, int ldi, cudaStream_t st) {
-  rvgp::note_launch(); trinv_kernel<T><<<ceil_div((long long)p * 32, 128), 128, 0, st>>>(L, ldl, p, Linv, ldi);
+  // shared memory: 2p values per warp, at most 48 KB per CTA
+  const int warps = (int)std::max<size_t>(1, std::min<size_t>(4, (48 * 1024) / (2 * sizeof(T) * (size_t)p)));
+  const size_t smem = sizeof(T) * 2 * (size_t)warps * p;
+  rvgp::note_launch(); trinv_kernel<T><<<ceil_div(p, warps), 32 * warps, smem, st>>>(L, ldl, p, Linv, ldi, warps);
   return check_launch("tri_inv_lower");
 }
+
+constexpr int kMaxCoopGrid = 1024;
 
 template <typename T>
 size_t jacobi_workspace(int p) {
   const int P = p + (p & 1);
   return sizeof(T) * (size_t)p * p * 3 + sizeof(int) * (size_t)(P - 1) * p + 2 * sizeof(double) +
-         sizeof(T) * 2 * (size_t)p + sizeof(int2) * (size_t)p + 8192;
+         sizeof(T) * 2 * (size_t)p + sizeof(int2) * (size_t)p + sizeof(double) * 2 * kMaxCoopGrid + sizeof(unsigned int) * (kMaxCoopGrid + 1) + 8192;
 }
 
 template <typename T>
@@ -617,6 +785,41 @@ int jacobi_eigh(T* H, int p, T* w, T* V, int max_sweeps, double tol, int* sweeps
   const std::vector<int>& tab = schedule(p);
   cudaMemcpyAsync(part, tab.data(), sizeof(int) * tab.size(), cudaMemcpyHostToDevice, st);
   const long long pp = (long long)p * p;
+
+  // one cooperative launch for all sweeps when the device supports it
+  double* gpart = W.take<double>(2 * (size_t)kMaxCoopGrid);
+  unsigned int* bar = W.take<unsigned int>(kMaxCoopGrid + 1);
+  int* flags = W.take<int>(2);  // [0] barrier error, [1] sweeps used
+  // dynamic shared memory: the round's coefficients during the sweeps, the sort buffers at the end
+  const size_t smem = std::max(sizeof(T) * 2 * (size_t)p + sizeof(int2) * (size_t)p,
+                               2048 * sizeof(T) + 2048 * sizeof(int));
+  int G = smem <= 48 * 1024 ? std::min(cooperative_grid(jacobi_persistent<T>, 256, smem), kMaxCoopGrid) : 0;
+  if (G > 0 && p > 1) {
+    cudaMemsetAsync(bar, 0, (G + 1) * sizeof(unsigned int), st);
+    cudaMemsetAsync(flags, 0, 2 * sizeof(int), st);
+    T* Hp = H;
+    int pv = p, rv = rounds, ms = max_sweeps;
+    double t2 = tol * tol;
+    int* err_dev = flags;
+    int* sweeps_dev = flags + 1;
+    void* args[] = {&Hp, &Hb, &Va, &Vb, &pv, &part, &rv, &gpart, &ms, &t2, &bar, &err_dev, &sweeps_dev, &w, &V};
+    rvgp::note_launch();
+    cudaError_t e = cudaLaunchCooperativeKernel((const void*)jacobi_persistent<T>, dim3(G), dim3(256), args, smem, st);
+    if (e != cudaSuccess) {
+      set_error("jacobi_eigh: cooperative launch failed: %s", cudaGetErrorString(e));
+      return RVGP_ELAUNCH;
+    }
+    int hv[2] = {0, 0};
+    cudaMemcpyAsync(hv, flags, sizeof(hv), cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return check_launch("jacobi_eigh");
+    if (hv[0] != 0) {
+      set_error("jacobi_eigh: a grid barrier timed out");
+      return RVGP_ELAUNCH;
+    }
+    if (sweeps_used) *sweeps_used = hv[1];
+    return check_launch("jacobi_eigh");
+  }
+
   rvgp::note_launch(); set_identity<T><<<ceil_div(pp, 256), 256, 0, st>>>(Va, p);
   rvgp::note_launch(); symmetrise<T><<<ceil_div(pp, 256), 256, 0, st>>>(H, p);
   T *h0 = H, *h1 = Hb, *v0 = Va, *v1 = Vb;
@@ -636,7 +839,6 @@ int jacobi_eigh(T* H, int p, T* w, T* V, int max_sweeps, double tol, int* sweeps
     ++used;
   }
   if (sweeps_used) *sweeps_used = used;
-  const size_t smem = 2048 * sizeof(T) + 2048 * sizeof(int);
   rvgp::note_launch(); sort_eig<T><<<1, 1024, smem, st>>>(h0, v0, p, w, V);
   return check_launch("jacobi_eigh");
 }

@@ -10,6 +10,35 @@
 
 namespace rvgp {
 
+// 1/sqrt(d) for d > 0 in FP64 with a short dependency chain: an FP32 estimate
+// refined by two Newton-Raphson steps y <- y + (y/2)(1 - d y²), each three
+// dependent FP64 operations (the FP64 divide and square root are long chains
+// of dependent operations on GB300).  Falls back to 1/sqrt(d) when d is
+// outside the normal FP32 range.  Relative error ~1e-16.
+__device__ __forceinline__ double rsqrt_nr(double d) {
+  if (!(d > 1e-30 && d < 1e30)) return 1.0 / sqrt(d);
+  double y = (double)rsqrtf((float)d);
+  double a = d * y;
+  double r = fma(-a, y, 1.0);
+  y = fma(0.5 * y, r, y);
+  a = d * y;
+  r = fma(-a, y, 1.0);
+  return fma(0.5 * y, r, y);
+}
+__device__ __forceinline__ float rsqrt_nr(float d) { return rsqrtf(d); }
+
+// 1/x in FP64 with an FP32 estimate and two Newton steps y <- y (2 - x y).
+__device__ __forceinline__ double rcp_nr(double x) {
+  const double ax = fabs(x);
+  if (!(ax > 1e-30 && ax < 1e30)) return 1.0 / x;
+  double y = (double)(1.0f / (float)x);
+  double e = fma(-x, y, 1.0);
+  y = fma(y, e, y);
+  e = fma(-x, y, 1.0);
+  return fma(y, e, y);
+}
+__device__ __forceinline__ float rcp_nr(float x) { return 1.0f / x; }
+
 // C (p x q, ldc) = alpha * Aᵀ B + beta * C,  A: N x p (lda), B: N x q (ldb).
 template <typename T>
 size_t gram_workspace(long long N, int p, int q);
