@@ -195,16 +195,17 @@ def run_ours(args):
     import torch.distributed as dist
     from rvgp_gb300 import _core
 
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
+    from rvgp_gb300 import replicas
+
+    rank, world, local = replicas.world()
     if world > 1:
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
     _core.require_cuda()
     wl = WORKLOADS[args.workload]
-    X, train, test = make_inputs(wl, seed=rank)
-    V = make_field(X, wl, seed=rank)
+    seed = replicas.replica_seed(0, rank)  # rank 0 uses seed 0, the reference arm's inputs
+    X, train, test = make_inputs(wl, seed=seed)
+    V = make_field(X, wl, seed=seed)
     Xd = torch.as_tensor(X, device="cuda")
     Vd = torch.as_tensor(V, device="cuda")
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MiB > L2
@@ -236,10 +237,7 @@ def run_ours(args):
     t_step = float(np.mean(times))
     stages = {}
     pipeline(Xd, Vd, train, test, wl, "mixed", timings=stages)  # untimed step with a per-stage breakdown
-    if world > 1:
-        tt = torch.tensor([t_step], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_step = float(tt.item())
+    t_step = replicas.max_over_ranks(t_step, device="cuda")
     out = {}
     if rank == 0:
         # the plain FP64 form of the same step, for the metric's comparison
@@ -286,7 +284,7 @@ def run_ours(args):
             "fp64_form_s": round(float(np.mean(fp64_times)), 5) if fp64_times else None,
             "mixed_speedup_vs_fp64": round(float(np.mean(fp64_times)) / t_step, 3) if fp64_times else None,
             "pred_rel_err_vs_fp64": pred_err,
-            "pipelines_per_s": round(world / t_step, 4),
+            "pipelines_per_s": round(replicas.job_throughput(t_step, world), 4),
             "stages_s": {k_: (round(v, 5) if isinstance(v, float) else v) for k_, v in stages.items()},
             "e2e": {"value": round(float(np.mean(e2e_times)), 5) if e2e_times else None, "unit": "s",
                     "h2d_bytes_per_step": int(X.nbytes + V.nbytes),

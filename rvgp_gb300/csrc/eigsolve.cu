@@ -18,9 +18,9 @@
 // Two precisions:
 //   plain (mode 0): everything in FP64;
 //   mixed (mode 1): SpMM and the tall products in FP32 (Gram partial sums
-//             reduced in FP64), the p x p Cholesky / Rayleigh-Ritz eigensolve in
-//             FP64, then FP64 refinement iterations starting from the FP32
-//             subspace until the FP64 tolerance is met.
+//             reduced in FP64), the p x p Cholesky in FP64, the Rayleigh-Ritz
+//             eigensolve in FP32, then FP64 refinement iterations starting
+//             from the FP32 subspace only if the FP64 tolerance asks for it.
 #include "common.cuh"
 #include "linalg.cuh"
 #include <math.h>
@@ -163,6 +163,7 @@ struct Small {
   size_t cn_bytes;
   float* Bf;
   double* Bd;
+  float *Hf, *thf;  // FP32 Rayleigh-Ritz matrix and its eigenvalues (mixed form)
   float* nf;
   double* nd;
 };
@@ -310,13 +311,20 @@ int rayleigh_ritz(const Problem& P, Block<T>& B, Small& s, Stats& stt, int max_s
   ++stt.spmm;
   TRY(gram_any(B.V, B.W, N, p, s.H, s, st));
   int used = 0;
-  // off(H) tolerance: the Ritz vectors of an FP32 block are accurate to ~1e-7 anyway
-  const double jtol = sizeof(T) == 4 ? 1e-10 : 1e-13;
   cudaEventRecord(ev.e[3], st);
-  TRY(jacobi_eigh<double>(s.H, p, s.theta, s.Q, max_sweeps, jtol, &used, s.jac_ws, s.jac_bytes, st));
+  if (sizeof(T) == 4) {
+    // FP32 block: the FP64-reduced H is diagonalised in FP32 (an FP64 Jacobi
+    // rotation costs ~64x an FP32 one on GB300).  Stop at off(H) <= 4e-6 ||H||_F,
+    // below the FP32 stage's residual tolerance and above FP32 rounding.
+    TRY(convert_f64_to_f32(s.H, p, s.Hf, p, p, p, st));
+    TRY(jacobi_eigh<float>(s.Hf, p, s.thf, s.Bf, std::min(max_sweeps, 12), 4e-6, &used, s.jac_ws, s.jac_bytes, st));
+    TRY(convert_f32_to_f64(s.thf, 1, s.theta, 1, p, 1, st));
+  } else {
+    TRY(jacobi_eigh<double>(s.H, p, s.theta, s.Q, max_sweeps, 1e-13, &used, s.jac_ws, s.jac_bytes, st));
+    rvgp::note_launch(); copy_to<T><<<ceil_div((long long)p * p, 256), 256, 0, st>>>(s.Q, (long long)p * p, Bmat<T>(s));
+  }
   cudaEventRecord(ev.e[4], st);
   stt.sweeps += used;
-  rvgp::note_launch(); copy_to<T><<<ceil_div((long long)p * p, 256), 256, 0, st>>>(s.Q, (long long)p * p, Bmat<T>(s));
   TRY(gemm_nn<T>(B.V, p, Bmat<T>(s), p, N, p, p, B.T1, p, T(1), T(0), st));
   TRY(gemm_nn<T>(B.W, p, Bmat<T>(s), p, N, p, p, B.T2, p, T(1), T(0), st));
   std::swap(B.V, B.T1);
@@ -431,6 +439,8 @@ Layout carve(Workspace& ws, long long N, int p, int mode) {
   s.Bd = ws.take<double>(pp);
   s.nf = ws.take<float>(p);
   s.nd = ws.take<double>(p);
+  s.Hf = ws.take<float>(pp);
+  s.thf = ws.take<float>(p);
   s.gram_bytes = std::max(gram_workspace<float>(N, p, p), gram_workspace<double>(N, p, p));
   s.gram_ws = ws.take<char>(s.gram_bytes);
   s.jac_bytes = jacobi_workspace<double>(p);

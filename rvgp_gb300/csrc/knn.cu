@@ -11,7 +11,8 @@
 //                 radius R = max |x - c| (two-stage deterministic reductions).
 //   2. screen   : FP32 brute force.  CTA = 128 queries x one slice of the
 //                 candidates staged through shared memory; every query keeps its
-//                 kc = k + 8 smallest FP32 squared distances.
+//                 kc smallest FP32 squared distances in a register-resident
+//                 sorted list (kc = k + 8 rounded up to 16, 32, 48 or 72).
 //   3. finish   : merge the slices, rescore the kc survivors in exact FP64, sort
 //                 by (d2, index) and certify: with u = 2^-24 the FP32 distance f
 //                 of any pair satisfies  true >= (f/(1+g) - 4.01 u R)/(1+u),
@@ -103,7 +104,97 @@ __global__ void prep_radius(const double* __restrict__ part_r2, int nblk, double
   *radius = sqrt(m) * (1.0 + 1e-12);
 }
 
-// Keeps the kc smallest values seen; "worst" is the largest kept value once full.
+// The KC smallest (value, index) pairs seen, ascending, held in registers:
+// every position is a compile-time index, so nothing spills to local memory.
+// Empty slots hold (FLT_MAX, -1).
+template <int KC>
+struct RegTop {
+  float d[KC];
+  int i[KC];
+  __device__ __forceinline__ void init() {
+#pragma unroll
+    for (int r = 0; r < KC; ++r) {
+      d[r] = FLT_MAX;
+      i[r] = -1;
+    }
+  }
+  __device__ __forceinline__ float worst() const { return d[KC - 1]; }
+  // Insert keeping the order (equal values stay in arrival order); call only
+  // when v < worst().  Each position decides from the old values of itself and
+  // its predecessor, so the KC selects are independent of one another.
+  __device__ __forceinline__ void insert(float v, int idx) {
+#pragma unroll
+    for (int r = KC - 1; r > 0; --r) {
+      const bool shift = d[r - 1] > v;
+      const bool here = d[r] > v;
+      d[r] = shift ? d[r - 1] : (here ? v : d[r]);
+      i[r] = shift ? i[r - 1] : (here ? idx : i[r]);
+    }
+    if (d[0] > v) {
+      d[0] = v;
+      i[0] = idx;
+    }
+  }
+};
+
+template <int DP, int KC>
+__global__ void __launch_bounds__(kQB) knn_screen(const float* __restrict__ Xf, int n, int nsplit,
+                                                  float* __restrict__ part_d, int* __restrict__ part_i) {
+  constexpr int kTile = kTileElems / DP;
+  __shared__ float tile[kTile * DP];
+  const int q = blockIdx.x * kQB + threadIdx.x;
+  const int split = blockIdx.y;
+  const long long chunk = ((long long)n + nsplit - 1) / nsplit;
+  const int c0 = (int)min((long long)n, split * chunk);
+  const int c1 = (int)min((long long)n, c0 + chunk);
+  float xq[DP];
+#pragma unroll
+  for (int j = 0; j < DP; ++j) xq[j] = q < n ? Xf[(size_t)q * DP + j] : 0.f;
+  RegTop<KC> L;
+  L.init();
+  for (int t0 = c0; t0 < c1; t0 += kTile) {
+    const int tn = min(kTile, c1 - t0);
+    __syncthreads();
+    for (int e = threadIdx.x; e < tn * DP; e += kQB) tile[e] = Xf[(size_t)t0 * DP + e];
+    __syncthreads();
+    if (q < n) {
+      for (int c = 0; c < tn; ++c) {
+        float acc = 0.f;
+#pragma unroll
+        for (int j = 0; j < DP; ++j) {
+          float df = xq[j] - tile[c * DP + j];
+          acc = fmaf(df, df, acc);
+        }
+        const int ci = t0 + c;
+        if (acc < L.worst() && ci != q) L.insert(acc, ci);
+      }
+    }
+  }
+  if (q < n) {
+    const size_t base = ((size_t)q * nsplit + split) * KC;
+#pragma unroll
+    for (int r = 0; r < KC; ++r) {
+      part_d[base + r] = L.d[r];
+      part_i[base + r] = L.i[r];
+    }
+  }
+}
+
+__device__ __forceinline__ double exact_d2(const double* __restrict__ X, int D, int a, int b) {
+  double acc = 0.0;
+  for (int j = 0; j < D; ++j) {
+    double df = __dsub_rn(X[(size_t)a * D + j], X[(size_t)b * D + j]);
+    acc = __dadd_rn(acc, __dmul_rn(df, df));
+  }
+  return acc;
+}
+
+__device__ __forceinline__ bool lex_less(double da, int ia, double db, int ib) {
+  return da < db || (da == db && ia < ib);
+}
+
+// Keeps the kc smallest values seen (runtime kc, arrays in local memory; the
+// merge runs once per query, so its cost is small next to the screen).
 struct TopList {
   float d[kMaxKC];
   int i[kMaxKC];
@@ -130,61 +221,6 @@ struct TopList {
     }
   }
 };
-
-template <int DP>
-__global__ void __launch_bounds__(kQB) knn_screen(const float* __restrict__ Xf, int n, int kc, int nsplit,
-                                                  float* __restrict__ part_d, int* __restrict__ part_i) {
-  constexpr int kTile = kTileElems / DP;
-  __shared__ float tile[kTile * DP];
-  const int q = blockIdx.x * kQB + threadIdx.x;
-  const int split = blockIdx.y;
-  const long long chunk = ((long long)n + nsplit - 1) / nsplit;
-  const int c0 = (int)min((long long)n, split * chunk);
-  const int c1 = (int)min((long long)n, c0 + chunk);
-  float xq[DP];
-#pragma unroll
-  for (int j = 0; j < DP; ++j) xq[j] = q < n ? Xf[(size_t)q * DP + j] : 0.f;
-  TopList L;
-  L.init(kc);
-  for (int t0 = c0; t0 < c1; t0 += kTile) {
-    const int tn = min(kTile, c1 - t0);
-    __syncthreads();
-    for (int e = threadIdx.x; e < tn * DP; e += kQB) tile[e] = Xf[(size_t)t0 * DP + e];
-    __syncthreads();
-    if (q < n) {
-      for (int c = 0; c < tn; ++c) {
-        float acc = 0.f;
-#pragma unroll
-        for (int j = 0; j < DP; ++j) {
-          float df = xq[j] - tile[c * DP + j];
-          acc = fmaf(df, df, acc);
-        }
-        const int ci = t0 + c;
-        if (ci != q && (L.cnt < kc || acc < L.worst)) L.push(acc, ci);
-      }
-    }
-  }
-  if (q < n) {
-    size_t base = ((size_t)q * nsplit + split) * kc;
-    for (int r = 0; r < kc; ++r) {
-      part_d[base + r] = r < L.cnt ? L.d[r] : FLT_MAX;
-      part_i[base + r] = r < L.cnt ? L.i[r] : -1;
-    }
-  }
-}
-
-__device__ __forceinline__ double exact_d2(const double* __restrict__ X, int D, int a, int b) {
-  double acc = 0.0;
-  for (int j = 0; j < D; ++j) {
-    double df = __dsub_rn(X[(size_t)a * D + j], X[(size_t)b * D + j]);
-    acc = __dadd_rn(acc, __dmul_rn(df, df));
-  }
-  return acc;
-}
-
-__device__ __forceinline__ bool lex_less(double da, int ia, double db, int ib) {
-  return da < db || (da == db && ia < ib);
-}
 
 __global__ void knn_finish(const double* __restrict__ X, int n, int D, int DP, int k, int kc, int nsplit,
                            const float* __restrict__ part_d, const int* __restrict__ part_i,
@@ -298,6 +334,24 @@ int padded_dim(int D) {
   return -1;
 }
 
+// survivors kept per slice: k + kExtra rounded up to a register-list size
+int kc_bucket(int k) {
+  const int c = k + kExtra;
+  return c <= 16 ? 16 : c <= 32 ? 32 : c <= 48 ? 48 : 72;
+}
+
+template <int KC>
+void launch_screen(int DP, dim3 grid, cudaStream_t st, const float* Xf, int n, int nsplit, float* pd, int* pi) {
+  switch (DP) {
+    case 4: knn_screen<4, KC><<<grid, kQB, 0, st>>>(Xf, n, nsplit, pd, pi); break;
+    case 8: knn_screen<8, KC><<<grid, kQB, 0, st>>>(Xf, n, nsplit, pd, pi); break;
+    case 16: knn_screen<16, KC><<<grid, kQB, 0, st>>>(Xf, n, nsplit, pd, pi); break;
+    case 32: knn_screen<32, KC><<<grid, kQB, 0, st>>>(Xf, n, nsplit, pd, pi); break;
+    case 64: knn_screen<64, KC><<<grid, kQB, 0, st>>>(Xf, n, nsplit, pd, pi); break;
+    default: knn_screen<128, KC><<<grid, kQB, 0, st>>>(Xf, n, nsplit, pd, pi); break;
+  }
+}
+
 struct KnnPlan {
   int DP, kc, nsplit, nblk_prep;
 };
@@ -305,7 +359,7 @@ struct KnnPlan {
 KnnPlan plan(int n, int D, int k) {
   KnnPlan p;
   p.DP = padded_dim(D);
-  p.kc = min(k + kExtra, n - 1);
+  p.kc = kc_bucket(k);
   int qblocks = ceil_div(n, kQB);
   p.nsplit = max(1, min(16, ceil_div(4 * kNumSMs, qblocks)));
   p.nblk_prep = min(kNumSMs * 2, max(1, ceil_div(n, 256)));
@@ -367,16 +421,15 @@ RVGP_API int rvgp_knn(const double* X, int n, int D, int k, int* idx, void* work
   rvgp::note_launch(); prep_radius<<<1, 32, 0, st>>>(b.part_r2, p.nblk_prep, b.radius);
   cudaMemsetAsync(b.nflag, 0, sizeof(int), st);
   dim3 grid(ceil_div(n, kQB), p.nsplit);
-  switch (p.DP) {
-    case 4: rvgp::note_launch(); knn_screen<4><<<grid, kQB, 0, st>>>(b.Xf, n, p.kc, p.nsplit, b.part_d, b.part_i); break;
-    case 8: rvgp::note_launch(); knn_screen<8><<<grid, kQB, 0, st>>>(b.Xf, n, p.kc, p.nsplit, b.part_d, b.part_i); break;
-    case 16: rvgp::note_launch(); knn_screen<16><<<grid, kQB, 0, st>>>(b.Xf, n, p.kc, p.nsplit, b.part_d, b.part_i); break;
-    case 32: rvgp::note_launch(); knn_screen<32><<<grid, kQB, 0, st>>>(b.Xf, n, p.kc, p.nsplit, b.part_d, b.part_i); break;
-    case 64: rvgp::note_launch(); knn_screen<64><<<grid, kQB, 0, st>>>(b.Xf, n, p.kc, p.nsplit, b.part_d, b.part_i); break;
-    default: rvgp::note_launch(); knn_screen<128><<<grid, kQB, 0, st>>>(b.Xf, n, p.kc, p.nsplit, b.part_d, b.part_i); break;
+  rvgp::note_launch();
+  switch (p.kc) {
+    case 16: launch_screen<16>(p.DP, grid, st, b.Xf, n, p.nsplit, b.part_d, b.part_i); break;
+    case 32: launch_screen<32>(p.DP, grid, st, b.Xf, n, p.nsplit, b.part_d, b.part_i); break;
+    case 48: launch_screen<48>(p.DP, grid, st, b.Xf, n, p.nsplit, b.part_d, b.part_i); break;
+    default: launch_screen<72>(p.DP, grid, st, b.Xf, n, p.nsplit, b.part_d, b.part_i); break;
   }
-  rvgp::note_launch(); knn_finish<<<ceil_div(n, 128), 128, 0, st>>>(X, n, D, p.DP, k, p.kc, p.nsplit, b.part_d, b.part_i, b.radius,
-                                               idx, b.nflag, b.flag_list);
+  rvgp::note_launch(); knn_finish<<<ceil_div(n, 128), 128, 0, st>>>(X, n, D, p.DP, k, p.kc, p.nsplit, b.part_d, b.part_i,
+                                                                 b.radius, idx, b.nflag, b.flag_list);
   rvgp::note_launch(); knn_fallback<<<kNumSMs, kFbThreads, 0, st>>>(X, n, D, k, b.nflag, b.flag_list, idx);
   RVGP_LAUNCH_CHECK("rvgp_knn");
   return RVGP_OK;
@@ -396,7 +449,7 @@ RVGP_API int rvgp_knn(const double* X, int n, int D, int k, int* idx, void* work
 // Limits and behaviour:
 //  * the buffer holds kNoAllocScratchBytes (32 MiB); a problem whose scratch
 //    (rvgp_knn_workspace(n, D, k)) is larger is rejected with an error.  Every
-//    n up to 70,000 fits at D = 3, k = 20 (up to 50,000 at D = 64, k = 15);
+//    n up to 63,000 fits at D = 3, k = 20 (up to 32,500 at D = 64, k = 15);
 //    query rvgp_knn_workspace for other shapes;
 //  * the buffer is a file-scope device array, so every GPU that loads this
 //    library keeps those 32 MiB until the process exits;

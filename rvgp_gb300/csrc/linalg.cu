@@ -179,43 +179,55 @@ __global__ void __launch_bounds__(1024) chol_kernel(T* __restrict__ A, int lda, 
 // ------------------------------------------------------------------ blocked Cholesky (many CTAs)
 constexpr int NB = 32;
 
-// Factor the diagonal block [k0, k0+nb) with one warp: lane i keeps row i of
-// the block in registers, L_kj comes by shuffle, so no step waits on memory or
-// a CTA barrier (FP64 latency, not throughput, bounds these small blocks).
+// Factor the diagonal block [k0, k0+nb) in shared memory.  On GB300 a warp-wide
+// FP64 instruction occupies its SM sub-partition's FP64 pipe for tens of
+// cycles, so the work per pivot is spread over four warps (one per
+// sub-partition) and the only serial FP64 chain is thread 0's pivot
+// (short-chain 1/sqrt).  Pivot j: thread 0 forms 1/sqrt(d_j) and L_jj; after
+// one barrier every thread scales column j-1 (read for the last time by the
+// previous update) and applies the rank-1 update with the unscaled column j
+// times 1/d_j, so each pivot costs two barriers.
 template <typename T>
-__global__ void __launch_bounds__(32) potrf_diag(T* __restrict__ A, int lda, int k0, int nb, int* __restrict__ info) {
+__global__ void __launch_bounds__(128) potrf_diag(T* __restrict__ A, int lda, int k0, int nb, int* __restrict__ info) {
+  __shared__ T L[NB][NB + 1];
+  __shared__ T sinv[NB];
+  __shared__ int bad;
   if (*info) return;  // an earlier block already failed
-  const int lane = threadIdx.x;
-  T a[NB];
-#pragma unroll
-  for (int c = 0; c < NB; ++c)
-    a[c] = (lane < nb && c <= lane) ? A[(size_t)(k0 + lane) * lda + k0 + c] : T(0);
-  int fail = -1;
-#pragma unroll
-  for (int j = 0; j < NB; ++j) {
-    if (j < nb && fail < 0) {
-      const T d = __shfl_sync(0xffffffffu, a[j], j);
+  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
+    const int i = e / nb, c = e % nb;
+    if (c <= i) L[i][c] = A[(size_t)(k0 + i) * lda + k0 + c];
+  }
+  if (threadIdx.x == 0) bad = 0;
+  __syncthreads();
+  for (int j = 0; j < nb; ++j) {
+    if (threadIdx.x == 0) {
+      const T d = L[j][j];
       if (!(d > T(0))) {
-        fail = j;
+        bad = 1;
+        atomicCAS(info, 0, k0 + j + 1);
       } else {
-        const T inv = rsqrt_nr(d), ljj = d * inv;
-        if (lane == j) a[j] = ljj;
-        else if (lane > j) a[j] *= inv;
-#pragma unroll
-        for (int k = j + 1; k < NB; ++k) {
-          const T lkj = __shfl_sync(0xffffffffu, a[j], k);
-          if (lane >= k) a[k] -= a[j] * lkj;
-        }
+        const T inv = rsqrt_nr(d);
+        sinv[j] = inv;
+        L[j][j] = d * inv;
       }
     }
+    __syncthreads();
+    if (bad) return;
+    if (j > 0)
+      for (int i = j + threadIdx.x; i < nb; i += blockDim.x) L[i][j - 1] *= sinv[j - 1];
+    const T inv2 = sinv[j] * sinv[j];
+    const int m = nb - j - 1;
+    for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
+      const int ii = e / m, kk = e % m;
+      if (kk <= ii) L[j + 1 + ii][j + 1 + kk] -= L[j + 1 + ii][j] * (L[j + 1 + kk][j] * inv2);
+    }
+    __syncthreads();
   }
-  if (fail >= 0) {
-    if (lane == 0) atomicCAS(info, 0, k0 + fail + 1);
-    return;
+  // column nb-1 has no rows below its pivot, so every column is final here
+  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
+    const int i = e / nb, c = e % nb;
+    if (c <= i) A[(size_t)(k0 + i) * lda + k0 + c] = L[i][c];
   }
-#pragma unroll
-  for (int c = 0; c < NB; ++c)
-    if (lane < nb && c <= lane) A[(size_t)(k0 + lane) * lda + k0 + c] = a[c];
 }
 
 // panel: rows [k0+nb, p) of columns [k0, k0+nb) <- A L_kkᵀ⁻¹, one row per
@@ -733,7 +745,7 @@ int cholesky(T* A, int lda, int p, int* info, cudaStream_t st) {
   cudaMemsetAsync(info, 0, sizeof(int), st);
   for (int k0 = 0; k0 < p; k0 += NB) {
     const int nb = std::min(NB, p - k0);
-    rvgp::note_launch(); potrf_diag<T><<<1, 32, 0, st>>>(A, lda, k0, nb, info);
+    rvgp::note_launch(); potrf_diag<T><<<1, 128, 0, st>>>(A, lda, k0, nb, info);
     const int rest = p - k0 - nb;
     if (rest <= 0) break;
     const int rb = ceil_div(rest, NB);
@@ -793,7 +805,11 @@ int jacobi_eigh(T* H, int p, T* w, T* V, int max_sweeps, double tol, int* sweeps
   // dynamic shared memory: the round's coefficients during the sweeps, the sort buffers at the end
   const size_t smem = std::max(sizeof(T) * 2 * (size_t)p + sizeof(int2) * (size_t)p,
                                2048 * sizeof(T) + 2048 * sizeof(int));
+  // grid: about eight (FP32) or two (FP64) rotated elements per thread and
+  // round; fewer CTAs make each round's grid barrier cheaper
+  const long long per_cta = 256LL * (sizeof(T) == 4 ? 8 : 2);
   int G = smem <= 48 * 1024 ? std::min(cooperative_grid(jacobi_persistent<T>, 256, smem), kMaxCoopGrid) : 0;
+  if (G > 0) G = (int)std::max<long long>(1, std::min<long long>(G, (2 * pp + per_cta - 1) / per_cta));
   if (G > 0 && p > 1) {
     cudaMemsetAsync(bar, 0, (G + 1) * sizeof(unsigned int), st);
     cudaMemsetAsync(flags, 0, 2 * sizeof(int), st);

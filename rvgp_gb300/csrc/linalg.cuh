@@ -25,7 +25,9 @@ __device__ __forceinline__ double rsqrt_nr(double d) {
   r = fma(-a, y, 1.0);
   return fma(0.5 * y, r, y);
 }
-__device__ __forceinline__ float rsqrt_nr(float d) { return rsqrtf(d); }
+// FP32: correctly rounded square root and divide (rsqrtf's extra ulps would
+// accumulate over the many rotations of a Jacobi sweep).
+__device__ __forceinline__ float rsqrt_nr(float d) { return 1.0f / sqrtf(d); }
 
 // 1/x in FP64 with an FP32 estimate and two Newton steps y <- y (2 - x y).
 __device__ __forceinline__ double rcp_nr(double x) {
