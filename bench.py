@@ -88,6 +88,7 @@ def pipeline(X, V, train, test, wl, precision, timings=None):
         timings["gp_predict"] = ev[1].elapsed_time(ev[2]) / 1e3
         timings["eig_L_info"] = d._dev.eig_info_L
         timings["eig_Lc_info"] = d._dev.eig_info_Lc
+        timings["gp_fit_form"] = getattr(gp, "fit_form", None)
     return out
 
 

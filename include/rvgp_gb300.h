@@ -152,6 +152,21 @@ int rvgp_gp_fit_adam(const double* C, const double* b, const double* yy, long lo
                      double n_rows, int typ, const double* theta0, const double* lower, const int* mask, int steps,
                      double lr, double beta1, double beta2, double eps, double* theta_out, double* hist, double* out,
                      double* state, void* workspace, size_t ws_bytes, void* stream);
+/* Mixed-precision form of rvgp_gp_fit_adam (the same Adam steps on the same
+ * likelihood, RVGP/main.py:55-95 with GPflow's GPR): the m x m algebra of every
+ * step runs in FP32 (Jacobi-scaled capacitance matrix, blocked Cholesky and
+ * triangular inverse in one SM's shared memory), all steps in one launch of
+ * one CTA; S(θ) and the gradient assembly stay FP64, and out / state are FP64
+ * at theta_out.  *status (host): 0 = done, 1 = an FP32 pivot was not positive
+ * (nothing written; run rvgp_gp_fit_adam instead).  Requires
+ * m <= rvgp_gp_fit_mixed_max_m().  Synchronises the stream. */
+int rvgp_gp_fit_mixed_max_m(void);
+size_t rvgp_gp_fit_mixed_workspace(int m);
+int rvgp_gp_fit_adam_mixed(const double* C, const double* b, const double* yy, long long N, int m,
+                           const double* evals, double n_rows, int typ, const double* theta0, const double* lower,
+                           const int* mask, int steps, double lr, double beta1, double beta2, double eps,
+                           double* theta_out, double* hist, double* out, double* state, int* status, void* workspace,
+                           size_t ws_bytes, void* stream);
 /* predict_f(full_cov=False) mean and variance at Nte rows (RVGP/main.py:102-116). */
 size_t rvgp_gp_predict_workspace(long long Nte, int m, int mode);
 int rvgp_gp_predict(const double* Phi_star, const float* Phi_star32, long long Nte, int m, int mode,

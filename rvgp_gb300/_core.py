@@ -46,6 +46,10 @@ SIGNATURES = {
     "rvgp_gp_lml": (c_int, [P, P, P, ctypes.c_longlong, c_int, P, c_double, c_int, P, P, P, P, c_size_t, P]),
     "rvgp_gp_fit_adam": (c_int, [P, P, P, ctypes.c_longlong, c_int, P, c_double, c_int, P, P, P, c_int, c_double,
                                  c_double, c_double, c_double, P, P, P, P, P, c_size_t, P]),
+    "rvgp_gp_fit_mixed_max_m": (c_int, []),
+    "rvgp_gp_fit_mixed_workspace": (c_size_t, [c_int]),
+    "rvgp_gp_fit_adam_mixed": (c_int, [P, P, P, ctypes.c_longlong, c_int, P, c_double, c_int, P, P, P, c_int,
+                                       c_double, c_double, c_double, c_double, P, P, P, P, P, P, c_size_t, P]),
     "rvgp_gp_predict_workspace": (c_size_t, [ctypes.c_longlong, c_int, c_int]),
     "rvgp_gp_predict": (c_int, [P, P, ctypes.c_longlong, c_int, c_int, P, P, P, P, c_size_t, P]),
     "rvgp_kernel_matrix": (c_int, [P, ctypes.c_longlong, P, ctypes.c_longlong, c_int, P, P, P]),
@@ -346,6 +350,34 @@ def gp_fit_adam(C, b, yy, N, evals, n_rows, theta0, lower, mask, steps, lr=0.05,
                                  float(betas[1]), float(eps), ptr(theta), ptr(hist), ptr(work.out), ptr(work.state),
                                  ptr(work.ws), work.ws.numel(), stream()), "rvgp_gp_fit_adam")
     return theta, work.out, hist, work
+
+
+def gp_fit_mixed_max_m():
+    """Largest number of eigenpairs the one-CTA mixed-precision fit handles."""
+    return int(lib().rvgp_gp_fit_mixed_max_m())
+
+
+def gp_fit_adam_mixed(C, b, yy, N, evals, n_rows, theta0, lower, mask, steps, lr=0.05, betas=(0.9, 0.999),
+                      eps=1e-8, typ="matern", work=None, history=False):
+    """Adam with the m x m algebra of every step in FP32 inside one launch
+    (rvgp_gp_fit_adam_mixed).  Returns (theta, out, history, work, ok); ok is
+    False when an FP32 pivot failed, and nothing was fitted."""
+    m = evals.numel()
+    dev = evals.device
+    work = work or LMLWorkspace(m, dev)
+    L = lib()
+    ws = workspace(L.rvgp_gp_fit_mixed_workspace(m), dev)
+    theta = torch.empty(4, dtype=torch.float64, device=dev)
+    hist = torch.empty(max(steps, 1), dtype=torch.float64, device=dev) if history else None
+    lo = (ctypes.c_double * 4)(*[float(v) for v in lower])
+    mk = (ctypes.c_int * 4)(*[int(bool(v)) for v in mask])
+    status = ctypes.c_int(0)
+    check(L.rvgp_gp_fit_adam_mixed(ptr(C), ptr(b), ptr(yy), int(N), m, ptr(evals), float(n_rows), KERNEL_TYPES[typ],
+                                   ptr(theta0.contiguous()), lo, mk, int(steps), float(lr), float(betas[0]),
+                                   float(betas[1]), float(eps), ptr(theta), ptr(hist), ptr(work.out),
+                                   ptr(work.state), ctypes.byref(status), ptr(ws), ws.numel(), stream()),
+          "rvgp_gp_fit_adam_mixed")
+    return theta, work.out, hist, work, status.value == 0
 
 
 def gp_predict(Phi_star, state, m, Phi_star32=None, mode="fp64"):

@@ -143,9 +143,16 @@ class manifold_GPR:
         slots = self._slots()
         lower = [p.lower if p is not None else 0.0 for p in slots]
         mask = [p is not None and p.trainable for p in slots]
-        theta, out, hist, _ = _core.gp_fit_adam(self.C, self.b, self.yy, self.N, self.kernel.eigenvalues,
-                                                self.kernel.num_verticies, self.theta(), lower, mask, steps, lr=lr,
-                                                typ=self.kernel.typ, work=self.work, history=True)
+        args = (self.C, self.b, self.yy, self.N, self.kernel.eigenvalues, self.kernel.num_verticies, self.theta(),
+                lower, mask, steps)
+        ok = False
+        self.fit_form = "fp64"
+        if self.precision == "mixed" and self.m <= _core.gp_fit_mixed_max_m():
+            theta, out, hist, _, ok = _core.gp_fit_adam_mixed(*args, lr=lr, typ=self.kernel.typ, work=self.work,
+                                                              history=True)
+            self.fit_form = "mixed" if ok else "fp64 (an FP32 pivot failed)"
+        if not ok:
+            theta, out, hist, _ = _core.gp_fit_adam(*args, lr=lr, typ=self.kernel.typ, work=self.work, history=True)
         vals = theta.cpu().numpy()
         for p, v in zip(slots, vals):
             if p is not None and p.trainable:

@@ -174,3 +174,54 @@ def test_non_pd_reports_nan(core):
     th = np.array([1.5, 5.0, -1.0, 1e-2])  # negative sigma_f: A is not positive definite
     out, _ = core.gp_lml(C, b, yy, len(y), cu(lam), 900.0, cu(th))
     assert np.isnan(out.cpu().numpy()[0])
+
+
+def structured_problem(seed, N, m):
+    """Rows of an orthonormal basis and a target with most energy in the low modes."""
+    rng = np.random.default_rng(seed)
+    Q, _ = np.linalg.qr(rng.standard_normal((N, m)))
+    Phi = Q * np.sqrt(N)
+    lam = np.sort(rng.uniform(0.0, 3.0, m))
+    coef = rng.standard_normal(m) / (1.0 + lam) ** 2
+    y = Phi @ coef + 0.05 * rng.standard_normal(N)
+    return Phi, y, lam
+
+
+@pytest.mark.parametrize("m,N,typ", [(24, 300, "matern"), (50, 800, "se"), (97, 1500, "matern"),
+                                     (200, 4000, "matern")])
+def test_mixed_fit_matches_fp64_fit(core, m, N, typ):
+    """The one-launch FP32 fit (rvgp_gp_fit_adam_mixed) follows the FP64 Adam
+    trajectory: 200 steps from the reference's initial values, parameters to
+    1e-4 relative, the LML history to 1e-4 of its largest magnitude (the FP32
+    log-determinant), posterior means to 1e-6."""
+    assert m <= core.gp_fit_mixed_max_m()
+    Phi, y, lam = structured_problem(11, N, m)
+    C, b, yy = core.gp_prepare(cu(Phi), cu(y))
+    th0 = cu([3.0, 4.0, 1.0, 1.0])
+    lower, mask, steps = [0.0, 0.0, 0.0, 1e-6], [1, 1, 1, 1], 200
+    n_rows = 3.0 * N
+    th64, _, h64, w64 = core.gp_fit_adam(C, b, yy, N, cu(lam), n_rows, th0, lower, mask, steps, typ=typ,
+                                         history=True)
+    mean64, _ = core.gp_predict(cu(Phi[:200]), w64.state, m)
+    th32, out32, h32, w32, ok = core.gp_fit_adam_mixed(C, b, yy, N, cu(lam), n_rows, th0, lower, mask, steps,
+                                                       typ=typ, history=True)
+    assert ok
+    np.testing.assert_allclose(th32.cpu().numpy(), th64.cpu().numpy(), rtol=1e-4)
+    h64n = h64.cpu().numpy()
+    np.testing.assert_allclose(h32.cpu().numpy(), h64n, rtol=0, atol=1e-4 * np.abs(h64n).max())
+    mean32, _ = core.gp_predict(cu(Phi[:200]), w32.state, m)
+    err = (torch.linalg.vector_norm(mean32 - mean64) / torch.linalg.vector_norm(mean64)).item()
+    assert err <= 1e-6
+    # out / state are the FP64 likelihood at the returned parameters
+    ref, _ = core.gp_lml(C, b, yy, N, cu(lam), n_rows, th32, typ=typ)
+    np.testing.assert_allclose(out32.cpu().numpy(), ref.cpu().numpy(), rtol=1e-12)
+
+
+def test_mixed_fit_reports_failed_pivot(core):
+    """A start with a negative kernel variance makes the FP32 capacitance matrix
+    invalid: the launch stops, reports it, and writes no parameters."""
+    Phi, y, lam = structured_problem(3, 300, 24)
+    C, b, yy = core.gp_prepare(cu(Phi), cu(y))
+    th, _, _, _, ok = core.gp_fit_adam_mixed(C, b, yy, 300, cu(lam), 900.0, cu([1.5, 5.0, -1.0, 1e-2]),
+                                             [0.0, 0.0, 0.0, 1e-6], [1, 1, 1, 1], 5)
+    assert not ok
