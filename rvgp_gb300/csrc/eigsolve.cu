@@ -164,6 +164,8 @@ struct Small {
   float* Bf;
   double* Bd;
   float *Hf, *thf;  // FP32 Rayleigh-Ritz matrix and its eigenvalues (mixed form)
+  float *L32, *Mb32;  // FP32 Cholesky QR factor and its diagonal-block inverses
+  int cholqr32;       // p fits the one-CTA FP32 Cholesky QR
   float* nf;
   double* nd;
 };
@@ -271,6 +273,18 @@ int orthonormalise(const Problem& P, Block<T>& B, Small& s, Stats& stt, cudaStre
     TRY(col_norms<T>(B.V, p, N, p, nrm<T>(s), s.cn_ws, s.cn_bytes, st));
     TRY(scale_cols<T>(B.V, p, N, p, nrm<T>(s), true, st));
     TRY(gram_any(B.V, B.V, N, p, s.G, s, st));
+    if (sizeof(T) == 4 && s.cholqr32) {
+      // FP32 factorisation in one CTA and an FP32 triangular solve of the block;
+      // a failed pivot falls through to the FP64 factorisation of the same Gram
+      TRY(chol32_gram(s.G, p, s.L32, s.Mb32, s.info, st));
+      int info32 = 0;
+      cudaMemcpyAsync(&info32, s.info, sizeof(int), cudaMemcpyDeviceToHost, st);
+      if (cudaStreamSynchronize(st) != cudaSuccess) return check_launch("orthonormalise");
+      if (info32 == 0) {
+        TRY(trsm_rows_f32(reinterpret_cast<float*>(B.V), p, N, p, s.L32, s.Mb32, st));
+        continue;
+      }
+    }
     TRY(cholesky<double>(s.G, p, p, s.info, st));
     int info = 0;
     cudaMemcpyAsync(&info, s.info, sizeof(int), cudaMemcpyDeviceToHost, st);
@@ -441,6 +455,9 @@ Layout carve(Workspace& ws, long long N, int p, int mode) {
   s.nd = ws.take<double>(p);
   s.Hf = ws.take<float>(pp);
   s.thf = ws.take<float>(p);
+  s.L32 = ws.take<float>(pp);
+  s.Mb32 = ws.take<float>((size_t)((p + 31) / 32) * 32 * 32);
+  s.cholqr32 = 0;
   s.gram_bytes = std::max(gram_workspace<float>(N, p, p), gram_workspace<double>(N, p, p));
   s.gram_ws = ws.take<char>(s.gram_bytes);
   s.jac_bytes = jacobi_workspace<double>(p);
@@ -485,6 +502,7 @@ RVGP_API int rvgp_eigsh(const int* indptr, const int* indices, const double* val
   Workspace ws(workspace, ws_bytes);
   Layout L = carve(ws, N, p, mode);
   Small& s = L.s;
+  s.cholqr32 = (mode == 1 && p <= cholqr32_max_p()) ? 1 : 0;
   Problem P{n, DB, N, indptr, indices, vals64, vals32, m, p};
   Stats stt;
 

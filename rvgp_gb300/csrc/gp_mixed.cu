@@ -10,7 +10,8 @@
 // fraction of that rate.
 //
 // Per step (FP64 unless noted):
-//   1. S(θ), ∂S/∂(ν, κ, σ_f)                       (as rvgp_spectral_S)
+//   1. S(θ), ∂S/∂(ν, κ, σ_f) as rvgp_spectral_S, with the log / exp of each
+//      eigenvalue term in FP32 (the accuracy of the FP32 algebra below)
 //   2. Jacobi scaling: Δ_l = A_ll = 1 + S_l C_ll/σ², h_l = √S_l /(σ √Δ_l);
 //      Ã = Δ^-½ A Δ^-½ has unit diagonal, Ã_ij = C_ij h_i h_j   (FP32)
 //   3. Ã = L Lᵀ, blocked right-looking Cholesky in shared memory, 32-wide
@@ -31,25 +32,18 @@
 // posterior built from them) are FP64.
 #include "common.cuh"
 #include "linalg.cuh"
+#include "chol32.cuh"
 #include <math.h>
 #include <float.h>
 
 namespace rvgp {
 namespace {
 
-constexpr int kThreads = 1024;
+constexpr int kThreads = 512;
 constexpr int kWarps = kThreads / 32;
-constexpr int FB = 32;      // panel width (one warp)
+using chol32::FB;
+using chol32::lda32;
 constexpr int kLdT = FB + 4;  // T rows: 16-byte aligned
-
-// Row stride of the m x m FP32 matrix: a multiple of 4 (16-byte rows for
-// float4 loads) with ld/4 odd, so eight consecutive rows read as float4 fall
-// in eight distinct 4-bank groups.
-__host__ __device__ inline int lda_of(int m) {
-  int q = (m + 3) / 4;
-  if (q % 2 == 0) ++q;
-  return 4 * q;
-}
 
 // shared-memory layout (bytes), doubles first
 struct Layout {
@@ -79,7 +73,7 @@ __host__ __device__ inline Layout layout(int m) {
   L.th = take(8 * 4);
   L.adam = take(8 * 16);
   L.outv = take(8 * 8);
-  L.A = take(4 * (size_t)m * lda_of(m));
+  L.A = take(4 * (size_t)m * lda32(m));
   L.T = take(4 * (size_t)m * kLdT);
   L.u = take(f);
   L.z = take(f);
@@ -87,11 +81,6 @@ __host__ __device__ inline Layout layout(int m) {
   L.L = take(f);
   L.total = o;
   return L;
-}
-
-__device__ __forceinline__ double softplus_d(double u) { return u > 0.0 ? u + log1p(exp(-u)) : log1p(exp(u)); }
-__device__ __forceinline__ double sigmoid_d(double u) {
-  return u >= 0.0 ? 1.0 / (1.0 + exp(-u)) : exp(u) / (1.0 + exp(u));
 }
 
 // FP64 reductions.  A warp-wide FP64 instruction costs the same however few
@@ -144,138 +133,10 @@ __device__ __forceinline__ double cta_max(double v, double* red, int nw) {
   return red[8 * kWarps + 7];
 }
 
-// 1/sqrt(d) in FP32: hardware estimate plus one Newton step.
-__device__ __forceinline__ float rsqrt_f(float d) {
-  const float r = rsqrtf(d);
-  return r * fmaf(-0.5f * d * r, r, 1.5f);
-}
-
-// Warp 0: Cholesky of the nb x nb diagonal block at (j0, j0) of A.  Lane i
-// keeps row i in registers, shifted so that the current pivot column is
-// always a[0]: each pivot is one compact loop iteration (31 shuffles, 31
-// fused multiply-adds, 31 moves), so the code stays in the instruction cache.
-// Writes L into the block's lower triangle and 1/L_ii into dinvL.  Returns
-// false on a non-positive pivot.
-__device__ bool chol_diag_block(float* A, int ld, int j0, int nb, float* dinvL) {
-  const int lane = threadIdx.x & 31;
-  float a[FB];
-#pragma unroll
-  for (int c = 0; c < FB; ++c) a[c] = (lane < nb && c <= lane) ? A[(j0 + lane) * ld + j0 + c] : 0.f;
-  bool ok = true;
-  for (int j = 0; j < nb; ++j) {
-    const float d = __shfl_sync(0xffffffffu, a[0], j);
-    ok = ok && (d > 0.f);
-    const float rs = rsqrt_f(fmaxf(d, FLT_MIN));
-    const float l = (lane == j) ? d * rs : a[0] * rs;  // L_ij for lane i >= j
-    if (lane >= j && lane < nb) A[(j0 + lane) * ld + j0 + j] = l;
-    if (lane == j) dinvL[j0 + j] = rs;
-#pragma unroll
-    for (int k = 1; k < FB; ++k) {
-      const float lk = __shfl_sync(0xffffffffu, l, (j + k) & 31);  // L_(j+k),j
-      if (lane >= j + k) a[k] = fmaf(-l, lk, a[k]);
-    }
-#pragma unroll
-    for (int k = 0; k < FB - 1; ++k) a[k] = a[k + 1];
-    a[FB - 1] = 0.f;
-  }
-  return __all_sync(0xffffffffu, ok);
-}
-
-// Rows [j0+32, m) of block column j0 <- A21 L11⁻ᵀ by forward substitution,
-// one thread per row, the row solved in place.
-__device__ void panel_solve(float* A, int ld, int j0, int m, const float* dinvL) {
-  const int r = j0 + FB + threadIdx.x;
-  if (r >= m) return;
-  float* row = A + r * ld + j0;
-  const float* Lb = A + j0 * ld + j0;
-  for (int c = 0; c < FB; ++c) {
-    float s0 = row[c], s1 = 0.f;
-    int cp = 0;
-#pragma unroll 4
-    for (; cp + 1 < c; cp += 2) {
-      s0 = fmaf(-row[cp], Lb[c * ld + cp], s0);
-      s1 = fmaf(-row[cp + 1], Lb[c * ld + cp + 1], s1);
-    }
-    if (cp < c) s0 = fmaf(-row[cp], Lb[c * ld + cp], s0);
-    row[c] = (s0 + s1) * dinvL[j0 + c];
-  }
-}
-
-// Trailing update of the lower part: A[i][k] -= Σ_c L[i][j0+c] L[k][j0+c] for
-// r0 <= k <= i < m, 4 x 4 register tiles, operands read as float4 along c.
-__device__ void trailing_update(float* A, int ld, int j0, int m) {
-  const int r0 = j0 + FB;
-  const int R = m - r0;
-  if (R <= 0) return;
-  const int TR = (R + 3) / 4;
-  const int tiles = TR * (TR + 1) / 2;
-  for (int t = threadIdx.x; t < tiles; t += kThreads) {
-    int ti = (int)((sqrtf(8.f * t + 1.f) - 1.f) * 0.5f);
-    while (ti * (ti + 1) / 2 > t) --ti;
-    while ((ti + 1) * (ti + 2) / 2 <= t) ++ti;
-    const int tk = t - ti * (ti + 1) / 2;
-    const int i0 = r0 + 4 * ti, k0 = r0 + 4 * tk;
-    float acc[4][4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u)
-#pragma unroll
-      for (int v = 0; v < 4; ++v) acc[u][v] = 0.f;
-    int oa[4], ob[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      oa[u] = min(i0 + u, m - 1) * ld + j0;
-      ob[u] = min(k0 + u, m - 1) * ld + j0;
-    }
-#pragma unroll 1
-    for (int c = 0; c < FB; c += 4) {
-      float4 b[4];
-#pragma unroll
-      for (int v = 0; v < 4; ++v) b[v] = *reinterpret_cast<const float4*>(A + ob[v] + c);
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const float4 a = *reinterpret_cast<const float4*>(A + oa[u] + c);
-#pragma unroll
-        for (int v = 0; v < 4; ++v) {
-          acc[u][v] = fmaf(a.x, b[v].x, acc[u][v]);
-          acc[u][v] = fmaf(a.y, b[v].y, acc[u][v]);
-          acc[u][v] = fmaf(a.z, b[v].z, acc[u][v]);
-          acc[u][v] = fmaf(a.w, b[v].w, acc[u][v]);
-        }
-      }
-    }
-#pragma unroll
-    for (int u = 0; u < 4; ++u)
-#pragma unroll
-      for (int v = 0; v < 4; ++v) {
-        const int i = i0 + u, k = k0 + v;
-        if (i < m && k <= i) A[i * ld + k] -= acc[u][v];
-      }
-  }
-}
-
-// Warp w < nblk: inverse Mb of the factor's diagonal block w (lane = column c,
-// forward substitution in axpy form).  Mb is written transposed into the
-// block's strict upper triangle (Mb[i][c] at A[j0+c][j0+i], i > c); its
-// diagonal is dinvL.
-__device__ void invert_diag_blocks(float* A, int ld, int m, int nblk, const float* dinvL) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (warp >= nblk) return;
-  const int j0 = warp * FB, nb = min(FB, m - j0);
-  float* B = A + j0 * ld + j0;
-  if (lane < nb) {
-    const float xl = dinvL[j0 + lane];
-    for (int k = lane + 1; k < nb; ++k) B[lane * ld + k] = -B[k * ld + lane] * xl;
-    for (int i = lane + 1; i < nb; ++i) {
-      const float xi = B[lane * ld + i] * dinvL[j0 + i];
-      B[lane * ld + i] = xi;
-#pragma unroll 4
-      for (int k = i + 1; k < nb; ++k) B[lane * ld + k] = fmaf(-B[k * ld + i], xi, B[lane * ld + k]);
-    }
-  }
-}
-
 // T[i - r0][c] = Σ_{k=r0}^{i} M[i][k] Lt[c][k] with Lt[c][k] = A[j0+c][k]
-// (the block column's L, copied into the free upper triangle), 4 x 4 tiles.
+// (the block column's L, copied into the free upper triangle), 4 x 4 tiles,
+// operands read as float4 along k (r0 and ld are multiples of 4); the entries
+// of M beyond the diagonal (k > i, the upper triangle's contents) are masked.
 __device__ void inverse_product(const float* A, int ld, int j0, int m, float* T) {
   const int r0 = j0 + FB;
   const int R = m - r0;
@@ -289,21 +150,33 @@ __device__ void inverse_product(const float* A, int ld, int j0, int m, float* T)
     for (int u = 0; u < 4; ++u)
 #pragma unroll
       for (int v = 0; v < 4; ++v) acc[u][v] = 0.f;
-    int ri[4];
+    int oa[4], ob[4];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) ri[u] = min(i0 + u, m - 1);
-    const int kend = min(i0 + 3, m - 1);
-#pragma unroll 2
-    for (int k = r0; k <= kend; ++k) {
-      float a[4], b[4];
+    for (int u = 0; u < 4; ++u) {
+      oa[u] = min(i0 + u, m - 1) * ld;
+      ob[u] = (j0 + c0 + u) * ld;
+    }
+    const int kend = min(i0 + 3, m - 1);  // last k any row of the tile uses
+    for (int k = r0; k <= kend; k += 4) {
+      float4 b[4];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) a[u] = (k <= i0 + u) ? A[ri[u] * ld + k] : 0.f;
+      for (int v = 0; v < 4; ++v) b[v] = *reinterpret_cast<const float4*>(A + ob[v] + k);
 #pragma unroll
-      for (int v = 0; v < 4; ++v) b[v] = A[(j0 + c0 + v) * ld + k];
+      for (int u = 0; u < 4; ++u) {
+        float4 a = *reinterpret_cast<const float4*>(A + oa[u] + k);
+        const int i = i0 + u;  // mask M[i][k'] for k' > i
+        if (k + 0 > i) a.x = 0.f;
+        if (k + 1 > i) a.y = 0.f;
+        if (k + 2 > i) a.z = 0.f;
+        if (k + 3 > i) a.w = 0.f;
 #pragma unroll
-      for (int u = 0; u < 4; ++u)
-#pragma unroll
-        for (int v = 0; v < 4; ++v) acc[u][v] = fmaf(a[u], b[v], acc[u][v]);
+        for (int v = 0; v < 4; ++v) {
+          acc[u][v] = fmaf(a.x, b[v].x, acc[u][v]);
+          acc[u][v] = fmaf(a.y, b[v].y, acc[u][v]);
+          acc[u][v] = fmaf(a.z, b[v].z, acc[u][v]);
+          acc[u][v] = fmaf(a.w, b[v].w, acc[u][v]);
+        }
+      }
     }
 #pragma unroll
     for (int u = 0; u < 4; ++u)
@@ -381,14 +254,17 @@ __global__ void __launch_bounds__(kThreads, 1)
   float* cf = reinterpret_cast<float*>(sm + Ly.c);
   float* dinvL = reinterpret_cast<float*>(sm + Ly.L);
   float* zf = hf;
-  __shared__ int s_bad;
+  __shared__ int s_bad, s_chol;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int ld = lda_of(m);
+  const int ld = lda32(m);
   const int nblk = (m + FB - 1) / FB;
   const int nw = (m + 31) / 32;  // warps holding the per-eigenpair values
   const double yy = yy_p[0];
   const double Nd = (double)N;
   for (int l = tid; l < m; l += kThreads) cdg[l] = Cd[(size_t)l * m + l];
+  // row padding [m, ld) is read (and multiplied by masked zeros) by the float4
+  // loops; it must hold finite values
+  for (int e = tid; e < m * (ld - m); e += kThreads) A[(e / (ld - m)) * ld + m + e % (ld - m)] = 0.f;
   if (tid == 0) {
     s_bad = 0;
     for (int q = 0; q < 4; ++q) {
@@ -413,7 +289,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         const double ik2 = rcp_nr(kappa * kappa);
         const double uu = lam + 2.0 * nu * ik2;
         const double iu = rcp_nr(uu);
-        const double lu = log(uu);
+        const double lu = (double)logf((float)uu);  // FP32 accuracy, as the m x m algebra
         a = -nu * lu;
         b = -lu - nu * (2.0 * ik2) * iu;
         c = 4.0 * nu * nu * ik2 * rcp_nr(kappa) * iu;
@@ -431,7 +307,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     {
       double v[1] = {0.0};
       for (int l = tid; l < m; l += kThreads) {
-        S[l] = exp(tmp[l] - mx);  // unnormalised weight, normalised below
+        S[l] = (double)expf((float)(tmp[l] - mx));  // unnormalised weight (<= 1), normalised below
         v[0] += S[l];
       }
       cta_sum<1>(v, red, nw);
@@ -469,29 +345,18 @@ __global__ void __launch_bounds__(kThreads, 1)
     // ---- 2. scaled capacitance matrix (lower triangle, unit diagonal), FP32
     for (int i = warp; i < m; i += kWarps) {
       const float hi = hf[i];
-      for (int j = lane; j <= i; j += 32) A[i * ld + j] = (j == i) ? 1.f : C32[(size_t)i * m + j] * hi * hf[j];
+#pragma unroll 4
+      for (int j = lane; j <= i; j += 32) A[i * ld + j] = (j == i) ? 1.f : __ldg(C32 + (size_t)i * m + j) * hi * hf[j];
     }
     __syncthreads();
     // ---- 3. blocked Cholesky Ã = L Lᵀ
-    for (int jb = 0; jb < nblk; ++jb) {
-      const int j0 = jb * FB, nb = min(FB, m - j0);
-      if (warp == 0) {
-        const bool ok = chol_diag_block(A, ld, j0, nb, dinvL);
-        if (!ok && lane == 0) s_bad = 1;
-      }
-      __syncthreads();
-      if (s_bad) break;
-      if (j0 + FB < m) {
-        panel_solve(A, ld, j0, m, dinvL);
-        __syncthreads();
-        trailing_update(A, ld, j0, m);
-        __syncthreads();
-      }
+    if (!chol32::chol32_cta<kThreads>(A, ld, m, dinvL, &s_chol)) {
+      if (tid == 0) s_bad = 1;
+      break;
     }
-    if (s_bad) break;
     // ---- 4. M = L⁻¹ in place: the diagonal blocks' inverses (one warp each),
     // moved from the upper triangle to the lower; log L_ll for |Ã|
-    invert_diag_blocks(A, ld, m, nblk, dinvL);
+    chol32::invert_diag_blocks(A, ld, m, nblk, dinvL);
     __syncthreads();
     double logL = 0.0;
     for (int e = tid; e < nblk * FB * FB; e += kThreads) {
@@ -583,7 +448,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     __syncthreads();
     // ---- 7. Adam on u (value = softplus(u) + lower), minimising -LML; lane q of
-    // warp 0 updates parameter q (the arithmetic of the FP64 form's adam_step)
+    // warp 0 updates parameter q: the FP64 form's adam_step with the moments in
+    // FP64 and sigmoid / softplus / square root in FP32
     if (warp == 0 && lane < 4) {
       bool finite = true;
       for (int q = 0; q < 5; ++q) finite = finite && isfinite(outv[q]);
@@ -593,11 +459,15 @@ __global__ void __launch_bounds__(kThreads, 1)
         double* uq = adam + q;
         double* m1 = adam + 4 + q;
         double* v1 = adam + 8 + q;
-        const double g = -outv[1 + q] * sigmoid_d(*uq);
+        const float uf32 = (float)*uq;
+        const double sig = (double)(1.0f / (1.0f + expf(-uf32)));
+        const double g = -outv[1 + q] * sig;
         *m1 = beta1 * *m1 + (1.0 - beta1) * g;
         *v1 = beta2 * *v1 + (1.0 - beta2) * g * g;
-        *uq -= lr * (*m1 / b1t) / (sqrt(*v1 / b2t) + eps);
-        th[q] = softplus_d(*uq) + lower[q];
+        *uq -= lr * (*m1 / b1t) / ((double)sqrtf((float)(*v1 / b2t)) + eps);
+        const float un = (float)*uq;
+        const float sp = un > 15.f ? un + log1pf(expf(-un)) : log1pf(expf(un));
+        th[q] = (double)sp + lower[q];
       }
     }
     __syncthreads();

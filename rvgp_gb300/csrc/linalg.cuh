@@ -86,6 +86,16 @@ size_t col_norms_workspace(long long N, int b);
 template <typename T>
 int scale_cols(T* X, int ld, long long N, int b, const T* s, bool inverse, cudaStream_t st);
 
+// FP32 Cholesky QR step (cholqr.cu): chol32_gram factors the p x p FP64 Gram
+// G in FP32 in one CTA, writing L (p x p, lower, ld p) and the inverses of its
+// 32 x 32 diagonal blocks (Mb, ceil(p/32) x 32 x 32); *info (device) = 0, or 1
+// for a non-positive pivot.  trsm_rows_f32 overwrites V (N x p, ld) with
+// V L⁻ᵀ.  Both need p <= cholqr32_max_p().
+int cholqr32_max_p();
+size_t cholqr32_workspace(int p);
+int chol32_gram(const double* G, int p, float* L, float* Mb, int* info, cudaStream_t st);
+int trsm_rows_f32(float* V, int ldv, long long N, int p, const float* L, const float* Mb, cudaStream_t st);
+
 // Dtype conversion of an N x b block (ld in/out).
 int convert_f32_to_f64(const float* in, int ldi, double* out, int ldo, long long N, int b, cudaStream_t st);
 int convert_f64_to_f32(const double* in, int ldi, float* out, int ldo, long long N, int b, cudaStream_t st);
