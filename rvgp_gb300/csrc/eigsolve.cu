@@ -166,6 +166,9 @@ struct Small {
   float *Hf, *thf;  // FP32 Rayleigh-Ritz matrix and its eigenvalues (mixed form)
   float *L32, *Mb32;  // FP32 Cholesky QR factor and its diagonal-block inverses
   int cholqr32;       // p fits the one-CTA FP32 Cholesky QR
+  int jac32;          // p fits the one-CTA FP32 Jacobi
+  void* jac32_ws;
+  size_t jac32_bytes;
   float* nf;
   double* nd;
 };
@@ -205,6 +208,8 @@ inline int gram_any(const float* A, const float* B, long long N, int p, double* 
 inline int gram_any(const double* A, const double* B, long long N, int p, double* C, Small& s, cudaStream_t st) {
   return gram<double>(A, p, B, p, N, p, p, C, p, 1.0, 0.0, s.gram_ws, s.gram_bytes, st);
 }
+
+constexpr int kFp32Sweeps = 12;  // FP32 Jacobi sweeps are capped: off(H) stalls at FP32 rounding
 
 #define TRY(x)                  \
   do {                          \
@@ -331,7 +336,12 @@ int rayleigh_ritz(const Problem& P, Block<T>& B, Small& s, Stats& stt, int max_s
     // rotation costs ~64x an FP32 one on GB300).  Stop at off(H) <= 4e-6 ||H||_F,
     // below the FP32 stage's residual tolerance and above FP32 rounding.
     TRY(convert_f64_to_f32(s.H, p, s.Hf, p, p, p, st));
-    TRY(jacobi_eigh<float>(s.Hf, p, s.thf, s.Bf, std::min(max_sweeps, 12), 4e-6, &used, s.jac_ws, s.jac_bytes, st));
+    if (s.jac32)
+      TRY(jacobi32_eigh(s.Hf, p, s.thf, s.Bf, std::min(max_sweeps, kFp32Sweeps), 4e-6, &used, s.jac32_ws,
+                        s.jac32_bytes, st));
+    else
+      TRY(jacobi_eigh<float>(s.Hf, p, s.thf, s.Bf, std::min(max_sweeps, kFp32Sweeps), 4e-6, &used, s.jac_ws,
+                             s.jac_bytes, st));
     TRY(convert_f32_to_f64(s.thf, 1, s.theta, 1, p, 1, st));
   } else {
     TRY(jacobi_eigh<double>(s.H, p, s.theta, s.Q, max_sweeps, 1e-13, &used, s.jac_ws, s.jac_bytes, st));
@@ -458,6 +468,9 @@ Layout carve(Workspace& ws, long long N, int p, int mode) {
   s.L32 = ws.take<float>(pp);
   s.Mb32 = ws.take<float>((size_t)((p + 31) / 32) * 32 * 32);
   s.cholqr32 = 0;
+  s.jac32 = 0;
+  s.jac32_bytes = jacobi32_workspace(p, kFp32Sweeps);
+  s.jac32_ws = ws.take<char>(s.jac32_bytes);
   s.gram_bytes = std::max(gram_workspace<float>(N, p, p), gram_workspace<double>(N, p, p));
   s.gram_ws = ws.take<char>(s.gram_bytes);
   s.jac_bytes = jacobi_workspace<double>(p);
@@ -503,6 +516,7 @@ RVGP_API int rvgp_eigsh(const int* indptr, const int* indices, const double* val
   Layout L = carve(ws, N, p, mode);
   Small& s = L.s;
   s.cholqr32 = (mode == 1 && p <= cholqr32_max_p()) ? 1 : 0;
+  s.jac32 = (mode == 1 && p % 2 == 0 && p <= jacobi32_max_p()) ? 1 : 0;
   Problem P{n, DB, N, indptr, indices, vals64, vals32, m, p};
   Stats stt;
 

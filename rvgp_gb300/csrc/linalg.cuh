@@ -96,6 +96,15 @@ size_t cholqr32_workspace(int p);
 int chol32_gram(const double* G, int p, float* L, float* Mb, int* info, cudaStream_t st);
 int trsm_rows_f32(float* V, int ldv, long long N, int p, const float* L, const float* Mb, cudaStream_t st);
 
+// FP32 symmetric eigensolver with the matrix in one SM's shared memory
+// (jacobi32.cu): H (p x p, FP32, not modified) -> eigenvalues w ascending and
+// eigenvectors V (p x p, columns), parallel cyclic Jacobi stopping at
+// off(H) <= tol ||H||_F or after max_sweeps sweeps.  p even, p <= jacobi32_max_p().
+int jacobi32_max_p();
+size_t jacobi32_workspace(int p, int max_sweeps);
+int jacobi32_eigh(const float* H, int p, float* w, float* V, int max_sweeps, double tol, int* sweeps_used, void* ws,
+                  size_t ws_bytes, cudaStream_t st);
+
 // Dtype conversion of an N x b block (ld in/out).
 int convert_f32_to_f64(const float* in, int ldi, double* out, int ldo, long long N, int b, cudaStream_t st);
 int convert_f64_to_f32(const double* in, int ldi, float* out, int ldo, long long N, int b, cudaStream_t st);
