@@ -22,6 +22,7 @@ Differences from the reference, each deliberate:
 from __future__ import annotations
 
 import math
+import threading
 from types import SimpleNamespace
 
 import numpy as np
@@ -63,7 +64,17 @@ class data:
         knn = _core.knn(X, n_neighbors)
         indptr, indices, maxdeg = _core.graph_build(knn)
         dev.indptr, dev.indices, dev.maxdeg = indptr, indices, maxdeg
+        dev.L_vals = _core.laplacian_values(indptr, indices)
+        dev.bound = 2.0 * maxdeg * (1.0 + 1e-12)  # spectral bound of L and Lc (|D| + |A|)
         mark("graph")
+
+        # The eigenpairs of L feed nothing downstream (the kernel is built on
+        # those of Lc), so they are computed on a second stream by a host
+        # thread while this one runs the gauges, the connections and the Lc
+        # eigensolve; every reader of evals_L / evecs_L waits for them (wait()).
+        m = n if n_eigenpairs is None else min(int(n_eigenpairs), n)
+        mode = "mixed" if precision == "mixed" else "fp64"
+        self._eig_L = self._start_eig_L(dev, n, m, mode, eig_tol, seed, timings is not None)
 
         _log(verbose, "Fit tangent spaces")
         K = int(n_neighbors * frac_geodesic_neighbours)
@@ -97,25 +108,26 @@ class data:
         _log(verbose, "Fit connections")
 
         _log(verbose, "Compute Laplacians")
-        dev.L_vals = _core.laplacian_values(indptr, indices)
-        dev.bound = 2.0 * maxdeg * (1.0 + 1e-12)  # spectral bound of L and Lc (|D| + |A|)
         mark("connections")
 
         _log(verbose, "Compute eigendecompositions")
-        m = n if n_eigenpairs is None else min(int(n_eigenpairs), n)
-        mode = "mixed" if precision == "mixed" else "fp64"
-        dev.evals_L, dev.evecs_L, dev.eig_info_L = _core.eigsh(indptr, indices, dev.L_vals, None, m=m, mode=mode,
-                                                               tol=eig_tol, seed=seed, scale=math.sqrt(n))
-        mark("eigsh_L")
-        dev.evals_Lc, U, dev.eig_info_Lc = _core.eigsh(indptr, indices, lc64, lc32, m=m, mode=mode, tol=eig_tol,
-                                                       seed=seed + 1, scale=math.sqrt(n * dim))
+        try:
+            dev.evals_Lc, U, dev.eig_info_Lc = _core.eigsh(indptr, indices, lc64, lc32, m=m, mode=mode, tol=eig_tol,
+                                                           seed=seed + 1, scale=math.sqrt(n * dim))
+        except BaseException:
+            self._eig_L["thread"].join()
+            raise
         dev.evecs_Lc_local = U
         dev.evecs_Lc = _core.lift(T, dim, U)
         mark("eigsh_Lc")
+        self._dev = dev
         if timings is not None:
+            st = self._eig_L
+            self.wait()
             torch.cuda.synchronize()
             for (a, ea), (b, eb) in zip(marks[:-1], marks[1:]):
                 timings[b] = timings.get(b, 0.0) + ea.elapsed_time(eb) / 1e3
+            timings["eigsh_L (concurrent)"] = st["seconds"]
         dev.vectors = None
         self._dev = dev
         self.n = n
@@ -123,6 +135,52 @@ class data:
         self.n_eigenpairs = m
         self._host = {}
         self.vectors = vectors
+
+    # ------------------------------------------------------------------ the concurrent eigensolve of L
+    @staticmethod
+    def _start_eig_L(dev, n, m, mode, eig_tol, seed, timed):
+        main = torch.cuda.current_stream()
+        side = torch.cuda.Stream()
+        side.wait_stream(main)  # L's CSR and values are ready
+        state = {"error": None, "seconds": None}
+
+        def run():
+            try:
+                with torch.cuda.device(main.device), torch.cuda.stream(side):
+                    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)] if timed else None
+                    if timed:
+                        ev[0].record()
+                    out = _core.eigsh(dev.indptr, dev.indices, dev.L_vals, None, m=m, mode=mode, tol=eig_tol,
+                                      seed=seed, scale=math.sqrt(n))
+                    if timed:
+                        ev[1].record()
+                    side.synchronize()
+                    dev.evals_L, dev.evecs_L, dev.eig_info_L = out
+                    if timed:
+                        state["seconds"] = ev[0].elapsed_time(ev[1]) / 1e3
+            except BaseException as e:  # re-raised by wait()
+                state["error"] = e
+
+        t = threading.Thread(target=run, name="rvgp-eigsh-L", daemon=True)
+        state["thread"] = t
+        state["stream"] = side
+        t.start()
+        return state
+
+    def wait(self):
+        """Block until the eigenpairs of L (computed concurrently) are ready; the
+        caller's current stream then also waits for them on the device."""
+        st = self.__dict__.get("_eig_L")
+        if st is None:
+            return self
+        st["thread"].join()
+        if st["error"] is not None:
+            err = st["error"]
+            st["error"] = None
+            raise err
+        torch.cuda.current_stream().wait_stream(st["stream"])
+        self.__dict__["_eig_L"] = None
+        return self
 
     # ------------------------------------------------------------------ host views
     def _cached(self, key, fn):
@@ -190,10 +248,12 @@ class data:
 
     @property
     def evals_L(self):
+        self.wait()
         return self._cached("evals_L", lambda: self._dev.evals_L.cpu().numpy())
 
     @property
     def evecs_L(self):
+        self.wait()
         return self._cached("evecs_L", lambda: self._dev.evecs_L.cpu().numpy())
 
     @property
