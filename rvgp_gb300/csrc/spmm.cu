@@ -10,7 +10,9 @@
 //
 // Thread mapping: one thread per (block-row, group of V consecutive columns),
 // V = 4 floats or 2 doubles (16-byte vector loads of X rows).  A row's gather
-// of X hits L2: the whole block (n*DB*b*size) is sized to stay resident.
+// of X hits L2: the whole block (n*DB*b*size) is sized to stay resident.  The
+// gather is latency-bound, so each thread keeps several neighbours' loads in
+// flight (the neighbour loop is unrolled with all loads ahead of the math).
 // HBM traffic per product ≈ E*(DB²*sv + 4) + 2*n*DB*b*sx (+ Z).
 #include "common.cuh"
 
@@ -57,11 +59,38 @@ __global__ void __launch_bounds__(256) bspmm_kernel(int n, const int* __restrict
 #pragma unroll
     for (int v = 0; v < V; ++v) acc[p][v] = T(0);
   const int s = indptr[i], e = indptr[i + 1];
-  for (int t = s; t < e; ++t) {
-    const int j = indices[t];
+  // U neighbours per iteration: all their index, block and X-row loads are
+  // issued before the first multiply-add, so U gathers are in flight at once
+  constexpr int U = DB <= 2 ? 4 : 2;
+  int t = s;
+  for (; t + U <= e; t += U) {
+    int j[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) j[u] = __ldg(indices + t + u);
+    T blk[U][DB * DB];
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int pq = 0; pq < DB * DB; ++pq) blk[u][pq] = __ldg(vals + (size_t)(t + u) * DB * DB + pq);
+    T x[U][DB][V];
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int q = 0; q < DB; ++q) vload(X + ((size_t)j[u] * DB + q) * ld + c0, x[u][q]);
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int q = 0; q < DB; ++q)
+#pragma unroll
+        for (int p = 0; p < DB; ++p)
+#pragma unroll
+          for (int v = 0; v < V; ++v) acc[p][v] = fma(blk[u][p * DB + q], x[u][q][v], acc[p][v]);
+  }
+  for (; t < e; ++t) {
+    const int j = __ldg(indices + t);
     T blk[DB * DB];
 #pragma unroll
-    for (int pq = 0; pq < DB * DB; ++pq) blk[pq] = vals[(size_t)t * DB * DB + pq];
+    for (int pq = 0; pq < DB * DB; ++pq) blk[pq] = __ldg(vals + (size_t)t * DB * DB + pq);
 #pragma unroll
     for (int q = 0; q < DB; ++q) {
       T x[V];
