@@ -111,14 +111,24 @@ class data:
         mark("connections")
 
         _log(verbose, "Compute eigendecompositions")
+        # The Lc eigensolve is on the critical path and shares the GPU with the
+        # L eigensolve: it runs on a higher-priority stream, so the block
+        # scheduler serves its kernels first.
+        caller = torch.cuda.current_stream()
+        hp = torch.cuda.Stream(priority=-1)
+        hp.wait_stream(caller)
         try:
-            dev.evals_Lc, U, dev.eig_info_Lc = _core.eigsh(indptr, indices, lc64, lc32, m=m, mode=mode, tol=eig_tol,
-                                                           seed=seed + 1, scale=math.sqrt(n * dim))
+            with torch.cuda.stream(hp):
+                dev.evals_Lc, U, dev.eig_info_Lc = _core.eigsh(indptr, indices, lc64, lc32, m=m, mode=mode,
+                                                               tol=eig_tol, seed=seed + 1, scale=math.sqrt(n * dim))
+                dev.evecs_Lc = _core.lift(T, dim, U)
         except BaseException:
             self._eig_L["thread"].join()
             raise
+        caller.wait_stream(hp)
+        for t_ in (dev.evals_Lc, U, dev.evecs_Lc):
+            t_.record_stream(caller)  # allocated on hp, used on the caller's stream
         dev.evecs_Lc_local = U
-        dev.evecs_Lc = _core.lift(T, dim, U)
         mark("eigsh_Lc")
         self._dev = dev
         if timings is not None:
