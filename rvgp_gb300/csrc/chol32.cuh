@@ -11,6 +11,7 @@
 #pragma once
 #include "common.cuh"
 #include <float.h>
+#include <limits.h>
 
 namespace rvgp {
 namespace chol32 {
@@ -106,14 +107,15 @@ __device__ void panel_solve(float* A, int ld, int j0, int m, const float* dinvL)
 
 // Trailing update of the lower part: A[i][k] -= Σ_c L[i][j0+c] L[k][j0+c] for
 // r0 <= k <= i < m, 4 x 4 register tiles, operands read as float4 along c.
-template <int NT>
-__device__ void trailing_update(float* A, int ld, int j0, int m) {
+// Tiles are numbered row by row over the lower triangle (t -> (ti, tk), tk <=
+// ti); this call does tiles t0 + first, t0 + first + stride, ... below t1.
+__device__ inline void update_tiles(float* A, int ld, int j0, int m, int t0, int t1, int first, int stride) {
   const int r0 = j0 + FB;
   const int R = m - r0;
   if (R <= 0) return;
   const int TR = (R + 3) / 4;
-  const int tiles = TR * (TR + 1) / 2;
-  for (int t = threadIdx.x; t < tiles; t += NT) {
+  const int tiles = min(t1, TR * (TR + 1) / 2);
+  for (int t = t0 + first; t < tiles; t += stride) {
     int ti = (int)((sqrtf(8.f * t + 1.f) - 1.f) * 0.5f);
     while (ti * (ti + 1) / 2 > t) --ti;
     while ((ti + 1) * (ti + 2) / 2 <= t) ++ti;
@@ -157,6 +159,11 @@ __device__ void trailing_update(float* A, int ld, int j0, int m) {
   }
 }
 
+template <int NT>
+__device__ void trailing_update(float* A, int ld, int j0, int m) {
+  update_tiles(A, ld, j0, m, 0, INT_MAX, threadIdx.x, NT);
+}
+
 // Warp w < nblk: inverse Mb of the factor's diagonal block w by solving
 // L X = I with lane i holding row i of X in registers: step c scales row c
 // (lane c) and every lane i > c subtracts L_ic times it (shuffled).  Mb is
@@ -190,26 +197,38 @@ __device__ inline void invert_diag_blocks(float* A, int ld, int m, int nblk, con
 // The blocked factorisation of the lower triangle of A in place (all threads
 // of the CTA call it).  dinvL[i] = 1/L_ii.  Returns false (on every thread) if
 // a pivot was not positive; *s_flag is a shared int the CTA uses for that.
+// Lookahead: after panel jb is solved, warp 0 applies panel jb's update to the
+// next diagonal block and factors it while the other warps update the rest of
+// the trailing matrix, so the diagonal chain overlaps the largest updates.
 template <int NT>
 __device__ bool chol32_cta(float* A, int ld, int m, float* dinvL, int* s_flag) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nblk = (m + FB - 1) / FB;
   if (threadIdx.x == 0) *s_flag = 0;
   __syncthreads();
-  for (int jb = 0; jb < nblk; ++jb) {
-    const int j0 = jb * FB, nb = min(FB, m - j0);
+  if (warp == 0 && !chol_diag_block(A, ld, 0, min(FB, m), dinvL) && lane == 0) *s_flag = 1;
+  __syncthreads();
+  if (*s_flag) return false;
+  for (int jb = 0; jb + 1 < nblk; ++jb) {
+    const int j0 = jb * FB, r0 = j0 + FB;
+    const int nb1 = min(FB, m - r0);
+    panel_solve<NT>(A, ld, j0, m, dinvL);
+    __syncthreads();
+    // tiles of the next diagonal block: tile rows ti < ceil(nb1 / 4)
+    const int tr1 = (nb1 + 3) / 4;
+    const int tdiag = tr1 * (tr1 + 1) / 2;
     if (warp == 0) {
-      const bool ok = chol_diag_block(A, ld, j0, nb, dinvL);
-      if (!ok && lane == 0) *s_flag = 1;
+      update_tiles(A, ld, j0, m, 0, tdiag, lane, 32);
+      __syncwarp();
+      if (!chol_diag_block(A, ld, r0, nb1, dinvL) && lane == 0) *s_flag = 1;
+    } else if (warp % 4 != 0) {
+      // warps 4, 8, ... share warp 0's scheduler (warp w issues on sub-partition
+      // w % 4) and stay idle, so the latency-bound diagonal chain is not starved
+      constexpr int kUpd = NT / 32 - NT / 128;
+      update_tiles(A, ld, j0, m, tdiag, INT_MAX, (warp - warp / 4 - 1) * 32 + lane, kUpd * 32);
     }
     __syncthreads();
     if (*s_flag) return false;
-    if (j0 + FB < m) {
-      panel_solve<NT>(A, ld, j0, m, dinvL);
-      __syncthreads();
-      trailing_update<NT>(A, ld, j0, m);
-      __syncthreads();
-    }
   }
   return true;
 }

@@ -6,7 +6,8 @@
 // (p - 1 rounds per sweep).  Here a round costs one CTA barrier: the p/2
 // rotations of a round (circle-method pairing) act on disjoint index pairs,
 // so the two-sided update H <- Jᵀ H J splits into independent 2 x 2 blocks
-// (pair a, pair b) that one thread reads, rotates and writes in place.
+// (pair a, pair b) that one thread reads, rotates and writes in place.  Only
+// the upper triangle is stored (a block and its transpose share storage).
 // The eigenvector matrix is not carried along: every round's (cos, sin) are
 // logged, and jacobi32_replay rotates rows of V = I independently (one CTA
 // per four rows), which also applies the final sort by eigenvalue.
@@ -69,9 +70,11 @@ __global__ void __launch_bounds__(kThreads, 1)
   int2* pq = reinterpret_cast<int2*>(key + 2 * p);
   int* key_idx = reinterpret_cast<int*>(pq + np);  // 2p ints
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  // symmetric storage: element (i, j) lives at (min, max) in the upper triangle
+  auto at = [&](int i, int j) -> float& { return H[min(i, j) * ldh + max(i, j)]; };
   for (int e = tid; e < p * p; e += kThreads) {
     const int i = e / p, j = e % p;
-    H[i * ldh + j] = 0.5f * (Hin[(size_t)i * p + j] + Hin[(size_t)j * p + i]);
+    if (i <= j) H[i * ldh + j] = 0.5f * (Hin[(size_t)i * p + j] + Hin[(size_t)j * p + i]);
   }
   __syncthreads();
   int used = 0;
@@ -80,9 +83,11 @@ __global__ void __launch_bounds__(kThreads, 1)
     float off = 0.f, tot = 0.f;
     for (int e = tid; e < p * p; e += kThreads) {
       const int i = e / p, j = e % p;
+      if (i > j) continue;
       const float v = H[i * ldh + j];
-      tot = fmaf(v, v, tot);
-      if (i != j) off = fmaf(v, v, off);
+      const float w2 = (i == j) ? v * v : 2.f * v * v;  // the upper entry stands for both
+      tot += w2;
+      if (i != j) off += w2;
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -115,7 +120,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       for (int k = tid; k < np; k += kThreads) {
         const int2 q = pair_of(r, k, p);
         float c, s;
-        rotation(H[q.x * ldh + q.x], H[q.y * ldh + q.y], H[q.x * ldh + q.y], c, s);
+        rotation(H[q.x * ldh + q.x], H[q.y * ldh + q.y], H[q.x * ldh + q.y], c, s);  // q.x < q.y
         cs[k] = c;
         sn[k] = s;
         pq[k] = q;
@@ -130,8 +135,8 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int b = a + lane; b < np; b += 32) {
           const int2 B = pq[b];
           const float cb = cs[b], sb = sn[b];
-          const float x00 = H[A.x * ldh + B.x], x01 = H[A.x * ldh + B.y];
-          const float x10 = H[A.y * ldh + B.x], x11 = H[A.y * ldh + B.y];
+          const float x00 = at(A.x, B.x), x01 = at(A.x, B.y);
+          const float x10 = at(A.y, B.x), x11 = at(A.y, B.y);
           // T = X J_b, J = [[c, s], [-s, c]]
           const float t00 = cb * x00 - sb * x01, t01 = sb * x00 + cb * x01;
           const float t10 = cb * x10 - sb * x11, t11 = sb * x10 + cb * x11;
@@ -141,17 +146,12 @@ __global__ void __launch_bounds__(kThreads, 1)
           if (a == b) {
             H[A.x * ldh + A.x] = y00;
             H[A.y * ldh + A.y] = y11;
-            H[A.x * ldh + A.y] = 0.f;
-            H[A.y * ldh + A.x] = 0.f;
+            H[A.x * ldh + A.y] = 0.f;  // A.x < A.y
           } else {
-            H[A.x * ldh + B.x] = y00;
-            H[A.x * ldh + B.y] = y01;
-            H[A.y * ldh + B.x] = y10;
-            H[A.y * ldh + B.y] = y11;
-            H[B.x * ldh + A.x] = y00;
-            H[B.y * ldh + A.x] = y01;
-            H[B.x * ldh + A.y] = y10;
-            H[B.y * ldh + A.y] = y11;
+            at(A.x, B.x) = y00;
+            at(A.x, B.y) = y01;
+            at(A.y, B.x) = y10;
+            at(A.y, B.y) = y11;
           }
         }
       }

@@ -90,6 +90,23 @@ def test_gauges_match_reference(core, name):
     assert np.abs(G - np.eye(T.shape[2])).max() < 1e-12
 
 
+def test_gauges_pool_overflow_fallback(core):
+    """k = 40 (K = 60): about 40 % of the searches touch more nodes than the
+    256-slot shared-memory pool holds and are redone by the global-memory
+    search; every neighbourhood must still equal the oracle's heap order."""
+    from rvgp_gb300.workloads import make_points
+    X = make_points("sphere", 3000, seed=4)
+    k, K = 40, 60
+    nn = O.knn(X, k)
+    ipn, ixn = O.symmetrised_csr(nn, len(X))
+    maxdeg = int(np.diff(ipn).max() - 1)
+    T, S, nbh = core.gauges(cu(X), cu(ipn, torch.int32), cu(ixn, torch.int32), K, maxdeg, 2, return_nbh=True)
+    assert np.array_equal(nbh.cpu().numpy(), O.geodesic_neighbourhoods(ipn, ixn, K))
+    Tr, Sr = O.tangent_frames(X, O.geodesic_neighbourhoods(ipn, ixn, K), 3)
+    np.testing.assert_allclose(S.cpu().numpy(), Sr, rtol=1e-10, atol=1e-13)
+    assert projector_distance(T.cpu().numpy(), Tr[:, :, :2]) < 1e-10
+
+
 def test_gauges_component_too_small(core):
     # two far-apart clusters of 5 points each: K=6 cannot be met inside a component
     rng = np.random.default_rng(0)
