@@ -167,10 +167,12 @@ SPMM_TRAFFIC_BYTES = 112_407_040
 def spmm_roofline(d, wl, peaks, flush, reps=20):
     """Achieved HBM bandwidth of the eigensolver's Chebyshev-step SpMM (FP32,
     block width p) on this workload's connection Laplacian: each launch timed
-    alone with CUDA events on the launching stream, L2 flushed before it."""
+    alone with CUDA events on the launching stream, L2 flushed before it.  The
+    matrix is the Morton-renumbered one the eigensolver multiplies by."""
     import torch
     from rvgp_gb300 import _core
     dev = d._dev
+    ip, ix, _, v32 = _core.permute_csr(dev.indptr, dev.indices, dev.Lc_vals, dev.Lc_vals32, dev.perm, dev.rank)
     n, k = d.n, d.dim_man
     N = n * k
     p = _core.block_size(wl["m"], N)
@@ -178,14 +180,14 @@ def spmm_roofline(d, wl, peaks, flush, reps=20):
     Z = torch.randn_like(X)
     Y = torch.empty_like(X)
     for _ in range(3):
-        _core.bspmm(dev.indptr, dev.indices, dev.Lc_vals32, X, Y, Z, 0.1, -0.2, 0.3)
+        _core.bspmm(ip, ix, v32, X, Y, Z, 0.1, -0.2, 0.3)
     s = torch.cuda.current_stream()
     times = []
     for _ in range(reps):
         flush_l2(flush)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(s)
-        _core.bspmm(dev.indptr, dev.indices, dev.Lc_vals32, X, Y, Z, 0.1, -0.2, 0.3)
+        _core.bspmm(ip, ix, v32, X, Y, Z, 0.1, -0.2, 0.3)
         e1.record(s)
         torch.cuda.synchronize()
         times.append(e0.elapsed_time(e1) / 1e3)

@@ -113,6 +113,35 @@ size_t rvgp_eigsh_workspace(int n, int DB, int m, int p, int mode);
 int rvgp_eigsh(const int* indptr, const int* indices, const double* vals64, const float* vals32, int n, int DB, int m,
                int p, int mode, double tol, double tol32, int max_iter, unsigned long long seed, double* evals,
                double* evecs, int ld_evecs, double scale, int* stats, void* workspace, size_t ws_bytes, void* stream);
+/* The same solve on a renumbered matrix (rvgp_permute_csr): block row r is the
+ * caller's block row perm[r].  The start block is the caller-order one,
+ * permuted, and evecs come back in the caller's row order, so the result is
+ * rvgp_eigsh's on the original matrix up to summation order. */
+int rvgp_eigsh_ordered(const int* indptr, const int* indices, const double* vals64, const float* vals32, int n,
+                       int DB, int m, int p, int mode, double tol, double tol32, int max_iter, unsigned long long seed,
+                       const int* perm, double* evals, double* evecs, int ld_evecs, double scale, int* stats,
+                       void* workspace, size_t ws_bytes, void* stream);
+
+/* ---- locality renumbering for the sparse products ---------------------- */
+
+/* perm (n, device): new position -> point, along a Morton curve of the three
+ * coordinates of largest extent (10 bits each over the bounding box; ties in
+ * point order); rank its inverse.  No reference counterpart: the sparse
+ * products of the eigensolves (RVGP/geometry.py:66-80) run on matrices
+ * renumbered by it.  Synchronises the stream once. */
+size_t rvgp_locality_order_workspace(int n, int D);
+int rvgp_locality_order(const double* X, int n, int D, int* perm, int* rank, void* workspace, size_t ws_bytes,
+                        void* stream);
+/* Block-CSR renumbered by perm/rank: new row r = old row perm[r], columns
+ * c -> rank[c], entries of a row in their original order.  vals32 and
+ * out_vals32 may be null. */
+size_t rvgp_permute_csr_workspace(int n);
+int rvgp_permute_csr(int n, int DB, const int* indptr, const int* indices, const double* vals64, const float* vals32,
+                     const int* perm, const int* rank, int* out_indptr, int* out_indices, double* out_vals64,
+                     float* out_vals32, void* workspace, size_t ws_bytes, void* stream);
+/* dst[(i*DB+q), :m] = src[(rank[i]*DB+q), :m]: renumbered rows back to point order. */
+int rvgp_unpermute_rows(const double* src, int lds, const int* rank, int n, int DB, int m, double* dst, int ldd,
+                        void* stream);
 
 /* ---- spectral kernel and GP ------------------------------------------- */
 
@@ -167,6 +196,17 @@ int rvgp_gp_fit_adam_mixed(const double* C, const double* b, const double* yy, l
                            const int* mask, int steps, double lr, double beta1, double beta2, double eps,
                            double* theta_out, double* hist, double* out, double* state, int* status, void* workspace,
                            size_t ws_bytes, void* stream);
+/* The same in two calls: _launch enqueues the fit without waiting (the host
+ * may queue other work, e.g. on another stream, while the one-CTA fit runs);
+ * _finish, on the same stream and workspace, waits and sets *status as above. */
+int rvgp_gp_fit_adam_mixed_launch(const double* C, const double* b, const double* yy, long long N, int m,
+                                  const double* evals, double n_rows, int typ, const double* theta0,
+                                  const double* lower, const int* mask, int steps, double lr, double beta1,
+                                  double beta2, double eps, double* theta_out, double* hist, void* workspace,
+                                  size_t ws_bytes, void* stream);
+int rvgp_gp_fit_adam_mixed_finish(const double* C, const double* b, const double* yy, long long N, int m,
+                                  const double* evals, double n_rows, int typ, const double* theta_out, double* out,
+                                  double* state, int* status, void* workspace, size_t ws_bytes, void* stream);
 /* predict_f(full_cov=False) mean and variance at Nte rows (RVGP/main.py:102-116). */
 size_t rvgp_gp_predict_workspace(long long Nte, int m, int mode);
 int rvgp_gp_predict(const double* Phi_star, const float* Phi_star32, long long Nte, int m, int mode,

@@ -50,6 +50,10 @@ SIGNATURES = {
     "rvgp_gp_fit_mixed_workspace": (c_size_t, [c_int]),
     "rvgp_gp_fit_adam_mixed": (c_int, [P, P, P, ctypes.c_longlong, c_int, P, c_double, c_int, P, P, P, c_int,
                                        c_double, c_double, c_double, c_double, P, P, P, P, P, P, c_size_t, P]),
+    "rvgp_gp_fit_adam_mixed_launch": (c_int, [P, P, P, ctypes.c_longlong, c_int, P, c_double, c_int, P, P, P, c_int,
+                                              c_double, c_double, c_double, c_double, P, P, P, c_size_t, P]),
+    "rvgp_gp_fit_adam_mixed_finish": (c_int, [P, P, P, ctypes.c_longlong, c_int, P, c_double, c_int, P, P, P, P, P,
+                                              c_size_t, P]),
     "rvgp_gp_predict_workspace": (c_size_t, [ctypes.c_longlong, c_int, c_int]),
     "rvgp_gp_predict": (c_int, [P, P, ctypes.c_longlong, c_int, c_int, P, P, P, P, c_size_t, P]),
     "rvgp_kernel_matrix": (c_int, [P, ctypes.c_longlong, P, ctypes.c_longlong, c_int, P, P, P]),
@@ -70,6 +74,13 @@ SIGNATURES = {
     "rvgp_diameter": (c_int, [P, c_int, c_int, P, P, c_size_t, P]),
     "rvgp_eigsh": (c_int, [P, P, P, P, c_int, c_int, c_int, c_int, c_int, c_double, c_double, c_int, ctypes.c_ulonglong,
                            P, P, c_int, c_double, P, P, c_size_t, P]),
+    "rvgp_eigsh_ordered": (c_int, [P, P, P, P, c_int, c_int, c_int, c_int, c_int, c_double, c_double, c_int,
+                                   ctypes.c_ulonglong, P, P, P, c_int, c_double, P, P, c_size_t, P]),
+    "rvgp_locality_order_workspace": (c_size_t, [c_int, c_int]),
+    "rvgp_locality_order": (c_int, [P, c_int, c_int, P, P, P, c_size_t, P]),
+    "rvgp_permute_csr_workspace": (c_size_t, [c_int]),
+    "rvgp_permute_csr": (c_int, [c_int, c_int, P, P, P, P, P, P, P, P, P, P, P, c_size_t, P]),
+    "rvgp_unpermute_rows": (c_int, [P, c_int, P, c_int, c_int, c_int, P, c_int, P]),
 }
 
 _LIB = None
@@ -227,11 +238,13 @@ def block_size(m, N):
 
 
 def eigsh(indptr, indices, vals64, vals32=None, m=10, mode="mixed", tol=None, tol32=2e-5, max_iter=60, seed=0,
-          scale=None, p=None):
+          scale=None, p=None, perm=None):
     """m smallest eigenpairs of the block-CSR matrix: (evals (m,), evecs (N, m), stats dict).
 
     evecs are orthonormal times ``scale`` (default 1).  mode: "mixed" (FP32
-    bulk + FP64 refinement) or "fp64" (plain FP64).
+    bulk + FP64 refinement) or "fp64" (plain FP64).  With ``perm`` the matrix
+    is a renumbered one (``permute_csr``): block row r is the caller's block
+    row perm[r], and evecs come back in the caller's row order.
     """
     n = indptr.numel() - 1
     DB = 1 if vals64.dim() == 1 else vals64.shape[-1]
@@ -250,9 +263,15 @@ def eigsh(indptr, indices, vals64, vals32=None, m=10, mode="mixed", tol=None, to
         tol = tol32 if imode == 1 else 1e-11
     L = lib()
     ws = workspace(L.rvgp_eigsh_workspace(n, DB, m, p, imode), dev)
-    st = L.rvgp_eigsh(ptr(indptr), ptr(indices), ptr(vals64), ptr(vals32), n, DB, m, p, imode, tol, tol32, max_iter,
-                      seed, ptr(evals), ptr(evecs), m, 1.0 if scale is None else float(scale), stats, ptr(ws),
-                      ws.numel(), stream())
+    sc = 1.0 if scale is None else float(scale)
+    if perm is None:
+        st = L.rvgp_eigsh(ptr(indptr), ptr(indices), ptr(vals64), ptr(vals32), n, DB, m, p, imode, tol, tol32,
+                          max_iter, seed, ptr(evals), ptr(evecs), m, sc, stats, ptr(ws), ws.numel(), stream())
+    else:
+        perm = _dev(perm, torch.int32, "perm")
+        st = L.rvgp_eigsh_ordered(ptr(indptr), ptr(indices), ptr(vals64), ptr(vals32), n, DB, m, p, imode, tol,
+                                  tol32, max_iter, seed, ptr(perm), ptr(evals), ptr(evecs), m, sc, stats, ptr(ws),
+                                  ws.numel(), stream())
     info = dict(iters=stats[0], spmm=stats[1], sweeps=stats[2], converged=stats[3], refine_iters=stats[4],
                 chol_rescues=stats[5], p=p, filter_ms=stats[8] / 1e3, orth_ms=stats[9] / 1e3,
                 rr_ms=stats[10] / 1e3, jacobi_ms=stats[11] / 1e3)
@@ -261,6 +280,46 @@ def eigsh(indptr, indices, vals64, vals32=None, m=10, mode="mixed", tol=None, to
     if st > 0:
         raise RuntimeError(f"ARPACK-equivalent no convergence: {lib().rvgp_last_error().decode()}")
     return evals, evecs, info
+
+
+def locality_order(X):
+    """Morton-curve renumbering of the points X (n, D) float64: (perm, rank),
+    perm[r] = point at new position r, rank its inverse (int32, device)."""
+    X = _dev(X, torch.float64, "X")
+    n, D = X.shape
+    perm = torch.empty(n, dtype=torch.int32, device=X.device)
+    rank = torch.empty(n, dtype=torch.int32, device=X.device)
+    ws = workspace(lib().rvgp_locality_order_workspace(n, D), X.device)
+    check(lib().rvgp_locality_order(ptr(X), n, D, ptr(perm), ptr(rank), ptr(ws), ws.numel(), stream()),
+          "rvgp_locality_order")
+    return perm, rank
+
+
+def permute_csr(indptr, indices, vals64, vals32, perm, rank):
+    """The block-CSR matrix renumbered by perm: (indptr, indices, vals64, vals32)."""
+    n = indptr.numel() - 1
+    DB = 1 if vals64.dim() == 1 else vals64.shape[-1]
+    dev = vals64.device
+    out_ptr = torch.empty(n + 1, dtype=torch.int32, device=dev)
+    out_idx = torch.empty_like(indices)
+    out64 = torch.empty_like(vals64)
+    out32 = None if vals32 is None else torch.empty_like(vals32)
+    ws = workspace(lib().rvgp_permute_csr_workspace(n), dev)
+    check(lib().rvgp_permute_csr(n, DB, ptr(indptr), ptr(indices), ptr(vals64.contiguous()),
+                                 ptr(None if vals32 is None else vals32.contiguous()), ptr(perm), ptr(rank),
+                                 ptr(out_ptr), ptr(out_idx), ptr(out64), ptr(out32), ptr(ws), ws.numel(), stream()),
+          "rvgp_permute_csr")
+    return out_ptr, out_idx, out64, out32
+
+
+def unpermute_rows(src, rank, DB=1):
+    """Rows of src (n*DB, m) float64 in the renumbered order -> caller's order."""
+    src = _dev(src, torch.float64, "src")
+    N, m = src.shape
+    n = N // DB
+    out = torch.empty_like(src)
+    check(lib().rvgp_unpermute_rows(ptr(src), m, ptr(rank), n, DB, m, ptr(out), m, stream()), "rvgp_unpermute_rows")
+    return out
 
 
 # ---------------------------------------------------------------------------- GP
@@ -358,10 +417,12 @@ def gp_fit_mixed_max_m():
 
 
 def gp_fit_adam_mixed(C, b, yy, N, evals, n_rows, theta0, lower, mask, steps, lr=0.05, betas=(0.9, 0.999),
-                      eps=1e-8, typ="matern", work=None, history=False):
+                      eps=1e-8, typ="matern", work=None, history=False, on_launch=None):
     """Adam with the m x m algebra of every step in FP32 inside one launch
     (rvgp_gp_fit_adam_mixed).  Returns (theta, out, history, work, ok); ok is
-    False when an FP32 pivot failed, and nothing was fitted."""
+    False when an FP32 pivot failed, and nothing was fitted.  ``on_launch``
+    (optional) is called once the one-CTA fit kernel is queued on an idle
+    device, before waiting for it."""
     m = evals.numel()
     dev = evals.device
     work = work or LMLWorkspace(m, dev)
@@ -372,10 +433,20 @@ def gp_fit_adam_mixed(C, b, yy, N, evals, n_rows, theta0, lower, mask, steps, lr
     lo = (ctypes.c_double * 4)(*[float(v) for v in lower])
     mk = (ctypes.c_int * 4)(*[int(bool(v)) for v in mask])
     status = ctypes.c_int(0)
-    check(L.rvgp_gp_fit_adam_mixed(ptr(C), ptr(b), ptr(yy), int(N), m, ptr(evals), float(n_rows), KERNEL_TYPES[typ],
-                                   ptr(theta0.contiguous()), lo, mk, int(steps), float(lr), float(betas[0]),
-                                   float(betas[1]), float(eps), ptr(theta), ptr(hist), ptr(work.out),
-                                   ptr(work.state), ctypes.byref(status), ptr(ws), ws.numel(), stream()),
+    theta0 = theta0.contiguous()
+    if on_launch is not None:
+        # the fit's single CTA needs most of an SM: queue it on an idle
+        # device, so it is resident before the caller's other work spreads
+        torch.cuda.current_stream().synchronize()
+    check(L.rvgp_gp_fit_adam_mixed_launch(ptr(C), ptr(b), ptr(yy), int(N), m, ptr(evals), float(n_rows),
+                                          KERNEL_TYPES[typ], ptr(theta0), lo, mk, int(steps), float(lr),
+                                          float(betas[0]), float(betas[1]), float(eps), ptr(theta), ptr(hist),
+                                          ptr(ws), ws.numel(), stream()), "rvgp_gp_fit_adam_mixed")
+    if on_launch is not None:
+        on_launch()
+    check(L.rvgp_gp_fit_adam_mixed_finish(ptr(C), ptr(b), ptr(yy), int(N), m, ptr(evals), float(n_rows),
+                                          KERNEL_TYPES[typ], ptr(theta), ptr(work.out), ptr(work.state),
+                                          ctypes.byref(status), ptr(ws), ws.numel(), stream()),
           "rvgp_gp_fit_adam_mixed")
     return theta, work.out, hist, work, status.value == 0
 

@@ -46,6 +46,17 @@ struct Workspace {
   bool ok() const { return base == nullptr || used <= cap; }
 };
 
+// Device-to-host read of results queued on `st`: waits for the stream first
+// and copies after.  A copy into pageable host memory issued while the
+// stream is still busy blocks the CUDA calls of every other host thread
+// until it completes; waiting in cudaStreamSynchronize does not.
+inline cudaError_t read_back(void* dst, const void* src, size_t bytes, cudaStream_t st) {
+  cudaError_t e = cudaStreamSynchronize(st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  return e;
+}
+
 inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 
 constexpr int kNumSMs = 152;  // GB300: 2 dies x 76 SMs

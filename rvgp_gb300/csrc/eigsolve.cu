@@ -74,13 +74,18 @@ __device__ __forceinline__ double hash_uniform(unsigned long long seed, unsigned
   return (double)(z >> 11) * (1.0 / 9007199254740992.0) - 0.5;
 }
 
+// Start block: entry (r, j) is a hash of its position in the caller's row
+// numbering, so a renumbered matrix (row r = original block row perm[r / DB])
+// starts from the same block, permuted.
 template <typename T>
-__global__ void random_block(T* __restrict__ V, long long N, int p, int ld, unsigned long long seed) {
+__global__ void random_block(T* __restrict__ V, long long N, int p, int ld, unsigned long long seed,
+                             const int* __restrict__ perm, int DB) {
   const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (e >= N * p) return;
   const long long r = e / p;
   const int j = (int)(e % p);
-  V[r * ld + j] = (T)hash_uniform(seed, (unsigned long long)e);
+  const long long ro = perm ? (long long)perm[r / DB] * DB + r % DB : r;
+  V[r * ld + j] = (T)hash_uniform(seed, (unsigned long long)(ro * p + j));
 }
 
 // B (p x p, type T) = Linvᵀ, i.e. B[k][j] = Linv[j][k]
@@ -135,12 +140,13 @@ __global__ void resid_final(const double* __restrict__ part, int nchunk, int b, 
 
 template <typename T>
 __global__ void write_output(const T* __restrict__ V, int ldv, long long N, int m, double scale, double* __restrict__ out,
-                             int ldo) {
+                             int ldo, const int* __restrict__ perm, int DB) {
   const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (e >= N * m) return;
   const long long r = e / m;
   const int j = (int)(e % m);
-  out[r * ldo + j] = scale * (double)V[r * ldv + j];
+  const long long ro = perm ? (long long)perm[r / DB] * DB + r % DB : r;
+  out[ro * ldo + j] = scale * (double)V[r * ldv + j];
 }
 
 int resid_chunks(long long N) { return (int)std::max<long long>(1, std::min<long long>(512, N / 128)); }
@@ -283,8 +289,7 @@ int orthonormalise(const Problem& P, Block<T>& B, Small& s, Stats& stt, cudaStre
       // a failed pivot falls through to the FP64 factorisation of the same Gram
       TRY(chol32_gram(s.G, p, s.L32, s.Mb32, s.info, st));
       int info32 = 0;
-      cudaMemcpyAsync(&info32, s.info, sizeof(int), cudaMemcpyDeviceToHost, st);
-      if (cudaStreamSynchronize(st) != cudaSuccess) return check_launch("orthonormalise");
+      if (read_back(&info32, s.info, sizeof(int), st) != cudaSuccess) return check_launch("orthonormalise");
       if (info32 == 0) {
         TRY(trsm_rows_f32(reinterpret_cast<float*>(B.V), p, N, p, s.L32, s.Mb32, st));
         continue;
@@ -292,8 +297,7 @@ int orthonormalise(const Problem& P, Block<T>& B, Small& s, Stats& stt, cudaStre
     }
     TRY(cholesky<double>(s.G, p, p, s.info, st));
     int info = 0;
-    cudaMemcpyAsync(&info, s.info, sizeof(int), cudaMemcpyDeviceToHost, st);
-    if (cudaStreamSynchronize(st) != cudaSuccess) return check_launch("orthonormalise");
+    if (read_back(&info, s.info, sizeof(int), st) != cudaSuccess) return check_launch("orthonormalise");
     if (info != 0) {
       // numerically rank-deficient block: shifted Cholesky QR on a fresh Gram
       ++stt.chol_rescues;
@@ -304,8 +308,7 @@ int orthonormalise(const Problem& P, Block<T>& B, Small& s, Stats& stt, cudaStre
       TRY(gram_any(B.V, B.V, N, p, s.G, s, st));
       rvgp::note_launch(); shift_diag<<<1, 256, 0, st>>>(s.G, p, 1e-6);
       TRY(cholesky<double>(s.G, p, p, s.info, st));
-      cudaMemcpyAsync(&info, s.info, sizeof(int), cudaMemcpyDeviceToHost, st);
-      if (cudaStreamSynchronize(st) != cudaSuccess) return check_launch("orthonormalise");
+      if (read_back(&info, s.info, sizeof(int), st) != cudaSuccess) return check_launch("orthonormalise");
       if (info != 0) {
         set_error("eigensolver: Cholesky QR failed (block lost rank)");
         return 1;
@@ -360,9 +363,9 @@ int rayleigh_ritz(const Problem& P, Block<T>& B, Small& s, Stats& stt, int max_s
   cudaEventRecord(ev.e[5], st);
   theta.resize(p);
   res.resize(p);
-  cudaMemcpyAsync(theta.data(), s.theta, sizeof(double) * p, cudaMemcpyDeviceToHost, st);
-  cudaMemcpyAsync(res.data(), s.res, sizeof(double) * p, cudaMemcpyDeviceToHost, st);
-  if (cudaStreamSynchronize(st) != cudaSuccess) return check_launch("rayleigh_ritz");
+  if (read_back(theta.data(), s.theta, sizeof(double) * p, st) != cudaSuccess ||
+      read_back(res.data(), s.res, sizeof(double) * p, st) != cudaSuccess)
+    return check_launch("rayleigh_ritz");
   ev.collect(stt);
   return check_launch("rayleigh_ritz");
 }
@@ -499,10 +502,10 @@ RVGP_API size_t rvgp_eigsh_workspace(int n, int DB, int m, int p, int mode) {
 // `scale`.  stats (host, 8 ints, may be null): iterations, SpMM count, Jacobi
 // sweeps, converged, FP64 refinement iterations, Cholesky rescues.
 // Returns 0, or the number of unconverged eigenpairs (> 0).  Synchronises.
-RVGP_API int rvgp_eigsh(const int* indptr, const int* indices, const double* vals64, const float* vals32, int n,
-                        int DB, int m, int p, int mode, double tol, double tol32, int max_iter,
-                        unsigned long long seed, double* evals, double* evecs, int ld_evecs, double scale, int* stats,
-                        void* workspace, size_t ws_bytes, void* stream) {
+static int eigsh_impl(const int* indptr, const int* indices, const double* vals64, const float* vals32, int n,
+                      int DB, int m, int p, int mode, double tol, double tol32, int max_iter,
+                      unsigned long long seed, const int* perm, double* evals, double* evecs, int ld_evecs,
+                      double scale, int* stats, void* workspace, size_t ws_bytes, void* stream) {
   const long long N = (long long)n * DB;
   RVGP_CHECK_ARG(indptr && indices && vals64 && evals && evecs, "rvgp_eigsh: null pointer");
   RVGP_CHECK_ARG(mode == 0 || (mode == 1 && vals32), "rvgp_eigsh: mode 1 needs FP32 values");
@@ -524,8 +527,7 @@ RVGP_API int rvgp_eigsh(const int* indptr, const int* indices, const double* val
   const int gb = std::min(kNumSMs * 2, ceil_div(N, 256));
   rvgp::note_launch(); gershgorin_kernel<<<gb, 256, 0, st>>>(n, DB, indptr, vals64, s.gersh);
   std::vector<double> gp(gb);
-  cudaMemcpyAsync(gp.data(), s.gersh, sizeof(double) * gb, cudaMemcpyDeviceToHost, st);
-  if (cudaStreamSynchronize(st) != cudaSuccess) return check_launch("rvgp_eigsh");
+  if (read_back(gp.data(), s.gersh, sizeof(double) * gb, st) != cudaSuccess) return check_launch("rvgp_eigsh");
   double bup = 0.0;
   for (double v : gp) bup = std::max(bup, v);
   bup = bup * (1.0 + 1e-12) + 1e-300;
@@ -534,7 +536,7 @@ RVGP_API int rvgp_eigsh(const int* indptr, const int* indices, const double* val
   int nconv = 0;
   const int first_deg = 12;
   if (mode == 1) {
-    rvgp::note_launch(); random_block<float><<<ceil_div(N * p, 256), 256, 0, st>>>(L.f.V, N, p, p, seed);
+    rvgp::note_launch(); random_block<float><<<ceil_div(N * p, 256), 256, 0, st>>>(L.f.V, N, p, p, seed, perm, DB);
     TRY(iterate<float>(P, L.f, s, stt, bup, tol32, max_iter, first_deg, 1e4, theta, res, false, &nconv, st));
     // FP64 refinement from the FP32 subspace
     TRY(convert_f32_to_f64(L.f.V, p, L.d.V, p, N, p, st));
@@ -547,12 +549,12 @@ RVGP_API int rvgp_eigsh(const int* indptr, const int* indices, const double* val
       stt.refine_iters = stt.iters - before;
     }
   } else {
-    rvgp::note_launch(); random_block<double><<<ceil_div(N * p, 256), 256, 0, st>>>(L.d.V, N, p, p, seed);
+    rvgp::note_launch(); random_block<double><<<ceil_div(N * p, 256), 256, 0, st>>>(L.d.V, N, p, p, seed, perm, DB);
     TRY(iterate<double>(P, L.d, s, stt, bup, tol, max_iter, first_deg, 1e10, theta, res, false, &nconv, st));
   }
   stt.conv = nconv;
   cudaMemcpyAsync(evals, s.theta, sizeof(double) * m, cudaMemcpyDeviceToDevice, st);
-  rvgp::note_launch(); write_output<double><<<ceil_div(N * m, 256), 256, 0, st>>>(L.d.V, p, N, m, scale, evecs, ld_evecs);
+  rvgp::note_launch(); write_output<double><<<ceil_div(N * m, 256), 256, 0, st>>>(L.d.V, p, N, m, scale, evecs, ld_evecs, perm, DB);
   if (stats) {
     stats[0] = stt.iters;
     stats[1] = stt.spmm;
@@ -569,4 +571,26 @@ RVGP_API int rvgp_eigsh(const int* indptr, const int* indices, const double* val
     return m - nconv;
   }
   return RVGP_OK;
+}
+
+RVGP_API int rvgp_eigsh(const int* indptr, const int* indices, const double* vals64, const float* vals32, int n,
+                        int DB, int m, int p, int mode, double tol, double tol32, int max_iter,
+                        unsigned long long seed, double* evals, double* evecs, int ld_evecs, double scale, int* stats,
+                        void* workspace, size_t ws_bytes, void* stream) {
+  return eigsh_impl(indptr, indices, vals64, vals32, n, DB, m, p, mode, tol, tol32, max_iter, seed, nullptr, evals,
+                    evecs, ld_evecs, scale, stats, workspace, ws_bytes, stream);
+}
+
+// The same solve on a renumbered matrix: block row r of (indptr, indices,
+// vals) is block row perm[r] of the caller's matrix, columns renumbered
+// alike (rvgp_permute_csr).  The start block is the caller-order one,
+// permuted, and evecs rows come back in the caller's order, so the result
+// equals rvgp_eigsh's on the original matrix up to summation order.
+RVGP_API int rvgp_eigsh_ordered(const int* indptr, const int* indices, const double* vals64, const float* vals32,
+                                int n, int DB, int m, int p, int mode, double tol, double tol32, int max_iter,
+                                unsigned long long seed, const int* perm, double* evals, double* evecs, int ld_evecs,
+                                double scale, int* stats, void* workspace, size_t ws_bytes, void* stream) {
+  RVGP_CHECK_ARG(perm, "rvgp_eigsh_ordered: null permutation");
+  return eigsh_impl(indptr, indices, vals64, vals32, n, DB, m, p, mode, tol, tol32, max_iter, seed, perm, evals,
+                    evecs, ld_evecs, scale, stats, workspace, ws_bytes, stream);
 }

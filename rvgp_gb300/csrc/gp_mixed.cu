@@ -508,49 +508,93 @@ RVGP_API size_t rvgp_gp_fit_mixed_workspace(int m) {
   return rvgp_gp_lml_workspace(m) + sizeof(float) * (size_t)m * m + 4 * sizeof(double) + 3 * 256 + 64;
 }
 
-// Mixed-form Adam fit (see the top of this file).  Arguments as
-// rvgp_gp_fit_adam, plus *status (host): 0 = done; 1 = an FP32 pivot was not
-// positive, nothing was written to theta_out / out / state and the caller
-// should run rvgp_gp_fit_adam instead.  Requires m <= rvgp_gp_fit_mixed_max_m().
-// Synchronises the stream (to read the status).
-RVGP_API int rvgp_gp_fit_adam_mixed(const double* C, const double* b, const double* yy, long long N, int m,
-                                    const double* evals, double n_rows, int typ, const double* theta0,
-                                    const double* lower, const int* mask, int steps, double lr, double beta1,
-                                    double beta2, double eps, double* theta_out, double* hist, double* out,
-                                    double* state, int* status, void* workspace, size_t ws_bytes, void* stream) {
-  RVGP_CHECK_ARG(C && b && yy && evals && theta0 && lower && mask && theta_out && out && state && status,
+namespace {
+struct FitBufs {
+  void* lml_ws;
+  float* C32;
+  double* dl;
+  int* dm;
+  int* dstat;
+};
+FitBufs carve_fit(void* workspace, size_t ws_bytes, int m) {
+  Workspace ws(workspace, ws_bytes);
+  FitBufs f;
+  f.lml_ws = ws.take<char>(rvgp_gp_lml_workspace(m));
+  f.C32 = ws.take<float>((size_t)m * m);
+  f.dl = ws.take<double>(4);
+  f.dm = ws.take<int>(4);
+  f.dstat = ws.take<int>(1);
+  return f;
+}
+}  // namespace
+
+// Mixed-form Adam fit (see the top of this file), enqueued without waiting:
+// arguments as rvgp_gp_fit_adam.  The workspace holds the fit's status until
+// rvgp_gp_fit_adam_mixed_finish.  Requires m <= rvgp_gp_fit_mixed_max_m().
+RVGP_API int rvgp_gp_fit_adam_mixed_launch(const double* C, const double* b, const double* yy, long long N, int m,
+                                           const double* evals, double n_rows, int typ, const double* theta0,
+                                           const double* lower, const int* mask, int steps, double lr, double beta1,
+                                           double beta2, double eps, double* theta_out, double* hist,
+                                           void* workspace, size_t ws_bytes, void* stream) {
+  RVGP_CHECK_ARG(C && b && yy && evals && theta0 && lower && mask && theta_out,
                  "rvgp_gp_fit_adam_mixed: null pointer");
   RVGP_CHECK_ARG(typ == 0 || typ == 1, "rvgp_gp_fit_adam_mixed: typ must be 0 (matern) or 1 (se)");
-  RVGP_CHECK_ARG(steps >= 0 && ws_bytes >= rvgp_gp_fit_mixed_workspace(m),
+  RVGP_CHECK_ARG(steps >= 0 && workspace && ws_bytes >= rvgp_gp_fit_mixed_workspace(m),
                  "rvgp_gp_fit_adam_mixed: bad steps or workspace");
   const int mmax = rvgp_gp_fit_mixed_max_m();
   RVGP_CHECK_ARG(m >= 1 && m <= mmax, "rvgp_gp_fit_adam_mixed: m=%d exceeds the shared-memory limit %d", m, mmax);
   cudaStream_t st = as_stream(stream);
-  Workspace ws(workspace, ws_bytes);
-  void* lml_ws = ws.take<char>(rvgp_gp_lml_workspace(m));
-  float* C32 = ws.take<float>((size_t)m * m);
-  double* dl = ws.take<double>(4);
-  int* dm = ws.take<int>(4);
-  int* dstat = ws.take<int>(1);
-  cudaMemcpyAsync(dl, lower, 4 * sizeof(double), cudaMemcpyHostToDevice, st);
-  cudaMemcpyAsync(dm, mask, 4 * sizeof(int), cudaMemcpyHostToDevice, st);
+  FitBufs f = carve_fit(workspace, ws_bytes, m);
+  cudaMemcpyAsync(f.dl, lower, 4 * sizeof(double), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(f.dm, mask, 4 * sizeof(int), cudaMemcpyHostToDevice, st);
   rvgp::note_launch();
-  to_f32<<<ceil_div((long long)m * m, 256), 256, 0, st>>>(C, (long long)m * m, C32);
+  to_f32<<<ceil_div((long long)m * m, 256), 256, 0, st>>>(C, (long long)m * m, f.C32);
   const size_t smem = layout(m).total;
   if (cudaFuncSetAttribute(gp_fit_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
     set_error("rvgp_gp_fit_adam_mixed: cannot reserve %zu bytes of shared memory", smem);
     return RVGP_ELAUNCH;
   }
   rvgp::note_launch();
-  gp_fit_f32<<<1, kThreads, smem, st>>>(C32, C, b, yy, N, m, evals, n_rows, typ, theta0, dl, dm, steps, lr, beta1,
-                                        beta2, eps, theta_out, hist, dstat);
+  gp_fit_f32<<<1, kThreads, smem, st>>>(f.C32, C, b, yy, N, m, evals, n_rows, typ, theta0, f.dl, f.dm, steps, lr,
+                                        beta1, beta2, eps, theta_out, hist, f.dstat);
   RVGP_LAUNCH_CHECK("rvgp_gp_fit_adam_mixed");
+  return RVGP_OK;
+}
+
+// Waits for the fit enqueued by rvgp_gp_fit_adam_mixed_launch on the same
+// stream and workspace.  *status (host): 0 = done, and out / state hold the
+// FP64 likelihood, gradient and posterior state at theta_out; 1 = an FP32
+// pivot was not positive, nothing was written to theta_out / out / state and
+// the caller should run rvgp_gp_fit_adam instead.
+RVGP_API int rvgp_gp_fit_adam_mixed_finish(const double* C, const double* b, const double* yy, long long N, int m,
+                                           const double* evals, double n_rows, int typ, const double* theta_out,
+                                           double* out, double* state, int* status, void* workspace,
+                                           size_t ws_bytes, void* stream) {
+  RVGP_CHECK_ARG(C && b && yy && evals && theta_out && out && state && status,
+                 "rvgp_gp_fit_adam_mixed_finish: null pointer");
+  RVGP_CHECK_ARG(workspace && ws_bytes >= rvgp_gp_fit_mixed_workspace(m), "rvgp_gp_fit_adam_mixed_finish: workspace");
+  cudaStream_t st = as_stream(stream);
+  FitBufs f = carve_fit(workspace, ws_bytes, m);
   int h = 0;
-  cudaMemcpyAsync(&h, dstat, sizeof(int), cudaMemcpyDeviceToHost, st);
-  if (cudaStreamSynchronize(st) != cudaSuccess) return check_launch("rvgp_gp_fit_adam_mixed");
+  if (read_back(&h, f.dstat, sizeof(int), st) != cudaSuccess) return check_launch("rvgp_gp_fit_adam_mixed");
   *status = h;
   if (h != 0) return RVGP_OK;
   // FP64 likelihood, gradient and posterior state at the final parameters
-  return rvgp_gp_lml(C, b, yy, N, m, evals, n_rows, typ, theta_out, out, state, lml_ws, rvgp_gp_lml_workspace(m),
+  return rvgp_gp_lml(C, b, yy, N, m, evals, n_rows, typ, theta_out, out, state, f.lml_ws, rvgp_gp_lml_workspace(m),
                      stream);
+}
+
+// rvgp_gp_fit_adam_mixed_launch followed by rvgp_gp_fit_adam_mixed_finish.
+// Synchronises the stream (to read the status).
+RVGP_API int rvgp_gp_fit_adam_mixed(const double* C, const double* b, const double* yy, long long N, int m,
+                                    const double* evals, double n_rows, int typ, const double* theta0,
+                                    const double* lower, const int* mask, int steps, double lr, double beta1,
+                                    double beta2, double eps, double* theta_out, double* hist, double* out,
+                                    double* state, int* status, void* workspace, size_t ws_bytes, void* stream) {
+  RVGP_CHECK_ARG(out && state && status, "rvgp_gp_fit_adam_mixed: null pointer");
+  const int rc = rvgp_gp_fit_adam_mixed_launch(C, b, yy, N, m, evals, n_rows, typ, theta0, lower, mask, steps, lr,
+                                               beta1, beta2, eps, theta_out, hist, workspace, ws_bytes, stream);
+  if (rc != RVGP_OK) return rc;
+  return rvgp_gp_fit_adam_mixed_finish(C, b, yy, N, m, evals, n_rows, typ, theta_out, out, state, status, workspace,
+                                       ws_bytes, stream);
 }

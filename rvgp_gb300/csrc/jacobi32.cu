@@ -281,8 +281,7 @@ int jacobi32_eigh(const float* H, int p, float* w, float* V, int max_sweeps, dou
       lg, p, sw, perm, V);
   if (sweeps_used) {
     int h = 0;
-    cudaMemcpyAsync(&h, sw, sizeof(int), cudaMemcpyDeviceToHost, st);
-    if (cudaStreamSynchronize(st) != cudaSuccess) return check_launch("jacobi32_eigh");
+    if (read_back(&h, sw, sizeof(int), st) != cudaSuccess) return check_launch("jacobi32_eigh");
     *sweeps_used = h;
   }
   return check_launch("jacobi32_eigh");

@@ -507,7 +507,6 @@ RVGP_API int rvgp_knn_fallback_rows(int n, int D, int k, void* workspace, void* 
   Workspace ws(workspace, SIZE_MAX);
   KnnBufs b = carve(ws, plan(n, D, k), n, D);
   int h = -1;
-  if (cudaMemcpyAsync(&h, b.nflag, sizeof(int), cudaMemcpyDeviceToHost, as_stream(stream)) != cudaSuccess) return -1;
-  if (cudaStreamSynchronize(as_stream(stream)) != cudaSuccess) return -1;
+  if (read_back(&h, b.nflag, sizeof(int), as_stream(stream)) != cudaSuccess) return -1;
   return h;
 }

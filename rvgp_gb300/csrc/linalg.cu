@@ -826,8 +826,7 @@ int jacobi_eigh(T* H, int p, T* w, T* V, int max_sweeps, double tol, int* sweeps
       return RVGP_ELAUNCH;
     }
     int hv[2] = {0, 0};
-    cudaMemcpyAsync(hv, flags, sizeof(hv), cudaMemcpyDeviceToHost, st);
-    if (cudaStreamSynchronize(st) != cudaSuccess) return check_launch("jacobi_eigh");
+    if (read_back(hv, flags, sizeof(hv), st) != cudaSuccess) return check_launch("jacobi_eigh");
     if (hv[0] != 0) {
       set_error("jacobi_eigh: a grid barrier timed out");
       return RVGP_ELAUNCH;
@@ -843,8 +842,7 @@ int jacobi_eigh(T* H, int p, T* w, T* V, int max_sweeps, double tol, int* sweeps
   for (int sweep = 0; sweep < max_sweeps && p > 1; ++sweep) {
     rvgp::note_launch(); offnorm_kernel<T><<<1, 1024, 0, st>>>(h0, p, nrm);
     double hn[2];
-    cudaMemcpyAsync(hn, nrm, sizeof(hn), cudaMemcpyDeviceToHost, st);
-    if (cudaStreamSynchronize(st) != cudaSuccess) return check_launch("jacobi_eigh");
+    if (read_back(hn, nrm, sizeof(hn), st) != cudaSuccess) return check_launch("jacobi_eigh");
     if (!(hn[0] > tol * tol * hn[1])) break;
     for (int r = 0; r < rounds; ++r) {
       rvgp::note_launch(); jacobi_params<T><<<ceil_div(p, 128), 128, 0, st>>>(h0, p, part + (size_t)r * p, coef, pq);

@@ -3,6 +3,8 @@
 #include "common.cuh"
 
 namespace rvgp {
+// internal linkage: every translation unit that includes this gets its own copy
+namespace {
 
 constexpr int kScanBlock = 1024;  // elements per CTA in the first pass (256 threads x 4)
 
@@ -63,14 +65,15 @@ __global__ void scan_add(int* __restrict__ out, int n, const int* __restrict__ s
     if (base + r < n) out[base + r] += add;
 }
 
-inline size_t scan_workspace(int n) { return sizeof(int) * (size_t)(ceil_div(n, kScanBlock) + 1); }
+size_t scan_workspace(int n) { return sizeof(int) * (size_t)(ceil_div(n, kScanBlock) + 1); }
 
 // out[i] = sum_{j<i} in[j] for i < n; *total (device) = sum of all (may be nullptr).
-inline void exclusive_scan(const int* in, int n, int* out, int* total, int* ws, cudaStream_t st) {
+void exclusive_scan(const int* in, int n, int* out, int* total, int* ws, cudaStream_t st) {
   int nb = ceil_div(n, kScanBlock);
   rvgp::note_launch(); scan_blocks<<<nb, 256, 0, st>>>(in, n, out, ws);
   rvgp::note_launch(); scan_sums<<<1, 1024, 0, st>>>(ws, nb, total);
   rvgp::note_launch(); scan_add<<<nb, 256, 0, st>>>(out, n, ws);
 }
 
+}  // namespace
 }  // namespace rvgp

@@ -8,11 +8,17 @@
 // expm of RVGP/smoothing.py:15 become these).  X, Y, Z: (n*DB) x b row-major
 // with leading dimension ld.  Z may be null (gamma ignored).
 //
-// Thread mapping: one thread per (block-row, group of V consecutive columns),
-// V = 4 floats or 2 doubles (16-byte vector loads of X rows).  A row's gather
-// of X hits L2: the whole block (n*DB*b*size) is sized to stay resident.  The
-// gather is latency-bound, so each thread keeps several neighbours' loads in
-// flight (the neighbour loop is unrolled with all loads ahead of the math).
+// Mapping: W lanes per block row (W = 32, or the smallest power of two
+// covering the row's 16-byte column groups when there are fewer than 32, so
+// narrow blocks put several rows in a warp); sub-lane l owns the groups
+// l, l+W, ... (G per lane, V = 4 floats or 2 doubles per group).  A row's
+// column indices and DB x DB blocks are loaded once per neighbour by the whole
+// warp (one broadcast request each), so L1 wavefronts go almost entirely to
+// the gathered X rows; the kernel is bound by those L1 wavefronts (each
+// gathered row crosses the L1 data path once per use) and by L2 latency, so
+// there is no unrolling: more resident warps hide the latency better than
+// more loads in flight per warp.  Rows in a locality-preserving order
+// (neighbouring rows share neighbours) raise the L1 hit rate.
 // HBM traffic per product ≈ E*(DB²*sv + 4) + 2*n*DB*b*sx (+ Z).
 #include "common.cuh"
 
@@ -42,83 +48,92 @@ __device__ __forceinline__ void vstore(T* p, const T* in) {
   *reinterpret_cast<VT*>(p) = v;
 }
 
+// the DB x DB block of entry t, loaded by every lane of the warp (broadcast)
 template <typename T, int DB>
+__device__ __forceinline__ void load_block(const T* __restrict__ vals, int t, T* blk) {
+  constexpr int NB = DB * DB;
+  if constexpr ((NB * sizeof(T)) % 16 == 0) {
+    using VT = typename Vec<T>::type;
+    constexpr int V = Vec<T>::V;
+    const VT* p = reinterpret_cast<const VT*>(vals + (size_t)t * NB);
+#pragma unroll
+    for (int c = 0; c < NB / V; ++c) {
+      VT v = __ldg(p + c);
+      const T* e = reinterpret_cast<const T*>(&v);
+#pragma unroll
+      for (int q = 0; q < V; ++q) blk[c * V + q] = e[q];
+    }
+  } else {
+#pragma unroll
+    for (int pq = 0; pq < NB; ++pq) blk[pq] = __ldg(vals + (size_t)t * NB + pq);
+  }
+}
+
+template <typename T, int DB, int G>
 __global__ void __launch_bounds__(256) bspmm_kernel(int n, const int* __restrict__ indptr,
                                                     const int* __restrict__ indices, const T* __restrict__ vals,
                                                     const T* __restrict__ X, T* __restrict__ Y,
-                                                    const T* __restrict__ Z, int b, int ld, T alpha, T beta, T gamma) {
+                                                    const T* __restrict__ Z, int b, int ld, T alpha, T beta, T gamma,
+                                                    int wshift) {
   constexpr int V = Vec<T>::V;
+  const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const int W = 1 << wshift;
+  const int i = (int)(warp * (32 >> wshift) + (lane >> wshift));
+  const int sub = lane & (W - 1);
+  if (i >= n) return;
   const int groups = b / V;
-  const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (tid >= (long long)n * groups) return;
-  const int i = (int)(tid / groups);
-  const int c0 = (int)(tid % groups) * V;
-  T acc[DB][V];
+  bool on[G];
+#pragma unroll
+  for (int g = 0; g < G; ++g) on[g] = sub + W * g < groups;
+  T acc[DB][G][V];
 #pragma unroll
   for (int p = 0; p < DB; ++p)
 #pragma unroll
-    for (int v = 0; v < V; ++v) acc[p][v] = T(0);
-  const int s = indptr[i], e = indptr[i + 1];
-  // U neighbours per iteration: all their index, block and X-row loads are
-  // issued before the first multiply-add, so U gathers are in flight at once
-  constexpr int U = DB <= 2 ? 4 : 2;
-  int t = s;
-  for (; t + U <= e; t += U) {
-    int j[U];
+    for (int g = 0; g < G; ++g)
 #pragma unroll
-    for (int u = 0; u < U; ++u) j[u] = __ldg(indices + t + u);
-    T blk[U][DB * DB];
+      for (int v = 0; v < V; ++v) acc[p][g][v] = T(0);
+  const int s = __ldg(indptr + i), e = __ldg(indptr + i + 1);
+  for (int t = s; t < e; ++t) {
+    const int j = __ldg(indices + t);
+    T blk[DB * DB];
+    load_block<T, DB>(vals, t, blk);
 #pragma unroll
-    for (int u = 0; u < U; ++u)
+    for (int q = 0; q < DB; ++q) {
+      const T* xr = X + ((size_t)j * DB + q) * ld;
 #pragma unroll
-      for (int pq = 0; pq < DB * DB; ++pq) blk[u][pq] = __ldg(vals + (size_t)(t + u) * DB * DB + pq);
-    T x[U][DB][V];
-#pragma unroll
-    for (int u = 0; u < U; ++u)
-#pragma unroll
-      for (int q = 0; q < DB; ++q) vload(X + ((size_t)j[u] * DB + q) * ld + c0, x[u][q]);
-#pragma unroll
-    for (int u = 0; u < U; ++u)
-#pragma unroll
-      for (int q = 0; q < DB; ++q)
+      for (int g = 0; g < G; ++g) {
+        if (!on[g]) continue;
+        T x[V];
+        vload(xr + (sub + W * g) * V, x);
 #pragma unroll
         for (int p = 0; p < DB; ++p)
 #pragma unroll
-          for (int v = 0; v < V; ++v) acc[p][v] = fma(blk[u][p * DB + q], x[u][q][v], acc[p][v]);
-  }
-  for (; t < e; ++t) {
-    const int j = __ldg(indices + t);
-    T blk[DB * DB];
-#pragma unroll
-    for (int pq = 0; pq < DB * DB; ++pq) blk[pq] = __ldg(vals + (size_t)t * DB * DB + pq);
-#pragma unroll
-    for (int q = 0; q < DB; ++q) {
-      T x[V];
-      vload(X + ((size_t)j * DB + q) * ld + c0, x);
-#pragma unroll
-      for (int p = 0; p < DB; ++p)
-#pragma unroll
-        for (int v = 0; v < V; ++v) acc[p][v] = fma(blk[p * DB + q], x[v], acc[p][v]);
+          for (int v = 0; v < V; ++v) acc[p][g][v] = fma(blk[p * DB + q], x[v], acc[p][g][v]);
+      }
     }
   }
 #pragma unroll
-  for (int p = 0; p < DB; ++p) {
-    const size_t row = ((size_t)i * DB + p) * ld + c0;
-    T out[V], x[V];
+  for (int p = 0; p < DB; ++p)
 #pragma unroll
-    for (int v = 0; v < V; ++v) out[v] = alpha * acc[p][v];
-    if (beta != T(0)) {
-      vload(X + row, x);
+    for (int g = 0; g < G; ++g) {
+      if (!on[g]) continue;
+      const size_t row = ((size_t)i * DB + p) * ld + (sub + W * g) * V;
+      T out[V], x[V];
 #pragma unroll
-      for (int v = 0; v < V; ++v) out[v] = fma(beta, x[v], out[v]);
+      for (int v = 0; v < V; ++v) out[v] = alpha * acc[p][g][v];
+      if (beta != T(0)) {
+        vload(X + row, x);
+#pragma unroll
+        for (int v = 0; v < V; ++v) out[v] = fma(beta, x[v], out[v]);
+      }
+      if (Z && gamma != T(0)) {
+        vload(Z + row, x);
+#pragma unroll
+        for (int v = 0; v < V; ++v) out[v] = fma(gamma, x[v], out[v]);
+      }
+      vstore(Y + row, out);
     }
-    if (Z && gamma != T(0)) {
-      vload(Z + row, x);
-#pragma unroll
-      for (int v = 0; v < V; ++v) out[v] = fma(gamma, x[v], out[v]);
-    }
-    vstore(Y + row, out);
-  }
 }
 
 template <typename T>
@@ -127,15 +142,33 @@ int launch(int n, int DB, const int* indptr, const int* indices, const T* vals, 
   constexpr int V = Vec<T>::V;
   RVGP_CHECK_ARG(b % V == 0 && ld % V == 0 && b <= ld, "rvgp_bspmm: b=%d and ld=%d must be multiples of %d", b, ld, V);
   RVGP_CHECK_ARG(((uintptr_t)X | (uintptr_t)Y | (uintptr_t)(Z ? Z : X)) % 16 == 0, "rvgp_bspmm: 16-byte alignment");
-  long long threads = (long long)n * (b / V);
-  int grid = ceil_div(threads, 256);
-  switch (DB) {
-    case 1: rvgp::note_launch(); bspmm_kernel<T, 1><<<grid, 256, 0, st>>>(n, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma); break;
-    case 2: rvgp::note_launch(); bspmm_kernel<T, 2><<<grid, 256, 0, st>>>(n, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma); break;
-    case 3: rvgp::note_launch(); bspmm_kernel<T, 3><<<grid, 256, 0, st>>>(n, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma); break;
-    case 4: rvgp::note_launch(); bspmm_kernel<T, 4><<<grid, 256, 0, st>>>(n, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma); break;
-    default: rvgp::set_error("rvgp_bspmm: block size %d not supported (1..4)", DB); return RVGP_ENOTSUP;
+  const int groups = b / V;
+  const int G = groups <= 32 ? 1 : groups <= 64 ? 2 : groups <= 128 ? 4 : groups <= 256 ? 8 : 16;
+  RVGP_CHECK_ARG(groups <= 32 * 16, "rvgp_bspmm: block width b=%d too large", b);
+  RVGP_CHECK_ARG(DB >= 1 && DB <= 4, "rvgp_bspmm: block size %d not supported (1..4)", DB);
+  int wshift = 5;
+  while (wshift > 0 && (1 << (wshift - 1)) >= groups) --wshift;
+  const long long warps = ((long long)n + (32 >> wshift) - 1) / (32 >> wshift);
+  const int grid = ceil_div(warps * 32, 256);
+  rvgp::note_launch();
+#define RVGP_SPMM_G(DBv, Gv) \
+  bspmm_kernel<T, DBv, Gv><<<grid, 256, 0, st>>>(n, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, wshift)
+#define RVGP_SPMM_DB(DBv)              \
+  switch (G) {                         \
+    case 1: RVGP_SPMM_G(DBv, 1); break; \
+    case 2: RVGP_SPMM_G(DBv, 2); break; \
+    case 4: RVGP_SPMM_G(DBv, 4); break; \
+    case 8: RVGP_SPMM_G(DBv, 8); break; \
+    default: RVGP_SPMM_G(DBv, 16);      \
   }
+  switch (DB) {
+    case 1: RVGP_SPMM_DB(1); break;
+    case 2: RVGP_SPMM_DB(2); break;
+    case 3: RVGP_SPMM_DB(3); break;
+    default: RVGP_SPMM_DB(4);
+  }
+#undef RVGP_SPMM_DB
+#undef RVGP_SPMM_G
   RVGP_LAUNCH_CHECK("rvgp_bspmm");
   return RVGP_OK;
 }

@@ -66,15 +66,27 @@ class data:
         dev.indptr, dev.indices, dev.maxdeg = indptr, indices, maxdeg
         dev.L_vals = _core.laplacian_values(indptr, indices)
         dev.bound = 2.0 * maxdeg * (1.0 + 1e-12)  # spectral bound of L and Lc (|D| + |A|)
+        # The eigensolves run on the matrices renumbered along a Morton curve
+        # of the points: neighbouring rows share neighbours, so the sparse
+        # products hit L1 more often.  Their eigenpairs come back in the
+        # caller's order.
+        dev.perm, dev.rank = _core.locality_order(X)
+        dev.ord_indptr, dev.ord_indices, dev.ord_L_vals, _ = _core.permute_csr(indptr, indices, dev.L_vals, None,
+                                                                               dev.perm, dev.rank)
         mark("graph")
 
         # The eigenpairs of L feed nothing downstream (the kernel is built on
         # those of Lc), so they are computed on a second stream by a host
-        # thread while this one runs the gauges, the connections and the Lc
-        # eigensolve; every reader of evals_L / evecs_L waits for them (wait()).
+        # thread, off the critical path; every reader of evals_L / evecs_L
+        # waits for them (wait()).  In the mixed form the solve is deferred
+        # until the GP fit's one-CTA kernel occupies a single SM (fit() starts
+        # it then), so it fills the other SMs instead of competing with the Lc
+        # eigensolve; the FP64 form starts it at once.
         m = n if n_eigenpairs is None else min(int(n_eigenpairs), n)
         mode = "mixed" if precision == "mixed" else "fp64"
-        self._eig_L = self._start_eig_L(dev, n, m, mode, eig_tol, seed, timings is not None)
+        self._eig_L = self._prepare_eig_L(dev, n, m, mode, eig_tol, seed, timings)
+        if mode == "fp64":
+            self._release_eig_L()
 
         _log(verbose, "Fit tangent spaces")
         K = int(n_neighbors * frac_geodesic_neighbours)
@@ -119,11 +131,15 @@ class data:
         hp.wait_stream(caller)
         try:
             with torch.cuda.stream(hp):
-                dev.evals_Lc, U, dev.eig_info_Lc = _core.eigsh(indptr, indices, lc64, lc32, m=m, mode=mode,
-                                                               tol=eig_tol, seed=seed + 1, scale=math.sqrt(n * dim))
+                _, _, o64, o32 = _core.permute_csr(indptr, indices, lc64, lc32, dev.perm, dev.rank)
+                dev.evals_Lc, U, dev.eig_info_Lc = _core.eigsh(dev.ord_indptr, dev.ord_indices, o64, o32, m=m,
+                                                               mode=mode, tol=eig_tol, seed=seed + 1,
+                                                               scale=math.sqrt(n * dim), perm=dev.perm)
+                del o64, o32
                 dev.evecs_Lc = _core.lift(T, dim, U)
         except BaseException:
-            self._eig_L["thread"].join()
+            if self._eig_L["thread"] is not None:
+                self._eig_L["thread"].join()
             raise
         caller.wait_stream(hp)
         for t_ in (dev.evals_Lc, U, dev.evecs_Lc):
@@ -132,12 +148,9 @@ class data:
         mark("eigsh_Lc")
         self._dev = dev
         if timings is not None:
-            st = self._eig_L
-            self.wait()
             torch.cuda.synchronize()
             for (a, ea), (b, eb) in zip(marks[:-1], marks[1:]):
                 timings[b] = timings.get(b, 0.0) + ea.elapsed_time(eb) / 1e3
-            timings["eigsh_L (concurrent)"] = st["seconds"]
         dev.vectors = None
         self._dev = dev
         self.n = n
@@ -148,20 +161,23 @@ class data:
 
     # ------------------------------------------------------------------ the concurrent eigensolve of L
     @staticmethod
-    def _start_eig_L(dev, n, m, mode, eig_tol, seed, timed):
+    def _prepare_eig_L(dev, n, m, mode, eig_tol, seed, timings):
         main = torch.cuda.current_stream()
+        ready = torch.cuda.Event()
+        ready.record(main)  # L's renumbered CSR and values are ready
         side = torch.cuda.Stream()
-        side.wait_stream(main)  # L's CSR and values are ready
-        state = {"error": None, "seconds": None}
+        state = {"error": None, "seconds": None, "thread": None, "stream": side, "timings": timings}
+        timed = timings is not None
 
         def run():
             try:
                 with torch.cuda.device(main.device), torch.cuda.stream(side):
+                    side.wait_event(ready)
                     ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)] if timed else None
                     if timed:
                         ev[0].record()
-                    out = _core.eigsh(dev.indptr, dev.indices, dev.L_vals, None, m=m, mode=mode, tol=eig_tol,
-                                      seed=seed, scale=math.sqrt(n))
+                    out = _core.eigsh(dev.ord_indptr, dev.ord_indices, dev.ord_L_vals, None, m=m, mode=mode,
+                                      tol=eig_tol, seed=seed, scale=math.sqrt(n), perm=dev.perm)
                     if timed:
                         ev[1].record()
                     side.synchronize()
@@ -171,11 +187,15 @@ class data:
             except BaseException as e:  # re-raised by wait()
                 state["error"] = e
 
-        t = threading.Thread(target=run, name="rvgp-eigsh-L", daemon=True)
-        state["thread"] = t
-        state["stream"] = side
-        t.start()
+        state["run"] = run
         return state
+
+    def _release_eig_L(self):
+        """Start the pending eigensolve of L (once)."""
+        st = self.__dict__.get("_eig_L")
+        if st is not None and st["thread"] is None:
+            st["thread"] = threading.Thread(target=st["run"], name="rvgp-eigsh-L", daemon=True)
+            st["thread"].start()
 
     def wait(self):
         """Block until the eigenpairs of L (computed concurrently) are ready; the
@@ -183,7 +203,10 @@ class data:
         st = self.__dict__.get("_eig_L")
         if st is None:
             return self
+        self._release_eig_L()
         st["thread"].join()
+        if st["timings"] is not None and st["seconds"] is not None:
+            st["timings"]["eigsh_L (concurrent)"] = st["seconds"]
         if st["error"] is not None:
             err = st["error"]
             st["error"] = None

@@ -148,8 +148,10 @@ class manifold_GPR:
         ok = False
         self.fit_form = "fp64"
         if self.precision == "mixed" and self.m <= _core.gp_fit_mixed_max_m():
+            # the data object's deferred eigensolve of L runs beside the one-CTA fit
             theta, out, hist, _, ok = _core.gp_fit_adam_mixed(*args, lr=lr, typ=self.kernel.typ, work=self.work,
-                                                              history=True)
+                                                              history=True,
+                                                              on_launch=getattr(self.data_obj, "_release_eig_L", None))
             self.fit_form = "mixed" if ok else "fp64 (an FP32 pivot failed)"
         if not ok:
             theta, out, hist, _ = _core.gp_fit_adam(*args, lr=lr, typ=self.kernel.typ, work=self.work, history=True)

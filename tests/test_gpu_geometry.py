@@ -134,7 +134,9 @@ def test_connections_and_lc(core, name):
 
 
 @pytest.mark.parametrize("d,dtype,b", [(1, torch.float64, 6), (2, torch.float64, 40), (2, torch.float32, 64),
-                                       (3, torch.float32, 8), (1, torch.float32, 12)])
+                                       (3, torch.float32, 8), (1, torch.float32, 12), (1, torch.float32, 4),
+                                       (2, torch.float32, 228), (2, torch.float64, 228), (4, torch.float32, 20),
+                                       (3, torch.float64, 130), (1, torch.float32, 1040)])
 def test_bspmm(core, d, dtype, b):
     rng = np.random.default_rng(d * 100 + b)
     n = 700

@@ -161,3 +161,28 @@ def test_fit_optimises_likelihood(RVGP):
     assert gpa.log_marginal_likelihood() > gp0.log_marginal_likelihood()
     mean, var = gp.transform(d, np.arange(10))
     assert mean.shape == (10, 3) and var.shape == (10, 3) and np.all(var >= 0)
+
+
+def test_deferred_eigsh_L_beside_mixed_fit(RVGP):
+    """Mixed form: the eigensolve of L waits for the GP fit's one-CTA kernel
+    and runs beside it; its eigenpairs equal a direct solve's."""
+    from rvgp_gb300 import _core
+    g = load_golden("torus")
+    m = int(g["m"])
+    d = RVGP.create_data_object(g["X"], n_neighbors=20, n_eigenpairs=m, precision="mixed", verbose=False)
+    assert d._eig_L["thread"] is None  # not started by create_data_object
+    d.random_vector_field(seed=2)
+    d.smooth_vector_field(t=20)
+    st = d._eig_L
+    gpa = RVGP.fit(d, epochs=30, optimizer="adam", lr=0.05, verbose=False)
+    assert gpa.fit_form == "mixed"
+    assert st["thread"] is not None  # released by the fit
+    ev = d.evals_L
+    ip = torch.as_tensor(g["L_indptr"], device="cuda", dtype=torch.int32)
+    ix = torch.as_tensor(g["L_indices"], device="cuda", dtype=torch.int32)
+    ev_ref, _, _ = _core.eigsh(ip, ix, torch.as_tensor(g["L_data"], device="cuda"), m=m, mode="mixed")
+    np.testing.assert_allclose(ev, ev_ref.cpu().numpy(), rtol=1e-5, atol=1e-6)
+    np.testing.assert_allclose(ev, g["evals_L"], rtol=1e-5, atol=1e-6)
+    # a data object whose L pairs are read before any fit solves them on demand
+    d2 = RVGP.create_data_object(g["X"], n_neighbors=20, n_eigenpairs=m, precision="mixed", verbose=False)
+    np.testing.assert_allclose(d2.evals_L, ev, rtol=0, atol=0)
