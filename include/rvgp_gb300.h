@@ -105,9 +105,11 @@ int rvgp_bspmm_f64(int n, int DB, const int* indptr, const int* indices, const d
  * (m < p <= n*DB, multiple of 4).  tol / tol32: residual tolerances relative to
  * the Gershgorin bound.  evals ascending (m); evecs N x m (ld_evecs) times
  * `scale` (the reference scales by sqrt(N)).  stats: 16 host ints (iterations,
- * SpMMs, Jacobi sweeps, converged, refinement iterations, Cholesky rescues, -,
- * -, then microseconds spent in filter / orthonormalisation / Rayleigh-Ritz
- * tall products / Jacobi).  When tol >= tol32 (mode 1) no FP64 iteration runs.
+ * SpMMs, Jacobi sweeps, converged, refinement iterations, Cholesky rescues,
+ * 1 when the FP32 Grams and block products ran on the tensor cores (mode 1,
+ * p <= 256; RVGP_TENSOR_CORES=0 in the environment selects the CUDA-core
+ * kernels), -, then microseconds spent in filter / orthonormalisation /
+ * Rayleigh-Ritz tall products / Jacobi).  When tol >= tol32 (mode 1) no FP64 iteration runs.
  * Returns 0, or the number of unconverged pairs.  Synchronises the stream. */
 size_t rvgp_eigsh_workspace(int n, int DB, int m, int p, int mode);
 int rvgp_eigsh(const int* indptr, const int* indices, const double* vals64, const float* vals32, int n, int DB, int m,
@@ -121,6 +123,23 @@ int rvgp_eigsh_ordered(const int* indptr, const int* indices, const double* vals
                        int DB, int m, int p, int mode, double tol, double tol32, int max_iter, unsigned long long seed,
                        const int* perm, double* evals, double* evecs, int ld_evecs, double scale, int* stats,
                        void* workspace, size_t ws_bytes, void* stream);
+
+/* ---- tensor-core tall products ----------------------------------------- */
+
+/* The eigensolver's FP32 tall products on the tcgen05 tensor cores with
+ * split-TF32 operands (x = tf32(x) + remainder; three TF32 products per
+ * term, FP32-level accuracy), p, q, K <= 256.  No reference counterpart: they
+ * are the block operations inside the subspace iteration that replaces ARPACK
+ * (RVGP/geometry.py:66-80).  Synchronous; a timed-out pipeline wait returns
+ * RVGP_ELAUNCH.
+ * gram: C (p x q, FP64, ldc) = Aᵀ B, A: N x p (lda), B: N x q (ldb).
+ * gemm: C (N x q, ldc) = A (N x K, lda % 4 == 0, 16-byte aligned) Bm (K x q, ldb). */
+size_t rvgp_tc_gram_workspace(long long N, int p, int q);
+int rvgp_tc_gram_f32(const float* A, int lda, const float* B, int ldb, long long N, int p, int q, double* C, int ldc,
+                     void* workspace, size_t ws_bytes, void* stream);
+size_t rvgp_tc_gemm_workspace(int K, int q);
+int rvgp_tc_gemm_f32(const float* A, int lda, long long N, int K, const float* Bm, int ldb, int q, float* C, int ldc,
+                     void* workspace, size_t ws_bytes, void* stream);
 
 /* ---- locality renumbering for the sparse products ---------------------- */
 

@@ -76,6 +76,10 @@ SIGNATURES = {
                            P, P, c_int, c_double, P, P, c_size_t, P]),
     "rvgp_eigsh_ordered": (c_int, [P, P, P, P, c_int, c_int, c_int, c_int, c_int, c_double, c_double, c_int,
                                    ctypes.c_ulonglong, P, P, P, c_int, c_double, P, P, c_size_t, P]),
+    "rvgp_tc_gram_workspace": (c_size_t, [ctypes.c_longlong, c_int, c_int]),
+    "rvgp_tc_gram_f32": (c_int, [P, c_int, P, c_int, ctypes.c_longlong, c_int, c_int, P, c_int, P, c_size_t, P]),
+    "rvgp_tc_gemm_workspace": (c_size_t, [c_int, c_int]),
+    "rvgp_tc_gemm_f32": (c_int, [P, c_int, ctypes.c_longlong, c_int, P, c_int, c_int, P, c_int, P, c_size_t, P]),
     "rvgp_locality_order_workspace": (c_size_t, [c_int, c_int]),
     "rvgp_locality_order": (c_int, [P, c_int, c_int, P, P, P, c_size_t, P]),
     "rvgp_permute_csr_workspace": (c_size_t, [c_int]),
@@ -273,13 +277,39 @@ def eigsh(indptr, indices, vals64, vals32=None, m=10, mode="mixed", tol=None, to
                                   tol32, max_iter, seed, ptr(perm), ptr(evals), ptr(evecs), m, sc, stats, ptr(ws),
                                   ws.numel(), stream())
     info = dict(iters=stats[0], spmm=stats[1], sweeps=stats[2], converged=stats[3], refine_iters=stats[4],
-                chol_rescues=stats[5], p=p, filter_ms=stats[8] / 1e3, orth_ms=stats[9] / 1e3,
+                chol_rescues=stats[5], tensor_cores=bool(stats[6]), p=p, filter_ms=stats[8] / 1e3, orth_ms=stats[9] / 1e3,
                 rr_ms=stats[10] / 1e3, jacobi_ms=stats[11] / 1e3)
     if st < 0:
         check(st, "rvgp_eigsh")
     if st > 0:
         raise RuntimeError(f"ARPACK-equivalent no convergence: {lib().rvgp_last_error().decode()}")
     return evals, evecs, info
+
+
+def tc_gram(A, B=None):
+    """Aᵀ B (FP64 out) on the tensor cores, split-TF32: A (N, p), B (N, q) FP32, p, q <= 256."""
+    A = _dev(A, torch.float32, "A")
+    B = A if B is None else _dev(B, torch.float32, "B")
+    N, p = A.shape
+    q = B.shape[1]
+    C = torch.empty((p, q), dtype=torch.float64, device=A.device)
+    ws = workspace(lib().rvgp_tc_gram_workspace(N, p, q), A.device)
+    check(lib().rvgp_tc_gram_f32(ptr(A), p, ptr(B), q, N, p, q, ptr(C), q, ptr(ws), ws.numel(), stream()),
+          "rvgp_tc_gram_f32")
+    return C
+
+
+def tc_gemm(A, Bm):
+    """A (N, K) @ Bm (K, q) in FP32 on the tensor cores, split-TF32; K, q <= 256."""
+    A = _dev(A, torch.float32, "A")
+    Bm = _dev(Bm, torch.float32, "Bm")
+    N, K = A.shape
+    q = Bm.shape[1]
+    C = torch.empty((N, q), dtype=torch.float32, device=A.device)
+    ws = workspace(lib().rvgp_tc_gemm_workspace(K, q), A.device)
+    check(lib().rvgp_tc_gemm_f32(ptr(A), K, N, K, ptr(Bm), q, q, ptr(C), q, ptr(ws), ws.numel(), stream()),
+          "rvgp_tc_gemm_f32")
+    return C
 
 
 def locality_order(X):

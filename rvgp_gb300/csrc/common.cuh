@@ -71,6 +71,12 @@ constexpr int kNumSMs = 152;  // GB300: 2 dies x 76 SMs
     }                                    \
   } while (0)
 
+#define TRY_RC(x)               \
+  do {                          \
+    int _rc = (x);              \
+    if (_rc != RVGP_OK) return _rc; \
+  } while (0)
+
 #define RVGP_LAUNCH_CHECK(what)                         \
   do {                                                  \
     int _st = rvgp::check_launch(what);                 \

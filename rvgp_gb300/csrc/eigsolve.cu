@@ -177,6 +177,10 @@ struct Small {
   size_t jac32_bytes;
   float* nf;
   double* nd;
+  int tc;             // FP32 tall products on the tensor cores (tc_gemm.cu)
+  int* tc_err;        // raised by a tensor-core kernel whose pipeline wait timed out
+  void* tc_ws;
+  size_t tc_bytes;
 };
 
 struct Problem {
@@ -209,7 +213,16 @@ template <>
 double* nrm<double>(Small& s) { return s.nd; }
 
 inline int gram_any(const float* A, const float* B, long long N, int p, double* C, Small& s, cudaStream_t st) {
+  if (s.tc) return tc_gram_f32_out64(A, p, B, p, N, p, p, C, p, s.tc_err, s.tc_ws, s.tc_bytes, st);
   return gram_f32_out64(A, p, B, p, N, p, p, C, p, 1.0, 0.0, s.gram_ws, s.gram_bytes, st);
+}
+// C (N x p) = A (N x p) Bm (p x p), ld = p
+inline int block_product(const float* A, const float* Bm, long long N, int p, float* C, Small& s, cudaStream_t st) {
+  if (s.tc) return tc_gemm_f32(A, p, N, p, Bm, p, p, C, p, s.tc_err, s.tc_ws, s.tc_bytes, st);
+  return gemm_nn<float>(A, p, Bm, p, N, p, p, C, p, 1.f, 0.f, st);
+}
+inline int block_product(const double* A, const double* Bm, long long N, int p, double* C, Small&, cudaStream_t st) {
+  return gemm_nn<double>(A, p, Bm, p, N, p, p, C, p, 1.0, 0.0, st);
 }
 inline int gram_any(const double* A, const double* B, long long N, int p, double* C, Small& s, cudaStream_t st) {
   return gram<double>(A, p, B, p, N, p, p, C, p, 1.0, 0.0, s.gram_ws, s.gram_bytes, st);
@@ -317,7 +330,7 @@ int orthonormalise(const Problem& P, Block<T>& B, Small& s, Stats& stt, cudaStre
     }
     TRY(tri_inv_lower<double>(s.G, p, p, s.Linv, p, st));
     rvgp::note_launch(); transpose_to<T><<<ceil_div((long long)p * p, 256), 256, 0, st>>>(s.Linv, p, Bmat<T>(s));
-    TRY(gemm_nn<T>(B.V, p, Bmat<T>(s), p, N, p, p, B.T1, p, T(1), T(0), st));
+    TRY(block_product(B.V, Bmat<T>(s), N, p, B.T1, s, st));
     std::swap(B.V, B.T1);
   }
   return RVGP_OK;
@@ -352,8 +365,8 @@ int rayleigh_ritz(const Problem& P, Block<T>& B, Small& s, Stats& stt, int max_s
   }
   cudaEventRecord(ev.e[4], st);
   stt.sweeps += used;
-  TRY(gemm_nn<T>(B.V, p, Bmat<T>(s), p, N, p, p, B.T1, p, T(1), T(0), st));
-  TRY(gemm_nn<T>(B.W, p, Bmat<T>(s), p, N, p, p, B.T2, p, T(1), T(0), st));
+  TRY(block_product(B.V, Bmat<T>(s), N, p, B.T1, s, st));
+  TRY(block_product(B.W, Bmat<T>(s), N, p, B.T2, s, st));
   std::swap(B.V, B.T1);
   std::swap(B.W, B.T2);
   const int nc = resid_chunks(N);
@@ -480,6 +493,10 @@ Layout carve(Workspace& ws, long long N, int p, int mode) {
   s.jac_ws = ws.take<char>(s.jac_bytes);
   s.cn_bytes = std::max(col_norms_workspace<float>(N, p), col_norms_workspace<double>(N, p));
   s.cn_ws = ws.take<char>(s.cn_bytes);
+  s.tc = 0;
+  s.tc_err = ws.take<int>(1);
+  s.tc_bytes = (mode == 1 && p <= 256) ? std::max(tc_gram_workspace(N, p, p), tc_gemm_workspace(p, p)) : 0;
+  s.tc_ws = ws.take<char>(s.tc_bytes);
   return L;
 }
 
@@ -520,6 +537,8 @@ static int eigsh_impl(const int* indptr, const int* indices, const double* vals6
   Small& s = L.s;
   s.cholqr32 = (mode == 1 && p <= cholqr32_max_p()) ? 1 : 0;
   s.jac32 = (mode == 1 && p % 2 == 0 && p <= jacobi32_max_p()) ? 1 : 0;
+  s.tc = (mode == 1 && s.tc_bytes > 0 && tc_enabled() && tc_supported(p, p)) ? 1 : 0;
+  cudaMemsetAsync(s.tc_err, 0, sizeof(int), st);
   Problem P{n, DB, N, indptr, indices, vals64, vals32, m, p};
   Stats stt;
 
@@ -562,10 +581,16 @@ static int eigsh_impl(const int* indptr, const int* indices, const double* vals6
     stats[3] = stt.conv;
     stats[4] = stt.refine_iters;
     stats[5] = stt.chol_rescues;
+    stats[6] = s.tc;
     for (int q = 0; q < 4; ++q) stats[8 + q] = (int)(stt.ms[q] * 1000.f);  // microseconds per phase
   }
   RVGP_LAUNCH_CHECK("rvgp_eigsh");
-  if (cudaStreamSynchronize(st) != cudaSuccess) return check_launch("rvgp_eigsh");
+  int tc_fail = 0;
+  if (read_back(&tc_fail, s.tc_err, sizeof(int), st) != cudaSuccess) return check_launch("rvgp_eigsh");
+  if (tc_fail) {
+    set_error("eigensolver: a tensor-core pipeline wait timed out");
+    return RVGP_ELAUNCH;
+  }
   if (nconv < m) {
     set_error("eigensolver: %d of %d eigenpairs did not converge in %d iterations", m - nconv, m, max_iter);
     return m - nconv;

@@ -77,11 +77,33 @@ __global__ void reduce_splits_f32_to_f64(const float* __restrict__ part, int spl
   const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (e >= (long long)p * q) return;
   const int i = (int)(e / q), j = (int)(e % q);
+  // groups of eight splits are added in FP32 (at most 7 roundings of partials
+  // of similar size, well below their own FP32 accumulation error), the
+  // group sums in FP64 in a fixed order: few FP64 operations, 8 loads in flight
+  const size_t stride = (size_t)p * q;
+  const float* src = part + (size_t)i * q + j;
   double s = 0.0;
-  for (int t = 0; t < splits; ++t) s += (double)part[((size_t)t * p + i) * q + j];
+  int t = 0;
+  for (; t + 8 <= splits; t += 8) {
+    float v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) v[u] = __ldg(src + (size_t)(t + u) * stride);
+    s += (double)(((v[0] + v[1]) + (v[2] + v[3])) + ((v[4] + v[5]) + (v[6] + v[7])));
+  }
+  for (; t < splits; ++t) s += (double)__ldg(src + (size_t)t * stride);
   double* c = C + (size_t)i * ldc + j;
   *c = beta == 0.0 ? alpha * s : alpha * s + beta * (*c);
 }
+
+}  // namespace
+
+int reduce_f32_splits_to_f64(const float* part, int splits, int p, int q, double* C, int ldc, cudaStream_t st) {
+  rvgp::note_launch();
+  reduce_splits_f32_to_f64<<<ceil_div((long long)p * q, 256), 256, 0, st>>>(part, splits, p, q, C, ldc, 1.0, 0.0);
+  return check_launch("reduce_f32_splits_to_f64");
+}
+
+namespace {
 
 template <typename T>
 int gram_splits(long long N, int p, int q) {

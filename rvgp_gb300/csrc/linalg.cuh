@@ -52,6 +52,24 @@ int gram(const T* A, int lda, const T* B, int ldb, long long N, int p, int q, T*
 int gram_f32_out64(const float* A, int lda, const float* B, int ldb, long long N, int p, int q, double* C, int ldc,
                    double alpha, double beta, void* ws, size_t ws_bytes, cudaStream_t st);
 
+// C (p x q, ldc) = sum over splits of part[split][p][q] (FP32) in FP64.
+int reduce_f32_splits_to_f64(const float* part, int splits, int p, int q, double* C, int ldc, cudaStream_t st);
+
+// Tensor-core (tcgen05, split-TF32) forms of the FP32 tall products for
+// p, q <= 256 (tc_gemm.cu).  They do not synchronise; a timed-out pipeline
+// wait sets *err (device) to 1.
+bool tc_supported(int p, int q);
+// false when the environment sets RVGP_TENSOR_CORES=0 (CUDA-core products instead)
+bool tc_enabled();
+// C (p x q, FP64) = Aᵀ B, A: N x p, B: N x q.
+size_t tc_gram_workspace(long long N, int p, int q);
+int tc_gram_f32_out64(const float* A, int lda, const float* B, int ldb, long long N, int p, int q, double* C, int ldc,
+                      int* err, void* ws, size_t ws_bytes, cudaStream_t st);
+// C (N x q) = A (N x K, lda % 4 == 0 for vector loads) Bm (K x q).  C must not alias A.
+size_t tc_gemm_workspace(int K, int q);
+int tc_gemm_f32(const float* A, int lda, long long N, int K, const float* Bm, int ldb, int q, float* C, int ldc,
+                int* err, void* ws, size_t ws_bytes, cudaStream_t st);
+
 // C (N x q, ldc) = alpha * A (N x p, lda) * B (p x q, ldb) + beta * C.  C must not alias A or B.
 template <typename T>
 int gemm_nn(const T* A, int lda, const T* B, int ldb, long long N, int p, int q, T* C, int ldc, T alpha, T beta,
