@@ -115,18 +115,51 @@ __global__ void shift_diag(double* __restrict__ G, int p, double rel) {
   for (int i = threadIdx.x; i < p; i += blockDim.x) G[(size_t)i * p + i] += rel * tr;
 }
 
+// part[c][j] = sum over rows of chunk c of (W[r][j] - theta_j V[r][j])²:
+// grid (chunks, ceil(b / 32)); warp w takes rows r0 + w, r0 + w + 8, ... for
+// columns j = 32 blockIdx.y + lane (coalesced); the 8 warp sums are added in
+// a fixed order.  FP32 blocks use FP32 fused differences (W and V are FP32
+// already, so one rounding of d adds nothing to their own) with FP32 partial
+// sums over the warp's rows.
 template <typename T>
-__global__ void resid_partial(const T* __restrict__ W, const T* __restrict__ V, const double* __restrict__ theta,
-                              int ld, long long N, int b, long long chunk, double* __restrict__ part) {
+__global__ void __launch_bounds__(256) resid_partial(const T* __restrict__ W, const T* __restrict__ V,
+                                                     const double* __restrict__ theta, int ld, long long N, int b,
+                                                     long long chunk, double* __restrict__ part) {
+  __shared__ double sh[8][32];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int j = blockIdx.y * 32 + lane;
   const long long r0 = blockIdx.x * chunk, r1 = min(N, r0 + chunk);
-  for (int j = threadIdx.x; j < b; j += blockDim.x) {
-    const double th = theta[j];
-    double s = 0.0;
-    for (long long r = r0; r < r1; ++r) {
-      double d = (double)W[r * ld + j] - th * (double)V[r * ld + j];
-      s += d * d;
+  double s = 0.0;
+  if (j < b) {
+    if constexpr (sizeof(T) == 4) {
+      const float th = (float)theta[j];
+      float a0 = 0.f, a1 = 0.f;
+      long long r = r0 + warp;
+      for (; r + 8 < r1; r += 16) {
+        const float d0 = fmaf(-th, V[r * ld + j], W[r * ld + j]);
+        const float d1 = fmaf(-th, V[(r + 8) * ld + j], W[(r + 8) * ld + j]);
+        a0 = fmaf(d0, d0, a0);
+        a1 = fmaf(d1, d1, a1);
+      }
+      for (; r < r1; r += 8) {
+        const float d = fmaf(-th, V[r * ld + j], W[r * ld + j]);
+        a0 = fmaf(d, d, a0);
+      }
+      s = (double)a0 + (double)a1;
+    } else {
+      const double th = theta[j];
+      for (long long r = r0 + warp; r < r1; r += 8) {
+        const double d = (double)W[r * ld + j] - th * (double)V[r * ld + j];
+        s += d * d;
+      }
     }
-    part[(size_t)blockIdx.x * b + j] = s;
+  }
+  sh[warp][lane] = s;
+  __syncthreads();
+  if (warp == 0 && j < b) {
+    double t = 0.0;
+    for (int w = 0; w < 8; ++w) t += sh[w][lane];
+    part[(size_t)blockIdx.x * b + j] = t;
   }
 }
 
@@ -149,7 +182,7 @@ __global__ void write_output(const T* __restrict__ V, int ldv, long long N, int 
   out[ro * ldo + j] = scale * (double)V[r * ldv + j];
 }
 
-int resid_chunks(long long N) { return (int)std::max<long long>(1, std::min<long long>(512, N / 128)); }
+int resid_chunks(long long N) { return (int)std::max<long long>(1, std::min<long long>(512, (N + 1023) / 1024)); }
 
 // ------------------------------------------------------------------------------ solver state
 template <typename T>
@@ -371,7 +404,8 @@ int rayleigh_ritz(const Problem& P, Block<T>& B, Small& s, Stats& stt, int max_s
   std::swap(B.W, B.T2);
   const int nc = resid_chunks(N);
   const long long chunk = (N + nc - 1) / nc;
-  rvgp::note_launch(); resid_partial<T><<<nc, 256, 0, st>>>(B.W, B.V, s.theta, p, N, p, chunk, s.resid_part);
+  rvgp::note_launch();
+  resid_partial<T><<<dim3(nc, ceil_div(p, 32)), 256, 0, st>>>(B.W, B.V, s.theta, p, N, p, chunk, s.resid_part);
   rvgp::note_launch(); resid_final<<<ceil_div(p, 256), 256, 0, st>>>(s.resid_part, nc, p, s.res);
   cudaEventRecord(ev.e[5], st);
   theta.resize(p);

@@ -16,6 +16,8 @@
 #include "common.cuh"
 #include "linalg.cuh"
 #include <float.h>
+#include <algorithm>
+#include <cstdint>
 
 namespace rvgp {
 namespace {
@@ -39,9 +41,15 @@ __device__ __forceinline__ int2 pair_of(int r, int k, int p) {
   return a < b ? make_int2(a, b) : make_int2(b, a);
 }
 
+// shared memory: H (p x ldh), the round's pairs as float4 (c, s, P, Q), the
+// reduction scratch, and the (a, b) block table (2 bytes per block, a <= b <
+// p/2), which the final sort's keys overlay once the sweeps are done
 size_t jac_smem(int p) {
-  return sizeof(float) * ((size_t)p * ldh_of(p) + 2 * (size_t)(p / 2) + 64 + 2 * (size_t)p) +
-         sizeof(int2) * (size_t)(p / 2) + sizeof(int) * (size_t)(2 * p) + 256;
+  const size_t np = p / 2, nblk = np * (np + 1) / 2;
+  size_t P2 = 1;
+  while (P2 < (size_t)p) P2 <<= 1;
+  const size_t table = std::max(sizeof(uint16_t) * nblk, (sizeof(float) + sizeof(int)) * P2);
+  return sizeof(float) * (size_t)p * ldh_of(p) + 16 * np + sizeof(float) * 64 + table + 256;
 }
 
 // Rutishauser's rotation annihilating H_PQ: cos, sin with t = sign(θ)/(|θ| + sqrt(θ²+1)).
@@ -62,19 +70,23 @@ __global__ void __launch_bounds__(kThreads, 1)
   extern __shared__ __align__(16) unsigned char smraw[];
   const int ldh = ldh_of(p);
   const int np = p / 2, rounds = p - 1;
+  const int nblk = np * (np + 1) / 2;
   float* H = reinterpret_cast<float*>(smraw);
-  float* cs = H + (size_t)p * ldh;  // np cosines
-  float* sn = cs + np;              // np sines
-  float* red = sn + np;             // 64
-  float* key = red + 64;                           // 2p floats for the final sort
-  int2* pq = reinterpret_cast<int2*>(key + 2 * p);
-  int* key_idx = reinterpret_cast<int*>(pq + np);  // 2p ints
+  float4* pd = reinterpret_cast<float4*>(H + (size_t)p * ldh + ((4 - (p * ldh) % 4) % 4));  // (c, s, P, Q)
+  float* red = reinterpret_cast<float*>(pd + np);                 // 64
+  uint16_t* table = reinterpret_cast<uint16_t*>(red + 64);        // nblk blocks (a | b << 8)
+  float* key = reinterpret_cast<float*>(table);                   // final sort, overlays the table
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   // symmetric storage: element (i, j) lives at (min, max) in the upper triangle
-  auto at = [&](int i, int j) -> float& { return H[min(i, j) * ldh + max(i, j)]; };
+  auto idx = [&](int i, int j) { return min(i, j) * ldh + max(i, j); };
   for (int e = tid; e < p * p; e += kThreads) {
     const int i = e / p, j = e % p;
     if (i <= j) H[i * ldh + j] = 0.5f * (Hin[(size_t)i * p + j] + Hin[(size_t)j * p + i]);
+  }
+  // block table: row a holds blocks (a, a) .. (a, np - 1) from offset a np - a (a - 1) / 2
+  for (int a = tid; a < np; a += kThreads) {
+    const int off = a * np - a * (a - 1) / 2;
+    for (int b = a; b < np; ++b) table[off + b - a] = (uint16_t)(a | (b << 8));
   }
   __syncthreads();
   int used = 0;
@@ -121,38 +133,37 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int2 q = pair_of(r, k, p);
         float c, s;
         rotation(H[q.x * ldh + q.x], H[q.y * ldh + q.y], H[q.x * ldh + q.y], c, s);  // q.x < q.y
-        cs[k] = c;
-        sn[k] = s;
-        pq[k] = q;
+        pd[k] = make_float4(c, s, __int_as_float(q.x), __int_as_float(q.y));
         lg[2 * k] = c;
         lg[2 * k + 1] = s;
       }
       __syncthreads();
-      // blocks (a, b), a <= b: warp w takes block rows a = w, w + 32, ...
-      for (int a = warp; a < np; a += kThreads / 32) {
-        const int2 A = pq[a];
-        const float ca = cs[a], sa = sn[a];
-        for (int b = a + lane; b < np; b += 32) {
-          const int2 B = pq[b];
-          const float cb = cs[b], sb = sn[b];
-          const float x00 = at(A.x, B.x), x01 = at(A.x, B.y);
-          const float x10 = at(A.y, B.x), x11 = at(A.y, B.y);
-          // T = X J_b, J = [[c, s], [-s, c]]
+      // the round's blocks (a, b), a <= b, dealt evenly over the threads
+      for (int t = tid; t < nblk; t += kThreads) {
+        const uint16_t e = table[t];
+        const int a = e & 255, b = e >> 8;
+        const float4 PA = pd[a], PB = pd[b];
+        const float ca = PA.x, sa = PA.y, cb = PB.x, sb = PB.y;
+        if (sa == 0.f && sb == 0.f) continue;  // both rotations are the identity
+        const int ax = __float_as_int(PA.z), ay = __float_as_int(PA.w);
+        const int bx = __float_as_int(PB.z), by = __float_as_int(PB.w);
+        if (a == b) {
+          const float x00 = H[ax * ldh + ax], x01 = H[ax * ldh + ay], x11 = H[ay * ldh + ay];
+          const float t00 = ca * x00 - sa * x01, t01 = sa * x00 + ca * x01;
+          const float t10 = ca * x01 - sa * x11, t11 = sa * x01 + ca * x11;
+          H[ax * ldh + ax] = ca * t00 - sa * t10;
+          H[ay * ldh + ay] = sa * t01 + ca * t11;
+          H[ax * ldh + ay] = 0.f;  // ax < ay
+        } else {
+          const int i00 = idx(ax, bx), i01 = idx(ax, by), i10 = idx(ay, bx), i11 = idx(ay, by);
+          const float x00 = H[i00], x01 = H[i01], x10 = H[i10], x11 = H[i11];
+          // T = X J_b, J = [[c, s], [-s, c]]; H' = J_aᵀ T
           const float t00 = cb * x00 - sb * x01, t01 = sb * x00 + cb * x01;
           const float t10 = cb * x10 - sb * x11, t11 = sb * x10 + cb * x11;
-          // H' = J_aᵀ T
-          const float y00 = ca * t00 - sa * t10, y01 = ca * t01 - sa * t11;
-          const float y10 = sa * t00 + ca * t10, y11 = sa * t01 + ca * t11;
-          if (a == b) {
-            H[A.x * ldh + A.x] = y00;
-            H[A.y * ldh + A.y] = y11;
-            H[A.x * ldh + A.y] = 0.f;  // A.x < A.y
-          } else {
-            at(A.x, B.x) = y00;
-            at(A.x, B.y) = y01;
-            at(A.y, B.x) = y10;
-            at(A.y, B.y) = y11;
-          }
+          H[i00] = ca * t00 - sa * t10;
+          H[i01] = ca * t01 - sa * t11;
+          H[i10] = sa * t00 + ca * t10;
+          H[i11] = sa * t01 + ca * t11;
         }
       }
       __syncthreads();
@@ -162,6 +173,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   // sort the diagonal ascending, ties by index (bitonic over a power of two)
   int P2 = 1;
   while (P2 < p) P2 <<= 1;
+  int* key_idx = reinterpret_cast<int*>(key + P2);
   for (int t = tid; t < P2; t += kThreads) {
     key[t] = t < p ? H[t * ldh + t] : FLT_MAX;
     key_idx[t] = t < p ? t : INT_MAX;
