@@ -204,6 +204,7 @@ struct Small {
   double* Bd;
   float *Hf, *thf;  // FP32 Rayleigh-Ritz matrix and its eigenvalues (mixed form)
   float *L32, *Mb32;  // FP32 Cholesky QR factor and its diagonal-block inverses
+  float* d32;         // its column scaling diag(VᵀV)^-½
   int cholqr32;       // p fits the one-CTA FP32 Cholesky QR
   int jac32;          // p fits the one-CTA FP32 Jacobi
   void* jac32_ws;
@@ -320,27 +321,31 @@ int filter(const Problem& P, Block<T>& B, int deg, double a, double b, double a0
   return RVGP_OK;
 }
 
-// V <- orthonormal basis of span(V): column scaling + Cholesky QR (twice).
+// V <- orthonormal basis of span(V): Cholesky QR with column scaling, twice.
+// FP32 block: the scaling d = diag(VᵀV)^-½ is applied to the Gram inside the
+// one-CTA FP32 factorisation and to V inside the triangular solve, so V is
+// read twice per pass (Gram, solve).  Otherwise (or when an FP32 pivot fails)
+// V is scaled explicitly and the FP64 Gram is factored in FP64.
 template <typename T>
 int orthonormalise(const Problem& P, Block<T>& B, Small& s, Stats& stt, cudaStream_t st) {
   const long long N = P.N;
   const int p = P.p;
   int rescues = 0;
   for (int pass = 0; pass < 2; ++pass) {
-    TRY(col_norms<T>(B.V, p, N, p, nrm<T>(s), s.cn_ws, s.cn_bytes, st));
-    TRY(scale_cols<T>(B.V, p, N, p, nrm<T>(s), true, st));
-    TRY(gram_any(B.V, B.V, N, p, s.G, s, st));
     if (sizeof(T) == 4 && s.cholqr32) {
-      // FP32 factorisation in one CTA and an FP32 triangular solve of the block;
-      // a failed pivot falls through to the FP64 factorisation of the same Gram
-      TRY(chol32_gram(s.G, p, s.L32, s.Mb32, s.info, st));
+      TRY(gram_any(B.V, B.V, N, p, s.G, s, st));
+      TRY(chol32_gram(s.G, p, s.L32, s.Mb32, s.d32, s.info, st));
       int info32 = 0;
       if (read_back(&info32, s.info, sizeof(int), st) != cudaSuccess) return check_launch("orthonormalise");
       if (info32 == 0) {
-        TRY(trsm_rows_f32(reinterpret_cast<float*>(B.V), p, N, p, s.L32, s.Mb32, st));
+        TRY(trsm_rows_f32(reinterpret_cast<float*>(B.V), p, N, p, s.L32, s.Mb32, s.d32, st));
         continue;
       }
+      // a failed FP32 pivot: the same pass in FP64 on the explicitly scaled block
     }
+    TRY(col_norms<T>(B.V, p, N, p, nrm<T>(s), s.cn_ws, s.cn_bytes, st));
+    TRY(scale_cols<T>(B.V, p, N, p, nrm<T>(s), true, st));
+    TRY(gram_any(B.V, B.V, N, p, s.G, s, st));
     TRY(cholesky<double>(s.G, p, p, s.info, st));
     int info = 0;
     if (read_back(&info, s.info, sizeof(int), st) != cudaSuccess) return check_launch("orthonormalise");
@@ -517,6 +522,7 @@ Layout carve(Workspace& ws, long long N, int p, int mode) {
   s.thf = ws.take<float>(p);
   s.L32 = ws.take<float>(pp);
   s.Mb32 = ws.take<float>((size_t)((p + 31) / 32) * 32 * 32);
+  s.d32 = ws.take<float>(p);
   s.cholqr32 = 0;
   s.jac32 = 0;
   s.jac32_bytes = jacobi32_workspace(p, kFp32Sweeps);

@@ -23,6 +23,7 @@
 // The m x m factorisation is FP64 in both forms (cond(A) grows like
 // λ_max(RCR)/σ²); the tall products (C = ΦᵀΦ, Φ* Bᵀ) are FP32 in the mixed form.
 #include "common.cuh"
+#include <algorithm>
 #include "linalg.cuh"
 #include <math.h>
 #include <float.h>
@@ -260,6 +261,51 @@ __global__ void adam_init(const double* __restrict__ theta0, const double* __res
 }
 
 // Φ[(t*D + a), :] = src[(idx[t]*D + a), :],  y[(t*D + a)] = vec[idx[t]*D + a]
+// part[c][j] = Σ over rows of chunk c of Phi[r][j] y[r] (j < m), and
+// part[c][m] = Σ y[r]² over the chunk: grid (chunks, ceil((m + 1) / 32)), warp
+// w takes rows r0 + w, r0 + w + 8, ... for columns 32 blockIdx.y + lane
+// (coalesced); the 8 warp sums are added in a fixed order.
+__global__ void __launch_bounds__(256) phity_partial(const double* __restrict__ Phi, const double* __restrict__ y,
+                                                     long long N, int m, long long chunk, double* __restrict__ part) {
+  __shared__ double sh[8][32];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int j = blockIdx.y * 32 + lane;
+  const long long r0 = blockIdx.x * chunk, r1 = min(N, r0 + chunk);
+  double s0 = 0.0, s1 = 0.0;
+  if (j < m) {
+    long long r = r0 + warp;
+    for (; r + 8 < r1; r += 16) {
+      s0 = fma(Phi[r * m + j], y[r], s0);
+      s1 = fma(Phi[(r + 8) * m + j], y[r + 8], s1);
+    }
+    for (; r < r1; r += 8) s0 = fma(Phi[r * m + j], y[r], s0);
+  } else if (j == m) {
+    for (long long r = r0 + warp; r < r1; r += 8) s0 = fma(y[r], y[r], s0);
+  }
+  sh[warp][lane] = s0 + s1;
+  __syncthreads();
+  if (warp == 0 && j <= m) {
+    double t = 0.0;
+    for (int w = 0; w < 8; ++w) t += sh[w][lane];
+    part[(size_t)blockIdx.x * (m + 1) + j] = t;
+  }
+}
+
+// b[j] = Σ_c part[c][j] (j < m), yy = Σ_c part[c][m]
+__global__ void phity_final(const double* __restrict__ part, int nchunk, int m, double* __restrict__ b,
+                            double* __restrict__ yy) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j > m) return;
+  double s = 0.0;
+  for (int c = 0; c < nchunk; ++c) s += part[(size_t)c * (m + 1) + j];
+  if (j < m)
+    b[j] = s;
+  else
+    *yy = s;
+}
+
+int phity_chunks(long long N) { return (int)std::max<long long>(1, std::min<long long>(256, (N + 511) / 512)); }
+
 __global__ void gather_rows(const double* __restrict__ src, int m, int D, const int* __restrict__ idx, int nt,
                             const double* __restrict__ vec, double* __restrict__ Phi, float* __restrict__ Phi32,
                             double* __restrict__ y) {
@@ -436,7 +482,8 @@ RVGP_API int rvgp_gather_rows(const double* src, int m, int D, const int* idx, i
 }
 
 RVGP_API size_t rvgp_gp_prepare_workspace(long long N, int m) {
-  return gram_workspace<double>(N, m, m) + gram_workspace<float>(N, m, m) + 1024;
+  return std::max(gram_workspace<double>(N, m, m), gram_workspace<float>(N, m, m)) +
+         sizeof(double) * (size_t)phity_chunks(N) * (m + 1) + 1024;
 }
 
 // C = ΦᵀΦ (m x m), b = Φᵀy (m), yy = yᵀy.  mode 1 uses Phi32 for C (FP32
@@ -453,10 +500,16 @@ RVGP_API int rvgp_gp_prepare(const double* Phi, const float* Phi32, const double
   else
     rc = gram<double>(Phi, m, Phi, m, N, m, m, C, m, 1.0, 0.0, workspace, ws_bytes, st);
   if (rc) return rc;
-  rc = gram<double>(Phi, m, y, 1, N, m, 1, b, 1, 1.0, 0.0, workspace, ws_bytes, st);
-  if (rc) return rc;
-  rc = gram<double>(y, 1, y, 1, N, 1, 1, yy, 1, 1.0, 0.0, workspace, ws_bytes, st);
-  if (rc) return rc;
+  // b and yy: one column reduction of [Phi y | y y] in FP64 (after the Gram's
+  // scratch, which the Gram's reduction may still be reading in stream order)
+  const size_t gbytes = std::max(gram_workspace<double>(N, m, m), gram_workspace<float>(N, m, m));
+  double* part = reinterpret_cast<double*>(static_cast<char*>(workspace) + ((gbytes + 255) & ~size_t(255)));
+  const int nc = phity_chunks(N);
+  const long long chunk = (N + nc - 1) / nc;
+  rvgp::note_launch();
+  phity_partial<<<dim3(nc, ceil_div(m + 1, 32)), 256, 0, st>>>(Phi, y, N, m, chunk, part);
+  rvgp::note_launch();
+  phity_final<<<ceil_div(m + 1, 256), 256, 0, st>>>(part, nc, m, b, yy);
   RVGP_LAUNCH_CHECK("rvgp_gp_prepare");
   return RVGP_OK;
 }

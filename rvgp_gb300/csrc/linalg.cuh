@@ -104,15 +104,17 @@ size_t col_norms_workspace(long long N, int b);
 template <typename T>
 int scale_cols(T* X, int ld, long long N, int b, const T* s, bool inverse, cudaStream_t st);
 
-// FP32 Cholesky QR step (cholqr.cu): chol32_gram factors the p x p FP64 Gram
-// G in FP32 in one CTA, writing L (p x p, lower, ld p) and the inverses of its
-// 32 x 32 diagonal blocks (Mb, ceil(p/32) x 32 x 32); *info (device) = 0, or 1
-// for a non-positive pivot.  trsm_rows_f32 overwrites V (N x p, ld) with
-// V L⁻ᵀ.  Both need p <= cholqr32_max_p().
+// FP32 Cholesky QR step (cholqr.cu): chol32_gram scales the p x p FP64 Gram
+// G to unit diagonal (d = diag(G)^-½, p floats) and factors D G D in FP32 in
+// one CTA, writing L (p x p, lower, ld p) and the inverses of its 32 x 32
+// diagonal blocks (Mb, ceil(p/32) x 32 x 32); *info (device) = 0, or 1 for a
+// non-positive pivot.  trsm_rows_f32 overwrites V (N x p, ld) with V D L⁻ᵀ
+// (D = diag(d); d null: the identity).  Both need p <= cholqr32_max_p().
 int cholqr32_max_p();
 size_t cholqr32_workspace(int p);
-int chol32_gram(const double* G, int p, float* L, float* Mb, int* info, cudaStream_t st);
-int trsm_rows_f32(float* V, int ldv, long long N, int p, const float* L, const float* Mb, cudaStream_t st);
+int chol32_gram(const double* G, int p, float* L, float* Mb, float* d, int* info, cudaStream_t st);
+int trsm_rows_f32(float* V, int ldv, long long N, int p, const float* L, const float* Mb, const float* d,
+                  cudaStream_t st);
 
 // FP32 symmetric eigensolver with the matrix in one SM's shared memory
 // (jacobi32.cu): H (p x p, FP32, not modified) -> eigenvalues w ascending and

@@ -83,6 +83,7 @@ class manifold_GPR:
         self.m = kernel.eigenvalues.numel()
         self.work = _core.LMLWorkspace(self.m, dev.X.device)
         self.n_evals = 0
+        self._eval_key, self._eval_out = None, None  # parameters of the state held in self.work
 
     # ------------------------------------------------------------------ parameters
     @property
@@ -93,11 +94,20 @@ class manifold_GPR:
     def theta(self):
         return self.kernel.theta(float(self.likelihood.variance))
 
+    def _theta_key(self):
+        return tuple(float(p) if p is not None else None for p in self._slots()) + (self.kernel.typ,)
+
     def _evaluate(self):
+        """FP64 likelihood, gradient and posterior state (in self.work) at the
+        current parameters; reused while the parameters are unchanged."""
+        key = self._theta_key()
+        if self._eval_key == key:
+            return self._eval_out
         out, _ = _core.gp_lml(self.C, self.b, self.yy, self.N, self.kernel.eigenvalues, self.kernel.num_verticies,
                               self.theta(), self.kernel.typ, self.work)
         self.n_evals += 1
-        return out.cpu().numpy()
+        self._eval_key, self._eval_out = key, out.cpu().numpy()
+        return self._eval_out
 
     def log_marginal_likelihood(self):
         return float(self._evaluate()[0])
@@ -161,6 +171,8 @@ class manifold_GPR:
                 p.assign(float(v))
         self.n_evals += steps + 1
         self.lml_history = hist
+        # self.work holds the FP64 likelihood, gradient and state at the fitted parameters
+        self._eval_key, self._eval_out = self._theta_key(), out.cpu().numpy()
         return vals
 
     # ------------------------------------------------------------------ prediction
