@@ -306,6 +306,7 @@ def run_ours(args):
             "roofline": roof,
             "clocks": clk.summary(),
             "gpu_launches": int(launches),
+            "step_times_s": [round(t, 5) for t in times],
         }
         if not args.skip_cpu:
             out["cpu_baseline"] = cpu_baseline(wl, X, V, train, test, budget=args.cpu_budget)
