@@ -32,18 +32,24 @@ __device__ __forceinline__ float rsqrt_f(float d) {
   return r * fmaf(-0.5f * d * r, r, 1.5f);
 }
 
-// Warp 0: Cholesky of the nb x nb diagonal block at (j0, j0) of A.  Lane i
+// One warp: Cholesky of the nb x nb diagonal block at (j0, j0) of A.  Lane i
 // keeps row i in registers; pivots are processed four at a time with compile-
 // time register indices, then the row shifts left by four, so the code stays
-// small enough for the instruction cache.  Updates are predicated (no
-// branches): lane i applies column j's multiplier only where i >= column.
-// Writes L into the block's lower triangle and 1/L_ii into dinvL.  Returns
-// false on a non-positive pivot.
+// small enough for the instruction cache.  Each pivot's column of L goes to a
+// per-CTA shared buffer once (one store per lane) and comes back as 16-byte
+// broadcast loads: register a[k] holds column j4 + k, so the entries it needs
+// are buffer words j4 + k, chunk (j4 + k) / 4 with a compile-time component.
+// Entries above the diagonal are updated too but never feed a stored value
+// (the buffer holds zeros for rows <= the pivot).  Writes L into the block's
+// lower triangle and 1/L_ii into dinvL.  Returns false on a non-positive pivot.
+// Only one warp of a CTA may be inside this function at a time.
 __device__ inline bool chol_diag_block(float* A, int ld, int j0, int nb, float* dinvL) {
+  __shared__ __align__(16) float lcol[2 * FB];  // column j of L (rows 0..31), zeros beyond
   const int lane = threadIdx.x & 31;
   float a[FB];
 #pragma unroll
   for (int c = 0; c < FB; ++c) a[c] = (lane < nb && c <= lane) ? A[(j0 + lane) * ld + j0 + c] : 0.f;
+  lcol[FB + lane] = 0.f;
   bool ok = true;
   for (int j4 = 0; j4 < nb; j4 += 4) {
 #pragma unroll
@@ -56,11 +62,17 @@ __device__ inline bool chol_diag_block(float* A, int ld, int j0, int nb, float* 
         const float l = (lane == j) ? d * rs : a[jj] * rs;  // L_ij for lane i >= j
         if (lane >= j && lane < nb) A[(j0 + lane) * ld + j0 + j] = l;
         if (lane == j) dinvL[j0 + j] = rs;
+        __syncwarp();
+        lcol[lane] = (lane > j && lane < nb) ? l : 0.f;
+        __syncwarp();
+        const float4* l4 = reinterpret_cast<const float4*>(lcol + j4);
 #pragma unroll
-        for (int k = jj + 1; k < FB; ++k) {
-          const int col = j + (k - jj);
-          const float lk = __shfl_sync(0xffffffffu, l, col & 31);  // L_col,j
-          a[k] = fmaf(-l, lane >= col ? lk : 0.f, a[k]);
+        for (int q = (jj + 1) / 4; q < FB / 4; ++q) {
+          const float4 v = l4[q];  // L_{j4+4q+c, j}
+          if (4 * q + 0 > jj) a[4 * q + 0] = fmaf(-l, v.x, a[4 * q + 0]);
+          if (4 * q + 1 > jj) a[4 * q + 1] = fmaf(-l, v.y, a[4 * q + 1]);
+          if (4 * q + 2 > jj) a[4 * q + 2] = fmaf(-l, v.z, a[4 * q + 2]);
+          if (4 * q + 3 > jj) a[4 * q + 3] = fmaf(-l, v.w, a[4 * q + 3]);
         }
       }
     }
@@ -69,6 +81,7 @@ __device__ inline bool chol_diag_block(float* A, int ld, int j0, int nb, float* 
 #pragma unroll
     for (int k = FB - 4; k < FB; ++k) a[k] = 0.f;
   }
+  __syncwarp();
   return __all_sync(0xffffffffu, ok);
 }
 

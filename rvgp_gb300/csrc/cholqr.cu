@@ -177,7 +177,8 @@ int cholqr32_max_p() {
   if (cudaGetDevice(&dev) != cudaSuccess) return 0;
   if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return 0;
   int p = 32;
-  while (chol_smem(p + 4) <= (size_t)optin && trsm_smem(p + 4) <= (size_t)optin) p += 4;
+  // + 512: the factorisation's static shared memory
+  while (chol_smem(p + 4) + 512 <= (size_t)optin && trsm_smem(p + 4) <= (size_t)optin) p += 4;
   return p;
 }
 

@@ -500,7 +500,7 @@ RVGP_API int rvgp_gp_fit_mixed_max_m(void) {
   if (cudaGetDevice(&dev) != cudaSuccess) return 0;
   if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return 0;
   int m = 8;
-  while (layout(m + 1).total + 64 <= (size_t)optin) ++m;
+  while (layout(m + 1).total + 512 <= (size_t)optin) ++m;  // + the kernel's static shared memory
   return m;
 }
 
