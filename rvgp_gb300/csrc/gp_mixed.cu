@@ -50,7 +50,13 @@ struct Layout {
   size_t S, dS, tmp, Dm1, invD, invS, isd, rb, w, cdg, red, th, adam, outv, A, T, u, z, c, L, total;
 };
 
-__host__ __device__ inline Layout layout(int m) {
+// sweep form: the lower triangle of Ã in 8 x 8 register tiles, one per thread
+constexpr int kSweepThreads = 384;
+constexpr int kSweepMaxM = 200;  // 25 x 26 / 2 = 325 tiles <= kSweepThreads
+__host__ __device__ inline int sweep_pad(int m) { return (m + 7) / 8 * 8; }
+__host__ __device__ inline int sweep_tiles(int m) { return (m + 7) / 8 * ((m + 7) / 8 + 1) / 2; }
+
+__host__ __device__ inline Layout layout(int m, bool sweep = false) {
   Layout L{};
   size_t o = 0;
   auto take = [&](size_t bytes) {
@@ -73,8 +79,15 @@ __host__ __device__ inline Layout layout(int m) {
   L.th = take(8 * 4);
   L.adam = take(8 * 16);
   L.outv = take(8 * 8);
-  L.A = take(4 * (size_t)m * lda32(m));
-  L.T = take(4 * (size_t)m * kLdT);
+  if (sweep) {
+    // A: two pivot-column buffers (np + 8 floats each), the pivots, and the
+    // per-tile partial sums of Ã⁻¹u
+    L.A = take(4 * (3 * (size_t)sweep_pad(m) + 16 + 16 * (size_t)sweep_tiles(m)));
+    L.T = take(0);
+  } else {
+    L.A = take(4 * (size_t)m * lda32(m));
+    L.T = take(4 * (size_t)m * kLdT);
+  }
   L.u = take(f);
   L.z = take(f);
   L.c = take(f);
@@ -225,14 +238,163 @@ __device__ void inverse_finish(float* A, int ld, int j0, int m, const float* T) 
   }
 }
 
-__global__ void __launch_bounds__(kThreads, 1)
-    gp_fit_f32(const float* __restrict__ C32, const double* __restrict__ Cd, const double* __restrict__ bvec,
+// Gauss-Jordan sweep of the n x n symmetric positive definite Ã (n <= 200) by
+// the CTA: thread t < tiles(n) holds the 8 x 8 tile (ti, tj), tj <= ti, of the
+// lower triangle in registers.  Pivot k replaces Ã by its sweep on k:
+//   a_kk <- -1/d,  a_ik <- a_ik/d,  a_ij <- a_ij - a_ik a_kj/d   (d = a_kk),
+// so after all n pivots the tiles hold -Ã⁻¹; the pivots are the LDLᵀ pivots
+// (log|Ã| = Σ log d_k).  Column k of the symmetric matrix is published to a
+// shared buffer (rows >= k from tile column k / 8, rows < k from tile row
+// k / 8), one CTA barrier per pivot, double-buffered; pivots are unrolled
+// eight at a time so every register index is a compile-time constant.
+// Entries above the diagonal inside diagonal tiles are updated but never read.
+// Returns in cf (l < n) the diagonal of Ã⁻¹, in wf the product Ã⁻¹ u, in piv the
+// pivots; *bad is set when a pivot is not positive.
+template <int NT>
+__device__ void sweep_inverse(const float* __restrict__ C32, int n, const float* hf, const float* uf, float* colb,
+                              float* piv, float* part, float* cf, float* wf, int* bad) {
+  const int tid = threadIdx.x;
+  const int np = sweep_pad(n), nt = np / 8, tiles = sweep_tiles(n);
+  const int cs = np + 8;  // column buffer stride: np rows, then 1/d at [np]
+  const bool own = tid < tiles;
+  int ti = 0, tj = 0;
+  if (own) {
+    ti = (int)((sqrtf(8.f * tid + 1.f) - 1.f) * 0.5f);
+    while (ti * (ti + 1) / 2 > tid) --ti;
+    while ((ti + 1) * (ti + 2) / 2 <= tid) ++ti;
+    tj = tid - ti * (ti + 1) / 2;
+  }
+  float a[8][8];
+#pragma unroll
+  for (int r = 0; r < 8; ++r)
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      const int i = 8 * ti + r, j = 8 * tj + c;
+      a[r][c] = (i == j) ? 1.f : (own && i < n && j < n) ? __ldg(C32 + (size_t)i * n + j) * hf[i] * hf[j] : 0.f;
+    }
+  // column 0 (the owner of a diagonal entry also publishes 1/d and the pivot)
+  if (own && tj == 0) {
+#pragma unroll
+    for (int r = 0; r < 8; ++r) colb[8 * ti + r] = a[r][0];
+    if (ti == 0) {
+      colb[np] = 1.f / a[0][0];
+      piv[0] = a[0][0];
+    }
+  }
+  __syncthreads();
+  for (int kb = 0; kb < nt; ++kb) {
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+      const int k = 8 * kb + s;
+      if (k < n) {
+        const float* cb = colb + (k & 1) * cs;
+        if (own) {
+          const float id = cb[np];
+          float ci[8], cj[8];
+          const float4 i0 = *reinterpret_cast<const float4*>(cb + 8 * ti);
+          const float4 i1 = *reinterpret_cast<const float4*>(cb + 8 * ti + 4);
+          const float4 j0 = *reinterpret_cast<const float4*>(cb + 8 * tj);
+          const float4 j1 = *reinterpret_cast<const float4*>(cb + 8 * tj + 4);
+          ci[0] = i0.x; ci[1] = i0.y; ci[2] = i0.z; ci[3] = i0.w;
+          ci[4] = i1.x; ci[5] = i1.y; ci[6] = i1.z; ci[7] = i1.w;
+          cj[0] = j0.x * id; cj[1] = j0.y * id; cj[2] = j0.z * id; cj[3] = j0.w * id;
+          cj[4] = j1.x * id; cj[5] = j1.y * id; cj[6] = j1.z * id; cj[7] = j1.w * id;
+          // column k + 1 after this pivot, published first (same arithmetic as
+          // the update below), so the next pivot's data does not wait for the
+          // bulk of the update
+          const int s1 = (s + 1) & 7;
+          const int kb1 = kb + (s == 7 ? 1 : 0), k1 = k + 1;
+          if (k1 < n) {
+            float* nb = colb + (k1 & 1) * cs;
+            if (tj == kb1) {  // rows >= k + 1 of column k + 1
+#pragma unroll
+              for (int r = 0; r < 8; ++r)
+                if (8 * ti + r >= k1) nb[8 * ti + r] = fmaf(-ci[r], cj[s1], a[r][s1]);
+              if (ti == kb1) {
+                const float d1 = fmaf(-ci[s1], cj[s1], a[s1][s1]);
+                // 1/d: hardware estimate refined by one Newton step r (2 - d r)
+                const float r0 = __fdividef(1.f, d1);
+                nb[np] = r0 * fmaf(-d1, r0, 2.f);
+                piv[k1] = d1;
+              }
+            }
+            if (ti == kb1)  // rows < k + 1, from row k + 1 (entry k: the column-k value a_{k+1,k}/d)
+#pragma unroll
+              for (int c = 0; c < 8; ++c) {
+                const int j = 8 * tj + c;
+                if (j < k) nb[j] = fmaf(-ci[s1], cj[c], a[s1][c]);
+                if (j == k) nb[j] = ci[s1] * id;
+              }
+          }
+#pragma unroll
+          for (int r = 0; r < 8; ++r)
+#pragma unroll
+            for (int c = 0; c < 8; ++c) a[r][c] = fmaf(-ci[r], cj[c], a[r][c]);
+          if (tj == kb)  // column k: a_ik / d below the diagonal, -1/d on it
+#pragma unroll
+            for (int r = 0; r < 8; ++r) {
+              const int i = 8 * ti + r;
+              if (i > k) a[r][s] = ci[r] * id;
+              if (i == k) a[r][s] = -id;
+            }
+          if (ti == kb)  // row k left of the diagonal: a_kj / d
+#pragma unroll
+            for (int c = 0; c < 8; ++c)
+              if (8 * tj + c < k) a[s][c] = cj[c];
+        }
+        __syncthreads();
+      }
+    }
+  }
+  for (int k = tid; k < n; k += NT)
+    if (!(piv[k] > 0.f)) *bad = 1;  // a non-positive pivot: Ã is not (numerically) positive definite
+  // diagonal of Ã⁻¹ and the partial sums of Ã⁻¹ u: a tile contributes its rows
+  // (Σ_j a_ij u_j) and, off the diagonal, its columns (Σ_i a_ij u_i)
+  if (own) {
+    float rs[8], cs[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) rs[q] = cs[q] = 0.f;
+#pragma unroll
+    for (int r = 0; r < 8; ++r)
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        const int i = 8 * ti + r, j = 8 * tj + c;
+        const float ui = i < n ? uf[i] : 0.f, uj = j < n ? uf[j] : 0.f;
+        if (ti > tj || r >= c) rs[r] = fmaf(a[r][c], uj, rs[r]);
+        if (ti > tj || r > c) cs[c] = fmaf(a[r][c], ui, cs[c]);
+      }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      part[16 * tid + q] = rs[q];
+      part[16 * tid + 8 + q] = cs[q];
+    }
+    if (ti == tj)
+#pragma unroll
+      for (int r = 0; r < 8; ++r)
+        if (8 * ti + r < n) cf[8 * ti + r] = -a[r][r];
+  }
+  __syncthreads();
+  // row i: tiles (ti(i), tj <= ti(i)) by rows, then tiles (ti' > tj(i), tj(i)) by columns, fixed order
+  for (int i = tid; i < n; i += NT) {
+    const int b = i / 8, q = i % 8;
+    float acc = 0.f;
+    for (int t2 = 0; t2 <= b; ++t2) acc += part[16 * (b * (b + 1) / 2 + t2) + q];
+    for (int t1 = b + 1; t1 < nt; ++t1) acc += part[16 * (t1 * (t1 + 1) / 2 + b) + 8 + q];
+    wf[i] = -acc;
+  }
+  __syncthreads();
+}
+
+template <bool SWEEP>
+__global__ void __launch_bounds__(SWEEP ? kSweepThreads : kThreads, 1)
+    gp_fit_kernel(const float* __restrict__ C32, const double* __restrict__ Cd, const double* __restrict__ bvec,
                const double* __restrict__ yy_p, long long N, int m, const double* __restrict__ evals, double n_rows,
                int typ, const double* __restrict__ theta0, const double* __restrict__ lower,
                const int* __restrict__ mask, int steps, double lr, double beta1, double beta2, double eps,
                double* __restrict__ theta_out, double* __restrict__ hist, int* __restrict__ status) {
+  constexpr int NT = SWEEP ? kSweepThreads : kThreads;
   extern __shared__ __align__(16) unsigned char sm[];
-  const Layout Ly = layout(m);
+  const Layout Ly = layout(m, SWEEP);
   double* S = reinterpret_cast<double*>(sm + Ly.S);
   double* dS = reinterpret_cast<double*>(sm + Ly.dS);
   double* tmp = reinterpret_cast<double*>(sm + Ly.tmp);
@@ -261,10 +423,11 @@ __global__ void __launch_bounds__(kThreads, 1)
   const int nw = (m + 31) / 32;  // warps holding the per-eigenpair values
   const double yy = yy_p[0];
   const double Nd = (double)N;
-  for (int l = tid; l < m; l += kThreads) cdg[l] = Cd[(size_t)l * m + l];
+  for (int l = tid; l < m; l += NT) cdg[l] = Cd[(size_t)l * m + l];
   // row padding [m, ld) is read (and multiplied by masked zeros) by the float4
   // loops; it must hold finite values
-  for (int e = tid; e < m * (ld - m); e += kThreads) A[(e / (ld - m)) * ld + m + e % (ld - m)] = 0.f;
+  if (!SWEEP)
+    for (int e = tid; e < m * (ld - m); e += NT) A[(e / (ld - m)) * ld + m + e % (ld - m)] = 0.f;
   if (tid == 0) {
     s_bad = 0;
     for (int q = 0; q < 4; ++q) {
@@ -282,7 +445,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     const double nu = th[0], kappa = th[1], sf = th[2], s2 = th[3];
     // ---- 1. spectral weights and their derivatives (log domain), FP64
     double mx = -DBL_MAX;
-    for (int l = tid; l < m; l += kThreads) {
+    for (int l = tid; l < m; l += NT) {
       const double lam = evals[l];
       double a, b, c;
       if (typ == 0) {
@@ -306,21 +469,21 @@ __global__ void __launch_bounds__(kThreads, 1)
     mx = cta_max(mx, red, nw);
     {
       double v[1] = {0.0};
-      for (int l = tid; l < m; l += kThreads) {
+      for (int l = tid; l < m; l += NT) {
         S[l] = (double)expf((float)(tmp[l] - mx));  // unnormalised weight (<= 1), normalised below
         v[0] += S[l];
       }
       cta_sum<1>(v, red, nw);
       const double iz = rcp_nr(v[0]);
       double g[2] = {0.0, 0.0};
-      for (int l = tid; l < m; l += kThreads) {
+      for (int l = tid; l < m; l += NT) {
         const double wl = S[l] * iz;
         g[0] += wl * tmp[m + l];
         g[1] += wl * tmp[2 * m + l];
       }
       cta_sum<2>(g, red, nw);
       const double is2 = rcp_nr(s2), isf = rcp_nr(sf);
-      for (int l = tid; l < m; l += kThreads) {
+      for (int l = tid; l < m; l += NT) {
         const double Sl = sf * n_rows * S[l] * iz;
         S[l] = Sl;
         dS[l] = Sl * (tmp[m + l] - g[0]);
@@ -342,8 +505,28 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     __syncthreads();
     if (s_bad) break;
+    double logL = 0.0;
+    if constexpr (SWEEP) {
+      // ---- 2-5 (sweep form): Ã⁻¹ by a Gauss-Jordan sweep in registers; w̃ = Ã⁻¹ u,
+      // c_l = (Ã⁻¹)_ll, log|Ã|/2 from the pivots
+      float* colb = A;
+      float* piv = colb + 2 * (sweep_pad(m) + 8);
+      float* part = piv + sweep_pad(m);
+      if (tid == 0) s_chol = 0;
+      __syncthreads();
+      sweep_inverse<NT>(C32, m, hf, uf, colb, piv, part, cf, zf, &s_chol);
+      if (s_chol) {
+        if (tid == 0) s_bad = 1;
+        break;
+      }
+      for (int l = tid; l < m; l += NT) {
+        uf[l] = zf[l];  // w̃_l
+        logL += 0.5 * (double)logf(piv[l]);
+      }
+      __syncthreads();
+    } else {
     // ---- 2. scaled capacitance matrix (lower triangle, unit diagonal), FP32
-    for (int i = warp; i < m; i += kWarps) {
+    for (int i = warp; i < m; i += NT / 32) {
       const float hi = hf[i];
 #pragma unroll 4
       for (int j = lane; j <= i; j += 32) A[i * ld + j] = (j == i) ? 1.f : __ldg(C32 + (size_t)i * m + j) * hi * hf[j];
@@ -358,8 +541,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     // moved from the upper triangle to the lower; log L_ll for |Ã|
     chol32::invert_diag_blocks(A, ld, m, nblk, dinvL);
     __syncthreads();
-    double logL = 0.0;
-    for (int e = tid; e < nblk * FB * FB; e += kThreads) {
+    for (int e = tid; e < nblk * FB * FB; e += NT) {
       const int jb = e / (FB * FB), r = (e / FB) % FB, c = e % FB;
       const int j0 = jb * FB, i = j0 + r, j = j0 + c;
       if (i < m && j < m) {
@@ -374,7 +556,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (int jb = nblk - 2; jb >= 0; --jb) {
       const int j0 = jb * FB, r0 = j0 + FB;
       // the block column's L (rows >= r0) into the upper triangle, transposed
-      for (int e = tid; e < (m - r0) * FB; e += kThreads) {
+      for (int e = tid; e < (m - r0) * FB; e += NT) {
         const int k = r0 + e / FB, c = e % FB;
         A[(j0 + c) * ld + k] = A[k * ld + j0 + c];
       }
@@ -385,7 +567,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       __syncthreads();
     }
     // ---- 5. z̃ = M u (warp per row), then w̃ = Mᵀ z̃ and column norms (warp per column)
-    for (int i = warp; i < m; i += kWarps) {
+    for (int i = warp; i < m; i += NT / 32) {
       float s = 0.f;
       for (int k = lane; k <= i; k += 32) s = fmaf(A[i * ld + k], uf[k], s);
 #pragma unroll
@@ -393,7 +575,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       if (lane == 0) zf[i] = s;
     }
     __syncthreads();
-    for (int l = warp; l < m; l += kWarps) {
+    for (int l = warp; l < m; l += NT / 32) {
       float s = 0.f, q = 0.f;
       for (int k = l + lane; k < m; k += 32) {
         const float v = A[k * ld + l];
@@ -411,10 +593,11 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
     }
     __syncthreads();
+    }
     // ---- 6. likelihood and gradient (FP64)
     {
       double v[7] = {0, 0, 0, 0, 0, 0, 0};  // zz, ww, log|Ã|/2 + log|Δ|, tr A⁻¹, g_nu, g_kappa, g_sf
-      for (int l = tid; l < m; l += kThreads) {
+      for (int l = tid; l < m; l += NT) {
         const double wl = (double)uf[l] * isd[l];
         wv[l] = wl;
         const double cl = (double)cf[l];
@@ -549,14 +732,21 @@ RVGP_API int rvgp_gp_fit_adam_mixed_launch(const double* C, const double* b, con
   cudaMemcpyAsync(f.dm, mask, 4 * sizeof(int), cudaMemcpyHostToDevice, st);
   rvgp::note_launch();
   to_f32<<<ceil_div((long long)m * m, 256), 256, 0, st>>>(C, (long long)m * m, f.C32);
-  const size_t smem = layout(m).total;
-  if (cudaFuncSetAttribute(gp_fit_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+  // m <= 200: the register-tile Gauss-Jordan sweep; larger m: the shared-memory Cholesky and inverse
+  const bool sweep = m <= kSweepMaxM;
+  const size_t smem = layout(m, sweep).total;
+  const void* fn = sweep ? (const void*)gp_fit_kernel<true> : (const void*)gp_fit_kernel<false>;
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
     set_error("rvgp_gp_fit_adam_mixed: cannot reserve %zu bytes of shared memory", smem);
     return RVGP_ELAUNCH;
   }
   rvgp::note_launch();
-  gp_fit_f32<<<1, kThreads, smem, st>>>(f.C32, C, b, yy, N, m, evals, n_rows, typ, theta0, f.dl, f.dm, steps, lr,
-                                        beta1, beta2, eps, theta_out, hist, f.dstat);
+  if (sweep)
+    gp_fit_kernel<true><<<1, kSweepThreads, smem, st>>>(f.C32, C, b, yy, N, m, evals, n_rows, typ, theta0, f.dl, f.dm,
+                                                        steps, lr, beta1, beta2, eps, theta_out, hist, f.dstat);
+  else
+    gp_fit_kernel<false><<<1, kThreads, smem, st>>>(f.C32, C, b, yy, N, m, evals, n_rows, typ, theta0, f.dl, f.dm,
+                                                    steps, lr, beta1, beta2, eps, theta_out, hist, f.dstat);
   RVGP_LAUNCH_CHECK("rvgp_gp_fit_adam_mixed");
   return RVGP_OK;
 }
