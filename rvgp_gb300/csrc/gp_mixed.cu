@@ -80,9 +80,9 @@ __host__ __device__ inline Layout layout(int m, bool sweep = false) {
   L.adam = take(8 * 16);
   L.outv = take(8 * 8);
   if (sweep) {
-    // A: two pivot-column buffers (np + 8 floats each), the pivots, and the
-    // per-tile partial sums of Ã⁻¹u
-    L.A = take(4 * (3 * (size_t)sweep_pad(m) + 16 + 16 * (size_t)sweep_tiles(m)));
+    // A: two buffers of a pivot pair's columns (2 np + 8 floats each), the
+    // pivots (np), and the per-tile partial sums of Ã⁻¹u
+    L.A = take(4 * (5 * (size_t)sweep_pad(m) + 16 + 16 * (size_t)sweep_tiles(m)));
     L.T = take(0);
   } else {
     L.A = take(4 * (size_t)m * lda32(m));
@@ -250,12 +250,19 @@ __device__ void inverse_finish(float* A, int ld, int j0, int m, const float* T) 
 // Entries above the diagonal inside diagonal tiles are updated but never read.
 // Returns in cf (l < n) the diagonal of Ã⁻¹, in wf the product Ã⁻¹ u, in piv the
 // pivots; *bad is set when a pivot is not positive.
+// 1/x: hardware estimate refined by one Newton step r (2 - x r)
+__device__ __forceinline__ float rcp_f(float x) {
+  const float r0 = __fdividef(1.f, x);
+  return r0 * fmaf(-x, r0, 2.f);
+}
+
 template <int NT>
 __device__ void sweep_inverse(const float* __restrict__ C32, int n, const float* hf, const float* uf, float* colb,
                               float* piv, float* part, float* cf, float* wf, int* bad) {
   const int tid = threadIdx.x;
   const int np = sweep_pad(n), nt = np / 8, tiles = sweep_tiles(n);
-  const int cs = np + 8;  // column buffer stride: np rows, then 1/d at [np]
+  const int ne = (n + 1) / 2 * 2;     // pivots in pairs; an odd n also sweeps the padding index n (identity)
+  const int cs = 2 * np + 8;          // buffer stride: column k (u) at [0, np), column k + 1 (v) at [np, 2 np)
   const bool own = tid < tiles;
   int ti = 0, tj = 0;
   if (own) {
@@ -272,75 +279,126 @@ __device__ void sweep_inverse(const float* __restrict__ C32, int n, const float*
       const int i = 8 * ti + r, j = 8 * tj + c;
       a[r][c] = (i == j) ? 1.f : (own && i < n && j < n) ? __ldg(C32 + (size_t)i * n + j) * hf[i] * hf[j] : 0.f;
     }
-  // column 0 (the owner of a diagonal entry also publishes 1/d and the pivot)
+  // columns 0 and 1
   if (own && tj == 0) {
 #pragma unroll
-    for (int r = 0; r < 8; ++r) colb[8 * ti + r] = a[r][0];
-    if (ti == 0) {
-      colb[np] = 1.f / a[0][0];
-      piv[0] = a[0][0];
+    for (int r = 0; r < 8; ++r) {
+      colb[8 * ti + r] = a[r][0];
+      if (8 * ti + r >= 1) colb[np + 8 * ti + r] = a[r][1];
     }
+    if (ti == 0) colb[np] = a[1][0];
   }
   __syncthreads();
+  // Two pivots (k, k + 1) per barrier: with u, v columns k, k + 1 before the
+  // pair, d = u_k, e = u_{k+1}, t = e/d, d' = v_{k+1} - e t, v' = v - u t, the
+  // pair's sweep is A <- A - u uᵀ/d - v' v'ᵀ/d' off rows / columns k, k + 1;
+  // column k becomes u/d - v' f (f = t/d'), column k + 1 v'/d', the 2 x 2
+  // block [-1/d - t f, f; f, -1/d'].
   for (int kb = 0; kb < nt; ++kb) {
 #pragma unroll
-    for (int s = 0; s < 8; ++s) {
+    for (int s = 0; s < 8; s += 2) {
       const int k = 8 * kb + s;
-      if (k < n) {
-        const float* cb = colb + (k & 1) * cs;
+      if (k < ne) {
+        const float* U = colb + ((k >> 1) & 1) * cs;
+        const float* V = U + np;
+        const float d = U[k], e = U[k + 1], vkk = V[k + 1];
+        const float idk = rcp_f(d);
+        const float t = e * idk;
+        const float d2 = fmaf(-e, t, vkk);
+        const float id2 = rcp_f(d2);
+        const float f = t * id2;
+        if (tid == 0) {
+          piv[k] = d;
+          piv[k + 1] = d2;
+        }
         if (own) {
-          const float id = cb[np];
-          float ci[8], cj[8];
-          const float4 i0 = *reinterpret_cast<const float4*>(cb + 8 * ti);
-          const float4 i1 = *reinterpret_cast<const float4*>(cb + 8 * ti + 4);
-          const float4 j0 = *reinterpret_cast<const float4*>(cb + 8 * tj);
-          const float4 j1 = *reinterpret_cast<const float4*>(cb + 8 * tj + 4);
-          ci[0] = i0.x; ci[1] = i0.y; ci[2] = i0.z; ci[3] = i0.w;
-          ci[4] = i1.x; ci[5] = i1.y; ci[6] = i1.z; ci[7] = i1.w;
-          cj[0] = j0.x * id; cj[1] = j0.y * id; cj[2] = j0.z * id; cj[3] = j0.w * id;
-          cj[4] = j1.x * id; cj[5] = j1.y * id; cj[6] = j1.z * id; cj[7] = j1.w * id;
-          // column k + 1 after this pivot, published first (same arithmetic as
-          // the update below), so the next pivot's data does not wait for the
-          // bulk of the update
-          const int s1 = (s + 1) & 7;
-          const int kb1 = kb + (s == 7 ? 1 : 0), k1 = k + 1;
-          if (k1 < n) {
-            float* nb = colb + (k1 & 1) * cs;
-            if (tj == kb1) {  // rows >= k + 1 of column k + 1
+          float ui[8], vi[8], uj[8], vj[8];  // u_i, v'_i; u_j / d, v'_j / d'
+          {
+            const float4 a0 = *reinterpret_cast<const float4*>(U + 8 * ti);
+            const float4 a1 = *reinterpret_cast<const float4*>(U + 8 * ti + 4);
+            const float4 b0 = *reinterpret_cast<const float4*>(V + 8 * ti);
+            const float4 b1 = *reinterpret_cast<const float4*>(V + 8 * ti + 4);
+            const float uu[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+            const float vv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
 #pragma unroll
-              for (int r = 0; r < 8; ++r)
-                if (8 * ti + r >= k1) nb[8 * ti + r] = fmaf(-ci[r], cj[s1], a[r][s1]);
-              if (ti == kb1) {
-                const float d1 = fmaf(-ci[s1], cj[s1], a[s1][s1]);
-                // 1/d: hardware estimate refined by one Newton step r (2 - d r)
-                const float r0 = __fdividef(1.f, d1);
-                nb[np] = r0 * fmaf(-d1, r0, 2.f);
-                piv[k1] = d1;
+            for (int q = 0; q < 8; ++q) {
+              ui[q] = uu[q];
+              vi[q] = fmaf(-uu[q], t, vv[q]);
+            }
+          }
+          {
+            const float4 a0 = *reinterpret_cast<const float4*>(U + 8 * tj);
+            const float4 a1 = *reinterpret_cast<const float4*>(U + 8 * tj + 4);
+            const float4 b0 = *reinterpret_cast<const float4*>(V + 8 * tj);
+            const float4 b1 = *reinterpret_cast<const float4*>(V + 8 * tj + 4);
+            const float uu[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+            const float vv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+              uj[q] = uu[q] * idk;
+              vj[q] = fmaf(-uu[q], t, vv[q]) * id2;
+            }
+          }
+          // columns k + 2 and k + 3 after the pair, published before the bulk update
+          const int k2 = k + 2;
+          const int kb2 = kb + (s == 6 ? 1 : 0);
+          const int s2 = (s + 2) & 7, s3 = (s + 3) & 7;
+          if (k2 < ne) {
+            float* U2 = colb + (((k >> 1) + 1) & 1) * cs;
+            float* V2 = U2 + np;
+            if (tj == kb2) {  // rows >= k + 2 (column k + 2), rows >= k + 3 (column k + 3)
+#pragma unroll
+              for (int r = 0; r < 8; ++r) {
+                const int i = 8 * ti + r;
+                if (i >= k2) U2[i] = fmaf(-vi[r], vj[s2], fmaf(-ui[r], uj[s2], a[r][s2]));
+                if (i >= k2 + 1) V2[i] = fmaf(-vi[r], vj[s3], fmaf(-ui[r], uj[s3], a[r][s3]));
               }
             }
-            if (ti == kb1)  // rows < k + 1, from row k + 1 (entry k: the column-k value a_{k+1,k}/d)
+            if (ti == kb2) {  // rows < k + 2 from row k + 2, rows < k + 3 from row k + 3
 #pragma unroll
               for (int c = 0; c < 8; ++c) {
                 const int j = 8 * tj + c;
-                if (j < k) nb[j] = fmaf(-ci[s1], cj[c], a[s1][c]);
-                if (j == k) nb[j] = ci[s1] * id;
+                if (j < k) {
+                  U2[j] = fmaf(-vi[s2], vj[c], fmaf(-ui[s2], uj[c], a[s2][c]));
+                  V2[j] = fmaf(-vi[s3], vj[c], fmaf(-ui[s3], uj[c], a[s3][c]));
+                }
+                if (j == k) {
+                  U2[j] = fmaf(-vi[s2], f, ui[s2] * idk);
+                  V2[j] = fmaf(-vi[s3], f, ui[s3] * idk);
+                }
+                if (j == k + 1) {
+                  U2[j] = vi[s2] * id2;
+                  V2[j] = vi[s3] * id2;
+                }
+                if (j == k2) V2[j] = fmaf(-vi[s3], vj[c], fmaf(-ui[s3], uj[c], a[s3][c]));
               }
+            }
           }
 #pragma unroll
           for (int r = 0; r < 8; ++r)
 #pragma unroll
-            for (int c = 0; c < 8; ++c) a[r][c] = fmaf(-ci[r], cj[c], a[r][c]);
-          if (tj == kb)  // column k: a_ik / d below the diagonal, -1/d on it
+            for (int c = 0; c < 8; ++c) a[r][c] = fmaf(-vi[r], vj[c], fmaf(-ui[r], uj[c], a[r][c]));
+          if (tj == kb)  // columns k and k + 1
 #pragma unroll
             for (int r = 0; r < 8; ++r) {
               const int i = 8 * ti + r;
-              if (i > k) a[r][s] = ci[r] * id;
-              if (i == k) a[r][s] = -id;
+              if (i > k + 1) {
+                a[r][s] = fmaf(-vi[r], f, ui[r] * idk);
+                a[r][s + 1] = vi[r] * id2;
+              }
+              if (i == k) a[r][s] = fmaf(-t, f, -idk);
+              if (i == k + 1) {
+                a[r][s] = f;
+                a[r][s + 1] = -id2;
+              }
             }
-          if (ti == kb)  // row k left of the diagonal: a_kj / d
+          if (ti == kb)  // rows k and k + 1 left of column k
 #pragma unroll
             for (int c = 0; c < 8; ++c)
-              if (8 * tj + c < k) a[s][c] = cj[c];
+              if (8 * tj + c < k) {
+                a[s][c] = fmaf(-vj[c] * d2, f, uj[c]);
+                a[s + 1][c] = vj[c];
+              }
         }
         __syncthreads();
       }
@@ -510,7 +568,7 @@ __global__ void __launch_bounds__(SWEEP ? kSweepThreads : kThreads, 1)
       // ---- 2-5 (sweep form): Ã⁻¹ by a Gauss-Jordan sweep in registers; w̃ = Ã⁻¹ u,
       // c_l = (Ã⁻¹)_ll, log|Ã|/2 from the pivots
       float* colb = A;
-      float* piv = colb + 2 * (sweep_pad(m) + 8);
+      float* piv = colb + 2 * (2 * sweep_pad(m) + 8);
       float* part = piv + sweep_pad(m);
       if (tid == 0) s_chol = 0;
       __syncthreads();
