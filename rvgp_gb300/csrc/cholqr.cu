@@ -29,9 +29,10 @@ size_t chol_smem(int p) { return sizeof(float) * ((size_t)p * chol32::lda32(p) +
 
 __global__ void __launch_bounds__(kCholThreads, 1)
     chol32_gram_kernel(const double* __restrict__ G, int p, float* __restrict__ L, float* __restrict__ Mb,
-                       float* __restrict__ d, int* __restrict__ info) {
+                       float* __restrict__ d, float first_order, int* __restrict__ info) {
   extern __shared__ __align__(16) float A[];
   __shared__ int s_flag;
+  __shared__ unsigned s_emax;
   const int ld = chol32::lda32(p);
   float* dinvL = A + (size_t)p * ld;
   const int nblk = (p + FB - 1) / FB;
@@ -46,7 +47,26 @@ __global__ void __launch_bounds__(kCholThreads, 1)
     for (int j = threadIdx.x & 31; j <= i; j += 32)
       A[i * ld + j] = (i == j && dsh[i] > 0.f) ? 1.f : (float)G[(size_t)i * p + j] * dsh[i] * dsh[j];
   for (int i = threadIdx.x; i < p; i += kCholThreads) d[i] = dsh[i];
+  if (threadIdx.x == 0) s_emax = 0u;
   __syncthreads();
+  if (first_order > 0.f) {
+    // a nearly orthonormal block: E = D G D - I small, and V D (I - E/2) is
+    // orthonormal to O(|E|²); L receives B = D (I - E/2) (row-major, p x p)
+    float em = 0.f;
+    for (int i = threadIdx.x >> 5; i < p; i += kCholThreads / 32)
+      for (int j = threadIdx.x & 31; j <= i; j += 32) em = fmaxf(em, fabsf(A[i * ld + j] - (i == j ? 1.f : 0.f)));
+    atomicMax(&s_emax, __float_as_uint(em));  // non-negative floats order as their bits
+    __syncthreads();
+    if (__uint_as_float(s_emax) <= first_order) {
+      for (int i = threadIdx.x >> 5; i < p; i += kCholThreads / 32)
+        for (int j = threadIdx.x & 31; j < p; j += 32) {
+          const float e = (i == j) ? 0.f : A[max(i, j) * ld + min(i, j)];
+          L[(size_t)i * p + j] = dsh[i] * ((i == j ? 1.f : 0.f) - 0.5f * e);
+        }
+      if (threadIdx.x == 0) *info = 2;
+      return;
+    }
+  }
   if (!chol32::chol32_cta<kCholThreads>(A, ld, p, dinvL, &s_flag)) {
     if (threadIdx.x == 0) *info = 1;
     return;
@@ -187,14 +207,15 @@ size_t cholqr32_workspace(int p) {
   return sizeof(float) * ((size_t)p * p + (size_t)nblk * FB * FB) + 512;
 }
 
-int chol32_gram(const double* G, int p, float* L, float* Mb, float* d, int* info, cudaStream_t st) {
+int chol32_gram(const double* G, int p, float* L, float* Mb, float* d, float first_order, int* info,
+                cudaStream_t st) {
   const size_t smem = chol_smem(p);
   if (cudaFuncSetAttribute(chol32_gram_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
     set_error("chol32_gram: cannot reserve %zu bytes of shared memory", smem);
     return RVGP_ELAUNCH;
   }
   rvgp::note_launch();
-  chol32_gram_kernel<<<1, kCholThreads, smem, st>>>(G, p, L, Mb, d, info);
+  chol32_gram_kernel<<<1, kCholThreads, smem, st>>>(G, p, L, Mb, d, first_order, info);
   return check_launch("chol32_gram");
 }
 

@@ -262,7 +262,10 @@ inline int gram_any(const double* A, const double* B, long long N, int p, double
   return gram<double>(A, p, B, p, N, p, p, C, p, 1.0, 0.0, s.gram_ws, s.gram_bytes, st);
 }
 
-constexpr int kFp32Sweeps = 12;  // FP32 Jacobi sweeps are capped: off(H) stalls at FP32 rounding
+constexpr int kFp32Sweeps = 12;
+// second Cholesky QR pass: first-order correction when max |E| <= this (the
+// result's departure from orthonormality is ~0.75 |E|², 7.5e-7 at the bound)
+constexpr float kFirstOrderTol = 1e-3f;  // FP32 Jacobi sweeps are capped: off(H) stalls at FP32 rounding
 
 #define TRY(x)                  \
   do {                          \
@@ -334,9 +337,16 @@ int orthonormalise(const Problem& P, Block<T>& B, Small& s, Stats& stt, cudaStre
   for (int pass = 0; pass < 2; ++pass) {
     if (sizeof(T) == 4 && s.cholqr32) {
       TRY(gram_any(B.V, B.V, N, p, s.G, s, st));
-      TRY(chol32_gram(s.G, p, s.L32, s.Mb32, s.d32, s.info, st));
+      // the second pass usually meets a block orthonormal to ~1e-4: a first-order
+      // correction (one block product) then replaces factorisation and solve
+      TRY(chol32_gram(s.G, p, s.L32, s.Mb32, s.d32, pass == 1 ? kFirstOrderTol : 0.f, s.info, st));
       int info32 = 0;
       if (read_back(&info32, s.info, sizeof(int), st) != cudaSuccess) return check_launch("orthonormalise");
+      if (info32 == 2) {
+        TRY(block_product(reinterpret_cast<const float*>(B.V), s.L32, N, p, reinterpret_cast<float*>(B.T1), s, st));
+        std::swap(B.V, B.T1);
+        continue;
+      }
       if (info32 == 0) {
         TRY(trsm_rows_f32(reinterpret_cast<float*>(B.V), p, N, p, s.L32, s.Mb32, s.d32, st));
         continue;

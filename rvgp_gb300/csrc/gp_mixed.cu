@@ -50,13 +50,7 @@ struct Layout {
   size_t S, dS, tmp, Dm1, invD, invS, isd, rb, w, cdg, red, th, adam, outv, A, T, u, z, c, L, total;
 };
 
-// sweep form: the lower triangle of Ã in 8 x 8 register tiles, one per thread
-constexpr int kSweepThreads = 384;
-constexpr int kSweepMaxM = 200;  // 25 x 26 / 2 = 325 tiles <= kSweepThreads
-__host__ __device__ inline int sweep_pad(int m) { return (m + 7) / 8 * 8; }
-__host__ __device__ inline int sweep_tiles(int m) { return (m + 7) / 8 * ((m + 7) / 8 + 1) / 2; }
-
-__host__ __device__ inline Layout layout(int m, bool sweep = false) {
+__host__ __device__ inline Layout layout(int m) {
   Layout L{};
   size_t o = 0;
   auto take = [&](size_t bytes) {
@@ -79,15 +73,8 @@ __host__ __device__ inline Layout layout(int m, bool sweep = false) {
   L.th = take(8 * 4);
   L.adam = take(8 * 16);
   L.outv = take(8 * 8);
-  if (sweep) {
-    // A: two buffers of a pivot pair's columns (2 np + 8 floats each), the
-    // pivots (np), and the per-tile partial sums of Ã⁻¹u
-    L.A = take(4 * (5 * (size_t)sweep_pad(m) + 16 + 16 * (size_t)sweep_tiles(m)));
-    L.T = take(0);
-  } else {
-    L.A = take(4 * (size_t)m * lda32(m));
-    L.T = take(4 * (size_t)m * kLdT);
-  }
+  L.A = take(4 * (size_t)m * lda32(m));
+  L.T = take(4 * (size_t)m * kLdT);
   L.u = take(f);
   L.z = take(f);
   L.c = take(f);
@@ -238,221 +225,14 @@ __device__ void inverse_finish(float* A, int ld, int j0, int m, const float* T) 
   }
 }
 
-// Gauss-Jordan sweep of the n x n symmetric positive definite Ã (n <= 200) by
-// the CTA: thread t < tiles(n) holds the 8 x 8 tile (ti, tj), tj <= ti, of the
-// lower triangle in registers.  Pivot k replaces Ã by its sweep on k:
-//   a_kk <- -1/d,  a_ik <- a_ik/d,  a_ij <- a_ij - a_ik a_kj/d   (d = a_kk),
-// so after all n pivots the tiles hold -Ã⁻¹; the pivots are the LDLᵀ pivots
-// (log|Ã| = Σ log d_k).  Column k of the symmetric matrix is published to a
-// shared buffer (rows >= k from tile column k / 8, rows < k from tile row
-// k / 8), one CTA barrier per pivot, double-buffered; pivots are unrolled
-// eight at a time so every register index is a compile-time constant.
-// Entries above the diagonal inside diagonal tiles are updated but never read.
-// Returns in cf (l < n) the diagonal of Ã⁻¹, in wf the product Ã⁻¹ u, in piv the
-// pivots; *bad is set when a pivot is not positive.
-// 1/x: hardware estimate refined by one Newton step r (2 - x r)
-__device__ __forceinline__ float rcp_f(float x) {
-  const float r0 = __fdividef(1.f, x);
-  return r0 * fmaf(-x, r0, 2.f);
-}
-
-template <int NT>
-__device__ void sweep_inverse(const float* __restrict__ C32, int n, const float* hf, const float* uf, float* colb,
-                              float* piv, float* part, float* cf, float* wf, int* bad) {
-  const int tid = threadIdx.x;
-  const int np = sweep_pad(n), nt = np / 8, tiles = sweep_tiles(n);
-  const int ne = (n + 1) / 2 * 2;     // pivots in pairs; an odd n also sweeps the padding index n (identity)
-  const int cs = 2 * np + 8;          // buffer stride: column k (u) at [0, np), column k + 1 (v) at [np, 2 np)
-  const bool own = tid < tiles;
-  int ti = 0, tj = 0;
-  if (own) {
-    ti = (int)((sqrtf(8.f * tid + 1.f) - 1.f) * 0.5f);
-    while (ti * (ti + 1) / 2 > tid) --ti;
-    while ((ti + 1) * (ti + 2) / 2 <= tid) ++ti;
-    tj = tid - ti * (ti + 1) / 2;
-  }
-  float a[8][8];
-#pragma unroll
-  for (int r = 0; r < 8; ++r)
-#pragma unroll
-    for (int c = 0; c < 8; ++c) {
-      const int i = 8 * ti + r, j = 8 * tj + c;
-      a[r][c] = (i == j) ? 1.f : (own && i < n && j < n) ? __ldg(C32 + (size_t)i * n + j) * hf[i] * hf[j] : 0.f;
-    }
-  // columns 0 and 1
-  if (own && tj == 0) {
-#pragma unroll
-    for (int r = 0; r < 8; ++r) {
-      colb[8 * ti + r] = a[r][0];
-      if (8 * ti + r >= 1) colb[np + 8 * ti + r] = a[r][1];
-    }
-    if (ti == 0) colb[np] = a[1][0];
-  }
-  __syncthreads();
-  // Two pivots (k, k + 1) per barrier: with u, v columns k, k + 1 before the
-  // pair, d = u_k, e = u_{k+1}, t = e/d, d' = v_{k+1} - e t, v' = v - u t, the
-  // pair's sweep is A <- A - u uᵀ/d - v' v'ᵀ/d' off rows / columns k, k + 1;
-  // column k becomes u/d - v' f (f = t/d'), column k + 1 v'/d', the 2 x 2
-  // block [-1/d - t f, f; f, -1/d'].
-  for (int kb = 0; kb < nt; ++kb) {
-#pragma unroll
-    for (int s = 0; s < 8; s += 2) {
-      const int k = 8 * kb + s;
-      if (k < ne) {
-        const float* U = colb + ((k >> 1) & 1) * cs;
-        const float* V = U + np;
-        const float d = U[k], e = U[k + 1], vkk = V[k + 1];
-        const float idk = rcp_f(d);
-        const float t = e * idk;
-        const float d2 = fmaf(-e, t, vkk);
-        const float id2 = rcp_f(d2);
-        const float f = t * id2;
-        if (tid == 0) {
-          piv[k] = d;
-          piv[k + 1] = d2;
-        }
-        if (own) {
-          float ui[8], vi[8], uj[8], vj[8];  // u_i, v'_i; u_j / d, v'_j / d'
-          {
-            const float4 a0 = *reinterpret_cast<const float4*>(U + 8 * ti);
-            const float4 a1 = *reinterpret_cast<const float4*>(U + 8 * ti + 4);
-            const float4 b0 = *reinterpret_cast<const float4*>(V + 8 * ti);
-            const float4 b1 = *reinterpret_cast<const float4*>(V + 8 * ti + 4);
-            const float uu[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
-            const float vv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
-#pragma unroll
-            for (int q = 0; q < 8; ++q) {
-              ui[q] = uu[q];
-              vi[q] = fmaf(-uu[q], t, vv[q]);
-            }
-          }
-          {
-            const float4 a0 = *reinterpret_cast<const float4*>(U + 8 * tj);
-            const float4 a1 = *reinterpret_cast<const float4*>(U + 8 * tj + 4);
-            const float4 b0 = *reinterpret_cast<const float4*>(V + 8 * tj);
-            const float4 b1 = *reinterpret_cast<const float4*>(V + 8 * tj + 4);
-            const float uu[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
-            const float vv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
-#pragma unroll
-            for (int q = 0; q < 8; ++q) {
-              uj[q] = uu[q] * idk;
-              vj[q] = fmaf(-uu[q], t, vv[q]) * id2;
-            }
-          }
-          // columns k + 2 and k + 3 after the pair, published before the bulk update
-          const int k2 = k + 2;
-          const int kb2 = kb + (s == 6 ? 1 : 0);
-          const int s2 = (s + 2) & 7, s3 = (s + 3) & 7;
-          if (k2 < ne) {
-            float* U2 = colb + (((k >> 1) + 1) & 1) * cs;
-            float* V2 = U2 + np;
-            if (tj == kb2) {  // rows >= k + 2 (column k + 2), rows >= k + 3 (column k + 3)
-#pragma unroll
-              for (int r = 0; r < 8; ++r) {
-                const int i = 8 * ti + r;
-                if (i >= k2) U2[i] = fmaf(-vi[r], vj[s2], fmaf(-ui[r], uj[s2], a[r][s2]));
-                if (i >= k2 + 1) V2[i] = fmaf(-vi[r], vj[s3], fmaf(-ui[r], uj[s3], a[r][s3]));
-              }
-            }
-            if (ti == kb2) {  // rows < k + 2 from row k + 2, rows < k + 3 from row k + 3
-#pragma unroll
-              for (int c = 0; c < 8; ++c) {
-                const int j = 8 * tj + c;
-                if (j < k) {
-                  U2[j] = fmaf(-vi[s2], vj[c], fmaf(-ui[s2], uj[c], a[s2][c]));
-                  V2[j] = fmaf(-vi[s3], vj[c], fmaf(-ui[s3], uj[c], a[s3][c]));
-                }
-                if (j == k) {
-                  U2[j] = fmaf(-vi[s2], f, ui[s2] * idk);
-                  V2[j] = fmaf(-vi[s3], f, ui[s3] * idk);
-                }
-                if (j == k + 1) {
-                  U2[j] = vi[s2] * id2;
-                  V2[j] = vi[s3] * id2;
-                }
-                if (j == k2) V2[j] = fmaf(-vi[s3], vj[c], fmaf(-ui[s3], uj[c], a[s3][c]));
-              }
-            }
-          }
-#pragma unroll
-          for (int r = 0; r < 8; ++r)
-#pragma unroll
-            for (int c = 0; c < 8; ++c) a[r][c] = fmaf(-vi[r], vj[c], fmaf(-ui[r], uj[c], a[r][c]));
-          if (tj == kb)  // columns k and k + 1
-#pragma unroll
-            for (int r = 0; r < 8; ++r) {
-              const int i = 8 * ti + r;
-              if (i > k + 1) {
-                a[r][s] = fmaf(-vi[r], f, ui[r] * idk);
-                a[r][s + 1] = vi[r] * id2;
-              }
-              if (i == k) a[r][s] = fmaf(-t, f, -idk);
-              if (i == k + 1) {
-                a[r][s] = f;
-                a[r][s + 1] = -id2;
-              }
-            }
-          if (ti == kb)  // rows k and k + 1 left of column k
-#pragma unroll
-            for (int c = 0; c < 8; ++c)
-              if (8 * tj + c < k) {
-                a[s][c] = fmaf(-vj[c] * d2, f, uj[c]);
-                a[s + 1][c] = vj[c];
-              }
-        }
-        __syncthreads();
-      }
-    }
-  }
-  for (int k = tid; k < n; k += NT)
-    if (!(piv[k] > 0.f)) *bad = 1;  // a non-positive pivot: Ã is not (numerically) positive definite
-  // diagonal of Ã⁻¹ and the partial sums of Ã⁻¹ u: a tile contributes its rows
-  // (Σ_j a_ij u_j) and, off the diagonal, its columns (Σ_i a_ij u_i)
-  if (own) {
-    float rs[8], cs[8];
-#pragma unroll
-    for (int q = 0; q < 8; ++q) rs[q] = cs[q] = 0.f;
-#pragma unroll
-    for (int r = 0; r < 8; ++r)
-#pragma unroll
-      for (int c = 0; c < 8; ++c) {
-        const int i = 8 * ti + r, j = 8 * tj + c;
-        const float ui = i < n ? uf[i] : 0.f, uj = j < n ? uf[j] : 0.f;
-        if (ti > tj || r >= c) rs[r] = fmaf(a[r][c], uj, rs[r]);
-        if (ti > tj || r > c) cs[c] = fmaf(a[r][c], ui, cs[c]);
-      }
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      part[16 * tid + q] = rs[q];
-      part[16 * tid + 8 + q] = cs[q];
-    }
-    if (ti == tj)
-#pragma unroll
-      for (int r = 0; r < 8; ++r)
-        if (8 * ti + r < n) cf[8 * ti + r] = -a[r][r];
-  }
-  __syncthreads();
-  // row i: tiles (ti(i), tj <= ti(i)) by rows, then tiles (ti' > tj(i), tj(i)) by columns, fixed order
-  for (int i = tid; i < n; i += NT) {
-    const int b = i / 8, q = i % 8;
-    float acc = 0.f;
-    for (int t2 = 0; t2 <= b; ++t2) acc += part[16 * (b * (b + 1) / 2 + t2) + q];
-    for (int t1 = b + 1; t1 < nt; ++t1) acc += part[16 * (t1 * (t1 + 1) / 2 + b) + 8 + q];
-    wf[i] = -acc;
-  }
-  __syncthreads();
-}
-
-template <bool SWEEP>
-__global__ void __launch_bounds__(SWEEP ? kSweepThreads : kThreads, 1)
-    gp_fit_kernel(const float* __restrict__ C32, const double* __restrict__ Cd, const double* __restrict__ bvec,
+__global__ void __launch_bounds__(kThreads, 1)
+    gp_fit_f32(const float* __restrict__ C32, const double* __restrict__ Cd, const double* __restrict__ bvec,
                const double* __restrict__ yy_p, long long N, int m, const double* __restrict__ evals, double n_rows,
                int typ, const double* __restrict__ theta0, const double* __restrict__ lower,
                const int* __restrict__ mask, int steps, double lr, double beta1, double beta2, double eps,
                double* __restrict__ theta_out, double* __restrict__ hist, int* __restrict__ status) {
-  constexpr int NT = SWEEP ? kSweepThreads : kThreads;
   extern __shared__ __align__(16) unsigned char sm[];
-  const Layout Ly = layout(m, SWEEP);
+  const Layout Ly = layout(m);
   double* S = reinterpret_cast<double*>(sm + Ly.S);
   double* dS = reinterpret_cast<double*>(sm + Ly.dS);
   double* tmp = reinterpret_cast<double*>(sm + Ly.tmp);
@@ -481,11 +261,10 @@ __global__ void __launch_bounds__(SWEEP ? kSweepThreads : kThreads, 1)
   const int nw = (m + 31) / 32;  // warps holding the per-eigenpair values
   const double yy = yy_p[0];
   const double Nd = (double)N;
-  for (int l = tid; l < m; l += NT) cdg[l] = Cd[(size_t)l * m + l];
+  for (int l = tid; l < m; l += kThreads) cdg[l] = Cd[(size_t)l * m + l];
   // row padding [m, ld) is read (and multiplied by masked zeros) by the float4
   // loops; it must hold finite values
-  if (!SWEEP)
-    for (int e = tid; e < m * (ld - m); e += NT) A[(e / (ld - m)) * ld + m + e % (ld - m)] = 0.f;
+  for (int e = tid; e < m * (ld - m); e += kThreads) A[(e / (ld - m)) * ld + m + e % (ld - m)] = 0.f;
   if (tid == 0) {
     s_bad = 0;
     for (int q = 0; q < 4; ++q) {
@@ -503,7 +282,7 @@ __global__ void __launch_bounds__(SWEEP ? kSweepThreads : kThreads, 1)
     const double nu = th[0], kappa = th[1], sf = th[2], s2 = th[3];
     // ---- 1. spectral weights and their derivatives (log domain), FP64
     double mx = -DBL_MAX;
-    for (int l = tid; l < m; l += NT) {
+    for (int l = tid; l < m; l += kThreads) {
       const double lam = evals[l];
       double a, b, c;
       if (typ == 0) {
@@ -527,21 +306,21 @@ __global__ void __launch_bounds__(SWEEP ? kSweepThreads : kThreads, 1)
     mx = cta_max(mx, red, nw);
     {
       double v[1] = {0.0};
-      for (int l = tid; l < m; l += NT) {
+      for (int l = tid; l < m; l += kThreads) {
         S[l] = (double)expf((float)(tmp[l] - mx));  // unnormalised weight (<= 1), normalised below
         v[0] += S[l];
       }
       cta_sum<1>(v, red, nw);
       const double iz = rcp_nr(v[0]);
       double g[2] = {0.0, 0.0};
-      for (int l = tid; l < m; l += NT) {
+      for (int l = tid; l < m; l += kThreads) {
         const double wl = S[l] * iz;
         g[0] += wl * tmp[m + l];
         g[1] += wl * tmp[2 * m + l];
       }
       cta_sum<2>(g, red, nw);
       const double is2 = rcp_nr(s2), isf = rcp_nr(sf);
-      for (int l = tid; l < m; l += NT) {
+      for (int l = tid; l < m; l += kThreads) {
         const double Sl = sf * n_rows * S[l] * iz;
         S[l] = Sl;
         dS[l] = Sl * (tmp[m + l] - g[0]);
@@ -563,28 +342,8 @@ __global__ void __launch_bounds__(SWEEP ? kSweepThreads : kThreads, 1)
     }
     __syncthreads();
     if (s_bad) break;
-    double logL = 0.0;
-    if constexpr (SWEEP) {
-      // ---- 2-5 (sweep form): Ã⁻¹ by a Gauss-Jordan sweep in registers; w̃ = Ã⁻¹ u,
-      // c_l = (Ã⁻¹)_ll, log|Ã|/2 from the pivots
-      float* colb = A;
-      float* piv = colb + 2 * (2 * sweep_pad(m) + 8);
-      float* part = piv + sweep_pad(m);
-      if (tid == 0) s_chol = 0;
-      __syncthreads();
-      sweep_inverse<NT>(C32, m, hf, uf, colb, piv, part, cf, zf, &s_chol);
-      if (s_chol) {
-        if (tid == 0) s_bad = 1;
-        break;
-      }
-      for (int l = tid; l < m; l += NT) {
-        uf[l] = zf[l];  // w̃_l
-        logL += 0.5 * (double)logf(piv[l]);
-      }
-      __syncthreads();
-    } else {
     // ---- 2. scaled capacitance matrix (lower triangle, unit diagonal), FP32
-    for (int i = warp; i < m; i += NT / 32) {
+    for (int i = warp; i < m; i += kWarps) {
       const float hi = hf[i];
 #pragma unroll 4
       for (int j = lane; j <= i; j += 32) A[i * ld + j] = (j == i) ? 1.f : __ldg(C32 + (size_t)i * m + j) * hi * hf[j];
@@ -599,7 +358,8 @@ __global__ void __launch_bounds__(SWEEP ? kSweepThreads : kThreads, 1)
     // moved from the upper triangle to the lower; log L_ll for |Ã|
     chol32::invert_diag_blocks(A, ld, m, nblk, dinvL);
     __syncthreads();
-    for (int e = tid; e < nblk * FB * FB; e += NT) {
+    double logL = 0.0;
+    for (int e = tid; e < nblk * FB * FB; e += kThreads) {
       const int jb = e / (FB * FB), r = (e / FB) % FB, c = e % FB;
       const int j0 = jb * FB, i = j0 + r, j = j0 + c;
       if (i < m && j < m) {
@@ -614,7 +374,7 @@ __global__ void __launch_bounds__(SWEEP ? kSweepThreads : kThreads, 1)
     for (int jb = nblk - 2; jb >= 0; --jb) {
       const int j0 = jb * FB, r0 = j0 + FB;
       // the block column's L (rows >= r0) into the upper triangle, transposed
-      for (int e = tid; e < (m - r0) * FB; e += NT) {
+      for (int e = tid; e < (m - r0) * FB; e += kThreads) {
         const int k = r0 + e / FB, c = e % FB;
         A[(j0 + c) * ld + k] = A[k * ld + j0 + c];
       }
@@ -625,7 +385,7 @@ __global__ void __launch_bounds__(SWEEP ? kSweepThreads : kThreads, 1)
       __syncthreads();
     }
     // ---- 5. z̃ = M u (warp per row), then w̃ = Mᵀ z̃ and column norms (warp per column)
-    for (int i = warp; i < m; i += NT / 32) {
+    for (int i = warp; i < m; i += kWarps) {
       float s = 0.f;
       for (int k = lane; k <= i; k += 32) s = fmaf(A[i * ld + k], uf[k], s);
 #pragma unroll
@@ -633,7 +393,7 @@ __global__ void __launch_bounds__(SWEEP ? kSweepThreads : kThreads, 1)
       if (lane == 0) zf[i] = s;
     }
     __syncthreads();
-    for (int l = warp; l < m; l += NT / 32) {
+    for (int l = warp; l < m; l += kWarps) {
       float s = 0.f, q = 0.f;
       for (int k = l + lane; k < m; k += 32) {
         const float v = A[k * ld + l];
@@ -651,11 +411,10 @@ __global__ void __launch_bounds__(SWEEP ? kSweepThreads : kThreads, 1)
       }
     }
     __syncthreads();
-    }
     // ---- 6. likelihood and gradient (FP64)
     {
       double v[7] = {0, 0, 0, 0, 0, 0, 0};  // zz, ww, log|Ã|/2 + log|Δ|, tr A⁻¹, g_nu, g_kappa, g_sf
-      for (int l = tid; l < m; l += NT) {
+      for (int l = tid; l < m; l += kThreads) {
         const double wl = (double)uf[l] * isd[l];
         wv[l] = wl;
         const double cl = (double)cf[l];
@@ -790,21 +549,14 @@ RVGP_API int rvgp_gp_fit_adam_mixed_launch(const double* C, const double* b, con
   cudaMemcpyAsync(f.dm, mask, 4 * sizeof(int), cudaMemcpyHostToDevice, st);
   rvgp::note_launch();
   to_f32<<<ceil_div((long long)m * m, 256), 256, 0, st>>>(C, (long long)m * m, f.C32);
-  // m <= 200: the register-tile Gauss-Jordan sweep; larger m: the shared-memory Cholesky and inverse
-  const bool sweep = m <= kSweepMaxM;
-  const size_t smem = layout(m, sweep).total;
-  const void* fn = sweep ? (const void*)gp_fit_kernel<true> : (const void*)gp_fit_kernel<false>;
-  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+  const size_t smem = layout(m).total;
+  if (cudaFuncSetAttribute(gp_fit_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
     set_error("rvgp_gp_fit_adam_mixed: cannot reserve %zu bytes of shared memory", smem);
     return RVGP_ELAUNCH;
   }
   rvgp::note_launch();
-  if (sweep)
-    gp_fit_kernel<true><<<1, kSweepThreads, smem, st>>>(f.C32, C, b, yy, N, m, evals, n_rows, typ, theta0, f.dl, f.dm,
-                                                        steps, lr, beta1, beta2, eps, theta_out, hist, f.dstat);
-  else
-    gp_fit_kernel<false><<<1, kThreads, smem, st>>>(f.C32, C, b, yy, N, m, evals, n_rows, typ, theta0, f.dl, f.dm,
-                                                    steps, lr, beta1, beta2, eps, theta_out, hist, f.dstat);
+  gp_fit_f32<<<1, kThreads, smem, st>>>(f.C32, C, b, yy, N, m, evals, n_rows, typ, theta0, f.dl, f.dm, steps, lr,
+                                        beta1, beta2, eps, theta_out, hist, f.dstat);
   RVGP_LAUNCH_CHECK("rvgp_gp_fit_adam_mixed");
   return RVGP_OK;
 }

@@ -110,9 +110,14 @@ int scale_cols(T* X, int ld, long long N, int b, const T* s, bool inverse, cudaS
 // diagonal blocks (Mb, ceil(p/32) x 32 x 32); *info (device) = 0, or 1 for a
 // non-positive pivot.  trsm_rows_f32 overwrites V (N x p, ld) with V D L⁻ᵀ
 // (D = diag(d); d null: the identity).  Both need p <= cholqr32_max_p().
+// With first_order > 0 and max |D G D - I| <= first_order, chol32_gram instead
+// writes B = D (I - E/2), E = D G D - I, into L (row-major p x p) and sets
+// *info = 2: V B is then orthonormal to O(|E|²) (one block product, no
+// factorisation).
 int cholqr32_max_p();
 size_t cholqr32_workspace(int p);
-int chol32_gram(const double* G, int p, float* L, float* Mb, float* d, int* info, cudaStream_t st);
+int chol32_gram(const double* G, int p, float* L, float* Mb, float* d, float first_order, int* info,
+                cudaStream_t st);
 int trsm_rows_f32(float* V, int ldv, long long N, int p, const float* L, const float* Mb, const float* d,
                   cudaStream_t st);
 
