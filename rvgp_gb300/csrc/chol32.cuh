@@ -230,13 +230,17 @@ __device__ bool chol32_cta(float* A, int ld, int m, float* dinvL, int* s_flag) {
     // tiles of the next diagonal block: tile rows ti < ceil(nb1 / 4)
     const int tr1 = (nb1 + 3) / 4;
     const int tdiag = tr1 * (tr1 + 1) / 2;
-    if (warp == 0) {
-      update_tiles(A, ld, j0, m, 0, tdiag, lane, 32);
-      __syncwarp();
-      if (!chol_diag_block(A, ld, r0, nb1, dinvL) && lane == 0) *s_flag = 1;
-    } else if (warp % 4 != 0) {
-      // warps 4, 8, ... share warp 0's scheduler (warp w issues on sub-partition
-      // w % 4) and stay idle, so the latency-bound diagonal chain is not starved
+    if (warp % 4 == 0) {
+      // warps 0, 4, 8, ... (all on warp 0's scheduler: warp w issues on
+      // sub-partition w % 4) update the next diagonal block's tiles together;
+      // then warp 0 factors it while the others stay idle, so the
+      // latency-bound diagonal chain is not starved
+      static_assert(NT % 128 == 0, "chol32_cta: NT must be a multiple of 128");
+      constexpr int kDiagW = NT / 128;
+      update_tiles(A, ld, j0, m, 0, tdiag, (warp / 4) * 32 + lane, kDiagW * 32);
+      asm volatile("bar.sync 1, %0;" ::"n"(kDiagW * 32) : "memory");
+      if (warp == 0 && !chol_diag_block(A, ld, r0, nb1, dinvL) && lane == 0) *s_flag = 1;
+    } else {
       constexpr int kUpd = NT / 32 - NT / 128;
       update_tiles(A, ld, j0, m, tdiag, INT_MAX, (warp - warp / 4 - 1) * 32 + lane, kUpd * 32);
     }
