@@ -235,6 +235,23 @@ int rvgp_kernel_matrix(const double* X, long long N1, const double* X2, long lon
                        double* K, void* stream);
 int rvgp_kernel_diag(const double* X, long long N, int m, const double* S, double* out, void* stream);
 
+/* Sparse GP with M inducing inputs Z (M x m, M <= 3072): the collapsed bound
+ * of GPflow 2.6.5 SGPR (RVGP/main.py:59-67,119-137, manifold_SGPR; jitter on
+ * Kuu) from C = ΦᵀΦ, b = Φᵀy, yᵀy.  out (device, 5) = [F, ∂F/∂nu, ∂F/∂kappa,
+ * ∂F/∂sigma_f, ∂F/∂noise], F NaN when a Cholesky factorisation failed (info,
+ * device, 2 ints: Kuu, B).  dZ (device, M x m, optional) = ∂F/∂Z; state
+ * (device, rvgp_sgpr_state_size(m), optional) feeds rvgp_sgpr_predict.  No
+ * host synchronisation. */
+size_t rvgp_sgpr_workspace(int M, int m);
+size_t rvgp_sgpr_state_size(int m);
+int rvgp_sgpr_elbo(const double* C, const double* b, const double* yy, long long N, int m, const double* Z, int M,
+                   const double* evals, double n_rows, const double* theta, int typ, double jitter, double* out,
+                   double* dZ, double* state, int* info, void* workspace, size_t ws_bytes, void* stream);
+/* SGPR.predict_f(full_cov=False) mean and variance at Nte spectral rows. */
+size_t rvgp_sgpr_predict_workspace(long long Nte, int m);
+int rvgp_sgpr_predict(const double* Phi_star, long long Nte, int m, const double* state, double* mean, double* var,
+                      void* workspace, size_t ws_bytes, void* stream);
+
 /* ---- fields and diffusion --------------------------------------------- */
 
 /* manifold_dimension (RVGP/geometry.py:83-97): var_exp (c), dim (device int,

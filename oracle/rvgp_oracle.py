@@ -7,8 +7,8 @@ product package ``rvgp_gb300`` never does.
 Each function cites the reference code it restates (paths inside the
 agosztolai/RVGP checkout).  Third-party arithmetic the reference delegates to
 (sklearn ``kneighbors_graph`` / ``train_test_split`` / ``pairwise_distances``,
-networkx Laplacians, scipy ARPACK, LAPACK ``dgesvd``, GPflow ``GPR``) is restated
-from its published semantics.  GPflow 2.6.5 and TensorFlow are absent here, so
+networkx Laplacians, scipy ARPACK, LAPACK ``dgesvd``, GPflow ``GPR`` and ``SGPR``)
+is restated from its published semantics.  GPflow 2.6.5 and TensorFlow are absent here, so
 the GP functions below are "parity unpinned" against GPflow itself: they are
 pinned only by their internal consistency (dense vs low-rank algebra, finite
 differences).  Everything up to and including the eigenpairs and the vector
@@ -450,3 +450,67 @@ def predict_f_lowrank(Phi, y, S, noise, Phi_new):
     mean = Phi_new @ w
     B = scipy.linalg.solve_triangular(LA, (Phi_new * r).T, lower=True)
     return mean, (B * B).sum(0)
+
+
+# ----------------------------------------------------------------------------- sparse GP (SGPR)
+SGPR_JITTER = 1e-6  # gpflow.config.default_jitter(), added to Kuu
+
+
+def sgpr_elbo(Phi, y, S, noise, Z, jitter=SGPR_JITTER):
+    """Collapsed variational bound of GPflow 2.6.5 ``SGPR.elbo`` (Titsias 2009)
+    for the manifold kernel, as built at RVGP/main.py:59-67,119-121.
+
+    Kuu = K(Z, Z) + jitter I = L Lᵀ,  A = L⁻¹ K(Z, X) / σ,  B = I + A Aᵀ = L_B L_Bᵀ,
+    c = L_B⁻¹ A y / σ;
+    bound = −½N log 2π − Σ log diag L_B − ½N log σ² − ½ yᵀy/σ² + ½ cᵀc
+            − ½ Σ diag K(X, X)/σ² + ½ tr(A Aᵀ).
+    """
+    N = Phi.shape[0]
+    M = Z.shape[0]
+    Kuu = kernel_K(Z, S) + jitter * np.eye(M)
+    Kuf = kernel_K(Z, S, Phi)
+    L = np.linalg.cholesky(Kuu)
+    sigma = np.sqrt(noise)
+    A = scipy.linalg.solve_triangular(L, Kuf, lower=True) / sigma
+    AAT = A @ A.T
+    LB = np.linalg.cholesky(np.eye(M) + AAT)
+    c = scipy.linalg.solve_triangular(LB, A @ y, lower=True) / sigma
+    kdiag = (Phi * Phi) @ S
+    bound = -0.5 * N * np.log(2 * np.pi) - np.log(np.diag(LB)).sum() - 0.5 * N * np.log(noise)
+    bound += -0.5 * (y @ y) / noise + 0.5 * (c @ c)
+    bound += -0.5 * kdiag.sum() / noise + 0.5 * np.trace(AAT)
+    return float(bound)
+
+
+def sgpr_elbo_dense(Phi, y, S, noise, Z, jitter=SGPR_JITTER):
+    """The same bound in its defining N-space form:
+    log N(y | 0, Q + σ² I) − ½ tr(K − Q)/σ²,  Q = K(X, Z) Kuu⁻¹ K(Z, X)."""
+    N = Phi.shape[0]
+    M = Z.shape[0]
+    Kuu = kernel_K(Z, S) + jitter * np.eye(M)
+    Kuf = kernel_K(Z, S, Phi)
+    Q = Kuf.T @ np.linalg.solve(Kuu, Kuf)
+    Lc = np.linalg.cholesky(Q + noise * np.eye(N))
+    a = scipy.linalg.solve_triangular(Lc, y, lower=True)
+    lml = -0.5 * a @ a - np.log(np.diag(Lc)).sum() - 0.5 * N * np.log(2 * np.pi)
+    return float(lml - 0.5 * (np.einsum("ij,ij->i", Phi * S, Phi).sum() - np.trace(Q)) / noise)
+
+
+def sgpr_predict_f(Phi, y, S, noise, Z, Phi_new, jitter=SGPR_JITTER):
+    """GPflow 2.6.5 ``SGPR.predict_f(full_cov=False)``: mean tmp2ᵀ c and the
+    marginal variance diag K** + colsum(tmp2²) − colsum(tmp1²), with
+    tmp1 = L⁻¹ K(Z, X*), tmp2 = L_B⁻¹ tmp1."""
+    M = Z.shape[0]
+    Kuu = kernel_K(Z, S) + jitter * np.eye(M)
+    Kuf = kernel_K(Z, S, Phi)
+    Kus = kernel_K(Z, S, Phi_new)
+    sigma = np.sqrt(noise)
+    L = np.linalg.cholesky(Kuu)
+    A = scipy.linalg.solve_triangular(L, Kuf, lower=True) / sigma
+    LB = np.linalg.cholesky(A @ A.T + np.eye(M))
+    c = scipy.linalg.solve_triangular(LB, A @ y, lower=True) / sigma
+    tmp1 = scipy.linalg.solve_triangular(L, Kus, lower=True)
+    tmp2 = scipy.linalg.solve_triangular(LB, tmp1, lower=True)
+    mean = tmp2.T @ c
+    var = np.einsum("ij,ij->i", Phi_new * S, Phi_new) + (tmp2 * tmp2).sum(0) - (tmp1 * tmp1).sum(0)
+    return mean, var

@@ -56,6 +56,12 @@ SIGNATURES = {
                                               c_size_t, P]),
     "rvgp_gp_predict_workspace": (c_size_t, [ctypes.c_longlong, c_int, c_int]),
     "rvgp_gp_predict": (c_int, [P, P, ctypes.c_longlong, c_int, c_int, P, P, P, P, c_size_t, P]),
+    "rvgp_sgpr_workspace": (c_size_t, [c_int, c_int]),
+    "rvgp_sgpr_state_size": (c_size_t, [c_int]),
+    "rvgp_sgpr_elbo": (c_int, [P, P, P, ctypes.c_longlong, c_int, P, c_int, P, c_double, P, c_int, c_double, P, P, P,
+                               P, P, c_size_t, P]),
+    "rvgp_sgpr_predict_workspace": (c_size_t, [ctypes.c_longlong, c_int]),
+    "rvgp_sgpr_predict": (c_int, [P, ctypes.c_longlong, c_int, P, P, P, P, c_size_t, P]),
     "rvgp_kernel_matrix": (c_int, [P, ctypes.c_longlong, P, ctypes.c_longlong, c_int, P, P, P]),
     "rvgp_kernel_diag": (c_int, [P, ctypes.c_longlong, c_int, P, P, P]),
     "rvgp_manifold_dimension": (c_int, [P, c_int, c_int, c_double, P, P, P]),
@@ -439,6 +445,47 @@ def gp_fit_adam(C, b, yy, N, evals, n_rows, theta0, lower, mask, steps, lr=0.05,
                                  float(betas[1]), float(eps), ptr(theta), ptr(hist), ptr(work.out), ptr(work.state),
                                  ptr(work.ws), work.ws.numel(), stream()), "rvgp_gp_fit_adam")
     return theta, work.out, hist, work
+
+
+class SGPRWorkspace:
+    """Device buffers reused across bound evaluations of one sparse-GP problem."""
+
+    def __init__(self, M, m, device):
+        L = lib()
+        self.M, self.m = M, m
+        self.ws = workspace(L.rvgp_sgpr_workspace(M, m), device)
+        self.state = torch.empty(int(L.rvgp_sgpr_state_size(m)), dtype=torch.float64, device=device)
+        self.out = torch.empty(5, dtype=torch.float64, device=device)
+        self.dZ = torch.empty((M, m), dtype=torch.float64, device=device)
+        self.info = torch.zeros(2, dtype=torch.int32, device=device)
+
+
+def sgpr_elbo(C, b, yy, N, Z, evals, n_rows, theta, typ="matern", jitter=1e-6, work=None, grad_Z=True, state=True):
+    """[F, dF/dnu, dF/dkappa, dF/dsigma_f, dF/dnoise] of the sparse GP bound (rvgp_sgpr_elbo),
+    with dF/dZ in work.dZ and the posterior in work.state; no host sync."""
+    M, m = Z.shape
+    work = work or SGPRWorkspace(M, m, Z.device)
+    check(lib().rvgp_sgpr_elbo(ptr(C), ptr(b), ptr(yy), int(N), m, ptr(Z.contiguous()), M, ptr(evals),
+                               float(n_rows), ptr(theta), KERNEL_TYPES[typ], float(jitter), ptr(work.out),
+                               ptr(work.dZ if grad_Z else None), ptr(work.state if state else None), ptr(work.info),
+                               ptr(work.ws), work.ws.numel(), stream()), "rvgp_sgpr_elbo")
+    return work.out, work
+
+
+def sgpr_predict(Phi_star, state, m):
+    """Posterior mean and marginal variance at the spectral rows Phi_star (rvgp_sgpr_predict)."""
+    Phi_star = _dev(Phi_star, torch.float64, "Phi_star")
+    Nte = Phi_star.shape[0]
+    dev = Phi_star.device
+    mean = torch.empty(Nte, dtype=torch.float64, device=dev)
+    var = torch.empty(Nte, dtype=torch.float64, device=dev)
+    if Nte == 0:
+        return mean, var
+    L = lib()
+    ws = workspace(L.rvgp_sgpr_predict_workspace(Nte, m), dev)
+    check(L.rvgp_sgpr_predict(ptr(Phi_star), int(Nte), int(m), ptr(state), ptr(mean), ptr(var), ptr(ws), ws.numel(),
+                              stream()), "rvgp_sgpr_predict")
+    return mean, var
 
 
 def gp_fit_mixed_max_m():

@@ -6,8 +6,10 @@ rows = (training point, ambient coordinate), sklearn's seeded 80/20
 ``train_test_split`` of ``train_ind``, L-BFGS-B on the negative log marginal
 likelihood for at most ``epochs`` iterations, then the "Relative l2 error"
 print on the held-out 20 %.  Every likelihood evaluation, gradient and
-prediction is a CUDA computation (rvgp_gp_lml / rvgp_gp_predict); the
-optimiser loop itself runs on the host, as GPflow's Scipy optimiser does.
+prediction is a CUDA computation (rvgp_gp_lml / rvgp_gp_predict; with
+``n_inducing_points``, the sparse GP of RVGP/main.py:59-67 through
+rvgp_sgpr_elbo / rvgp_sgpr_predict); the optimiser loop itself runs on the
+host, as GPflow's Scipy optimiser does.
 
 Reference behaviours kept by default (``reference_quirks=True``): the
 likelihood variance starts at 1.0 because ``noise_variance`` never reaches
@@ -136,7 +138,9 @@ class manifold_GPR:
                 return f, g
             x0 = np.array([p.unconstrained for p in params])
             res = scipy.optimize.minimize(fun, x0, jac=True, method="L-BFGS-B",
-                                          options={"disp": disp, "maxiter": epochs})
+                                          options={"maxiter": epochs})
+            if disp:  # scipy's L-BFGS-B no longer takes "disp": report the outcome here
+                print(f"L-BFGS-B: {res.message} ({res.nit} iterations, loss {res.fun:.6g})")
             for p, u in zip(params, res.x):
                 p.unconstrained = float(u)
             return res
@@ -214,11 +218,155 @@ class manifold_GPR:
         return mean.numpy().reshape(n, -1), var.numpy().reshape(n, -1)
 
 
-class manifold_SGPR:
-    """Sparse variational GP with inducing points (RVGP/main.py:119-137) is not part of this build."""
+class InducingPoints:
+    """GPflow ``InducingPoints``: the M x m inducing inputs Z (CUDA f64), trainable by default."""
 
-    def __init__(self, *a, **k):
-        raise NotImplementedError("manifold_SGPR (n_inducing_points) is not implemented in rvgp_gb300 yet")
+    def __init__(self, Z):
+        self.Z = Z
+        self.trainable = True
+
+    @property
+    def num_inducing(self):
+        return int(self.Z.shape[0])
+
+    def numpy(self):
+        return self.Z.cpu().numpy()
+
+
+class manifold_SGPR(manifold_GPR):
+    """GPflow-SGPR-like sparse GP on the manifold kernel (RVGP/main.py:119-137).
+
+    The collapsed bound of Titsias (GPflow 2.6.5 ``SGPR.elbo``, jitter 1e-6 on
+    Kuu), its gradient with respect to the kernel parameters, the noise
+    variance and the inducing inputs Z, and ``predict_f`` are CUDA
+    computations (rvgp_sgpr_elbo / rvgp_sgpr_predict) from C = ΦᵀΦ, b = Φᵀy
+    and yᵀy, which are formed once.  ``inducing_variable`` (M x m spectral
+    rows) defaults to the furthest-point sample of ``n_inducing_points``
+    training rows, started at row 0, as RVGP/main.py:60-61 does.  Z is
+    trained with the other parameters unless ``inducing_variable.trainable``
+    is set to False (GPflow trains it by default).
+    """
+
+    def __init__(self, data, kernel, train_points, inducing_variable=None, n_inducing_points=None,
+                 noise_variance=1.0, precision="mixed", jitter=1e-6):
+        self.data_obj = data
+        self.kernel = kernel
+        self.precision = precision
+        self.jitter = float(jitter)
+        self.likelihood = type("Gaussian", (), {})()
+        self.likelihood.variance = Parameter(noise_variance, lower=1e-6, name="noise_variance")
+        dev = data._dev
+        if dev.vectors is None:
+            raise ValueError("the data object has no vectors to fit")
+        self.D = dev.X.shape[1]
+        idx = torch.as_tensor(np.asarray(train_points, dtype=np.int32), device=dev.X.device)
+        Phi, Phi32, y = _core.gather_rows(kernel.eigenvectors, self.D, idx, vec=dev.vectors,
+                                          want32=(precision == "mixed"))
+        self.C, self.b, self.yy = _core.gp_prepare(Phi, y, Phi32, precision)
+        self.N = Phi.shape[0]
+        self.m = kernel.eigenvalues.numel()
+        if inducing_variable is None:
+            if n_inducing_points is None:
+                raise ValueError("manifold_SGPR needs inducing_variable or n_inducing_points")
+            if not 1 <= int(n_inducing_points) <= self.N:
+                raise ValueError(f"n_inducing_points={n_inducing_points} must be in [1, {self.N}]")
+            perm, _ = _core.fps(Phi, N=int(n_inducing_points), start_idx=0)
+            Z = Phi[perm.long()].contiguous()
+        else:
+            Z = inducing_variable.to(Phi.device, torch.float64) if isinstance(inducing_variable, torch.Tensor) \
+                else torch.as_tensor(np.ascontiguousarray(inducing_variable, dtype=np.float64), device=Phi.device)
+            Z = Z.reshape(-1, self.m).contiguous().clone()
+        self.inducing_variable = InducingPoints(Z)
+        self.work = _core.SGPRWorkspace(Z.shape[0], self.m, Phi.device)
+        self.n_evals = 0
+        self._z_version = 0
+        self._eval_key, self._eval_out = None, None
+
+    def _theta_key(self):
+        return super()._theta_key() + (self._z_version,)
+
+    def _set_Z(self, values):
+        self.inducing_variable.Z.copy_(torch.as_tensor(values, dtype=torch.float64).reshape(self.inducing_variable.Z.shape))
+        self._z_version += 1
+
+    def _evaluate(self):
+        """FP64 bound, gradients (work.dZ) and posterior (work.state) at the
+        current parameters; reused while they are unchanged."""
+        key = self._theta_key()
+        if self._eval_key == key:
+            return self._eval_out
+        out, _ = _core.sgpr_elbo(self.C, self.b, self.yy, self.N, self.inducing_variable.Z, self.kernel.eigenvalues,
+                                 self.kernel.num_verticies, self.theta(), self.kernel.typ, self.jitter, self.work)
+        self.n_evals += 1
+        self._eval_key, self._eval_out = key, out.cpu().numpy()
+        return self._eval_out
+
+    def elbo(self):
+        """The collapsed lower bound on the log marginal likelihood (GPflow ``SGPR.elbo``)."""
+        return float(self._evaluate()[0])
+
+    def log_marginal_likelihood(self):
+        return self.elbo()
+
+    def _loss_and_grad(self, params, train_Z):
+        f, g = self._loss_and_grad_u(params)
+        if train_Z:
+            g = np.concatenate([g, -self.work.dZ.cpu().numpy().ravel()])
+        return f, g
+
+    def optimize(self, epochs=1000, method="l-bfgs-b", lr=0.05, disp=True):
+        params = self.trainable_parameters
+        train_Z = self.inducing_variable.trainable
+        if (not params and not train_Z) or epochs <= 0:
+            return None
+        n_p = len(params)
+
+        def assign(x):
+            for p, u in zip(params, x[:n_p]):
+                p.unconstrained = float(u)
+            if train_Z:
+                self._set_Z(x[n_p:])
+
+        x0 = np.array([p.unconstrained for p in params])
+        if train_Z:
+            x0 = np.concatenate([x0, self.inducing_variable.numpy().ravel()])
+        if method.lower() in ("l-bfgs-b", "lbfgs", "scipy"):
+            def fun(x):
+                assign(x)
+                f, g = self._loss_and_grad(params, train_Z)
+                if not np.isfinite(f):
+                    return np.inf, np.zeros_like(g)
+                return f, g
+            res = scipy.optimize.minimize(fun, x0, jac=True, method="L-BFGS-B",
+                                          options={"maxiter": epochs})
+            if disp:  # scipy's L-BFGS-B no longer takes "disp": report the outcome here
+                print(f"L-BFGS-B: {res.message} ({res.nit} iterations, loss {res.fun:.6g})")
+            assign(res.x)
+            return res
+        if method.lower() == "adam":
+            # the same update as the device Adam of manifold_GPR, on the host
+            b1, b2, eps = 0.9, 0.999, 1e-8
+            x = x0.copy()
+            m1 = np.zeros_like(x)
+            v1 = np.zeros_like(x)
+            hist = []
+            for step in range(epochs):
+                assign(x)
+                f, g = self._loss_and_grad(params, train_Z)
+                hist.append(f)
+                if not (np.isfinite(f) and np.isfinite(g).all()):
+                    continue  # keep the parameters; the history records the failure
+                m1 = b1 * m1 + (1 - b1) * g
+                v1 = b2 * v1 + (1 - b2) * g * g
+                x = x - lr * (m1 / (1 - b1 ** (step + 1))) / (np.sqrt(v1 / (1 - b2 ** (step + 1))) + eps)
+            assign(x)
+            self.lml_history = -np.asarray(hist)
+            return x
+        raise ValueError(f"unknown optimiser {method!r}")
+
+    def _predict_rows(self, Phi_star):
+        self._evaluate()  # posterior state at the current parameters
+        return _core.sgpr_predict(Phi_star, self.work.state, self.m)
 
 
 def optimize_model_with_scipy(model, epochs):
@@ -241,11 +389,13 @@ def train_gp(data, train_ind=None, n_inducing_points=None, test_size=0.2, kernel
     tr, te = train_test_split_indices(len(train_ind), test_size, seed)
     pts_train, pts_test = train_ind[tr], train_ind[te]
     set_default_positive_minimum(positivity_constraint)
-    if n_inducing_points is not None:
-        return manifold_SGPR()
     precision = precision or getattr(data, "precision", "mixed")
-    GP = manifold_GPR(data, kernel, pts_train, noise_variance=1.0 if reference_quirks else noise_variance,
-                      precision=precision)
+    noise0 = 1.0 if reference_quirks else noise_variance
+    if n_inducing_points is None:
+        GP = manifold_GPR(data, kernel, pts_train, noise_variance=noise0, precision=precision)
+    else:
+        GP = manifold_SGPR(data, kernel, pts_train, n_inducing_points=n_inducing_points, noise_variance=noise0,
+                           precision=precision)
     if kernel_variance is not None:
         kernel.sigma_f.assign(kernel_variance)
         kernel.sigma_f.trainable = False

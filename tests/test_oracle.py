@@ -179,3 +179,25 @@ def test_gp_gradient_formula_matches_fd():
     h = 1e-7  # the noise derivative is steep at σ²=0.1: a small step keeps truncation down
     fd = (O.lml_dense(Phi, y, S, 0.1 + h) - O.lml_dense(Phi, y, S, 0.1 - h)) / (2 * h)
     assert abs(fd - gn) < 1e-6 * max(1.0, abs(fd))
+
+
+def test_sgpr_bound_forms_agree_and_bound_the_lml():
+    """The M-space SGPR bound (GPflow's algorithm) equals its N-space definition,
+    lies below the exact LML, and equals it when Z spans the eigenbasis."""
+    Phi, y, lam = _gp_problem(2)
+    S = O.eval_S(lam, 1.5, 5.0, 1.3, Phi.shape[0])
+    rng = np.random.default_rng(5)
+    for M in (5, 20, 40):
+        Z = Phi[rng.choice(len(Phi), M, replace=False)]
+        for noise in (1.0, 0.05):
+            a, b = O.sgpr_elbo(Phi, y, S, noise, Z), O.sgpr_elbo_dense(Phi, y, S, noise, Z)
+            assert abs(a - b) < 1e-9 * abs(a)
+            assert a <= O.lml_dense(Phi, y, S, noise) + 1e-9 * abs(a)
+    m = Phi.shape[1]
+    for noise in (1.0, 0.05):
+        exact = O.lml_dense(Phi, y, S, noise)
+        assert abs(O.sgpr_elbo(Phi, y, S, noise, np.eye(m), jitter=0.0) - exact) < 1e-9 * abs(exact)
+        m1, v1 = O.sgpr_predict_f(Phi, y, S, noise, np.eye(m), Phi[:7] * 0.7, jitter=0.0)
+        m2, v2 = O.predict_f(Phi, y, S, noise, Phi[:7] * 0.7)
+        np.testing.assert_allclose(m1, m2, rtol=1e-8, atol=1e-10)
+        np.testing.assert_allclose(v1, v2, rtol=1e-6, atol=1e-9)
