@@ -16,6 +16,7 @@ relative L2 difference of the two forms' posterior means.  ``e2e`` = the same
 step through the public API with host numpy inputs and outputs.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+    python bench.py --model sgpr [--inducing M] [--sgpr-iters I]   # the sparse inducing-point GP
 """
 import os
 
@@ -411,6 +412,141 @@ def run_reference(args):
     print(json.dumps(out), flush=True)
 
 
+# ------------------------------------------------------------------------------ sparse GP (--model sgpr)
+SGPR_METRIC = "RVGP sparse-GP fit+predict wall s (FPS inducing rows, L-BFGS-B on kernel, noise and Z)"
+FP64_NOMINAL_TFLOPS = 1.25  # GB300 FP64 (CUDA cores), nominal: no measured FP64 peak exists for this machine
+
+
+def sgpr_flops(m, M):
+    """Algorithmic FP64 flops of one rvgp_sgpr_elbo call with ∂F/∂Z and the
+    posterior state: its matrix products (2 r c k each), two Cholesky
+    factorisations and two triangular inverses (M³/3 each); vector products
+    are left out."""
+    g = lambda r, c, k: 2.0 * r * c * k  # noqa: E731
+    f = g(M, M, m) + g(M, m, M) + g(M, m, m) + g(M, M, m)          # Kuu, L⁻¹Z, W C, Q0
+    f += 4 * M ** 3 / 3.0                                             # chol + inverse of Kuu and B
+    f += g(M, m, M) + g(M, m, m) + g(M, M, m) + g(m, M, M)            # V, V C, W Hᵀ, Ẑᵀ(W Hᵀ)
+    f += g(m, m, M) + g(M, m, m) + g(m, m, M) + g(M, m, M) + g(M, m, m)  # WᵀW, H Q, HᵀHQ, L⁻ᵀW, ∂F/∂Z
+    f += g(m, m, M)                                                   # VᵀV
+    return f
+
+
+def run_sgpr(args):
+    import torch
+    import rvgp_gb300 as RVGP
+    from rvgp_gb300 import _core
+    _core.require_cuda()
+    wl = WORKLOADS[args.workload]
+    M, iters = args.inducing, args.sgpr_iters
+    X, train, test = make_inputs(wl, seed=0)
+    V = make_field(X, wl, seed=0)
+    Xd = torch.as_tensor(X, device="cuda")
+    d = RVGP.create_data_object(Xd, n_neighbors=wl["k"], n_eigenpairs=wl["m"], precision="mixed", verbose=False)
+    d.vectors = V
+    d.wait()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MiB > L2
+    stream = torch.cuda.current_stream()
+
+    def step():
+        gp = RVGP.fit(d, train_ind=train, n_inducing_points=M, epochs=iters, verbose=False)
+        return gp, gp.predict_points(test)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    times, evals = [], []
+    launches0 = _core.launch_count()
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            flush_l2(flush)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            gp, (mean, var) = step()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1) / 1e3)
+            evals.append(gp.n_evals)
+    launches = _core.launch_count() - launches0
+    t_step = float(np.mean(times))
+    # one bound evaluation (with ∂F/∂Z and the posterior) timed alone, L2 flushed before each
+    Z = gp.inducing_variable.Z
+    th = gp.theta()
+    ev_t = []
+    torch.cuda.nvtx.range_push("sgpr_eval")  # lets a profiler select exactly these launches
+    for r in range(23):
+        flush_l2(flush)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        _core.sgpr_elbo(gp.C, gp.b, gp.yy, gp.N, Z, gp.kernel.eigenvalues, gp.kernel.num_verticies, th,
+                        gp.kernel.typ, gp.jitter, gp.work)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if r >= 3:
+            ev_t.append(e0.elapsed_time(e1) / 1e3)
+    torch.cuda.nvtx.range_pop()
+    t_eval = float(np.mean(ev_t))
+    flops = sgpr_flops(gp.m, M)
+    achieved = flops / t_eval / 1e12
+    # end to end through the public API with host buffers
+    e2e = []
+    for _ in range(2):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        d.vectors = V
+        g2 = RVGP.fit(d, train_ind=train, n_inducing_points=M, epochs=iters, verbose=False)
+        mh, vh = g2.transform(d, test)
+        e2e.append(time.perf_counter() - t0)
+    out = {
+        "metric": SGPR_METRIC, "value": round(t_step, 5), "unit": "s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(t_step * 1e3, 3), "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": args.workload, "model": "manifold_SGPR", "inducing": M, "lbfgsb_max_iter": iters,
+                   "N_train_rows": int(gp.N), "m": int(gp.m), "l2": "flushed between steps (256 MiB write)",
+                   "step": "fit (FPS, C/b/yᵀy, L-BFGS-B) + predict at the test points; data object built before"},
+        "bound_evals_per_step": [int(e) for e in evals], "elbo": gp.elbo(), "l2_error": getattr(gp, "l2_error", None),
+        "eval_ms": round(t_eval * 1e3, 4),
+        "roofline": {"kernel": "rvgp_sgpr_elbo chain (one bound + gradients + posterior)", "bound": "fp64",
+                     "achieved": round(achieved, 4), "peak": FP64_NOMINAL_TFLOPS, "unit": "TFLOP/s",
+                     "frac": round(achieved / FP64_NOMINAL_TFLOPS, 4), "traffic": None,
+                     "peak_source": "nominal", "algorithmic_flops": flops},
+        "e2e": {"value": round(float(np.mean(e2e)), 5), "unit": "s", "h2d_bytes_per_step": int(V.nbytes),
+                "d2h_bytes_per_step": int(mh.nbytes + vh.nbytes)},
+        "clocks": clk.summary(), "gpu_launches": int(launches / max(1, args.steps)),
+        "step_times_s": [round(t, 5) for t in times],
+    }
+    if not args.skip_cpu:
+        from oracle import rvgp_oracle as O
+        n, m = d.n, gp.m
+        ev = d.evecs_Lc.reshape(n, -1)
+        tr, _ = O.train_test_split_indices(len(train), 0.2, 0)
+        Phi = ev[train[tr]].reshape(-1, m)
+        y = V[train[tr]].reshape(-1)
+        Zh = Z.cpu().numpy()
+        S = O.eval_S(d.evals_Lc, float(gp.kernel.nu), float(gp.kernel.kappa), float(gp.kernel.sigma_f),
+                     d.evecs_Lc.shape[0])
+        noise = float(gp.likelihood.variance)
+        reps = 3
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            O.sgpr_elbo(Phi, y, S, noise, Zh)
+        one = (time.perf_counter() - t0) / reps
+        Phi_te = ev[test].reshape(-1, m)
+        sample = min(len(Phi_te), 2000)
+        t0 = time.perf_counter()
+        O.sgpr_predict_f(Phi, y, S, noise, Zh, Phi_te[:sample])
+        t_pred = (time.perf_counter() - t0) * len(Phi_te) / sample
+        n_ev = float(np.mean(evals))
+        out["cpu_baseline"] = {
+            "value": round(one * n_ev + t_pred, 3), "unit": "s", "cores": os.cpu_count(), "kind": "port",
+            "sample": (f"GPflow's SGPR bound (value only, no gradient) evaluated {reps}x on the full training rows "
+                       f"({one:.3f} s each) and scaled by the {n_ev:.0f} bound evaluations per fit, plus predict "
+                       f"on {sample} test rows scaled to all {len(Phi_te)}")}
+    print(json.dumps(out), flush=True)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -422,8 +558,18 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=240.0)
+    ap.add_argument("--model", choices=["gpr", "sgpr"], default="gpr",
+                    help="sgpr: the sparse inducing-point GP fit instead of the full pipeline")
+    ap.add_argument("--inducing", type=int, default=100, help="inducing rows for --model sgpr")
+    ap.add_argument("--sgpr-iters", type=int, default=200, help="L-BFGS-B iterations for --model sgpr")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.model == "sgpr":
+        if args.impl == "ours" and int(os.environ.get("RANK", "0")) == 0:
+            run_sgpr(args)
+        elif args.impl == "reference":
+            print(json.dumps({"impl": "reference", "metric": SGPR_METRIC,
+                              "unavailable": "the sparse-GP CPU baseline is the cpu_baseline of the ours arm"}))
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

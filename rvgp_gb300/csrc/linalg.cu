@@ -5,6 +5,7 @@
 #include <limits.h>
 #include <vector>
 #include <mutex>
+#include <atomic>
 #include <map>
 #include <algorithm>
 
@@ -200,6 +201,8 @@ __global__ void __launch_bounds__(1024) chol_kernel(T* __restrict__ A, int lda, 
 
 // ------------------------------------------------------------------ blocked Cholesky (many CTAs)
 constexpr int NB = 32;
+// largest shared-memory footprint of the one-CTA Cholesky (p = 160 in FP64)
+constexpr size_t kSmallCholSmem = 8 * (160 * 161 + 160);
 
 // Factor the diagonal block [k0, k0+nb) in shared memory.  On GB300 a warp-wide
 // FP64 instruction occupies its SM sub-partition's FP64 pipe for tens of
@@ -250,6 +253,59 @@ __global__ void __launch_bounds__(128) potrf_diag(T* __restrict__ A, int lda, in
     const int i = e / nb, c = e % nb;
     if (c <= i) A[(size_t)(k0 + i) * lda + k0 + c] = L[i][c];
   }
+}
+
+// Whole-matrix Cholesky in one CTA with the lower triangle in shared memory
+// (row stride p + 1), for p small enough to fit: one launch instead of three
+// per 32-column block.  Column j: warp 0 forms 1/sqrt(d_j), L_jj and the
+// scaled column (kept also in `col`); after a barrier every warp applies the
+// rank-1 update to its rows of the trailing lower triangle; a second barrier
+// ends the column.
+template <typename T>
+__global__ void __launch_bounds__(512) potrf_small(T* __restrict__ A, int lda, int p, int* __restrict__ info) {
+  extern __shared__ __align__(16) unsigned char chol_smem[];
+  T* L = reinterpret_cast<T*>(chol_smem);
+  T* col = L + (size_t)p * (p + 1);
+  __shared__ int bad;
+  const int ld = p + 1;
+  for (int i = threadIdx.x >> 5; i < p; i += blockDim.x >> 5)
+    for (int c = threadIdx.x & 31; c <= i; c += 32) L[i * ld + c] = A[(size_t)i * lda + c];
+  if (threadIdx.x == 0) bad = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int j = 0; j < p; ++j) {
+    if (w == 0) {
+      const T d = L[j * ld + j];
+      if (!(d > T(0))) {
+        if (lane == 0) {
+          bad = 1;
+          atomicCAS(info, 0, j + 1);
+        }
+      } else {
+        const T r = rsqrt_nr(d);
+        if (lane == 0) L[j * ld + j] = d * r;
+        for (int i = j + 1 + lane; i < p; i += 32) {
+          const T v = L[i * ld + j] * r;
+          L[i * ld + j] = v;
+          col[i] = v;
+        }
+      }
+    }
+    __syncthreads();
+    if (bad) return;  // uniform: read after the barrier
+    for (int i = j + 1 + w; i < p; i += nw) {
+      const T ci = col[i];
+      for (int k = j + 1 + lane; k <= i; k += 32) L[i * ld + k] -= ci * col[k];
+    }
+    __syncthreads();
+  }
+  for (int i = threadIdx.x >> 5; i < p; i += blockDim.x >> 5)
+    for (int c = threadIdx.x & 31; c <= i; c += 32) A[(size_t)i * lda + c] = L[i * ld + c];
+}
+
+template <typename T>
+size_t potrf_small_smem(int p) {
+  return sizeof(T) * ((size_t)p * (p + 1) + p);
 }
 
 // panel: rows [k0+nb, p) of columns [k0, k0+nb) <- A L_kkᵀ⁻¹, one row per
@@ -765,6 +821,20 @@ int gemm_nn(const T* A, int lda, const T* B, int ldb, long long N, int p, int q,
 template <typename T>
 int cholesky(T* A, int lda, int p, int* info, cudaStream_t st) {
   cudaMemsetAsync(info, 0, sizeof(int), st);
+  const size_t smem = potrf_small_smem<T>(p);
+  if (smem <= kSmallCholSmem) {
+    static std::atomic<bool> attr_set{false};  // per kernel; setting it twice is harmless
+    if (!attr_set.load()) {
+      if (cudaFuncSetAttribute(potrf_small<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmallCholSmem) !=
+          cudaSuccess) {
+        set_error("cholesky: cannot reserve %zu bytes of shared memory", kSmallCholSmem);
+        return RVGP_ELAUNCH;
+      }
+      attr_set = true;
+    }
+    rvgp::note_launch(); potrf_small<T><<<1, 512, smem, st>>>(A, lda, p, info);
+    return check_launch("cholesky");
+  }
   for (int k0 = 0; k0 < p; k0 += NB) {
     const int nb = std::min(NB, p - k0);
     rvgp::note_launch(); potrf_diag<T><<<1, 128, 0, st>>>(A, lda, k0, nb, info);

@@ -35,14 +35,24 @@ RVGP_API int rvgp_spectral_S(const double* evals, int m, const double* theta, do
 namespace rvgp {
 namespace {
 
-constexpr int kT = 32;  // GEMM tile (rows x columns x depth)
+// FP64 on GB300 issues about one warp instruction per ~19 SM cycles, so the
+// products below are sized by FP64 instruction count: no lanes computing
+// padding (dedicated matrix-vector kernels) and grids spread over all SMs
+// (the output tile shrinks until there are enough CTAs).
+constexpr int kT = 32;  // largest GEMM output tile
 
 // C (R x Q) = alpha op(A) op(B) + beta C, row-major; op(A) is R x K, op(B) K x Q.
 // TA: op(A)(i, k) = A[k * lda + i]; TB: op(B)(k, j) = B[j * ldb + k].
+__device__ __forceinline__ void store_out(double* C, int ldc, int i, int j, double alpha, double beta, double acc) {
+  double* c = C + (size_t)i * ldc + j;
+  *c = beta == 0.0 ? alpha * acc : fma(beta, *c, alpha * acc);
+}
+
+// 32 x 32 outputs per CTA, 4 per thread
 template <bool TA, bool TB>
-__global__ void __launch_bounds__(256) gemm64_kernel(int R, int Q, int K, double alpha, const double* __restrict__ A,
-                                                     int lda, const double* __restrict__ B, int ldb, double beta,
-                                                     double* __restrict__ C, int ldc) {
+__global__ void __launch_bounds__(256) gemm64_t32(int R, int Q, int K, double alpha, const double* __restrict__ A,
+                                                  int lda, const double* __restrict__ B, int ldb, double beta,
+                                                  double* __restrict__ C, int ldc) {
   __shared__ double As[kT][kT + 1];  // [i][k]
   __shared__ double Bs[kT][kT + 1];  // [k][j]
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
@@ -51,8 +61,7 @@ __global__ void __launch_bounds__(256) gemm64_kernel(int R, int Q, int K, double
   for (int k0 = 0; k0 < K; k0 += kT) {
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
-      const int a = ty + 8 * r;  // the strided index of this thread's load
-      // A tile: contiguous along k when !TA, along i when TA
+      const int a = ty + 8 * r;
       if (!TA) {
         const int i = i0 + a, k = k0 + tx;
         As[a][tx] = (i < R && k < K) ? A[(size_t)i * lda + k] : 0.0;
@@ -69,8 +78,8 @@ __global__ void __launch_bounds__(256) gemm64_kernel(int R, int Q, int K, double
       }
     }
     __syncthreads();
-#pragma unroll 8
-    for (int k = 0; k < kT; ++k) {
+    const int kn = min(kT, K - k0);
+    for (int k = 0; k < kn; ++k) {
       const double bv = Bs[k][tx];
 #pragma unroll
       for (int r = 0; r < 4; ++r) acc[r] = fma(As[ty + 8 * r][k], bv, acc[r]);
@@ -82,19 +91,144 @@ __global__ void __launch_bounds__(256) gemm64_kernel(int R, int Q, int K, double
 #pragma unroll
   for (int r = 0; r < 4; ++r) {
     const int i = i0 + ty + 8 * r;
-    if (i < R) {
-      double* c = C + (size_t)i * ldc + j;
-      *c = beta == 0.0 ? alpha * acc[r] : fma(beta, *c, alpha * acc[r]);
-    }
+    if (i < R) store_out(C, ldc, i, j, alpha, beta, acc[r]);
   }
 }
 
+// 16 x 16 outputs per CTA, one per thread
+template <bool TA, bool TB>
+__global__ void __launch_bounds__(256) gemm64_t16(int R, int Q, int K, double alpha, const double* __restrict__ A,
+                                                  int lda, const double* __restrict__ B, int ldb, double beta,
+                                                  double* __restrict__ C, int ldc) {
+  __shared__ double As[16][17];  // [i][k]
+  __shared__ double Bs[16][17];  // [k][j]
+  const int t = threadIdx.x, hi = t >> 4, lo = t & 15;
+  const int i0 = blockIdx.y * 16, j0 = blockIdx.x * 16;
+  double acc = 0.0;
+  for (int k0 = 0; k0 < K; k0 += 16) {
+    if (!TA) {
+      const int i = i0 + hi, k = k0 + lo;
+      As[hi][lo] = (i < R && k < K) ? A[(size_t)i * lda + k] : 0.0;
+    } else {
+      const int k = k0 + hi, i = i0 + lo;
+      As[lo][hi] = (i < R && k < K) ? A[(size_t)k * lda + i] : 0.0;
+    }
+    if (!TB) {
+      const int k = k0 + hi, j = j0 + lo;
+      Bs[hi][lo] = (k < K && j < Q) ? B[(size_t)k * ldb + j] : 0.0;
+    } else {
+      const int j = j0 + hi, k = k0 + lo;
+      Bs[lo][hi] = (k < K && j < Q) ? B[(size_t)j * ldb + k] : 0.0;
+    }
+    __syncthreads();
+    const int kn = min(16, K - k0);
+    for (int k = 0; k < kn; ++k) acc = fma(As[hi][k], Bs[k][lo], acc);
+    __syncthreads();
+  }
+  const int i = i0 + hi, j = j0 + lo;
+  if (i < R && j < Q) store_out(C, ldc, i, j, alpha, beta, acc);
+}
+
+// 8 x 8 outputs per CTA, each summed by 4 threads over interleaved quarters of
+// every 32-deep slab, then added in a fixed order
+template <bool TA, bool TB>
+__global__ void __launch_bounds__(256) gemm64_t8(int R, int Q, int K, double alpha, const double* __restrict__ A,
+                                                 int lda, const double* __restrict__ B, int ldb, double beta,
+                                                 double* __restrict__ C, int ldc) {
+  __shared__ double As[8][33];  // [i][k]
+  __shared__ double Bs[32][9];  // [k][j]
+  __shared__ double red[4][64];
+  const int t = threadIdx.x, o = t & 63, kg = t >> 6;
+  const int oy = o >> 3, ox = o & 7;
+  const int i0 = blockIdx.y * 8, j0 = blockIdx.x * 8;
+  double acc = 0.0;
+  for (int k0 = 0; k0 < K; k0 += 32) {
+    if (!TA) {
+      const int a = t >> 5, b = t & 31, i = i0 + a, k = k0 + b;
+      As[a][b] = (i < R && k < K) ? A[(size_t)i * lda + k] : 0.0;
+    } else {
+      const int a = t & 7, b = t >> 3, i = i0 + a, k = k0 + b;
+      As[a][b] = (i < R && k < K) ? A[(size_t)k * lda + i] : 0.0;
+    }
+    if (!TB) {
+      const int a = t & 7, b = t >> 3, j = j0 + a, k = k0 + b;
+      Bs[b][a] = (k < K && j < Q) ? B[(size_t)k * ldb + j] : 0.0;
+    } else {
+      const int a = t >> 5, b = t & 31, j = j0 + a, k = k0 + b;
+      Bs[b][a] = (k < K && j < Q) ? B[(size_t)j * ldb + k] : 0.0;
+    }
+    __syncthreads();
+    const int kn = min(32, K - k0);
+    for (int k = kg; k < kn; k += 4) acc = fma(As[oy][k], Bs[k][ox], acc);
+    __syncthreads();
+  }
+  red[kg][o] = acc;
+  __syncthreads();
+  if (t < 64) {
+    const int i = i0 + oy, j = j0 + ox;
+    if (i < R && j < Q) store_out(C, ldc, i, j, alpha, beta, ((red[0][o] + red[1][o]) + red[2][o]) + red[3][o]);
+  }
+}
+
+// y (R, stride ldy) = alpha A x + beta y, A row-major (lda), x stride ldx: one warp per row
+__global__ void __launch_bounds__(256) gemv64_n(int R, int K, double alpha, const double* __restrict__ A, int lda,
+                                                const double* __restrict__ x, int ldx, double beta,
+                                                double* __restrict__ y, int ldy) {
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (i >= R) return;
+  double s = 0.0;
+  for (int k = lane; k < K; k += 32) s = fma(A[(size_t)i * lda + k], x[(size_t)k * ldx], s);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) store_out(y, ldy, i, 0, alpha, beta, s);
+}
+
+// y (R) = alpha Aᵀ x + beta y with A stored K x R (lda): 32 outputs per CTA,
+// the 8 warps summing interleaved rows k, added in a fixed order
+__global__ void __launch_bounds__(256) gemv64_t(int R, int K, double alpha, const double* __restrict__ A, int lda,
+                                                const double* __restrict__ x, int ldx, double beta,
+                                                double* __restrict__ y, int ldy) {
+  __shared__ double red[8][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int i = blockIdx.x * 32 + lane;
+  double s = 0.0;
+  if (i < R)
+    for (int k = w; k < K; k += 8) s = fma(A[(size_t)k * lda + i], x[(size_t)k * ldx], s);
+  red[w][lane] = s;
+  __syncthreads();
+  if (w == 0 && i < R) {
+    double r = 0.0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) r += red[q][lane];
+    store_out(y, ldy, i, 0, alpha, beta, r);
+  }
+}
+
+long long tiles(int R, int Q, int T) { return (long long)ceil_div(R, T) * ceil_div(Q, T); }
+
+// op(B) with one column (TB false, Q == 1) is a matrix-vector product; otherwise
+// the output tile is the largest of 32, 16, 8 that still gives every SM a CTA.
 template <bool TA, bool TB>
 void gemm64(int R, int Q, int K, double alpha, const double* A, int lda, const double* B, int ldb, double beta,
             double* C, int ldc, cudaStream_t st) {
-  dim3 grid(ceil_div(Q, kT), ceil_div(R, kT));
   note_launch();
-  gemm64_kernel<TA, TB><<<grid, 256, 0, st>>>(R, Q, K, alpha, A, lda, B, ldb, beta, C, ldc);
+  if (Q == 1 && !TB) {
+    if (!TA)
+      gemv64_n<<<ceil_div((long long)R * 32, 256), 256, 0, st>>>(R, K, alpha, A, lda, B, ldb, beta, C, ldc);
+    else
+      gemv64_t<<<ceil_div(R, 32), 256, 0, st>>>(R, K, alpha, A, lda, B, ldb, beta, C, ldc);
+    return;
+  }
+  if (tiles(R, Q, 32) >= 2 * kNumSMs) {
+    gemm64_t32<TA, TB><<<dim3(ceil_div(Q, 32), ceil_div(R, 32)), 256, 0, st>>>(R, Q, K, alpha, A, lda, B, ldb, beta,
+                                                                               C, ldc);
+  } else if (tiles(R, Q, 16) >= kNumSMs) {
+    gemm64_t16<TA, TB><<<dim3(ceil_div(Q, 16), ceil_div(R, 16)), 256, 0, st>>>(R, Q, K, alpha, A, lda, B, ldb, beta,
+                                                                               C, ldc);
+  } else {
+    gemm64_t8<TA, TB><<<dim3(ceil_div(Q, 8), ceil_div(R, 8)), 256, 0, st>>>(R, Q, K, alpha, A, lda, B, ldb, beta, C,
+                                                                            ldc);
+  }
 }
 
 // out (R x m) = X ∘ S (column scaling)
@@ -150,14 +284,20 @@ __global__ void scale_by_inv_noise(double* __restrict__ x, int n, const double* 
   if (i < n) x[i] /= theta[3];
 }
 
+// CTA-wide sum in a fixed order; only warp 0 adds the per-warp partials (every
+// FP64 instruction costs the SM's shared FP64 pipe, so none is repeated)
 __device__ double cta_sum(double v, double* sh) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-  __syncthreads();
   if (lane == 0) sh[w] = v;
   __syncthreads();
-  double r = 0.0;
-  for (int k = 0; k < nw; ++k) r += sh[k];  // fixed order
+  if (w == 0) {
+    double r = lane < nw ? sh[lane] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+    if (lane == 0) sh[32] = r;
+  }
+  __syncthreads();
+  const double r = sh[32];
   __syncthreads();
   return r;
 }
@@ -170,32 +310,15 @@ struct FinalIn {
   int M, m;
 };
 
-// One CTA: the bound, ∂F/∂S (into gS) and the four hyperparameter gradients.
-__global__ void __launch_bounds__(1024) sgpr_final(FinalIn in, double* __restrict__ gS, double* __restrict__ out) {
-  __shared__ double sh[32];
+// One warp per row, spread over many CTAs: rows l < m give ∂F/∂S_l (into gS),
+// rows m + i give the squared norm of row i of L_B⁻¹ (into rowsq).
+//   ∂F/∂S_l = Yu_l u_l + Σ_k YHt_lk Hp_kl/σ⁴ − ½ Yu_l² − ½ Σ_k YHt_lk²/σ⁴ − ½ C_ll/σ²
+__global__ void __launch_bounds__(256) sgpr_rows(FinalIn in, double* __restrict__ gS, double* __restrict__ rowsq) {
+  const int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   const int M = in.M, m = in.m;
-  const double s2 = in.theta[3], s4 = s2 * s2;
-  double logdet = 0.0, trQ0 = 0.0, tt = 0.0, gg = 0.0, trBi = 0.0, trDC = 0.0;
-  for (int i = threadIdx.x; i < M; i += blockDim.x) {
-    logdet += log(in.LB[(size_t)i * M + i]);
-    trQ0 += in.Q0[(size_t)i * M + i];
-    tt += in.t[i] * in.t[i];
-    gg += in.g[i] * in.g[i];
-    for (int k = 0; k <= i; ++k) {
-      const double v = in.LBi[(size_t)i * M + k];
-      trBi = fma(v, v, trBi);
-    }
-  }
-  for (int l = threadIdx.x; l < m; l += blockDim.x) trDC += in.S[l] * in.C[(size_t)l * m + l];
-  logdet = cta_sum(logdet, sh);
-  trQ0 = cta_sum(trQ0, sh);
-  tt = cta_sum(tt, sh);
-  gg = cta_sum(gg, sh);
-  trBi = cta_sum(trBi, sh);
-  trDC = cta_sum(trDC, sh);
-  // ∂F/∂S_l: one warp per l, reductions over the M inducing rows
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int l = w; l < m; l += nw) {
+  if (r >= m + M) return;
+  if (r < m) {
+    const int l = r;
     double cross = 0.0, sq = 0.0;
     for (int k = lane; k < M; k += 32) {
       const double a = in.YHt[(size_t)l * M + k];
@@ -207,17 +330,50 @@ __global__ void __launch_bounds__(1024) sgpr_final(FinalIn in, double* __restric
       sq += __shfl_xor_sync(0xffffffffu, sq, o);
     }
     if (lane == 0) {
+      const double inv2 = rcp_nr(in.theta[3]), inv4 = inv2 * inv2;
       const double yu = in.Yu[l];
-      gS[l] = yu * in.u[l] + cross / s4 - 0.5 * yu * yu - 0.5 * sq / s4 - 0.5 * in.C[(size_t)l * m + l] / s2;
+      gS[l] = yu * in.u[l] + cross * inv4 - 0.5 * yu * yu - 0.5 * sq * inv4 - 0.5 * in.C[(size_t)l * m + l] * inv2;
     }
+  } else {
+    const int i = r - m;
+    double sq = 0.0;
+    for (int k = lane; k <= i; k += 32) {
+      const double v = in.LBi[(size_t)i * M + k];
+      sq = fma(v, v, sq);
+    }
+    for (int o = 16; o > 0; o >>= 1) sq += __shfl_xor_sync(0xffffffffu, sq, o);
+    if (lane == 0) rowsq[i] = sq;
   }
-  __syncthreads();
+}
+
+// One CTA: the bound and the four hyperparameter gradients from the scalar
+// sums, gS and rowsq (every sum in a fixed order).
+__global__ void __launch_bounds__(256) sgpr_final(FinalIn in, const double* __restrict__ gS,
+                                                  const double* __restrict__ rowsq, double* __restrict__ out) {
+  __shared__ double sh[33];
+  const int M = in.M, m = in.m;
+  const double s2 = in.theta[3], s4 = s2 * s2;
+  double logdet = 0.0, trQ0 = 0.0, tt = 0.0, gg = 0.0, trBi = 0.0, trDC = 0.0;
+  for (int i = threadIdx.x; i < M; i += blockDim.x) {
+    logdet += log(in.LB[(size_t)i * M + i]);
+    trQ0 += in.Q0[(size_t)i * M + i];
+    tt = fma(in.t[i], in.t[i], tt);
+    gg = fma(in.g[i], in.g[i], gg);
+    trBi += rowsq[i];
+  }
   double d0 = 0.0, d1 = 0.0, d2 = 0.0;
   for (int l = threadIdx.x; l < m; l += blockDim.x) {
+    trDC = fma(in.S[l], in.C[(size_t)l * m + l], trDC);
     d0 = fma(gS[l], in.dS[l], d0);
     d1 = fma(gS[l], in.dS[m + l], d1);
     d2 = fma(gS[l], in.dS[2 * m + l], d2);
   }
+  logdet = cta_sum(logdet, sh);
+  trQ0 = cta_sum(trQ0, sh);
+  tt = cta_sum(tt, sh);
+  gg = cta_sum(gg, sh);
+  trBi = cta_sum(trBi, sh);
+  trDC = cta_sum(trDC, sh);
   d0 = cta_sum(d0, sh);
   d1 = cta_sum(d1, sh);
   d2 = cta_sum(d2, sh);
@@ -239,7 +395,7 @@ __global__ void __launch_bounds__(1024) sgpr_final(FinalIn in, double* __restric
 
 struct Buffers {
   double *S, *dS, *tmp, *ZS, *K, *Li, *Zh, *W, *WC, *Q0, *LB, *LBi, *YHt, *X, *Qm, *G2, *HQ;
-  double *beta, *t, *g, *x, *y2, *u, *Wu, *Yu, *Qu, *gS;
+  double *beta, *t, *g, *x, *y2, *u, *Wu, *Yu, *Qu, *gS, *rowsq;
 };
 
 Buffers carve(Workspace& w, int M, int m) {
@@ -272,6 +428,7 @@ Buffers carve(Workspace& w, int M, int m) {
   B.Yu = w.take<double>(m);
   B.Qu = w.take<double>(m);
   B.gS = w.take<double>(m);
+  B.rowsq = w.take<double>(M);
   return B;
 }
 
@@ -350,7 +507,9 @@ RVGP_API int rvgp_sgpr_elbo(const double* C, const double* b, const double* yy, 
   gemm64<true, false>(m, M, M, 1.0, B.Zh, m, B.K, M, 0.0, B.YHt, M, st);
   FinalIn fi{B.S, B.dS, C, b, yy, theta, B.LB, B.LBi, B.Q0, B.t, B.g, B.u, B.Yu, B.YHt, Hp, info, (double)N, M, m};
   note_launch();
-  sgpr_final<<<1, 1024, 0, st>>>(fi, B.gS, out);
+  sgpr_rows<<<ceil_div((long long)(m + M) * 32, 256), 256, 0, st>>>(fi, B.gS, B.rowsq);
+  note_launch();
+  sgpr_final<<<1, 256, 0, st>>>(fi, B.gS, B.rowsq, out);
   if (dZ || state) {
     // Q = D − WᵀW
     gemm64<true, false>(m, m, M, -1.0, B.W, m, B.W, m, 0.0, B.Qm, m, st);

@@ -53,7 +53,7 @@ def inducing(Phi, M, seed):
     return Phi[rng.choice(len(Phi), M, replace=False)] + 0.05 * rng.standard_normal((M, Phi.shape[1]))
 
 
-@pytest.mark.parametrize("M", [7, 24, 40])
+@pytest.mark.parametrize("M", [7, 24, 40, 170])  # 170: past the one-CTA Cholesky (blocked factorisation)
 @pytest.mark.parametrize("typ", ["matern", "se"])
 @pytest.mark.parametrize("noise", [1.0, 0.05])
 def test_bound_and_hyperparameter_gradients(core, M, typ, noise):
@@ -97,7 +97,7 @@ def test_inducing_input_gradient(core, M):
         assert abs(dZ[i, j] - fd) <= 1e-5 * np.abs(dZ).max() + 1e-7
 
 
-@pytest.mark.parametrize("M", [7, 40])
+@pytest.mark.parametrize("M", [7, 40, 170])
 def test_posterior_matches_oracle(core, M):
     Phi, y, lam, Phi_te = problem(20 + M)
     Z = inducing(Phi, M, 3)
