@@ -247,6 +247,31 @@ size_t rvgp_sgpr_state_size(int m);
 int rvgp_sgpr_elbo(const double* C, const double* b, const double* yy, long long N, int m, const double* Z, int M,
                    const double* evals, double n_rows, const double* theta, int typ, double jitter, double* out,
                    double* dZ, double* state, int* info, void* workspace, size_t ws_bytes, void* stream);
+/* Divergence and curl estimates of B fields V (B x n x 3) at the points P
+ * (n x 3) from their k nearest neighbours nbr (n x k, the point excluded)
+ * (examples/eeg_example/eeg_utils.py:46-80): div (B x n), curl (B x n x 3).
+ * ref_first = 1 differences every unit vector against point 0's, as the
+ * reference does; 0 against the point's own. */
+int rvgp_vectorfield_features(const double* P, int n, const double* V, int B, const int* nbr, int k, int ref_first,
+                              double* div, double* curl, void* stream);
+
+/* Dense GP with GPflow's RBF kernel on N <= 3072 rows X (N x m) of the scalar
+ * eigenbasis and D <= 16 output columns Y (kernel='rbf', RVGP/main.py:33-37,
+ * 55-58): theta (device, 3) = [variance, lengthscale, noise].  out (device,
+ * 4) = [LML, ∂/∂variance, ∂/∂lengthscale, ∂/∂noise], LML NaN when the
+ * Cholesky factorisation failed (info, device).  state (device,
+ * rvgp_rbf_state_size(N, D)) feeds rvgp_rbf_predict: mean (Nte x D) and
+ * variance (Nte).  rvgp_rbf_matrix: the kernel matrix (N1 x N2). */
+size_t rvgp_rbf_workspace(long long N, int D);
+size_t rvgp_rbf_state_size(long long N, int D);
+int rvgp_rbf_matrix(const double* X1, long long N1, const double* X2, long long N2, int m, const double* theta,
+                    double* K, void* stream);
+int rvgp_rbf_lml(const double* X, long long N, int m, const double* Y, int D, const double* theta, double* out,
+                 double* state, int* info, void* workspace, size_t ws_bytes, void* stream);
+size_t rvgp_rbf_predict_workspace(long long Nte, long long N);
+int rvgp_rbf_predict(const double* Xs, long long Nte, const double* X, long long N, int m, int D,
+                     const double* theta, const double* state, double* mean, double* var, void* workspace,
+                     size_t ws_bytes, void* stream);
 /* SGPR.predict_f(full_cov=False) mean and variance at Nte spectral rows. */
 size_t rvgp_sgpr_predict_workspace(long long Nte, int m);
 int rvgp_sgpr_predict(const double* Phi_star, long long Nte, int m, const double* state, double* mean, double* var,

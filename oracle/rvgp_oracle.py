@@ -514,3 +514,50 @@ def sgpr_predict_f(Phi, y, S, noise, Z, Phi_new, jitter=SGPR_JITTER):
     mean = tmp2.T @ c
     var = np.einsum("ij,ij->i", Phi_new * S, Phi_new) + (tmp2 * tmp2).sum(0) - (tmp1 * tmp1).sum(0)
     return mean, var
+
+
+# ----------------------------------------------------------------------------- RBF GP (kernel='rbf')
+def rbf_K(X, X2, variance, lengthscale):
+    """GPflow 2.6.5 ``kernels.RBF`` as used at RVGP/main.py:33-37:
+    variance · exp(−½ |x − x'|² / lengthscale²)."""
+    d2 = ((X[:, None, :] - X2[None, :, :]) ** 2).sum(-1)
+    return variance * np.exp(-0.5 * d2 / lengthscale ** 2)
+
+
+def rbf_gpr_lml(X, Y, variance, lengthscale, noise):
+    """GPflow ``GPR.log_marginal_likelihood`` with D output columns sharing the
+    kernel (RVGP/main.py:36,55-58): Σ_c log N(y_c | 0, K + σ² I)."""
+    N, D = Y.shape
+    Lc = np.linalg.cholesky(rbf_K(X, X, variance, lengthscale) + noise * np.eye(N))
+    a = scipy.linalg.solve_triangular(Lc, Y, lower=True)
+    return float(-0.5 * (a * a).sum() - D * np.log(np.diag(Lc)).sum() - 0.5 * N * D * np.log(2 * np.pi))
+
+
+def rbf_gpr_predict_f(X, Y, variance, lengthscale, noise, Xs):
+    """GPflow ``GPR.predict_f(full_cov=False)``: mean (Nte, D) and the marginal
+    variance (Nte,), the same for every output column."""
+    N = X.shape[0]
+    Lc = np.linalg.cholesky(rbf_K(X, X, variance, lengthscale) + noise * np.eye(N))
+    Ks = rbf_K(X, Xs, variance, lengthscale)
+    A = scipy.linalg.solve_triangular(Lc, Ks, lower=True)
+    V = scipy.linalg.solve_triangular(Lc, Y, lower=True)
+    return A.T @ V, variance - (A * A).sum(0)
+
+
+# ----------------------------------------------------------------------------- vector-field features
+def vectorfield_features(positions, vectors, k=5, reference_quirks=True):
+    """Divergence and curl estimates of examples/eeg_example/eeg_utils.py:46-80:
+    unit vectors u; for each neighbour i of point j (the k nearest, exact
+    search, lower index first on ties) Δp = p_i − p_j, Δu = u_i − u_ref,
+    div_j = mean (Δu·Δp)/|Δp|², curl_j = mean (Δu × Δp)/|Δp|²; u_ref = u_0 for
+    every j as the reference computes it (eeg_utils.py:67), u_j otherwise."""
+    P = np.asarray(positions, dtype=np.float64)
+    U = vectors / np.linalg.norm(vectors, axis=1)[:, None]
+    nbr = knn(P, k)
+    dp = P[nbr] - P[:, None, :]                       # (n, k, 3)
+    ref = U[0][None, None, :] if reference_quirks else U[:, None, :]
+    du = U[nbr] - ref
+    r2 = np.linalg.norm(dp, axis=2) ** 2
+    div = ((du * dp).sum(2) / r2).sum(1) / k
+    curl = (np.cross(du, dp) / r2[:, :, None]).sum(1) / k
+    return div, curl

@@ -10,4 +10,5 @@ Drop-in names of the reference package (RVGP/__init__.py:1-3)::
 """
 from rvgp_gb300 import kernels  # noqa: F401
 from rvgp_gb300.dataclass import data as create_data_object  # noqa: F401
+from rvgp_gb300.dataclass import load_data_object  # noqa: F401
 from rvgp_gb300.main import train_gp as fit  # noqa: F401

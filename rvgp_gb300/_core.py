@@ -62,6 +62,14 @@ SIGNATURES = {
                                P, P, c_size_t, P]),
     "rvgp_sgpr_predict_workspace": (c_size_t, [ctypes.c_longlong, c_int]),
     "rvgp_sgpr_predict": (c_int, [P, ctypes.c_longlong, c_int, P, P, P, P, c_size_t, P]),
+    "rvgp_rbf_workspace": (c_size_t, [ctypes.c_longlong, c_int]),
+    "rvgp_rbf_state_size": (c_size_t, [ctypes.c_longlong, c_int]),
+    "rvgp_rbf_matrix": (c_int, [P, ctypes.c_longlong, P, ctypes.c_longlong, c_int, P, P, P]),
+    "rvgp_rbf_lml": (c_int, [P, ctypes.c_longlong, c_int, P, c_int, P, P, P, P, P, c_size_t, P]),
+    "rvgp_rbf_predict_workspace": (c_size_t, [ctypes.c_longlong, ctypes.c_longlong]),
+    "rvgp_rbf_predict": (c_int, [P, ctypes.c_longlong, P, ctypes.c_longlong, c_int, c_int, P, P, P, P, P, c_size_t,
+                                 P]),
+    "rvgp_vectorfield_features": (c_int, [P, c_int, P, c_int, P, c_int, c_int, P, P, P]),
     "rvgp_kernel_matrix": (c_int, [P, ctypes.c_longlong, P, ctypes.c_longlong, c_int, P, P, P]),
     "rvgp_kernel_diag": (c_int, [P, ctypes.c_longlong, c_int, P, P, P]),
     "rvgp_manifold_dimension": (c_int, [P, c_int, c_int, c_double, P, P, P]),
@@ -486,6 +494,71 @@ def sgpr_predict(Phi_star, state, m):
     check(L.rvgp_sgpr_predict(ptr(Phi_star), int(Nte), int(m), ptr(state), ptr(mean), ptr(var), ptr(ws), ws.numel(),
                               stream()), "rvgp_sgpr_predict")
     return mean, var
+
+
+class RBFWorkspace:
+    """Device buffers reused across likelihood evaluations of one RBF-GP problem."""
+
+    def __init__(self, N, D, device):
+        L = lib()
+        self.N, self.D = N, D
+        self.ws = workspace(L.rvgp_rbf_workspace(N, D), device)
+        self.state = torch.empty(int(L.rvgp_rbf_state_size(N, D)), dtype=torch.float64, device=device)
+        self.out = torch.empty(4, dtype=torch.float64, device=device)
+        self.info = torch.zeros(1, dtype=torch.int32, device=device)
+
+
+def rbf_matrix(X1, theta, X2=None):
+    """K(X1, X2) of the RBF kernel, theta = [variance, lengthscale, noise] (CUDA f64)."""
+    X1 = _dev(X1, torch.float64, "X1")
+    X2 = X1 if X2 is None else _dev(X2, torch.float64, "X2")
+    K = torch.empty((X1.shape[0], X2.shape[0]), dtype=torch.float64, device=X1.device)
+    check(lib().rvgp_rbf_matrix(ptr(X1), X1.shape[0], ptr(X2), X2.shape[0], X1.shape[1], ptr(theta), ptr(K),
+                                stream()), "rvgp_rbf_matrix")
+    return K
+
+
+def rbf_lml(X, Y, theta, work=None):
+    """[LML, d/dvariance, d/dlengthscale, d/dnoise] of the D-output RBF GP (rvgp_rbf_lml); no host sync."""
+    X = _dev(X, torch.float64, "X")
+    Y = _dev(Y, torch.float64, "Y")
+    N, m = X.shape
+    D = Y.shape[1]
+    work = work or RBFWorkspace(N, D, X.device)
+    check(lib().rvgp_rbf_lml(ptr(X), N, m, ptr(Y), D, ptr(theta), ptr(work.out), ptr(work.state), ptr(work.info),
+                             ptr(work.ws), work.ws.numel(), stream()), "rvgp_rbf_lml")
+    return work.out, work
+
+
+def rbf_predict(Xs, X, D, theta, state):
+    """Posterior mean (Nte, D) and marginal variance (Nte,) of the RBF GP (rvgp_rbf_predict)."""
+    Xs = _dev(Xs, torch.float64, "Xs")
+    X = _dev(X, torch.float64, "X")
+    Nte, m = Xs.shape
+    dev = Xs.device
+    mean = torch.empty((Nte, D), dtype=torch.float64, device=dev)
+    var = torch.empty(Nte, dtype=torch.float64, device=dev)
+    if Nte == 0:
+        return mean, var
+    L = lib()
+    ws = workspace(L.rvgp_rbf_predict_workspace(Nte, X.shape[0]), dev)
+    check(L.rvgp_rbf_predict(ptr(Xs), Nte, ptr(X), X.shape[0], m, D, ptr(theta), ptr(state), ptr(mean), ptr(var),
+                             ptr(ws), ws.numel(), stream()), "rvgp_rbf_predict")
+    return mean, var
+
+
+def vectorfield_features(P, V, nbr, ref_first=True):
+    """div (B, n) and curl (B, n, 3) of the fields V (B, n, 3) at the points P (n, 3)
+    from their neighbour lists nbr (n, k) (rvgp_vectorfield_features)."""
+    P = _dev(P, torch.float64, "P")
+    V = _dev(V, torch.float64, "V")
+    nbr = nbr.to(torch.int32).contiguous()
+    B, n = V.shape[0], P.shape[0]
+    div = torch.empty((B, n), dtype=torch.float64, device=P.device)
+    curl = torch.empty((B, n, 3), dtype=torch.float64, device=P.device)
+    check(lib().rvgp_vectorfield_features(ptr(P), n, ptr(V), B, ptr(nbr), nbr.shape[1], int(bool(ref_first)),
+                                          ptr(div), ptr(curl), stream()), "rvgp_vectorfield_features")
+    return div, curl
 
 
 def gp_fit_mixed_max_m():

@@ -215,6 +215,51 @@ class data:
         self.__dict__["_eig_L"] = None
         return self
 
+    # ------------------------------------------------------------------ persistence
+    _SAVED = ("X", "indptr", "indices", "L_vals", "perm", "rank", "ord_indptr", "ord_indices", "ord_L_vals", "T",
+              "Sigma", "R", "Lc_vals", "Lc_vals32", "evals_L", "evecs_L", "evals_Lc", "evecs_Lc", "evecs_Lc_local",
+              "vectors")
+    _FORMAT = 1
+
+    def save(self, path):
+        """Write the computed geometry (graph, gauges, connections, Laplacians,
+        both eigendecompositions, vectors) to one ``.npz`` file, so later fits
+        skip the eigensolves.  ``load_data_object(path)`` restores it on the
+        current device."""
+        import json
+        self.wait()
+        d = self._dev
+        arrays = {k: getattr(d, k).cpu().numpy() for k in self._SAVED if getattr(d, k, None) is not None}
+        meta = {"format": self._FORMAT, "n": self.n, "dim_man": self.dim_man, "n_eigenpairs": self.n_eigenpairs,
+                "precision": self.precision, "maxdeg": int(d.maxdeg), "bound": float(d.bound),
+                "eig_info_L": getattr(d, "eig_info_L", None), "eig_info_Lc": getattr(d, "eig_info_Lc", None)}
+        np.savez(path, __meta__=np.frombuffer(json.dumps(meta).encode(), dtype=np.uint8), **arrays)
+
+    @classmethod
+    def load(cls, path):
+        """A data object from a file written by ``save`` (no recomputation)."""
+        import json
+        _core.require_cuda()
+        device = torch.device("cuda", torch.cuda.current_device())
+        with np.load(path) as z:
+            meta = json.loads(bytes(z["__meta__"]).decode())
+            if meta.get("format") != cls._FORMAT:
+                raise ValueError(f"{path}: unsupported data-object format {meta.get('format')!r}")
+            dev = SimpleNamespace(**{k: torch.as_tensor(z[k], device=device) for k in cls._SAVED if k in z.files})
+        for k in cls._SAVED:
+            if not hasattr(dev, k):
+                setattr(dev, k, None)
+        dev.maxdeg, dev.bound = meta["maxdeg"], meta["bound"]
+        dev.eig_info_L, dev.eig_info_Lc = meta["eig_info_L"], meta["eig_info_Lc"]
+        obj = cls.__new__(cls)
+        obj._vertices_host = None
+        obj.precision = meta["precision"]
+        obj._eig_L = None
+        obj._dev = dev
+        obj.n, obj.dim_man, obj.n_eigenpairs = meta["n"], meta["dim_man"], meta["n_eigenpairs"]
+        obj._host = {}
+        return obj
+
     # ------------------------------------------------------------------ host views
     def _cached(self, key, fn):
         if key not in self._host:
@@ -334,3 +379,8 @@ class data:
         shift = max(0.0, float(d.evals_Lc[0]) * (1.0 - 1e-9) - 1e-12)
         loc = _core.vector_diffusion(d.indptr, d.indices, d.L_vals, d.Lc_vals, loc, t, d.bound, d.bound, shift)
         self.vectors = _core.frame_map(d.T, self.dim_man, loc, "from_local")
+
+
+def load_data_object(path):
+    """Restore a data object written by ``data.save`` on the current CUDA device."""
+    return data.load(path)

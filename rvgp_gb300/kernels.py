@@ -128,3 +128,35 @@ class ManifoldKernel:
         if not full_cov and X2 is None:
             return self.K_diag(X)
         return self.K(X, X2)
+
+
+class RBF:
+    """Squared-exponential kernel with GPflow ``kernels.RBF()``'s parameters and
+    defaults (``variance`` = 1, ``lengthscales`` = 1, both positive), used by
+    ``fit(..., kernel='rbf')`` on the scalar-Laplacian eigenbasis
+    (RVGP/main.py:33-37):  K(x, x') = variance · exp(−½ |x − x'|² / lengthscales²)."""
+
+    def __init__(self, variance=1.0, lengthscales=1.0):
+        self.variance = Parameter(variance, name="variance")
+        self.lengthscales = Parameter(lengthscales, name="lengthscales")
+
+    @property
+    def parameters(self):
+        return [self.variance, self.lengthscales]
+
+    def theta(self, noise=1.0, device="cuda"):
+        return torch.tensor([float(self.variance), float(self.lengthscales), noise], dtype=torch.float64,
+                            device=device)
+
+    def K(self, X, X2=None):
+        Xd = _to_dev(X, "cuda")
+        X2d = None if X2 is None else _to_dev(X2, "cuda")
+        return _core.rbf_matrix(Xd, self.theta(), X2d).cpu().numpy()
+
+    def K_diag(self, X):
+        return np.full(len(X), float(self.variance))
+
+    def __call__(self, X, X2=None, full_cov=True):
+        if not full_cov and X2 is None:
+            return self.K_diag(X)
+        return self.K(X, X2)

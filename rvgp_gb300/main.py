@@ -31,7 +31,7 @@ import scipy.optimize
 import torch
 
 from rvgp_gb300 import _core
-from rvgp_gb300.kernels import ManifoldKernel, Parameter, set_default_positive_minimum
+from rvgp_gb300.kernels import RBF, ManifoldKernel, Parameter, set_default_positive_minimum
 
 
 def train_test_split_indices(n_samples, test_size=0.2, seed=0):
@@ -62,6 +62,28 @@ class _LML(torch.autograd.Function):
 def log_marginal_likelihood(theta, model):
     """Differentiable LML: theta = CUDA f64 tensor [nu, kappa, sigma_f, noise]."""
     return _LML.apply(theta, model)
+
+
+def _host_adam(assign, loss_and_grad, x0, steps, lr, betas=(0.9, 0.999), eps=1e-8):
+    """Adam on the unconstrained vector x (the update of the device Adam of
+    rvgp_gp_fit_adam), one device evaluation per step.  Returns (x, history of
+    the objective −loss); a step whose loss or gradient is not finite keeps x."""
+    b1, b2 = betas
+    x = np.array(x0, dtype=np.float64)
+    m1 = np.zeros_like(x)
+    v1 = np.zeros_like(x)
+    hist = []
+    for step in range(steps):
+        assign(x)
+        f, g = loss_and_grad()
+        hist.append(-f)
+        if not (np.isfinite(f) and np.isfinite(g).all()):
+            continue
+        m1 = b1 * m1 + (1 - b1) * g
+        v1 = b2 * v1 + (1 - b2) * g * g
+        x = x - lr * (m1 / (1 - b1 ** (step + 1))) / (np.sqrt(v1 / (1 - b2 ** (step + 1))) + eps)
+    assign(x)
+    return x, np.asarray(hist)
 
 
 class manifold_GPR:
@@ -344,29 +366,100 @@ class manifold_SGPR(manifold_GPR):
             assign(res.x)
             return res
         if method.lower() == "adam":
-            # the same update as the device Adam of manifold_GPR, on the host
-            b1, b2, eps = 0.9, 0.999, 1e-8
-            x = x0.copy()
-            m1 = np.zeros_like(x)
-            v1 = np.zeros_like(x)
-            hist = []
-            for step in range(epochs):
-                assign(x)
-                f, g = self._loss_and_grad(params, train_Z)
-                hist.append(f)
-                if not (np.isfinite(f) and np.isfinite(g).all()):
-                    continue  # keep the parameters; the history records the failure
-                m1 = b1 * m1 + (1 - b1) * g
-                v1 = b2 * v1 + (1 - b2) * g * g
-                x = x - lr * (m1 / (1 - b1 ** (step + 1))) / (np.sqrt(v1 / (1 - b2 ** (step + 1))) + eps)
-            assign(x)
-            self.lml_history = -np.asarray(hist)
+            x, hist = _host_adam(assign, lambda: self._loss_and_grad(params, train_Z), x0, epochs, lr)
+            self.lml_history = hist
             return x
         raise ValueError(f"unknown optimiser {method!r}")
 
     def _predict_rows(self, Phi_star):
         self._evaluate()  # posterior state at the current parameters
         return _core.sgpr_predict(Phi_star, self.work.state, self.m)
+
+
+class rbf_GPR(manifold_GPR):
+    """GPflow GPR with ``kernels.RBF()`` on the scalar-Laplacian eigenbasis, the
+    D vector components as independent outputs sharing the kernel
+    (``fit(..., kernel='rbf')``, RVGP/main.py:33-37,55-58,99-116).
+
+    The likelihood, its gradient with respect to (variance, lengthscales,
+    noise) and the posterior are FP64 CUDA computations over the N training
+    points (rvgp_rbf_lml / rvgp_rbf_predict; N <= 3072).  ``transform`` with
+    integer indices predicts at those points' rows of the scalar eigenbasis.
+    """
+
+    max_rows = 3072
+
+    def __init__(self, data, kernel, train_points, noise_variance=1.0):
+        self.data_obj = data
+        self.kernel = kernel
+        self.precision = "fp64"
+        self.likelihood = type("Gaussian", (), {})()
+        self.likelihood.variance = Parameter(noise_variance, lower=1e-6, name="noise_variance")
+        dev = data._dev
+        if dev.vectors is None:
+            raise ValueError("the data object has no vectors to fit")
+        data.wait()  # the scalar eigenpairs may still be computed concurrently
+        self.D = dev.X.shape[1]
+        idx = torch.as_tensor(np.asarray(train_points, dtype=np.int64), device=dev.X.device)
+        self.X = dev.evecs_L[idx].contiguous()
+        self.Y = dev.vectors[idx].to(torch.float64).contiguous()
+        self.N = self.X.shape[0]
+        self.m = self.X.shape[1]
+        if self.N > self.max_rows:
+            raise ValueError(f"kernel='rbf' is a dense GP over the training points: {self.N} rows exceed "
+                             f"{self.max_rows}")
+        self.work = _core.RBFWorkspace(self.N, self.D, dev.X.device)
+        self.n_evals = 0
+        self._eval_key, self._eval_out = None, None
+
+    def _slots(self):
+        return [self.kernel.variance, self.kernel.lengthscales, self.likelihood.variance]
+
+    def theta(self):
+        return self.kernel.theta(float(self.likelihood.variance), device=self.X.device)
+
+    def _theta_key(self):
+        return tuple(float(p) for p in self._slots())
+
+    def _evaluate(self):
+        key = self._theta_key()
+        if self._eval_key == key:
+            return self._eval_out
+        out, _ = _core.rbf_lml(self.X, self.Y, self.theta(), self.work)
+        self.n_evals += 1
+        self._eval_key, self._eval_out = key, out.cpu().numpy()
+        return self._eval_out
+
+    def _loss_and_grad_u(self, params):
+        out = self._evaluate()
+        grads = {"variance": out[1], "lengthscales": out[2], "noise_variance": out[3]}
+        g = np.array([-grads[p.name] * p.dvalue_du() for p in params])
+        return -out[0], g
+
+    def _adam(self, params, steps, lr):
+        def assign(x):
+            for p, u in zip(params, x):
+                p.unconstrained = float(u)
+        x0 = np.array([p.unconstrained for p in params])
+        x, self.lml_history = _host_adam(assign, lambda: self._loss_and_grad_u(params), x0, steps, lr)
+        return x
+
+    def _predict_rows(self, Xs):
+        self._evaluate()  # posterior state at the current parameters
+        mean, var = _core.rbf_predict(Xs, self.X, self.D, self.theta(), self.work.state)
+        return mean, var[:, None].expand(-1, self.D)
+
+    def predict_f(self, Xnew):
+        """Mean and variance, each (rows, D), at rows of the scalar eigenbasis."""
+        Xd = Xnew.to(self.X.device, torch.float64) if isinstance(Xnew, torch.Tensor) else torch.as_tensor(
+            np.ascontiguousarray(Xnew, dtype=np.float64), device=self.X.device)
+        mean, var = self._predict_rows(Xd.reshape(-1, self.m).contiguous())
+        return mean.cpu(), var.cpu()
+
+    def predict_points(self, points):
+        dev = self.data_obj._dev
+        idx = torch.as_tensor(np.asarray(points, dtype=np.int64), device=self.X.device)
+        return self._predict_rows(dev.evecs_L[idx].contiguous())
 
 
 def optimize_model_with_scipy(model, epochs):
@@ -385,23 +478,34 @@ def train_gp(data, train_ind=None, n_inducing_points=None, test_size=0.2, kernel
     if kernel is None:
         kernel = ManifoldKernel(data, nu=3 / 2, kappa=5, typ="matern", sigma_f=1.0)
     elif isinstance(kernel, str):
-        raise NotImplementedError(f"kernel={kernel!r}: only the manifold kernel is implemented in rvgp_gb300")
+        if kernel != "rbf":
+            raise NotImplementedError(f"kernel={kernel!r}: use None (the manifold kernel) or 'rbf'")
+        kernel = RBF()
+        if verbose:
+            print("Using RBF kernel, treating vectors channel-wise.")
     tr, te = train_test_split_indices(len(train_ind), test_size, seed)
     pts_train, pts_test = train_ind[tr], train_ind[te]
     set_default_positive_minimum(positivity_constraint)
     precision = precision or getattr(data, "precision", "mixed")
     noise0 = 1.0 if reference_quirks else noise_variance
-    if n_inducing_points is None:
+    if isinstance(kernel, RBF):
+        if n_inducing_points is not None:
+            raise NotImplementedError("n_inducing_points with kernel='rbf' is not implemented in rvgp_gb300")
+        GP = rbf_GPR(data, kernel, pts_train, noise_variance=noise0)
+    elif n_inducing_points is None:
         GP = manifold_GPR(data, kernel, pts_train, noise_variance=noise0, precision=precision)
     else:
         GP = manifold_SGPR(data, kernel, pts_train, n_inducing_points=n_inducing_points, noise_variance=noise0,
                            precision=precision)
+    # RVGP/main.py:69-75 assigns kernel.variance / kernel.lengthscales: GPflow's
+    # names on the RBF kernel, sigma_f / kappa on the manifold kernel
+    var_p, len_p = (kernel.variance, kernel.lengthscales) if isinstance(kernel, RBF) else (kernel.sigma_f, kernel.kappa)
     if kernel_variance is not None:
-        kernel.sigma_f.assign(kernel_variance)
-        kernel.sigma_f.trainable = False
+        var_p.assign(kernel_variance)
+        var_p.trainable = False
     if kernel_lengthscale is not None:
-        kernel.kappa.assign(kernel_lengthscale)
-        kernel.kappa.trainable = False
+        len_p.assign(kernel_lengthscale)
+        len_p.trainable = False
     GP.optimize(epochs=epochs, method=optimizer, lr=lr, disp=verbose)
     if len(pts_test):
         mean, _ = GP.predict_points(pts_test)

@@ -201,3 +201,44 @@ def test_sgpr_bound_forms_agree_and_bound_the_lml():
         m2, v2 = O.predict_f(Phi, y, S, noise, Phi[:7] * 0.7)
         np.testing.assert_allclose(m1, m2, rtol=1e-8, atol=1e-10)
         np.testing.assert_allclose(v1, v2, rtol=1e-6, atol=1e-9)
+
+
+def test_rbf_gpr_oracle_matches_dense_forms():
+    """The multi-output RBF GPR oracle equals the sum of per-column Gaussian log
+    densities, and its posterior equals the textbook K*ᵀ K_y⁻¹ form."""
+    rng = np.random.default_rng(3)
+    X = rng.standard_normal((40, 5)) * 0.4
+    Y = rng.standard_normal((40, 3))
+    Xs = rng.standard_normal((9, 5)) * 0.4
+    var, ls, noise = 1.3, 0.8, 0.05
+    Ky = O.rbf_K(X, X, var, ls) + noise * np.eye(40)
+    _, logdet = np.linalg.slogdet(Ky)
+    Kinv = np.linalg.inv(Ky)
+    ref = sum(-0.5 * Y[:, c] @ Kinv @ Y[:, c] - 0.5 * logdet - 20 * np.log(2 * np.pi) for c in range(3))
+    assert abs(O.rbf_gpr_lml(X, Y, var, ls, noise) - ref) < 1e-9 * abs(ref)
+    mean, v = O.rbf_gpr_predict_f(X, Y, var, ls, noise, Xs)
+    Ks = O.rbf_K(Xs, X, var, ls)
+    np.testing.assert_allclose(mean, Ks @ Kinv @ Y, rtol=1e-8, atol=1e-10)
+    np.testing.assert_allclose(v, var - np.einsum("ij,jk,ik->i", Ks, Kinv, Ks), rtol=1e-7, atol=1e-10)
+
+
+@pytest.mark.parametrize("case", ["small", "large"])
+def test_vectorfield_features_match_reference(case):
+    g = load_golden("features")
+    div, curl = O.vectorfield_features(g[f"{case}_pos"], g[f"{case}_vec"], k=5)
+    np.testing.assert_allclose(div, g[f"{case}_div"], rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(curl, g[f"{case}_curl"], rtol=1e-12, atol=1e-12)
+
+
+def test_load_mesh_matches_reference(tmp_path):
+    from rvgp_gb300.utils import load_mesh
+    g = load_golden("features")
+    text = bytes(g["obj_text"]).decode()
+    (tmp_path / "uvsphere.obj").write_text(text)
+    v, f = load_mesh("uvsphere", folder=str(tmp_path))
+    np.testing.assert_array_equal(v, g["obj_vertices"])
+    np.testing.assert_array_equal(f, g["obj_faces"])
+    # records the reference rejects: blank lines and 'v/vt/vn' face entries
+    (tmp_path / "tolerant.obj").write_text("# c\n\nv 0 0 0\nv 1 0 0\nv 0 1 0\n\nf 1/1/1 2/2/2 3/3/3\n")
+    v, f = load_mesh("tolerant", folder=str(tmp_path))
+    assert v.shape == (3, 3) and f.tolist() == [[0, 1, 2]]
