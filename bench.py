@@ -17,6 +17,8 @@ step through the public API with host numpy inputs and outputs.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
     python bench.py --model sgpr [--inducing M] [--sgpr-iters I]   # the sparse inducing-point GP
+    python bench.py --model rbf [--sgpr-iters I]                    # kernel='rbf' GP
+    python bench.py --model features                                # div/curl vector-field features
 """
 import os
 
@@ -547,6 +549,175 @@ def run_sgpr(args):
     return out
 
 
+# ------------------------------------------------------------------------------ RBF GP and field features
+RBF_METRIC = "RVGP kernel='rbf' GP fit+predict wall s (scalar eigenbasis, L-BFGS-B on variance, lengthscale, noise)"
+FEATURES_METRIC = "vector-field div/curl features: (field, point) pairs per s"
+
+
+def run_rbf(args):
+    """The RBF-kernel GP (fit(kernel='rbf')) on the sphere workload: n = 2000,
+    k = 10, 50 eigenpairs, 50 % train (800 training rows after the internal
+    split), L-BFGS-B for --sgpr-iters iterations, predict at the other 1000 points."""
+    import torch
+    import rvgp_gb300 as RVGP
+    from rvgp_gb300 import _core
+    _core.require_cuda()
+    wl = WORKLOADS["sphere_n2000_k10_m50"]
+    X, train, test = make_inputs(wl, seed=0)
+    d = RVGP.create_data_object(X, n_neighbors=wl["k"], n_eigenpairs=wl["m"], precision="fp64", verbose=False)
+    d.random_vector_field(seed=0)
+    d.smooth_vector_field(t=wl["t_smooth"])
+    V = d.vectors
+    d.wait()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def step():
+        gp = RVGP.fit(d, train_ind=train, kernel="rbf", epochs=args.sgpr_iters, verbose=False)
+        return gp, gp.predict_points(test)
+
+    for _ in range(args.warmup):
+        step()
+    times, evals = [], []
+    launches0 = _core.launch_count()
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            flush_l2(flush)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            gp, _ = step()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1) / 1e3)
+            evals.append(gp.n_evals)
+    launches = _core.launch_count() - launches0
+    t_step = float(np.mean(times))
+    ev_t = []
+    for r in range(13):
+        flush_l2(flush)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        _core.rbf_lml(gp.X, gp.Y, gp.theta(), gp.work)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if r >= 3:
+            ev_t.append(e0.elapsed_time(e1) / 1e3)
+    t_eval = float(np.mean(ev_t))
+    N, m, D = gp.N, gp.m, gp.D
+    flops = N ** 3 / 3.0 + N ** 3 / 3.0 + 2.0 * N ** 3 + 3.0 * N * N * m + 4.0 * N * N * D  # chol, L⁻¹, K⁻¹, K, products
+    achieved = flops / t_eval / 1e12
+    e2e = []
+    for _ in range(2):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        d.vectors = V
+        g2 = RVGP.fit(d, train_ind=train, kernel="rbf", epochs=args.sgpr_iters, verbose=False)
+        mh, vh = g2.transform(d, test)
+        e2e.append(time.perf_counter() - t0)
+    out = {"metric": RBF_METRIC, "value": round(t_step, 5), "unit": "s", "n_gpus": 1, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": round(t_step * 1e3, 3), "higher_is_better": False,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": "sphere_n2000_k10_m50", "model": "rbf_GPR", "N_train_rows": int(N), "m": int(m),
+                      "outputs": int(D), "lbfgsb_max_iter": args.sgpr_iters, "l2": "flushed between steps"},
+           "lml_evals_per_step": [int(e) for e in evals], "l2_error": getattr(gp, "l2_error", None),
+           "eval_ms": round(t_eval * 1e3, 4),
+           "roofline": {"kernel": "rvgp_rbf_lml chain (likelihood + gradient + posterior state)", "bound": "fp64",
+                        "achieved": round(achieved, 4), "peak": FP64_NOMINAL_TFLOPS, "unit": "TFLOP/s",
+                        "frac": round(achieved / FP64_NOMINAL_TFLOPS, 4), "traffic": None, "peak_source": "nominal",
+                        "algorithmic_flops": flops},
+           "e2e": {"value": round(float(np.mean(e2e)), 5), "unit": "s", "h2d_bytes_per_step": int(V.nbytes),
+                   "d2h_bytes_per_step": int(mh.nbytes + vh.nbytes)},
+           "clocks": clk.summary(), "gpu_launches": int(launches / max(1, args.steps)),
+           "step_times_s": [round(t, 5) for t in times]}
+    if not args.skip_cpu:
+        from oracle import rvgp_oracle as O
+        Xh, Yh = gp.X.cpu().numpy(), gp.Y.cpu().numpy()
+        th = [float(p) for p in gp._slots()]
+        t0 = time.perf_counter()
+        for _ in range(3):
+            O.rbf_gpr_lml(Xh, Yh, *th)
+            Ky = O.rbf_K(Xh, Xh, th[0], th[1]) + th[2] * np.eye(N)
+            np.linalg.inv(Ky)  # the gradient's K_y⁻¹
+        one = (time.perf_counter() - t0) / 3
+        t0 = time.perf_counter()
+        O.rbf_gpr_predict_f(Xh, Yh, *th, d.evecs_L[test])
+        t_pred = time.perf_counter() - t0
+        n_ev = float(np.mean(evals))
+        out["cpu_baseline"] = {"value": round(one * n_ev + t_pred, 3), "unit": "s", "cores": os.cpu_count(),
+                               "kind": "port",
+                               "sample": (f"GPflow's GPR likelihood with the RBF kernel plus the K_y⁻¹ of its "
+                                          f"gradient, 3x ({one * 1e3:.1f} ms each), scaled by {n_ev:.0f} "
+                                          f"evaluations per fit, plus the predict")}
+    print(json.dumps(out), flush=True)
+    return out
+
+
+def run_features(args):
+    """div/curl features of B = 1024 time samples of a field on n = 20000 torus
+    points, k = 5, in one launch per step (compute_vectorfield_features_time)."""
+    import torch
+    from rvgp_gb300 import _core
+    from rvgp_gb300.features import compute_vectorfield_features_time
+    _core.require_cuda()
+    wl = WORKLOADS["torus_n20000_k20_m200"]
+    X, _, _ = make_inputs(wl, seed=0)
+    n, B, k = X.shape[0], 1024, 5
+    rng = np.random.default_rng(0)
+    Vh = rng.standard_normal((B, n, 3))
+    P = torch.as_tensor(X, device="cuda")
+    V = torch.as_tensor(Vh, device="cuda")
+    nbr = _core.knn(P, k)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        _core.vectorfield_features(P, V, nbr)
+    times = []
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            flush_l2(flush)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            _core.vectorfield_features(P, V, nbr)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1) / 1e3)
+    t = float(np.mean(times))
+    alg = B * n * (3 * 8 + 4 * 8) + n * k * 4 + n * 3 * 8  # fields read once, div + curl written, lists, points
+    peaks, src = measured_peaks()
+    gbs = alg / t / 1e9
+    e2e = []
+    for _ in range(2):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        div, curl = compute_vectorfield_features_time(range(B), X, Vh, k=k)
+        e2e.append(time.perf_counter() - t0)
+    out = {"metric": FEATURES_METRIC, "value": round(B * n / t, 1), "unit": "pairs/s", "n_gpus": 1,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t * 1e3, 4), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": "torus_n20000 points, 1024 fields, k=5", "l2": "flushed between steps; the "
+                      "fields (491 MB) exceed L2"},
+           "roofline": {"kernel": "vf_features_kernel", "bound": "hbm", "achieved": round(gbs, 1),
+                        "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": round(gbs / peaks["hbm_gbs"], 4),
+                        "traffic": None, "peak_source": src, "algorithmic_bytes": int(alg)},
+           "e2e": {"value": round(B * n / float(np.mean(e2e)), 1), "unit": "pairs/s",
+                   "h2d_bytes_per_step": int(Vh.nbytes + X.nbytes), "d2h_bytes_per_step": int(div.nbytes + curl.nbytes)},
+           "clocks": clk.summary(), "gpu_launches": 1, "step_times_s": [round(x, 6) for x in times]}
+    if not args.skip_cpu:
+        from oracle import rvgp_oracle as O
+        s = 4
+        t0 = time.perf_counter()
+        for b in range(s):
+            O.vectorfield_features(X, Vh[b], k=k)
+        tc = (time.perf_counter() - t0) / s
+        out["cpu_baseline"] = {"value": round(n / tc, 1), "unit": "pairs/s", "cores": os.cpu_count(), "kind": "port",
+                               "sample": f"the oracle (vectorised numpy, exact kNN per field) on {s} of the fields"}
+    print(json.dumps(out), flush=True)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -558,17 +729,19 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=240.0)
-    ap.add_argument("--model", choices=["gpr", "sgpr"], default="gpr",
-                    help="sgpr: the sparse inducing-point GP fit instead of the full pipeline")
+    ap.add_argument("--model", choices=["gpr", "sgpr", "rbf", "features"], default="gpr",
+                    help="sgpr: the sparse inducing-point GP fit; rbf: the kernel='rbf' GP; features: div/curl")
     ap.add_argument("--inducing", type=int, default=100, help="inducing rows for --model sgpr")
-    ap.add_argument("--sgpr-iters", type=int, default=200, help="L-BFGS-B iterations for --model sgpr")
+    ap.add_argument("--sgpr-iters", type=int, default=200, help="L-BFGS-B iterations for --model sgpr / rbf")
     args = ap.parse_args()
-    if args.model == "sgpr":
+    if args.model != "gpr":
+        runner, metric = {"sgpr": (run_sgpr, SGPR_METRIC), "rbf": (run_rbf, RBF_METRIC),
+                          "features": (run_features, FEATURES_METRIC)}[args.model]
         if args.impl == "ours" and int(os.environ.get("RANK", "0")) == 0:
-            run_sgpr(args)
+            runner(args)
         elif args.impl == "reference":
-            print(json.dumps({"impl": "reference", "metric": SGPR_METRIC,
-                              "unavailable": "the sparse-GP CPU baseline is the cpu_baseline of the ours arm"}))
+            print(json.dumps({"impl": "reference", "metric": metric,
+                              "unavailable": "this model's CPU baseline is the cpu_baseline of the ours arm"}))
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -252,8 +252,9 @@ int rvgp_sgpr_elbo(const double* C, const double* b, const double* yy, long long
  * (examples/eeg_example/eeg_utils.py:46-80): div (B x n), curl (B x n x 3).
  * ref_first = 1 differences every unit vector against point 0's, as the
  * reference does; 0 against the point's own. */
+size_t rvgp_vectorfield_features_workspace(int n, int B, int k);
 int rvgp_vectorfield_features(const double* P, int n, const double* V, int B, const int* nbr, int k, int ref_first,
-                              double* div, double* curl, void* stream);
+                              double* div, double* curl, void* workspace, size_t ws_bytes, void* stream);
 
 /* Dense GP with GPflow's RBF kernel on N <= 3072 rows X (N x m) of the scalar
  * eigenbasis and D <= 16 output columns Y (kernel='rbf', RVGP/main.py:33-37,

@@ -69,7 +69,8 @@ SIGNATURES = {
     "rvgp_rbf_predict_workspace": (c_size_t, [ctypes.c_longlong, ctypes.c_longlong]),
     "rvgp_rbf_predict": (c_int, [P, ctypes.c_longlong, P, ctypes.c_longlong, c_int, c_int, P, P, P, P, P, c_size_t,
                                  P]),
-    "rvgp_vectorfield_features": (c_int, [P, c_int, P, c_int, P, c_int, c_int, P, P, P]),
+    "rvgp_vectorfield_features_workspace": (c_size_t, [c_int, c_int, c_int]),
+    "rvgp_vectorfield_features": (c_int, [P, c_int, P, c_int, P, c_int, c_int, P, P, P, c_size_t, P]),
     "rvgp_kernel_matrix": (c_int, [P, ctypes.c_longlong, P, ctypes.c_longlong, c_int, P, P, P]),
     "rvgp_kernel_diag": (c_int, [P, ctypes.c_longlong, c_int, P, P, P]),
     "rvgp_manifold_dimension": (c_int, [P, c_int, c_int, c_double, P, P, P]),
@@ -556,8 +557,10 @@ def vectorfield_features(P, V, nbr, ref_first=True):
     B, n = V.shape[0], P.shape[0]
     div = torch.empty((B, n), dtype=torch.float64, device=P.device)
     curl = torch.empty((B, n, 3), dtype=torch.float64, device=P.device)
-    check(lib().rvgp_vectorfield_features(ptr(P), n, ptr(V), B, ptr(nbr), nbr.shape[1], int(bool(ref_first)),
-                                          ptr(div), ptr(curl), stream()), "rvgp_vectorfield_features")
+    L = lib()
+    ws = workspace(L.rvgp_vectorfield_features_workspace(n, B, nbr.shape[1]), P.device)
+    check(L.rvgp_vectorfield_features(ptr(P), n, ptr(V), B, ptr(nbr), nbr.shape[1], int(bool(ref_first)), ptr(div),
+                                      ptr(curl), ptr(ws), ws.numel(), stream()), "rvgp_vectorfield_features")
     return div, curl
 
 
