@@ -699,12 +699,13 @@ def run_features(args):
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
            "config": {"workload": "torus_n20000 points, 1024 fields, k=5", "l2": "flushed between steps; the "
                       "fields (491 MB) exceed L2"},
-           "roofline": {"kernel": "vf_features_kernel", "bound": "hbm", "achieved": round(gbs, 1),
+           "roofline": {"kernel": "rvgp_vectorfield_features (vf_geometry, vf_unit, vf_features_kernel)",
+                        "bound": "hbm", "achieved": round(gbs, 1),
                         "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": round(gbs / peaks["hbm_gbs"], 4),
                         "traffic": None, "peak_source": src, "algorithmic_bytes": int(alg)},
            "e2e": {"value": round(B * n / float(np.mean(e2e)), 1), "unit": "pairs/s",
                    "h2d_bytes_per_step": int(Vh.nbytes + X.nbytes), "d2h_bytes_per_step": int(div.nbytes + curl.nbytes)},
-           "clocks": clk.summary(), "gpu_launches": 1, "step_times_s": [round(x, 6) for x in times]}
+           "clocks": clk.summary(), "gpu_launches": 3, "step_times_s": [round(x, 6) for x in times]}
     if not args.skip_cpu:
         from oracle import rvgp_oracle as O
         s = 4
