@@ -230,6 +230,14 @@ int rvgp_gp_fit_adam_mixed_finish(const double* C, const double* b, const double
 size_t rvgp_gp_predict_workspace(long long Nte, int m, int mode);
 int rvgp_gp_predict(const double* Phi_star, const float* Phi_star32, long long Nte, int m, int mode,
                     const double* state, double* mean, double* var, void* workspace, size_t ws_bytes, void* stream);
+/* Posterior means (Nte x B) and LMLs (B, optional) of B fields Y (N x B)
+ * observed at the rows Phi (N x m), from the state and theta of an
+ * rvgp_gp_lml evaluation on the same rows: the per-time-sample fits of a field
+ * sequence (examples/eeg_example/eeg_utils.py:26-35) for every field at once. */
+size_t rvgp_gp_posterior_batch_workspace(int m, int B);
+int rvgp_gp_posterior_batch(const double* Phi, long long N, int m, const double* Y, int B, const double* theta,
+                            const double* state, const double* Phi_star, long long Nte, double* mean, double* lml,
+                            void* workspace, size_t ws_bytes, void* stream);
 /* K = (X S) X2ᵀ and diag((X S) Xᵀ): ManifoldKernel.K / K_diag (RVGP/kernels.py:55-67). */
 int rvgp_kernel_matrix(const double* X, long long N1, const double* X2, long long N2, int m, const double* S,
                        double* K, void* stream);

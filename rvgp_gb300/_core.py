@@ -71,6 +71,9 @@ SIGNATURES = {
                                  P]),
     "rvgp_vectorfield_features_workspace": (c_size_t, [c_int, c_int, c_int]),
     "rvgp_vectorfield_features": (c_int, [P, c_int, P, c_int, P, c_int, c_int, P, P, P, c_size_t, P]),
+    "rvgp_gp_posterior_batch_workspace": (c_size_t, [c_int, c_int]),
+    "rvgp_gp_posterior_batch": (c_int, [P, ctypes.c_longlong, c_int, P, c_int, P, P, P, ctypes.c_longlong, P, P, P,
+                                        c_size_t, P]),
     "rvgp_kernel_matrix": (c_int, [P, ctypes.c_longlong, P, ctypes.c_longlong, c_int, P, P, P]),
     "rvgp_kernel_diag": (c_int, [P, ctypes.c_longlong, c_int, P, P, P]),
     "rvgp_manifold_dimension": (c_int, [P, c_int, c_int, c_double, P, P, P]),
@@ -562,6 +565,25 @@ def vectorfield_features(P, V, nbr, ref_first=True):
     check(L.rvgp_vectorfield_features(ptr(P), n, ptr(V), B, ptr(nbr), nbr.shape[1], int(bool(ref_first)), ptr(div),
                                       ptr(curl), ptr(ws), ws.numel(), stream()), "rvgp_vectorfield_features")
     return div, curl
+
+
+def gp_posterior_batch(Phi, Y, theta, state, Phi_star, want_lml=True):
+    """Posterior means (Nte, B) and log marginal likelihoods (B,) of the B fields
+    Y (N, B) observed at the rows Phi (rvgp_gp_posterior_batch)."""
+    Phi = _dev(Phi, torch.float64, "Phi")
+    Y = _dev(Y, torch.float64, "Y")
+    Phi_star = _dev(Phi_star, torch.float64, "Phi_star")
+    N, m = Phi.shape
+    B = Y.shape[1]
+    dev = Phi.device
+    mean = torch.empty((Phi_star.shape[0], B), dtype=torch.float64, device=dev)
+    lml = torch.empty(B, dtype=torch.float64, device=dev) if want_lml else None
+    L = lib()
+    ws = workspace(L.rvgp_gp_posterior_batch_workspace(m, B), dev)
+    check(L.rvgp_gp_posterior_batch(ptr(Phi), N, m, ptr(Y), B, ptr(theta), ptr(state), ptr(Phi_star),
+                                    Phi_star.shape[0], ptr(mean), ptr(lml), ptr(ws), ws.numel(), stream()),
+          "rvgp_gp_posterior_batch")
+    return mean, lml
 
 
 def gp_fit_mixed_max_m():

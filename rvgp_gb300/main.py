@@ -108,6 +108,7 @@ class manifold_GPR:
         self.work = _core.LMLWorkspace(self.m, dev.X.device)
         self.n_evals = 0
         self._eval_key, self._eval_out = None, None  # parameters of the state held in self.work
+        self._train_idx = idx
 
     # ------------------------------------------------------------------ parameters
     @property
@@ -223,6 +224,27 @@ class manifold_GPR:
         mean, var = self._predict_rows(Phi)
         return mean.reshape(-1, self.D), var.reshape(-1, self.D)
 
+    def predict_fields(self, fields, points):
+        """Posterior means (B, len(points), D) and log marginal likelihoods (B,)
+        of B fields ``fields`` (B, n, D) observed at this model's training
+        points, with this model's hyperparameters: the per-time-sample fits of
+        a field sequence (RVGP's EEG use, eeg_utils.py:26-35) solved for every
+        field at once (rvgp_gp_posterior_batch).  The posterior variance does
+        not depend on the field: ``predict_points(points)`` gives it."""
+        self._evaluate()  # posterior state at the current parameters
+        dev = self.kernel.device
+        F = fields.to(dev, torch.float64) if isinstance(fields, torch.Tensor) else torch.as_tensor(
+            np.ascontiguousarray(fields, dtype=np.float64), device=dev)
+        if F.ndim != 3 or F.shape[2] != self.D:
+            raise ValueError(f"fields must be (B, n, {self.D}), got {tuple(F.shape)}")
+        B = F.shape[0]
+        Y = F[:, self._train_idx.long(), :].reshape(B, -1).t().contiguous()  # (N, B), rows (point, coordinate)
+        Phi, _, _ = _core.gather_rows(self.kernel.eigenvectors, self.D, self._train_idx)
+        idx = torch.as_tensor(np.asarray(points, dtype=np.int32), device=dev)
+        Phi_star, _, _ = _core.gather_rows(self.kernel.eigenvectors, self.D, idx)
+        mean, lml = _core.gp_posterior_batch(Phi, Y, self.theta(), self.work.state, Phi_star)
+        return mean.t().reshape(B, len(idx), self.D), lml
+
     def transform(self, data, test_ind):
         """Posterior mean and variance (the reference names it f_pred_std, but it
         is the variance) at test points, as in RVGP/main.py:102-116.  Integer
@@ -306,6 +328,9 @@ class manifold_SGPR(manifold_GPR):
 
     def _theta_key(self):
         return super()._theta_key() + (self._z_version,)
+
+    def predict_fields(self, fields, points):
+        raise NotImplementedError("predict_fields is implemented for the full GP (manifold_GPR)")
 
     def _set_Z(self, values):
         self.inducing_variable.Z.copy_(torch.as_tensor(values, dtype=torch.float64).reshape(self.inducing_variable.Z.shape))
@@ -414,6 +439,9 @@ class rbf_GPR(manifold_GPR):
 
     def _slots(self):
         return [self.kernel.variance, self.kernel.lengthscales, self.likelihood.variance]
+
+    def predict_fields(self, fields, points):
+        raise NotImplementedError("predict_fields is implemented for the full GP (manifold_GPR)")
 
     def theta(self):
         return self.kernel.theta(float(self.likelihood.variance), device=self.X.device)

@@ -188,3 +188,31 @@ def test_deferred_eigsh_L_beside_mixed_fit(RVGP):
     # a data object whose L pairs are read before any fit solves them on demand
     d2 = RVGP.create_data_object(g["X"], n_neighbors=20, n_eigenpairs=m, precision="mixed", verbose=False)
     np.testing.assert_allclose(d2.evals_L, ev, rtol=0, atol=0)
+
+
+@pytest.mark.parametrize("B", [1, 6])
+def test_predict_fields_matches_per_field_fits(RVGP, B):
+    """Many fields at the same training points: predict_fields (one batched
+    solve) equals a separate fit(epochs=0) + transform per field, and each
+    field's log marginal likelihood equals that fit's."""
+    g = load_golden("sphere")
+    d = RVGP.create_data_object(g["X"], n_neighbors=10, n_eigenpairs=int(g["m"]), precision="fp64", verbose=False)
+    fields = []
+    for s in range(B):
+        d.random_vector_field(seed=s)
+        d.smooth_vector_field(t=10 + 5 * s)
+        fields.append(d.vectors)
+    fields = np.stack(fields)
+    train = np.arange(0, d.n, 3)
+    test = np.arange(1, d.n, 3)
+    d.vectors = fields[0]
+    gp = RVGP.fit(d, train_ind=train, epochs=0, verbose=False)
+    means, lml = gp.predict_fields(fields, test)
+    means, lml = means.cpu().numpy(), lml.cpu().numpy()
+    assert means.shape == (B, len(test), 3)
+    for b in range(B):
+        d.vectors = fields[b]
+        gb = RVGP.fit(d, train_ind=train, epochs=0, verbose=False)
+        mb, _ = gb.transform(d, test)
+        assert np.linalg.norm(means[b] - mb) <= 1e-10 * np.linalg.norm(mb)
+        assert abs(lml[b] - gb.log_marginal_likelihood()) <= 1e-10 * abs(lml[b])
