@@ -21,9 +21,9 @@
 // Σ = D − WᵀW + VᵀV, i.e. GPflow's diag K** + colsum(tmp2²) − colsum(tmp1²).
 //
 // Everything is FP64: the bound's Cholesky factors have condition numbers up
-// to |Kuu|/ε.  The small products go through one tiled FP64 GEMM with
-// transpose flags; the two Cholesky factorisations and triangular inverses are
-// the library's blocked FP64 ones.
+// to |Kuu|/ε.  The products use the FP64 GEMM and matrix-vector kernels of
+// fp64_gemm.cuh; the two Cholesky factorisations (one CTA for M <= 160,
+// blocked above) and triangular inverses are the library's FP64 ones.
 #include "common.cuh"
 #include "linalg.cuh"
 #include "fp64_gemm.cuh"
