@@ -545,15 +545,22 @@ def rbf_gpr_predict_f(X, Y, variance, lengthscale, noise, Xs):
 
 
 # ----------------------------------------------------------------------------- vector-field features
-def vectorfield_features(positions, vectors, k=5, reference_quirks=True):
+def vectorfield_features(positions, vectors, k=5, reference_quirks=True, kdtree=False):
     """Divergence and curl estimates of examples/eeg_example/eeg_utils.py:46-80:
     unit vectors u; for each neighbour i of point j (the k nearest, exact
     search, lower index first on ties) Δp = p_i − p_j, Δu = u_i − u_ref,
     div_j = mean (Δu·Δp)/|Δp|², curl_j = mean (Δu × Δp)/|Δp|²; u_ref = u_0 for
-    every j as the reference computes it (eeg_utils.py:67), u_j otherwise."""
+    every j as the reference computes it (eeg_utils.py:67), u_j otherwise.
+    ``kdtree=True`` finds the neighbours with scipy's KD-tree, as the reference
+    does (eeg_utils.py:54-60; the same neighbours when distances do not tie),
+    which is the fast CPU form used as the timing baseline."""
     P = np.asarray(positions, dtype=np.float64)
     U = vectors / np.linalg.norm(vectors, axis=1)[:, None]
-    nbr = knn(P, k)
+    if kdtree:
+        from scipy.spatial import KDTree
+        nbr = KDTree(P).query(P, k + 1)[1][:, 1:]
+    else:
+        nbr = knn(P, k)
     dp = P[nbr] - P[:, None, :]                       # (n, k, 3)
     ref = U[0][None, None, :] if reference_quirks else U[:, None, :]
     du = U[nbr] - ref

@@ -242,3 +242,11 @@ def test_load_mesh_matches_reference(tmp_path):
     (tmp_path / "tolerant.obj").write_text("# c\n\nv 0 0 0\nv 1 0 0\nv 0 1 0\n\nf 1/1/1 2/2/2 3/3/3\n")
     v, f = load_mesh("tolerant", folder=str(tmp_path))
     assert v.shape == (3, 3) and f.tolist() == [[0, 1, 2]]
+
+
+def test_vectorfield_features_kdtree_form_matches():
+    g = load_golden("features")
+    a = O.vectorfield_features(g["large_pos"], g["large_vec"], k=5)
+    b = O.vectorfield_features(g["large_pos"], g["large_vec"], k=5, kdtree=True)
+    np.testing.assert_array_equal(a[0], b[0])
+    np.testing.assert_array_equal(a[1], b[1])
