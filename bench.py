@@ -328,7 +328,7 @@ def run_ours(args):
 # ------------------------------------------------------------------------------ CPU baseline (oracle port)
 def cpu_stage_times(wl, X, V, train, test, budget=240.0):
     """Per-stage seconds of the reference algorithm's CPU restatement (oracle):
-    brute-force kNN, heap Dijkstra gauges, LAPACK SVDs, connections,
+    KD-tree kNN, heap Dijkstra gauges, LAPACK SVDs, connections,
     Laplacians, ARPACK eigsh(which='SM') for L and Lc, one dense GPflow-GPR
     LML + gradient evaluation (scaled by the number of optimiser steps) and the
     dense predict."""
@@ -337,7 +337,7 @@ def cpu_stage_times(wl, X, V, train, test, budget=240.0):
     n, k, m = wl["n"], wl["k"], wl["m"]
     T = {}
     t0 = time.perf_counter()
-    nn = O.knn(X, k)
+    nn = O.knn_kdtree(X, k)  # tree search, as sklearn's kneighbors_graph does for 3-d points
     ip, ix = O.symmetrised_csr(nn, n)
     T["graph"] = time.perf_counter() - t0
     t0 = time.perf_counter()

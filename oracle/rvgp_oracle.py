@@ -98,6 +98,21 @@ def knn(X, k, chunk=2048):
     return out
 
 
+def knn_kdtree(X, k):
+    """The k nearest neighbours by scipy's KD-tree, the tree search sklearn's
+    ``kneighbors_graph`` uses for low-dimensional points (RVGP/geometry.py:103-110).
+    The same lists as ``knn`` when distances do not tie; the timing form of the
+    CPU baseline."""
+    from scipy.spatial import KDTree
+    X = np.ascontiguousarray(X, dtype=np.float64)
+    idx = KDTree(X).query(X, k + 1)[1]
+    out = np.empty((len(X), k), dtype=np.int32)
+    for r in range(len(X)):  # drop the point itself wherever the tree returned it
+        row = idx[r][idx[r] != r]
+        out[r] = row[:k]
+    return out
+
+
 def symmetrised_csr(knn_idx, n):
     """CSR (indptr, indices) of max(A, Aᵀ) with A = kNN connectivity + I.
 

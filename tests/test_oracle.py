@@ -250,3 +250,10 @@ def test_vectorfield_features_kdtree_form_matches():
     b = O.vectorfield_features(g["large_pos"], g["large_vec"], k=5, kdtree=True)
     np.testing.assert_array_equal(a[0], b[0])
     np.testing.assert_array_equal(a[1], b[1])
+
+
+@pytest.mark.parametrize("name", ["sphere", "torus"])
+def test_knn_kdtree_timing_form_matches(name):
+    g = load_golden(name)
+    X, k = g["X"], int(g["k"])
+    np.testing.assert_array_equal(np.sort(O.knn_kdtree(X, k), 1), np.sort(O.knn(X, k), 1))
