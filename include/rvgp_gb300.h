@@ -128,7 +128,8 @@ int rvgp_eigsh_ordered(const int* indptr, const int* indices, const double* vals
 
 /* The eigensolver's FP32 tall products on the tcgen05 tensor cores with
  * split-TF32 operands (x = tf32(x) + remainder; three TF32 products per
- * term, FP32-level accuracy), p, q, K <= 256.  No reference counterpart: they
+ * term, FP32-level accuracy), p, q, K <= 2048 (outputs wider than 256
+ * columns run as 256-column blocks of TMEM accumulators).  No reference counterpart: they
  * are the block operations inside the subspace iteration that replaces ARPACK
  * (RVGP/geometry.py:66-80).  Synchronous; a timed-out pipeline wait returns
  * RVGP_ELAUNCH.
@@ -226,6 +227,25 @@ int rvgp_gp_fit_adam_mixed_launch(const double* C, const double* b, const double
 int rvgp_gp_fit_adam_mixed_finish(const double* C, const double* b, const double* yy, long long N, int m,
                                   const double* evals, double n_rows, int typ, const double* theta_out, double* out,
                                   double* state, int* status, void* workspace, size_t ws_bytes, void* stream);
+/* The same C, b, yy for the lifted rows of the training points idx without
+ * forming them (the rows built at RVGP/main.py:31,47-50 from
+ * evecs_Lc = T_i U_i, RVGP/dataclass.py:57-59): with L_i the Cholesky factor
+ * of T_iᵀT_i, the d rows L_iᵀU_i and targets L_i⁻¹T_iᵀy_i give ΦᵀΦ and Φᵀy
+ * exactly (d rows per point instead of D); yy sums the full D-vectors.
+ * T: n x D x ld gauges (first d <= 8 columns used), U: n*d x m local
+ * eigenvectors, vec: n x D vectors. */
+size_t rvgp_gp_prepare_local_workspace(int nt, int d, int m, int mode);
+int rvgp_gp_prepare_local(const double* T, int n, int D, int ld, int d, const double* U, int m, const int* idx,
+                          int nt, const double* vec, int mode, double* C, double* b, double* yy, void* workspace,
+                          size_t ws_bytes, void* stream);
+/* predict_f(full_cov=False) mean and variance (nt x D each, the reshape of
+ * RVGP/main.py:114-116) at the test points idx from the lifted rows' local
+ * factors: Q = U_te (r ∘ L_A⁻ᵀ), then per point its d x d Gram of Q rows and
+ * the gauge's quadratic forms (d rows per point instead of D). */
+size_t rvgp_gp_predict_local_workspace(int nt, int d, int m, int mode);
+int rvgp_gp_predict_local(const double* T, int n, int D, int ld, int d, const double* U, int m, const int* idx,
+                          int nt, int mode, const double* state, double* mean, double* var, void* workspace,
+                          size_t ws_bytes, void* stream);
 /* predict_f(full_cov=False) mean and variance at Nte rows (RVGP/main.py:102-116). */
 size_t rvgp_gp_predict_workspace(long long Nte, int m, int mode);
 int rvgp_gp_predict(const double* Phi_star, const float* Phi_star32, long long Nte, int m, int mode,

@@ -56,6 +56,12 @@ SIGNATURES = {
                                               c_size_t, P]),
     "rvgp_gp_predict_workspace": (c_size_t, [ctypes.c_longlong, c_int, c_int]),
     "rvgp_gp_predict": (c_int, [P, P, ctypes.c_longlong, c_int, c_int, P, P, P, P, c_size_t, P]),
+    "rvgp_gp_prepare_local_workspace": (c_size_t, [c_int, c_int, c_int, c_int]),
+    "rvgp_gp_prepare_local": (c_int, [P, c_int, c_int, c_int, c_int, P, c_int, P, c_int, P, c_int, P, P, P, P,
+                                      c_size_t, P]),
+    "rvgp_gp_predict_local_workspace": (c_size_t, [c_int, c_int, c_int, c_int]),
+    "rvgp_gp_predict_local": (c_int, [P, c_int, c_int, c_int, c_int, P, c_int, P, c_int, c_int, P, P, P, P, c_size_t,
+                                      P]),
     "rvgp_sgpr_workspace": (c_size_t, [c_int, c_int]),
     "rvgp_sgpr_state_size": (c_size_t, [c_int]),
     "rvgp_sgpr_elbo": (c_int, [P, P, P, ctypes.c_longlong, c_int, P, c_int, P, c_double, P, c_int, c_double, P, P, P,
@@ -305,7 +311,7 @@ def eigsh(indptr, indices, vals64, vals32=None, m=10, mode="mixed", tol=None, to
 
 
 def tc_gram(A, B=None):
-    """Aᵀ B (FP64 out) on the tensor cores, split-TF32: A (N, p), B (N, q) FP32, p, q <= 256."""
+    """Aᵀ B (FP64 out) on the tensor cores, split-TF32: A (N, p), B (N, q) FP32, p, q <= 2048."""
     A = _dev(A, torch.float32, "A")
     B = A if B is None else _dev(B, torch.float32, "B")
     N, p = A.shape
@@ -318,7 +324,7 @@ def tc_gram(A, B=None):
 
 
 def tc_gemm(A, Bm):
-    """A (N, K) @ Bm (K, q) in FP32 on the tensor cores, split-TF32; K, q <= 256."""
+    """A (N, K) @ Bm (K, q) in FP32 on the tensor cores, split-TF32; K, q <= 2048."""
     A = _dev(A, torch.float32, "A")
     Bm = _dev(Bm, torch.float32, "Bm")
     N, K = A.shape
@@ -419,6 +425,48 @@ def gp_prepare(Phi, y, Phi32=None, mode="fp64"):
     check(L.rvgp_gp_prepare(ptr(Phi), ptr(Phi32), ptr(y), N, m, 1 if mode == "mixed" else 0, ptr(C), ptr(b), ptr(yy),
                             ptr(ws), ws.numel(), stream()), "rvgp_gp_prepare")
     return C, b, yy
+
+
+def gp_prepare_local(T, d, U, idx, vec, mode="fp64"):
+    """C = ΦᵀΦ, b = Φᵀy, yy = yᵀy of the lifted rows Φ_i = T_i U_i (and y_i the
+    D-vectors) of the points idx, from d rows per point (rvgp_gp_prepare_local)."""
+    T = _dev(T, torch.float64, "tangents")
+    U = _dev(U, torch.float64, "U")
+    vec = _dev(vec, torch.float64, "vectors")
+    n, D, ld = T.shape
+    m = U.shape[1]
+    idx = idx.to(torch.int32).contiguous()
+    nt = idx.numel()
+    dev = U.device
+    C = torch.empty((m, m), dtype=torch.float64, device=dev)
+    b = torch.empty(m, dtype=torch.float64, device=dev)
+    yy = torch.empty(1, dtype=torch.float64, device=dev)
+    imode = 1 if mode == "mixed" else 0
+    L = lib()
+    ws = workspace(L.rvgp_gp_prepare_local_workspace(nt, d, m, imode), dev)
+    check(L.rvgp_gp_prepare_local(ptr(T), n, D, ld, d, ptr(U), m, ptr(idx), nt, ptr(vec), imode, ptr(C), ptr(b),
+                                  ptr(yy), ptr(ws), ws.numel(), stream()), "rvgp_gp_prepare_local")
+    return C, b, yy
+
+
+def gp_predict_local(T, d, U, idx, state, mode="fp64"):
+    """Posterior mean and variance (len(idx), D) at the points idx from the
+    GP state, through the local factors of the lifted rows (rvgp_gp_predict_local)."""
+    T = _dev(T, torch.float64, "tangents")
+    U = _dev(U, torch.float64, "U")
+    n, D, ld = T.shape
+    m = U.shape[1]
+    idx = idx.to(torch.int32).contiguous()
+    nt = idx.numel()
+    dev = U.device
+    mean = torch.empty((nt, D), dtype=torch.float64, device=dev)
+    var = torch.empty((nt, D), dtype=torch.float64, device=dev)
+    imode = 1 if mode == "mixed" else 0
+    L = lib()
+    ws = workspace(L.rvgp_gp_predict_local_workspace(nt, d, m, imode), dev)
+    check(L.rvgp_gp_predict_local(ptr(T), n, D, ld, d, ptr(U), m, ptr(idx), nt, imode, ptr(state), ptr(mean),
+                                  ptr(var), ptr(ws), ws.numel(), stream()), "rvgp_gp_predict_local")
+    return mean, var
 
 
 class LMLWorkspace:

@@ -545,7 +545,7 @@ Layout carve(Workspace& ws, long long N, int p, int mode) {
   s.cn_ws = ws.take<char>(s.cn_bytes);
   s.tc = 0;
   s.tc_err = ws.take<int>(1);
-  s.tc_bytes = (mode == 1 && p <= 256) ? std::max(tc_gram_workspace(N, p, p), tc_gemm_workspace(p, p)) : 0;
+  s.tc_bytes = mode == 1 ? std::max(tc_gram_workspace(N, p, p), tc_gemm_workspace(p, p)) : 0;
   s.tc_ws = ws.take<char>(s.tc_bytes);
   return L;
 }

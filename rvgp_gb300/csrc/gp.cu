@@ -335,6 +335,187 @@ __global__ void lift_kernel(const double* __restrict__ T, int n, int D, int ld, 
   out[e] = s;
 }
 
+// ---------------------------------------------------------------- gauge-reduced rows
+// The lifted rows of one point i are Φ_i = T_i U_i (D x m: gauge T_i, D x d,
+// times the point's d rows U_i of the connection-Laplacian eigenvectors,
+// RVGP/dataclass.py:57-59).  Hence, with G_i = T_iᵀT_i = L_i L_iᵀ (d x d):
+//   Φ_iᵀΦ_i = (L_iᵀU_i)ᵀ(L_iᵀU_i),   Φ_iᵀy_i = (L_iᵀU_i)ᵀ(L_i⁻¹T_iᵀy_i),
+// so C = ΦᵀΦ and b = Φᵀy come exactly from d rows per point instead of D, and
+// yᵀy is summed over the full D-vectors.  kMaxLocalD bounds d.
+constexpr int kMaxLocalD = 8;
+
+// One warp per training point t (point i = idx[t]): L_t (d x d lower Cholesky
+// factor of T_iᵀT_i, row-major), yt[t*d + q] = (L_t⁻¹ T_iᵀ y_i)_q and
+// yyp[t] = |y_i|².  Lanes stride over the D coordinates; the d(d+1)/2 + d + 1
+// sums are reduced by shuffles in a fixed order.
+template <int d>
+__global__ void local_factor_kernel(const double* __restrict__ T, int D, int ld, const int* __restrict__ idx,
+                                    int nt, const double* __restrict__ vec, double* __restrict__ Lf,
+                                    double* __restrict__ yt, double* __restrict__ yyp) {
+  const int lane = threadIdx.x & 31;
+  const long long t = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  if (t >= nt) return;
+  const long long i = idx[t];
+  constexpr int NG = d * (d + 1) / 2;
+  double g[NG], ty[d], yy = 0.0;
+#pragma unroll
+  for (int e = 0; e < NG; ++e) g[e] = 0.0;
+#pragma unroll
+  for (int q = 0; q < d; ++q) ty[q] = 0.0;
+  for (int a = lane; a < D; a += 32) {
+    const double* Ta = T + ((size_t)i * D + a) * ld;
+    const double ya = vec ? vec[(size_t)i * D + a] : 0.0;
+#pragma unroll
+    for (int q = 0; q < d; ++q) {
+      const double tq = Ta[q];
+      ty[q] = fma(tq, ya, ty[q]);
+#pragma unroll
+      for (int r = 0; r <= q; ++r) g[q * (q + 1) / 2 + r] = fma(tq, Ta[r], g[q * (q + 1) / 2 + r]);
+    }
+    yy = fma(ya, ya, yy);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+    for (int e = 0; e < NG; ++e) g[e] += __shfl_xor_sync(0xffffffffu, g[e], o);
+#pragma unroll
+    for (int q = 0; q < d; ++q) ty[q] += __shfl_xor_sync(0xffffffffu, ty[q], o);
+    yy += __shfl_xor_sync(0xffffffffu, yy, o);
+  }
+  if (lane != 0) return;
+  // Cholesky of the packed lower triangle g (row q holds entries (q, 0..q))
+  double L[d][d];
+#pragma unroll
+  for (int q = 0; q < d; ++q)
+#pragma unroll
+    for (int r = 0; r < d; ++r) L[q][r] = 0.0;
+#pragma unroll
+  for (int q = 0; q < d; ++q) {
+#pragma unroll
+    for (int r = 0; r <= q; ++r) {
+      const int e = q * (q + 1) / 2 + r;
+      double s = g[e];
+      for (int k = 0; k < r; ++k) s -= L[q][k] * L[r][k];
+      if (r == q)
+        L[q][q] = sqrt(fmax(s, 0.0));
+      else
+        L[q][r] = s / L[r][r];
+    }
+  }
+  // forward solve L x = Tᵀy
+  for (int q = 0; q < d; ++q) {
+    double s = ty[q];
+    for (int k = 0; k < q; ++k) s -= L[q][k] * ty[k];
+    ty[q] = s / L[q][q];
+  }
+  for (int q = 0; q < d; ++q) {
+    for (int r = 0; r < d; ++r) Lf[((size_t)t * d + q) * d + r] = L[q][r];
+    if (yt) yt[(size_t)t * d + q] = ty[q];
+  }
+  if (yyp) yyp[t] = yy;
+}
+
+// Ut[(t*d + q), j] = Σ_{r >= q} L_t[r][q] U[(idx[t]*d + r), j]   (= (L_tᵀ U_i)[q][j])
+template <typename T>
+__global__ void local_rows_kernel(const double* __restrict__ U, int m, int d, const int* __restrict__ idx, int nt,
+                                  const double* __restrict__ Lf, T* __restrict__ Ut) {
+  const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e >= (long long)nt * d * m) return;
+  const long long row = e / m;
+  const int j = (int)(e % m);
+  const long long t = row / d;
+  const int q = (int)(row % d);
+  const double* Ui = U + (size_t)idx[t] * d * m + j;
+  const double* Lt = Lf + (size_t)t * d * d;
+  double s = 0.0;
+  for (int r = q; r < d; ++r) s = fma(Lt[r * d + q], Ui[(size_t)r * m], s);
+  Ut[e] = (T)s;
+}
+
+// Rows U[(idx[t]*d + q), :] of the test points (FP64 or FP32 copy).
+template <typename T>
+__global__ void gather_local_rows(const double* __restrict__ U, int m, int d, const int* __restrict__ idx, int nt,
+                                  T* __restrict__ out) {
+  const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e >= (long long)nt * d * m) return;
+  const long long row = e / m;
+  const int j = (int)(e % m);
+  out[e] = (T)U[((size_t)idx[row / d] * d + row % d) * m + j];
+}
+
+// Fixed-order sum of v[0..n) by one CTA of 1024 threads: *out = Σ v.
+__global__ void __launch_bounds__(1024) sum_fixed(const double* __restrict__ v, long long n, double* __restrict__ out) {
+  __shared__ double sh[1024];
+  double s = 0.0;
+  for (long long k = threadIdx.x; k < n; k += 1024) s += v[k];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = 512; w > 0; w >>= 1) {
+    if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = sh[0];
+}
+
+// Posterior at the test points from Q = U_te Bt (rows t*d + q): warp per test
+// point t (point i = idx[t]):
+//   μ_loc[q] = Σ_j U[(i*d + q), j] sp_j,   M[q][r] = Σ_k Q[t*d + q][k] Q[t*d + r][k]
+//   mean[t*D + a] = Σ_q T[i,a,q] μ_loc[q],  var[t*D + a] = Σ_{q,r} T[i,a,q] T[i,a,r] M[q][r]
+// which equal mean = Φ*sp and var = |L_A⁻¹ R φ*|² of the lifted rows φ* = t_aᵀU_i.
+template <int d, typename T>
+__global__ void predict_local_kernel(const double* __restrict__ Tg, int D, int ld, const double* __restrict__ U,
+                                     int m, const int* __restrict__ idx, int nt, const double* __restrict__ state,
+                                     const T* __restrict__ Q, double* __restrict__ mean, double* __restrict__ var) {
+  const int lane = threadIdx.x & 31;
+  const long long t = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  if (t >= nt) return;
+  const long long i = idx[t];
+  const double* sp = state + (size_t)m * m;
+  constexpr int NG = d * (d + 1) / 2;
+  double mu[d], M[NG];
+#pragma unroll
+  for (int q = 0; q < d; ++q) mu[q] = 0.0;
+#pragma unroll
+  for (int e = 0; e < NG; ++e) M[e] = 0.0;
+  const double* Ui = U + (size_t)i * d * m;
+  const T* Qt = Q + (size_t)t * d * m;
+  for (int j = lane; j < m; j += 32) {
+    const double s = sp[j];
+    double qv[d];
+#pragma unroll
+    for (int q = 0; q < d; ++q) {
+      mu[q] = fma(Ui[(size_t)q * m + j], s, mu[q]);
+      qv[q] = (double)Qt[(size_t)q * m + j];
+    }
+#pragma unroll
+    for (int q = 0; q < d; ++q)
+#pragma unroll
+      for (int r = 0; r <= q; ++r) M[q * (q + 1) / 2 + r] = fma(qv[q], qv[r], M[q * (q + 1) / 2 + r]);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+    for (int q = 0; q < d; ++q) mu[q] += __shfl_xor_sync(0xffffffffu, mu[q], o);
+#pragma unroll
+    for (int e = 0; e < NG; ++e) M[e] += __shfl_xor_sync(0xffffffffu, M[e], o);
+  }
+  for (int a = lane; a < D; a += 32) {
+    const double* Ta = Tg + ((size_t)i * D + a) * ld;
+    double tv[d], mv = 0.0, vv = 0.0;
+#pragma unroll
+    for (int q = 0; q < d; ++q) tv[q] = Ta[q];
+#pragma unroll
+    for (int q = 0; q < d; ++q) {
+      mv = fma(tv[q], mu[q], mv);
+#pragma unroll
+      for (int r = 0; r < q; ++r) vv = fma(2.0 * tv[q] * tv[r], M[q * (q + 1) / 2 + r], vv);
+      vv = fma(tv[q] * tv[q], M[q * (q + 1) / 2 + q], vv);
+    }
+    mean[(size_t)t * D + a] = mv;
+    var[(size_t)t * D + a] = vv;
+  }
+}
+
 // Bt[l][k] = r_l L_A⁻¹[k][l]   (so that Φ* Bt = (L_A⁻¹ R Φ*ᵀ)ᵀ)
 template <typename T>
 __global__ void make_Bt(const double* __restrict__ state, int m, T* __restrict__ Bt) {
@@ -605,6 +786,152 @@ RVGP_API int rvgp_gp_predict(const double* Phi_star, const float* Phi_star32, lo
     rvgp::note_launch(); predict_rows<double><<<ceil_div(Nte * 32, 256), 256, 0, st>>>(Phi_star, Nte, m, state, P, mean, var);
   }
   RVGP_LAUNCH_CHECK("rvgp_gp_predict");
+  return RVGP_OK;
+}
+
+#define RVGP_LOCAL_D_DISPATCH(d, F) \
+  switch (d) {                      \
+    case 1: F(1); break;            \
+    case 2: F(2); break;            \
+    case 3: F(3); break;            \
+    case 4: F(4); break;            \
+    case 5: F(5); break;            \
+    case 6: F(6); break;            \
+    case 7: F(7); break;            \
+    default: F(8); break;           \
+  }
+
+namespace {
+struct LocalPrepareBufs {
+  double *Lf, *yt, *yyp, *Ut;
+  float* Ut32;
+  void* gram_ws;
+  size_t gram_bytes;
+  double* part;
+};
+LocalPrepareBufs carve_local_prepare(Workspace& ws, int nt, int d, int m, int mode) {
+  LocalPrepareBufs B;
+  const long long rows = (long long)nt * d;
+  B.Lf = ws.take<double>((size_t)nt * d * d);
+  B.yt = ws.take<double>((size_t)rows);
+  B.yyp = ws.take<double>((size_t)std::max(nt, 1));
+  B.Ut = ws.take<double>((size_t)rows * m);
+  B.Ut32 = mode == 1 ? ws.take<float>((size_t)rows * m) : nullptr;
+  B.gram_bytes = mode == 1 ? gram_workspace<float>(rows, m, m) : gram_workspace<double>(rows, m, m);
+  B.gram_ws = ws.take<char>(B.gram_bytes);
+  B.part = ws.take<double>((size_t)phity_chunks(rows) * (m + 1));
+  return B;
+}
+}  // namespace
+
+RVGP_API size_t rvgp_gp_prepare_local_workspace(int nt, int d, int m, int mode) {
+  Workspace ws(nullptr, 0);
+  carve_local_prepare(ws, nt, d, m, mode);
+  return ws.used + 256;
+}
+
+// C = ΦᵀΦ (m x m), b = Φᵀy (m) and yy = yᵀy for the lifted rows Φ of the
+// training points idx (nt) without forming them: Φ_i = T_i U_i (gauges T,
+// n x D x ld with d <= ld used columns; U, n*d x m, the eigenvectors of the
+// connection Laplacian in local coordinates; vectors vec, n x D).  Per point
+// the d x d Cholesky factor L_i of T_iᵀT_i gives the d rows L_iᵀU_i and the
+// targets L_i⁻¹T_iᵀy_i whose Gram and products are exactly ΦᵀΦ and Φᵀy
+// (RVGP/main.py:24-50 forms the D rows per point; the GP algebra only needs
+// these three sums).  mode 1 forms C from FP32 rows with FP64-reduced partial
+// sums; b and yy are FP64 in both modes.  Stream-ordered, no synchronisation.
+RVGP_API int rvgp_gp_prepare_local(const double* T, int n, int D, int ld, int d, const double* U, int m,
+                                   const int* idx, int nt, const double* vec, int mode, double* C, double* b,
+                                   double* yy, void* workspace, size_t ws_bytes, void* stream) {
+  RVGP_CHECK_ARG(T && U && idx && vec && C && b && yy, "rvgp_gp_prepare_local: null pointer");
+  RVGP_CHECK_ARG(n >= 1 && D >= 1 && m >= 1 && nt >= 1 && d >= 1 && d <= ld && d <= D && d <= kMaxLocalD,
+                 "rvgp_gp_prepare_local: bad sizes (d must be in [1, min(ld, D, %d)])", kMaxLocalD);
+  RVGP_CHECK_ARG(mode == 0 || mode == 1, "rvgp_gp_prepare_local: mode must be 0 or 1");
+  RVGP_CHECK_ARG(workspace && ws_bytes >= rvgp_gp_prepare_local_workspace(nt, d, m, mode),
+                 "rvgp_gp_prepare_local: workspace too small");
+  cudaStream_t st = as_stream(stream);
+  Workspace ws(workspace, ws_bytes);
+  LocalPrepareBufs B = carve_local_prepare(ws, nt, d, m, mode);
+  const long long rows = (long long)nt * d;
+  const int wb = ceil_div((long long)nt * 32, 256);
+#define RVGP_LF(DD) local_factor_kernel<DD><<<wb, 256, 0, st>>>(T, D, ld, idx, nt, vec, B.Lf, B.yt, B.yyp)
+  rvgp::note_launch();
+  RVGP_LOCAL_D_DISPATCH(d, RVGP_LF)
+#undef RVGP_LF
+  rvgp::note_launch();
+  local_rows_kernel<double><<<ceil_div(rows * m, 256), 256, 0, st>>>(U, m, d, idx, nt, B.Lf, B.Ut);
+  int rc;
+  if (mode == 1) {
+    rvgp::note_launch();
+    local_rows_kernel<float><<<ceil_div(rows * m, 256), 256, 0, st>>>(U, m, d, idx, nt, B.Lf, B.Ut32);
+    rc = gram_f32_out64(B.Ut32, m, B.Ut32, m, rows, m, m, C, m, 1.0, 0.0, B.gram_ws, B.gram_bytes, st);
+  } else {
+    rc = gram<double>(B.Ut, m, B.Ut, m, rows, m, m, C, m, 1.0, 0.0, B.gram_ws, B.gram_bytes, st);
+  }
+  if (rc) return rc;
+  const int nc = phity_chunks(rows);
+  const long long chunk = (rows + nc - 1) / nc;
+  rvgp::note_launch();
+  phity_partial<<<dim3(nc, ceil_div(m + 1, 32)), 256, 0, st>>>(B.Ut, B.yt, rows, m, chunk, B.part);
+  rvgp::note_launch();
+  phity_final<<<ceil_div(m + 1, 256), 256, 0, st>>>(B.part, nc, m, b, yy);  // yy: |L⁻¹Tᵀy|², replaced next
+  rvgp::note_launch();
+  sum_fixed<<<1, 1024, 0, st>>>(B.yyp, nt, yy);
+  RVGP_LAUNCH_CHECK("rvgp_gp_prepare_local");
+  return RVGP_OK;
+}
+
+RVGP_API size_t rvgp_gp_predict_local_workspace(int nt, int d, int m, int mode) {
+  const size_t s = mode == 1 ? sizeof(float) : sizeof(double);
+  return s * (2 * (size_t)nt * d * m + (size_t)m * m) + 1024;
+}
+
+// Posterior mean and marginal variance (each nt x D, rows = test points idx,
+// columns = ambient coordinates, as RVGP/main.py:102-116 reshapes them) from
+// the state of the last likelihood evaluation, without forming the lifted
+// rows: Q = U_te Bt (rows of U at the test points times r ∘ L_A⁻ᵀ), then per
+// point the d x d Gram of its Q rows and the gauge's quadratic forms.  mode 1
+// forms Q in FP32.  Stream-ordered, no synchronisation.
+RVGP_API int rvgp_gp_predict_local(const double* T, int n, int D, int ld, int d, const double* U, int m,
+                                   const int* idx, int nt, int mode, const double* state, double* mean, double* var,
+                                   void* workspace, size_t ws_bytes, void* stream) {
+  RVGP_CHECK_ARG(T && U && idx && state && mean && var, "rvgp_gp_predict_local: null pointer");
+  RVGP_CHECK_ARG(n >= 1 && D >= 1 && m >= 1 && nt >= 0 && d >= 1 && d <= ld && d <= D && d <= kMaxLocalD,
+                 "rvgp_gp_predict_local: bad sizes");
+  RVGP_CHECK_ARG(mode == 0 || mode == 1, "rvgp_gp_predict_local: mode must be 0 or 1");
+  RVGP_CHECK_ARG(workspace && ws_bytes >= rvgp_gp_predict_local_workspace(nt, d, m, mode),
+                 "rvgp_gp_predict_local: workspace too small");
+  if (nt == 0) return RVGP_OK;
+  cudaStream_t st = as_stream(stream);
+  Workspace ws(workspace, ws_bytes);
+  const long long rows = (long long)nt * d, mm = (long long)m * m;
+  const int wb = ceil_div((long long)nt * 32, 256);
+  int rc;
+  if (mode == 1) {
+    float* Bt = ws.take<float>(mm);
+    float* Ut = ws.take<float>((size_t)rows * m);
+    float* Q = ws.take<float>((size_t)rows * m);
+    rvgp::note_launch(); make_Bt<float><<<ceil_div(mm, 256), 256, 0, st>>>(state, m, Bt);
+    rvgp::note_launch(); gather_local_rows<float><<<ceil_div(rows * m, 256), 256, 0, st>>>(U, m, d, idx, nt, Ut);
+    rc = gemm_nn<float>(Ut, m, Bt, m, rows, m, m, Q, m, 1.f, 0.f, st);
+    if (rc) return rc;
+#define RVGP_PL(DD) predict_local_kernel<DD, float><<<wb, 256, 0, st>>>(T, D, ld, U, m, idx, nt, state, Q, mean, var)
+    rvgp::note_launch();
+    RVGP_LOCAL_D_DISPATCH(d, RVGP_PL)
+#undef RVGP_PL
+  } else {
+    double* Bt = ws.take<double>(mm);
+    double* Ut = ws.take<double>((size_t)rows * m);
+    double* Q = ws.take<double>((size_t)rows * m);
+    rvgp::note_launch(); make_Bt<double><<<ceil_div(mm, 256), 256, 0, st>>>(state, m, Bt);
+    rvgp::note_launch(); gather_local_rows<double><<<ceil_div(rows * m, 256), 256, 0, st>>>(U, m, d, idx, nt, Ut);
+    rc = gemm_nn<double>(Ut, m, Bt, m, rows, m, m, Q, m, 1.0, 0.0, st);
+    if (rc) return rc;
+#define RVGP_PL(DD) predict_local_kernel<DD, double><<<wb, 256, 0, st>>>(T, D, ld, U, m, idx, nt, state, Q, mean, var)
+    rvgp::note_launch();
+    RVGP_LOCAL_D_DISPATCH(d, RVGP_PL)
+#undef RVGP_PL
+  }
+  RVGP_LAUNCH_CHECK("rvgp_gp_predict_local");
   return RVGP_OK;
 }
 

@@ -34,6 +34,8 @@
 #include "linalg.cuh"
 #include "chol32.cuh"
 #include <math.h>
+#include <stdlib.h>
+#include <algorithm>
 #include <float.h>
 
 namespace rvgp {
@@ -489,13 +491,21 @@ __global__ void to_f32(const double* __restrict__ in, long long n, float* __rest
 
 using namespace rvgp;
 
+namespace rvgp {
+int gp_fit_cluster_max_m();
+int gp_fit_cluster_launch(const float* C32, const double* C, const double* b, const double* yy, long long N, int m,
+                          const double* evals, double n_rows, int typ, const double* theta0, const double* lower_dev,
+                          const int* mask_dev, int steps, double lr, double beta1, double beta2, double eps,
+                          double* theta_out, double* hist, int* status, cudaStream_t st);
+}  // namespace rvgp
+
 extern "C" size_t rvgp_gp_lml_workspace(int m);
 extern "C" int rvgp_gp_lml(const double* C, const double* b, const double* yy, long long N, int m,
                            const double* evals, double n_rows, int typ, const double* theta, double* out,
                            double* state, void* workspace, size_t ws_bytes, void* stream);
 
 // Largest m whose working set fits one SM's shared memory.
-RVGP_API int rvgp_gp_fit_mixed_max_m(void) {
+static int one_cta_max_m() {
   int dev = 0, optin = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return 0;
   if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return 0;
@@ -503,6 +513,10 @@ RVGP_API int rvgp_gp_fit_mixed_max_m(void) {
   while (layout(m + 1).total + 512 <= (size_t)optin) ++m;  // + the kernel's static shared memory
   return m;
 }
+
+// Largest m of the mixed fit: one CTA up to one SM's shared memory, then one
+// thread-block cluster with the matrix spread over its CTAs (gp_cluster.cu).
+RVGP_API int rvgp_gp_fit_mixed_max_m(void) { return std::max(one_cta_max_m(), gp_fit_cluster_max_m()); }
 
 RVGP_API size_t rvgp_gp_fit_mixed_workspace(int m) {
   return rvgp_gp_lml_workspace(m) + sizeof(float) * (size_t)m * m + 4 * sizeof(double) + 3 * 256 + 64;
@@ -549,6 +563,16 @@ RVGP_API int rvgp_gp_fit_adam_mixed_launch(const double* C, const double* b, con
   cudaMemcpyAsync(f.dm, mask, 4 * sizeof(int), cudaMemcpyHostToDevice, st);
   rvgp::note_launch();
   to_f32<<<ceil_div((long long)m * m, 256), 256, 0, st>>>(C, (long long)m * m, f.C32);
+  // RVGP_GP_FIT_CLUSTER=1 selects the cluster kernel wherever it applies (tests)
+  const char* force = getenv("RVGP_GP_FIT_CLUSTER");
+  const bool cluster = m > one_cta_max_m() || (force && force[0] == '1' && m > 32 && m <= gp_fit_cluster_max_m());
+  if (cluster) {
+    const int rc = gp_fit_cluster_launch(f.C32, C, b, yy, N, m, evals, n_rows, typ, theta0, f.dl, f.dm, steps, lr,
+                                         beta1, beta2, eps, theta_out, hist, f.dstat, st);
+    if (rc != RVGP_OK) return rc;
+    RVGP_LAUNCH_CHECK("rvgp_gp_fit_adam_mixed");
+    return RVGP_OK;
+  }
   const size_t smem = layout(m).total;
   if (cudaFuncSetAttribute(gp_fit_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
     set_error("rvgp_gp_fit_adam_mixed: cannot reserve %zu bytes of shared memory", smem);

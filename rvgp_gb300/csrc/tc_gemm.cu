@@ -3,15 +3,17 @@
 // x = hi + lo, hi = tf32(x), lo = x - hi, and A B ~ Ahi Bhi + Ahi Blo + Alo Bhi
 // (the dropped Alo Blo and the TF32 truncation of lo are ~2^-21 relative).
 //
-//   tc_gram_f32_out64 : C (p x q, FP64) = Aᵀ B for tall A (N x p), B (N x q),
-//                       p, q <= 256.  CTA = (128-row tile of C, split of the
-//                       N rows); FP32 partials in TMEM, summed over the
-//                       splits in FP64 (the Gram matrices of the Cholesky QR
-//                       and Rayleigh-Ritz steps).  For Aᵀ A the row slabs
-//                       are bulk-copied by the TMA engine and converted from
-//                       shared memory.
-//   tc_gemm_f32       : C (N x q) = A (N x K) Bm (K x q), K, q <= 256.  CTA =
-//                       128-row tile of A and C (block rotations V Q, W Q).
+//   tc_gram_f32_out64 : C (p x q, FP64) = Aᵀ B for tall A (N x p), B (N x q).
+//                       CTA = (128-row tile of C, split of the N rows); FP32
+//                       partials in TMEM, summed over the splits in FP64 (the
+//                       Gram matrices of the Cholesky QR and Rayleigh-Ritz
+//                       steps).  For Aᵀ A with p <= 256 the row slabs are
+//                       bulk-copied by the TMA engine and converted from
+//                       shared memory; wider products run as column blocks
+//                       of C (at most 256 columns, one TMEM accumulator).
+//   tc_gemm_f32       : C (N x q) = A (N x K) Bm (K x q).  CTA = 128-row tile
+//                       of A and C (block rotations V Q, W Q); K streams in
+//                       slabs, q > 256 runs as column blocks of C.
 //
 // Both stream 32-wide K slabs through a two-stage shared-memory pipeline
 // (even slabs accumulate in one TMEM accumulator, odd slabs in another):
@@ -454,24 +456,48 @@ bool tc_enabled() {
   return !(e && e[0] == '0');
 }
 
+// Products wider than one accumulator (256 FP32 columns) run as column blocks
+// of at most kColBlock output columns; K (the summed dimension) and the rows
+// of the Gram's first operand are not limited.
+constexpr int kColBlock = 256;
+constexpr int kMaxWidth = 2048;
+
 bool tc_supported(int p, int q) {
   int dev = 0, optin = 0;
-  if (p < 1 || q < 1 || p > 256 || q > 256) return false;
+  if (p < 1 || q < 1 || p > kMaxWidth || q > kMaxWidth) return false;
   if (cudaGetDevice(&dev) != cudaSuccess) return false;
   if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return false;
-  return gram_smem(true, p, q) <= (size_t)optin && gram_smem(false, p, q) <= (size_t)optin &&
-         gemm_smem(q) <= (size_t)optin;
+  const int pb = std::min(p, kColBlock), qb = std::min(q, kColBlock);
+  return gram_smem(true, pb, qb) <= (size_t)optin && gram_smem(false, pb, qb) <= (size_t)optin &&
+         gemm_smem(qb) <= (size_t)optin;
 }
 
 size_t tc_gram_workspace(long long N, int p, int q) {
   const GramPlan g = gram_plan(N, p);
-  return sizeof(float) * (size_t)g.splits * p * q + 512;
+  return sizeof(float) * (size_t)g.splits * p * std::min(q, kColBlock) + 512;
 }
+
+static int tc_gram_block(const float* A, int lda, const float* B, int ldb, long long N, int p, int q, double* C,
+                         int ldc, int* err, void* ws, size_t ws_bytes, cudaStream_t st);
 
 int tc_gram_f32_out64(const float* A, int lda, const float* B, int ldb, long long N, int p, int q, double* C, int ldc,
                       int* err, void* ws, size_t ws_bytes, cudaStream_t st) {
-  RVGP_CHECK_ARG(p >= 1 && q >= 1 && p <= 256 && q <= 256 && N >= 1, "tc_gram: p=%d q=%d out of range", p, q);
+  RVGP_CHECK_ARG(p >= 1 && q >= 1 && p <= kMaxWidth && q <= kMaxWidth && N >= 1, "tc_gram: p=%d q=%d out of range",
+                 p, q);
   RVGP_CHECK_ARG(ws && ws_bytes >= tc_gram_workspace(N, p, q), "tc_gram: workspace too small");
+  if (p <= kColBlock && q <= kColBlock) return tc_gram_block(A, lda, B, ldb, N, p, q, C, ldc, err, ws, ws_bytes, st);
+  // column blocks of C (the split partials of one block are reduced before the
+  // next block reuses the workspace, in stream order); the first operand's
+  // 128-row tiles span all of p, so every block runs the two-operand kernel
+  for (int j0 = 0; j0 < q; j0 += kColBlock) {
+    const int qb = std::min(kColBlock, q - j0);
+    TRY_RC(tc_gram_block(A, lda, B + j0, ldb, N, p, qb, C + j0, ldc, err, ws, ws_bytes, st));
+  }
+  return RVGP_OK;
+}
+
+static int tc_gram_block(const float* A, int lda, const float* B, int ldb, long long N, int p, int q, double* C,
+                         int ldc, int* err, void* ws, size_t ws_bytes, cudaStream_t st) {
   const GramPlan g = gram_plan(N, p);
   float* part = static_cast<float*>(ws);
   const bool same = (A == B && lda == ldb && p == q);
@@ -502,23 +528,30 @@ int tc_gram_f32_out64(const float* A, int lda, const float* B, int ldb, long lon
 }
 
 size_t tc_gemm_workspace(int K, int q) {
-  return (size_t)ceil_div(K, kSlab) * 2 * pad16(q) * 128 + 512;
+  return (size_t)ceil_div(K, kSlab) * 2 * pad16(std::min(q, kColBlock)) * 128 + 512;
 }
 
 int tc_gemm_f32(const float* A, int lda, long long N, int K, const float* Bm, int ldb, int q, float* C, int ldc,
                 int* err, void* ws, size_t ws_bytes, cudaStream_t st) {
-  RVGP_CHECK_ARG(K >= 1 && q >= 1 && K <= 256 && q <= 256 && N >= 1, "tc_gemm: K=%d q=%d out of range", K, q);
+  RVGP_CHECK_ARG(K >= 1 && q >= 1 && K <= kMaxWidth && q <= kMaxWidth && N >= 1, "tc_gemm: K=%d q=%d out of range",
+                 K, q);
   RVGP_CHECK_ARG(ws && ws_bytes >= tc_gemm_workspace(K, q), "tc_gemm: workspace too small");
   RVGP_CHECK_ARG((uintptr_t)A % 16 == 0, "tc_gemm: A must be 16-byte aligned");
-  const int Npad = pad16(q), kslabs = ceil_div(K, kSlab);
-  uint8_t* img = static_cast<uint8_t*>(ws);
-  rvgp::note_launch();
-  build_bimg<<<ceil_div((long long)kslabs * Npad * 8, 256), 256, 0, st>>>(Bm, ldb, K, q, Npad, kslabs, img);
-  const size_t smem = gemm_smem(q);
-  TRY_RC(set_smem((const void*)tc_gemm_kernel, smem, "tc_gemm"));
-  rvgp::note_launch();
-  tc_gemm_kernel<<<ceil_div(N, kTileM), kThreads, smem, st>>>(A, lda, N, K, img, Npad, q, C, ldc, err);
-  RVGP_LAUNCH_CHECK("tc_gemm");
+  // output column blocks of at most 256 (one accumulator each); the B image
+  // of a block is rebuilt in the workspace after the previous block's kernel
+  // (stream order)
+  for (int j0 = 0; j0 < q; j0 += kColBlock) {
+    const int qb = std::min(kColBlock, q - j0);
+    const int Npad = pad16(qb), kslabs = ceil_div(K, kSlab);
+    uint8_t* img = static_cast<uint8_t*>(ws);
+    rvgp::note_launch();
+    build_bimg<<<ceil_div((long long)kslabs * Npad * 8, 256), 256, 0, st>>>(Bm + j0, ldb, K, qb, Npad, kslabs, img);
+    const size_t smem = gemm_smem(qb);
+    TRY_RC(set_smem((const void*)tc_gemm_kernel, smem, "tc_gemm"));
+    rvgp::note_launch();
+    tc_gemm_kernel<<<ceil_div(N, kTileM), kThreads, smem, st>>>(A, lda, N, K, img, Npad, qb, C + j0, ldc, err);
+    RVGP_LAUNCH_CHECK("tc_gemm");
+  }
   return RVGP_OK;
 }
 

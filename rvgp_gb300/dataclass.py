@@ -136,15 +136,17 @@ class data:
                                                                mode=mode, tol=eig_tol, seed=seed + 1,
                                                                scale=math.sqrt(n * dim), perm=dev.perm)
                 del o64, o32
-                dev.evecs_Lc = _core.lift(T, dim, U)
         except BaseException:
             if self._eig_L["thread"] is not None:
                 self._eig_L["thread"].join()
             raise
         caller.wait_stream(hp)
-        for t_ in (dev.evals_Lc, U, dev.evecs_Lc):
+        for t_ in (dev.evals_Lc, U):
             t_.record_stream(caller)  # allocated on hp, used on the caller's stream
+        # The ambient (lifted) eigenvectors evecs_Lc = T_i U_i (n*D x m) are
+        # formed on first use: the GP works on U and the gauges directly.
         dev.evecs_Lc_local = U
+        dev.evecs_Lc = None
         mark("eigsh_Lc")
         self._dev = dev
         if timings is not None:
@@ -158,6 +160,14 @@ class data:
         self.n_eigenpairs = m
         self._host = {}
         self.vectors = vectors
+
+    def _evecs_Lc_dev(self):
+        """The lifted eigenvectors (n*D, m) on the device (RVGP/dataclass.py:57-59),
+        formed on first use from the gauges and the local eigenvectors."""
+        d = self._dev
+        if getattr(d, "evecs_Lc", None) is None:
+            d.evecs_Lc = _core.lift(d.T, self.dim_man, d.evecs_Lc_local)
+        return d.evecs_Lc
 
     # ------------------------------------------------------------------ the concurrent eigensolve of L
     @staticmethod
@@ -340,7 +350,7 @@ class data:
 
     @property
     def evecs_Lc(self):
-        return self._cached("evecs_Lc", lambda: self._dev.evecs_Lc.cpu().numpy())
+        return self._cached("evecs_Lc", lambda: self._evecs_Lc_dev().cpu().numpy())
 
     @property
     def G(self):

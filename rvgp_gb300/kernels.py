@@ -80,9 +80,9 @@ class ManifoldKernel:
 
     def __init__(self, data, nu=3, kappa=4, sigma_f=1, typ="matern", dtype=np.float64):
         dev = data._dev
-        self.eigenvectors = dev.evecs_Lc       # (n*D, m) CUDA f64
+        self.data = data
         self.eigenvalues = dev.evals_Lc        # (m,) CUDA f64
-        self.num_verticies = float(self.eigenvectors.shape[0])
+        self.num_verticies = float(dev.X.shape[0] * dev.X.shape[1])  # rows of evecs_Lc: n * D
         self.dtype = dtype
         self.typ = typ
         if typ not in ("se", "matern"):
@@ -91,6 +91,11 @@ class ManifoldKernel:
         self.kappa = Parameter(kappa, name="kappa")
         self.sigma_f = Parameter(sigma_f, name="sigma_f")
         self.device = self.eigenvalues.device
+
+    @property
+    def eigenvectors(self):
+        """The lifted eigenvectors evecs_Lc, (n*D, m) CUDA f64 (formed on first use)."""
+        return self.data._evecs_Lc_dev()
 
     @property
     def parameters(self):

@@ -100,10 +100,13 @@ class manifold_GPR:
             raise ValueError("the data object has no vectors to fit")
         self.D = dev.X.shape[1]
         idx = torch.as_tensor(np.asarray(train_points, dtype=np.int32), device=dev.X.device)
-        Phi, Phi32, y = _core.gather_rows(kernel.eigenvectors, self.D, idx, vec=dev.vectors,
-                                          want32=(precision == "mixed"))
-        self.C, self.b, self.yy = _core.gp_prepare(Phi, y, Phi32, precision)
-        self.N = Phi.shape[0]
+        # C = ΦᵀΦ, b = Φᵀy and yᵀy of the rows (training point, coordinate)
+        # of RVGP/main.py:24-50, from the gauges and local eigenvectors: the
+        # lifted rows Φ_i = T_i U_i are never formed (d rows per point, not D)
+        geo = kernel.data
+        self.C, self.b, self.yy = _core.gp_prepare_local(geo._dev.T, geo.dim_man, geo._dev.evecs_Lc_local, idx,
+                                                         dev.vectors, precision)
+        self.N = idx.numel() * self.D
         self.m = kernel.eigenvalues.numel()
         self.work = _core.LMLWorkspace(self.m, dev.X.device)
         self.n_evals = 0
@@ -220,9 +223,10 @@ class manifold_GPR:
     def predict_points(self, points):
         """Posterior mean and variance at manifold points (indices), each (len, D), on the device."""
         idx = torch.as_tensor(np.asarray(points, dtype=np.int32), device=self.kernel.device)
-        Phi, _, _ = _core.gather_rows(self.kernel.eigenvectors, self.D, idx)
-        mean, var = self._predict_rows(Phi)
-        return mean.reshape(-1, self.D), var.reshape(-1, self.D)
+        self._evaluate()  # posterior state at the current parameters
+        geo = self.kernel.data
+        return _core.gp_predict_local(geo._dev.T, geo.dim_man, geo._dev.evecs_Lc_local, idx, self.work.state,
+                                      self.precision)
 
     def predict_fields(self, fields, points):
         """Posterior means (B, len(points), D) and log marginal likelihoods (B,)

@@ -18,7 +18,7 @@ import numpy as np
 from scipy.spatial import KDTree
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = "/root/reference"
+REF = os.environ.get("RVGP_REFERENCE", "/root/reference")
 
 
 def reference_features():

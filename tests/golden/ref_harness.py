@@ -6,7 +6,11 @@ TensorFlow and GPflow are absent, so three harness-side shims are installed;
 no reference file is edited:
 
 1. a stub ``tensorflow`` with ``float64`` and ``convert_to_tensor`` returning an
-   ndarray subclass that has ``.numpy()`` (used by ``RVGP/geometry.py:7,77-78``);
+   ndarray subclass that has ``.numpy()`` (used by ``RVGP/geometry.py:7,77-78``),
+   and numpy-backed ``pow``, ``multiply``, ``reduce_sum``, ``exp``,
+   ``transpose``, ``cast``, ``shape`` and ``linalg.tensor_diag_part`` (every
+   TensorFlow operation of ``RVGP/kernels.py:41-67``), so the reference's own
+   ``ManifoldKernel`` runs in FP64;
 2. a stub ``gpflow`` exposing the names ``RVGP/kernels.py`` and ``RVGP/main.py``
    touch at import time;
 3. ``ptu_dijkstra.nx`` is wrapped so ``adjacency_matrix`` returns int32 CSR
@@ -33,6 +37,14 @@ def _install_stubs():
         tf = types.ModuleType("tensorflow")
         tf.float64 = np.float64
         tf.convert_to_tensor = lambda x, dtype=None: np.asarray(x, dtype=dtype).view(_TFArray)
+        tf.pow = lambda x, y: np.power(np.asarray(x, dtype=np.float64), y)
+        tf.multiply = lambda x, y: np.multiply(x, y)
+        tf.reduce_sum = lambda x: np.sum(x)
+        tf.exp = lambda x: np.exp(np.asarray(x, dtype=np.float64))
+        tf.transpose = lambda x: np.transpose(x)
+        tf.cast = lambda x, dtype=None: np.asarray(x, dtype=dtype)
+        tf.shape = lambda x: np.asarray(np.shape(x))
+        tf.linalg = types.SimpleNamespace(tensor_diag_part=lambda x: np.diagonal(x).copy())
         sys.modules["tensorflow"] = tf
     if "gpflow" not in sys.modules:
         gp = types.ModuleType("gpflow")
@@ -49,6 +61,13 @@ def _install_stubs():
         gp.optimizers = types.SimpleNamespace(Scipy=None)
         gp.set_trainable = lambda *a, **k: None
         sys.modules["gpflow"] = gp
+
+
+def load_reference_kernels():
+    """Return the reference's ``RVGP.kernels`` module (TensorFlow/GPflow stubbed)."""
+    load_reference()
+    from RVGP import kernels
+    return kernels
 
 
 def load_reference():

@@ -1,5 +1,7 @@
 """GPU: the tensor-core (tcgen05, split-TF32) tall products against FP64
-torch: Gram matrices Aᵀ B and block products A Bm, FP32-level accuracy."""
+torch: Gram matrices Aᵀ B and block products A Bm, FP32-level accuracy,
+including widths beyond one 256-column accumulator (column blocks) and K
+beyond 256."""
 import numpy as np
 import pytest
 import torch
@@ -16,7 +18,8 @@ def core():
 
 @pytest.mark.parametrize("N,p,q,same", [(1000, 228, 228, True), (40000, 228, 228, True), (5000, 100, 60, False),
                                         (333, 256, 256, True), (7, 20, 36, False), (40000, 228, 228, False),
-                                        (20001, 129, 129, True)])
+                                        (20001, 129, 129, True), (30000, 564, 564, True), (5000, 300, 257, False),
+                                        (2000, 700, 100, False), (777, 257, 600, False)])
 def test_tc_gram(core, N, p, q, same):
     g = torch.Generator(device="cuda").manual_seed(N + p)
     A = torch.randn((N, p), device="cuda", generator=g) * torch.logspace(-3, 2, p, device="cuda")
@@ -28,7 +31,8 @@ def test_tc_gram(core, N, p, q, same):
     assert err < 3e-6, err
 
 
-@pytest.mark.parametrize("N,K,q", [(40000, 228, 228), (1000, 50, 30), (129, 256, 256), (5, 3, 17), (20000, 228, 200)])
+@pytest.mark.parametrize("N,K,q", [(40000, 228, 228), (1000, 50, 30), (129, 256, 256), (5, 3, 17), (20000, 228, 200),
+                                   (30000, 564, 564), (1000, 300, 20), (513, 40, 700)])
 def test_tc_gemm(core, N, K, q):
     g = torch.Generator(device="cuda").manual_seed(N + K)
     A = torch.randn((N, K), device="cuda", generator=g)

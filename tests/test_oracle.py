@@ -257,3 +257,25 @@ def test_knn_kdtree_timing_form_matches(name):
     g = load_golden(name)
     X, k = g["X"], int(g["k"])
     np.testing.assert_array_equal(np.sort(O.knn_kdtree(X, k), 1), np.sort(O.knn(X, k), 1))
+
+
+def test_spectral_kernel_pinned_to_reference_kernels_py():
+    """eval_S, K and K_diag of the oracle equal the reference's own
+    ManifoldKernel (RVGP/kernels.py:41-67, run through the numpy-backed
+    TensorFlow stub by tests/golden/make_kernel_golden.py)."""
+    from conftest import load_golden
+    kg = load_golden("kernel")
+    for name in ("sphere", "torus", "ellipsoid", "swissroll64"):
+        g = load_golden(name)
+        n_rows = float(kg[f"{name}_n_rows"])
+        ev = g["evecs_Lc"] if "evecs_Lc" in g else O.lift(g["gauges"], g["evecs_Lc_local"], g["evals_Lc"].size)
+        X, X2 = ev[kg[f"{name}_rows"]], ev[kg[f"{name}_rows2"]]
+        for c, typ in enumerate(kg["params_typ"]):
+            nu, kappa, sf = kg["params"][c]
+            key = f"{name}_{c}"
+            S = O.eval_S(g["evals_Lc"], nu, kappa, sf, n_rows, str(typ))
+            np.testing.assert_allclose(S, kg[key + "_S"], rtol=1e-13)
+            np.testing.assert_allclose(O.kernel_K(X, S), kg[key + "_K"], rtol=1e-12, atol=1e-12 * np.abs(kg[key + "_K"]).max())
+            np.testing.assert_allclose(O.kernel_K(X, S, X2), kg[key + "_K2"], rtol=1e-12,
+                                       atol=1e-12 * np.abs(kg[key + "_K2"]).max())
+            np.testing.assert_allclose(np.einsum("ij,ij->i", X * S, X), kg[key + "_Kdiag"], rtol=1e-12)
