@@ -113,6 +113,36 @@ def knn_kdtree(X, k):
     return out
 
 
+def knn_gemm(X, k, rows=None, chunk=2000, threads=None):
+    """k nearest neighbours by brute force with the squared distances from
+    the expansion |x|² + |y|² - 2 x·y (one matrix product per chunk of
+    queries), the method sklearn's ``kneighbors_graph`` uses for
+    high-dimensional points (RVGP/geometry.py:103-110; sklearn's 'auto' picks
+    brute force above 15 dimensions).  The timing form of the CPU baseline at
+    D = 64; ties may order differently from ``knn`` (FP64 rounding of the
+    expansion).  ``rows``: query subset (default all points); chunks run on
+    ``threads`` host threads (default all cores).  Returns int32 (len(rows), k)."""
+    import os
+    from concurrent.futures import ThreadPoolExecutor
+    X = np.ascontiguousarray(X, dtype=np.float64)
+    n = X.shape[0]
+    if k >= n:
+        raise ValueError(f"Expected n_neighbors < n_samples, got {k} >= {n}")
+    q = np.arange(n) if rows is None else np.asarray(rows)
+    xx = np.einsum("ij,ij->i", X, X)
+
+    def one(s):
+        r = q[s:s + chunk]
+        D2 = xx[r, None] + xx[None, :] - 2.0 * (X[r] @ X.T)
+        D2[np.arange(len(r)), r] = np.inf
+        part = np.argpartition(D2, k, axis=1)[:, :k]
+        o = np.argsort(np.take_along_axis(D2, part, 1), axis=1, kind="stable")
+        return np.take_along_axis(part, o, 1)
+
+    with ThreadPoolExecutor(threads or os.cpu_count()) as ex:
+        return np.concatenate(list(ex.map(one, range(0, len(q), chunk)))).astype(np.int32)
+
+
 def symmetrised_csr(knn_idx, n):
     """CSR (indptr, indices) of max(A, Aᵀ) with A = kNN connectivity + I.
 

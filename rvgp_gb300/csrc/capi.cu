@@ -10,6 +10,24 @@ static std::atomic<long long> g_launches{0};
 
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
+int num_sms() {
+  constexpr int kMaxDevices = 64, kDefault = 152;
+  static std::atomic<int> cache[kMaxDevices] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+    cudaGetLastError();
+    return kDefault;  // no device (host-only size queries): the GB300 count
+  }
+  int v = cache[dev].load(std::memory_order_relaxed);
+  if (v > 0) return v;
+  if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) {
+    cudaGetLastError();
+    v = kDefault;
+  }
+  cache[dev].store(v, std::memory_order_relaxed);
+  return v;
+}
+
 void set_error(const char* fmt, ...) {
   va_list ap;
   va_start(ap, fmt);

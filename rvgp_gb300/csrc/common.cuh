@@ -59,7 +59,11 @@ inline cudaError_t read_back(void* dst, const void* src, size_t bytes, cudaStrea
 
 inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 
-constexpr int kNumSMs = 152;  // GB300: 2 dies x 76 SMs
+// Streaming multiprocessors of the current device (queried once per device
+// and cached; 152 on GB300, 2 dies x 76).  Host-side planning of grids and of
+// the workspaces that depend on them uses it; every entry point recomputes
+// its workspace need on the device it runs on.
+int num_sms();
 
 }  // namespace rvgp
 

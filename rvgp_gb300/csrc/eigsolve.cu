@@ -521,7 +521,7 @@ Layout carve(Workspace& ws, long long N, int p, int mode) {
   s.theta = ws.take<double>(p);
   s.res = ws.take<double>(p);
   s.norms64 = ws.take<double>(p);
-  s.gersh = ws.take<double>(kNumSMs * 2);
+  s.gersh = ws.take<double>(num_sms() * 2);
   s.resid_part = ws.take<double>((size_t)resid_chunks(N) * p);
   s.info = ws.take<int>(4);
   s.Bf = ws.take<float>(pp);
@@ -593,7 +593,7 @@ static int eigsh_impl(const int* indptr, const int* indices, const double* vals6
   Stats stt;
 
   // spectrum upper bound (Gershgorin)
-  const int gb = std::min(kNumSMs * 2, ceil_div(N, 256));
+  const int gb = std::min(num_sms() * 2, ceil_div(N, 256));
   rvgp::note_launch(); gershgorin_kernel<<<gb, 256, 0, st>>>(n, DB, indptr, vals64, s.gersh);
   std::vector<double> gp(gb);
   if (read_back(gp.data(), s.gersh, sizeof(double) * gb, st) != cudaSuccess) return check_launch("rvgp_eigsh");

@@ -192,10 +192,10 @@ void gemm64(int R, int Q, int K, double alpha, const double* A, int lda, const d
       gemv64_t<<<ceil_div(R, 32), 256, 0, st>>>(R, K, alpha, A, lda, B, ldb, beta, C, ldc);
     return;
   }
-  if (tiles(R, Q, 32) >= 2 * kNumSMs) {
+  if (tiles(R, Q, 32) >= 2 * num_sms()) {
     gemm64_t32<TA, TB><<<dim3(ceil_div(Q, 32), ceil_div(R, 32)), 256, 0, st>>>(R, Q, K, alpha, A, lda, B, ldb, beta,
                                                                                C, ldc);
-  } else if (tiles(R, Q, 16) >= kNumSMs) {
+  } else if (tiles(R, Q, 16) >= num_sms()) {
     gemm64_t16<TA, TB><<<dim3(ceil_div(Q, 16), ceil_div(R, 16)), 256, 0, st>>>(R, Q, K, alpha, A, lda, B, ldb, beta,
                                                                                C, ldc);
   } else {

@@ -135,7 +135,7 @@ __global__ void max_reduce(const double* __restrict__ part, int cnt, double* __r
   if (threadIdx.x == 0) *out = bb.v;
 }
 
-int fps_grid(int n) { return std::max(1, std::min(kNumSMs * 2, ceil_div(n, 1024))); }
+int fps_grid(int n) { return std::max(1, std::min(num_sms() * 2, ceil_div(n, 1024))); }
 
 }  // namespace
 }  // namespace rvgp
@@ -171,7 +171,7 @@ RVGP_API int rvgp_fps(const double* X, int n, int D, int N_max, int start, const
   return RVGP_OK;
 }
 
-RVGP_API size_t rvgp_diameter_workspace(int n) { return sizeof(double) * kNumSMs * 4 + 256; }
+RVGP_API size_t rvgp_diameter_workspace(int n) { return sizeof(double) * num_sms() * 4 + 256; }
 
 RVGP_API int rvgp_diameter(const double* X, int n, int D, double* out, void* workspace, size_t ws_bytes,
                            void* stream) {
@@ -179,8 +179,8 @@ RVGP_API int rvgp_diameter(const double* X, int n, int D, double* out, void* wor
   RVGP_CHECK_ARG(ws_bytes >= rvgp_diameter_workspace(n), "rvgp_diameter: workspace too small");
   cudaStream_t st = as_stream(stream);
   double* part = static_cast<double*>(workspace);
-  rvgp::note_launch(); diameter_tiles<<<kNumSMs * 4, kThreads, 0, st>>>(X, n, D, part);
-  rvgp::note_launch(); max_reduce<<<1, kThreads, 0, st>>>(part, kNumSMs * 4, out);
+  rvgp::note_launch(); diameter_tiles<<<num_sms() * 4, kThreads, 0, st>>>(X, n, D, part);
+  rvgp::note_launch(); max_reduce<<<1, kThreads, 0, st>>>(part, num_sms() * 4, out);
   RVGP_LAUNCH_CHECK("rvgp_diameter");
   return RVGP_OK;
 }

@@ -20,18 +20,24 @@
 //      queued for
 //   1b. the same search with the pool and hash in global memory, sized for
 //      the worst case 1 + K(maxdeg + 1) (one thread per queued point);
-//   2. one thread per point centres the D x (K+1) block of neighbourhood
-//      coordinates and takes its SVD by one-sided (Hestenes) Jacobi in FP64:
-//      on Mᵀ ((K+1) x D, rotations accumulated into U) when D <= K+1, on M
-//      (D x (K+1)) otherwise; it writes the first d_out left singular vectors
-//      (tangents, (n, D, d_out)) and the c = min(D, K+1) singular values
-//      (Sigma, (n, c)), descending (pyx:396-434).  Each singular vector is
-//      signed so its largest-magnitude entry is positive (the reference
-//      inherits LAPACK's arbitrary signs).
+//   2. one thread per point centres the D x (K+1) block M of neighbourhood
+//      coordinates and takes its SVD in FP64 (pyx:396-434): when D <= K+1 by
+//      one-sided (Hestenes) Jacobi on Mᵀ ((K+1) x D, rotations accumulated
+//      into U); otherwise (ambient dimension above the neighbourhood size,
+//      e.g. D = 64, K + 1 = 23) from the (K+1) x (K+1) Gram matrix MᵀM =
+//      V Λ Vᵀ (Householder tridiagonalisation and implicit QL, symeig.cuh):
+//      the columns of M V have norms σ_j (taken as the singular values, so
+//      small ones keep an absolute accuracy ~ε σ₁ rather than the √ε σ₁ of
+//      √λ_j) and are σ_j u_j.  It writes the first d_out left singular
+//      vectors (tangents, (n, D, d_out)) and the c = min(D, K+1) singular
+//      values (Sigma, (n, c)), descending.  Each singular vector is signed so
+//      its largest-magnitude entry is positive (the reference inherits
+//      LAPACK's arbitrary signs).
 //
 // Global scratch is interleaved worker-minor (field[slot * W + worker]) so the
 // SVD phase, where all threads walk the same loop, is coalesced.
 #include "common.cuh"
+#include "symeig.cuh"
 #include <limits.h>
 
 namespace rvgp {
@@ -451,6 +457,66 @@ struct GaugeLayout {
   int pool, hsize;  // its worst-case pool and hash per worker
 };
 
+// SVD of the centred D x c block M (column q at mat[(q * D + t) * W + w],
+// D > c) through its Gram matrix G = MᵀM (c x c at Jm, overwritten by its
+// eigenvectors V): singular values |M v_j| (descending), left singular
+// vectors M v_j / σ_j for the first d_out.
+__host__ __device__ void gauge_svd_gram(int i, int D, int c, int d_out, const GaugeLayout& L, double* mat, double* Jm,
+                                        int w, double* __restrict__ tangents, double* __restrict__ sigma) {
+  const int W = L.W;
+  auto m_ = [&](int q, int t) -> double& { return mat[((size_t)q * D + t) * W + w]; };
+  struct Acc {
+    double* p;
+    int c, W, w;
+    __host__ __device__ double& operator()(int a, int b) { return p[((size_t)a * c + b) * W + w]; }
+  } g{Jm, c, W, w};
+  for (int a = 0; a < c; ++a)
+    for (int b = 0; b <= a; ++b) {
+      double s = 0.0;
+      for (int t = 0; t < D; ++t) s += m_(a, t) * m_(b, t);
+      g(a, b) = s;
+      g(b, a) = s;
+    }
+  double lam[128], e[128], sv[128];
+  int order[128];
+  symeig::eigh(g, c, lam, e);
+  // σ_j = |M v_j| in the order of descending eigenvalue (ties keep column order)
+  for (int j = 0; j < c; ++j) {
+    double nrm = 0.0;
+    for (int t = 0; t < D; ++t) {
+      double u = 0.0;
+      for (int a = 0; a < c; ++a) u += m_(a, t) * g(a, j);
+      nrm += u * u;
+    }
+    const double v = sqrt(nrm);
+    int q = j;
+    while (q > 0 && (lam[order[q - 1]] < lam[j])) {
+      order[q] = order[q - 1];
+      --q;
+    }
+    order[q] = j;
+    sv[j] = v;
+  }
+  for (int q = 0; q < c; ++q) sigma[(size_t)i * c + q] = sv[order[q]];
+  for (int q = 0; q < d_out; ++q) {
+    const int j = order[q];
+    const double inv = 1.0 / sv[j];
+    double big = 0.0;
+    for (int t = 0; t < D; ++t) {
+      double u = 0.0;
+      for (int a = 0; a < c; ++a) u += m_(a, t) * g(a, j);
+      u *= inv;
+      if (fabs(u) > fabs(big)) big = u;
+    }
+    const double sg = big < 0.0 ? -1.0 : 1.0;
+    for (int t = 0; t < D; ++t) {
+      double u = 0.0;
+      for (int a = 0; a < c; ++a) u += m_(a, t) * g(a, j);
+      tangents[((size_t)i * D + t) * d_out + q] = sg * u * inv;
+    }
+  }
+}
+
 // Centring and SVD of point i's neighbourhood (pyx:396-434).
 __host__ __device__ void gauge_svd(int i, const double* __restrict__ X, int D, int K, const int* __restrict__ nbh_row,
                                    int d_out, const GaugeLayout& L, double* mat, double* Jm, int w,
@@ -466,6 +532,10 @@ __host__ __device__ void gauge_svd(int i, const double* __restrict__ X, int D, i
       const size_t e = L.accumulate ? ((size_t)p * r + q) : ((size_t)q * r + p);
       mat[e * L.W + w] = v;
     }
+  }
+  if (!L.accumulate) {
+    gauge_svd_gram(i, D, c, d_out, L, mat, Jm, w, tangents, sigma);
+    return;
   }
   hestenes(mat, L.accumulate ? Jm : nullptr, r, c, L.W, w);
   int order[128];
@@ -517,7 +587,7 @@ __global__ void __launch_bounds__(kSvdThreads)
 
 GaugeLayout layout(int n, int D, int K, int maxdeg) {
   GaugeLayout L;
-  L.W = min(n, kNumSMs * 256);
+  L.W = min(n, num_sms() * 256);
   L.accumulate = D <= K + 1;
   L.rows = L.accumulate ? K + 1 : D;
   L.cols = L.accumulate ? D : K + 1;
@@ -548,7 +618,7 @@ Bufs carve(Workspace& ws, const GaugeLayout& L, int n, int K, bool own_nbh) {
   b.s.hslot = ws.take<int>((size_t)L.hsize * L.Wf);
   b.s.roots = ws.take<int>((size_t)GlobalStore::kRanks * L.Wf);
   b.s.mat = ws.take<double>((size_t)L.rows * L.cols * L.W);
-  b.s.J = ws.take<double>((size_t)(L.accumulate ? L.cols * L.cols : 1) * L.W);
+  b.s.J = ws.take<double>((size_t)L.cols * L.cols * L.W);  // rotations (D <= K+1) or the Gram matrix
   b.nbh = own_nbh ? ws.take<int>((size_t)n * (K + 1)) : nullptr;
   b.ovf_count = ws.take<int>(1);
   b.ovf_list = ws.take<int>(n);

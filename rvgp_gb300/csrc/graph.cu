@@ -169,7 +169,7 @@ RVGP_API int rvgp_graph_build(const int* knn, int n, int k, int* indptr, int* in
   Workspace ws(workspace, ws_bytes);
   GraphBufs b = carve(ws, n, k);
   const long long nk = (long long)n * k;
-  const int eb = min(ceil_div(nk, 256), kNumSMs * 16);
+  const int eb = min(ceil_div(nk, 256), num_sms() * 16);
   cudaMemsetAsync(b.rev, 0, sizeof(int) * n, st);
   cudaMemsetAsync(b.cursor, 0, sizeof(int) * n, st);
   cudaMemsetAsync(maxdeg_out, 0, sizeof(int), st);

@@ -361,8 +361,8 @@ KnnPlan plan(int n, int D, int k) {
   p.DP = padded_dim(D);
   p.kc = kc_bucket(k);
   int qblocks = ceil_div(n, kQB);
-  p.nsplit = max(1, min(16, ceil_div(4 * kNumSMs, qblocks)));
-  p.nblk_prep = min(kNumSMs * 2, max(1, ceil_div(n, 256)));
+  p.nsplit = max(1, min(16, ceil_div(4 * num_sms(), qblocks)));
+  p.nblk_prep = min(num_sms() * 2, max(1, ceil_div(n, 256)));
   return p;
 }
 
@@ -397,8 +397,10 @@ size_t workspace_bytes(int n, int D, int k) {
 
 using namespace rvgp;
 
+// Scratch bytes rvgp_knn needs, or 0 for a shape it does not support
+// (n < 2, D outside [1, 128], k outside [1, n) or above its maximum).
 RVGP_API size_t rvgp_knn_workspace(int n, int D, int k) {
-  if (n < 2 || D < 1 || k < 1) return 0;
+  if (n < 2 || D < 1 || k < 1 || k >= n || padded_dim(D) < 0 || k + kExtra > kMaxKC) return 0;
   return workspace_bytes(n, D, k);
 }
 
@@ -430,7 +432,7 @@ RVGP_API int rvgp_knn(const double* X, int n, int D, int k, int* idx, void* work
   }
   rvgp::note_launch(); knn_finish<<<ceil_div(n, 128), 128, 0, st>>>(X, n, D, p.DP, k, p.kc, p.nsplit, b.part_d, b.part_i,
                                                                  b.radius, idx, b.nflag, b.flag_list);
-  rvgp::note_launch(); knn_fallback<<<kNumSMs, kFbThreads, 0, st>>>(X, n, D, k, b.nflag, b.flag_list, idx);
+  rvgp::note_launch(); knn_fallback<<<num_sms(), kFbThreads, 0, st>>>(X, n, D, k, b.nflag, b.flag_list, idx);
   RVGP_LAUNCH_CHECK("rvgp_knn");
   return RVGP_OK;
 }
@@ -473,7 +475,9 @@ void* g_scratch_ptr[kMaxDevices] = {};
 RVGP_API int rvgp_knn_noalloc(const double* X, int n, int D, int k, int* idx, void* stream) {
   RVGP_CHECK_ARG(n >= 2 && k >= 1 && k < n && D >= 1, "rvgp_knn_noalloc: bad sizes n=%d D=%d k=%d", n, D, k);
   const size_t need = rvgp_knn_workspace(n, D, k);
-  RVGP_CHECK_ARG(need > 0 && need <= kNoAllocScratchBytes,
+  RVGP_CHECK_ARG(need > 0, "rvgp_knn_noalloc: unsupported shape n=%d, D=%d, k=%d (D must be <= 128, k <= %d)", n,
+                 D, k, kMaxKC - kExtra);
+  RVGP_CHECK_ARG(need <= kNoAllocScratchBytes,
                  "rvgp_knn_noalloc: n=%d, D=%d, k=%d needs %zu bytes of scratch, more than the fixed %zu-byte "
                  "buffer; use rvgp_knn with a caller-provided workspace",
                  n, D, k, need, kNoAllocScratchBytes);

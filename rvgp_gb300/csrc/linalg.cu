@@ -109,7 +109,7 @@ namespace {
 template <typename T>
 int gram_splits(long long N, int p, int q) {
   const int tiles = ceil_div(p, TB) * ceil_div(q, TB);
-  int s = ceil_div(4 * kNumSMs, tiles);
+  int s = ceil_div(4 * num_sms(), tiles);
   s = (int)std::min<long long>(s, std::max<long long>(1, N / 512));
   return std::max(1, std::min(s, 1024));
 }

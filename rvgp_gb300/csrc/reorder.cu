@@ -203,7 +203,7 @@ RVGP_API int rvgp_locality_order(const double* X, int n, int D, int* perm, int* 
   rvgp::note_launch();
   bbox_init<<<1, 128, 0, st>>>(b.mm, D);
   rvgp::note_launch();
-  bbox_kernel<<<std::min(kNumSMs * 4, ceil_div((long long)n * D, 256)), 256, 0, st>>>(X, n, D, b.mm);
+  bbox_kernel<<<std::min(num_sms() * 4, ceil_div((long long)n * D, 256)), 256, 0, st>>>(X, n, D, b.mm);
   std::vector<unsigned long long> hm(2 * (size_t)D);
   if (read_back(hm.data(), b.mm, sizeof(unsigned long long) * 2 * D, st) != cudaSuccess) return check_launch("rvgp_locality_order");
   auto dec = [](unsigned long long v) {

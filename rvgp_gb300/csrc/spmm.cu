@@ -21,6 +21,7 @@
 // (neighbouring rows share neighbours) raise the L1 hit rate.
 // HBM traffic per product ≈ E*(DB²*sv + 4) + 2*n*DB*b*sx (+ Z).
 #include "common.cuh"
+#include <stdlib.h>
 
 namespace rvgp {
 namespace {
@@ -136,6 +137,125 @@ __global__ void __launch_bounds__(256) bspmm_kernel(int n, const int* __restrict
     }
 }
 
+// Wide blocks (more than 32 column groups): warp w takes block row
+// i = w / nch and the 32 column groups of chunk c = w % nch, one group per
+// lane, so the accumulators stay at DB x V registers and every SM holds its
+// full complement of warps; the chunks of a row are consecutive warps of one
+// CTA (its indices and blocks are fetched from L1 after the first).  Two
+// neighbours per iteration keep four gathers in flight per lane.
+template <typename T, int DB>
+__global__ void __launch_bounds__(256) bspmm_chunked_kernel(int n, int nch, const int* __restrict__ indptr,
+                                                            const int* __restrict__ indices,
+                                                            const T* __restrict__ vals, const T* __restrict__ X,
+                                                            T* __restrict__ Y, const T* __restrict__ Z, int b, int ld,
+                                                            T alpha, T beta, T gamma) {
+  constexpr int V = Vec<T>::V;
+  const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const long long i = warp / nch;
+  const int chunk = (int)(warp % nch);
+  if (i >= n) return;
+  const int grp = chunk * 32 + lane;
+  const bool on = grp < b / V;
+  const int col = grp * V;
+  T acc[DB][V];
+#pragma unroll
+  for (int p = 0; p < DB; ++p)
+#pragma unroll
+    for (int v = 0; v < V; ++v) acc[p][v] = T(0);
+  const int s = __ldg(indptr + i), e = __ldg(indptr + i + 1);
+  int t = s;
+  for (; t + 1 < e; t += 2) {
+    const int j0 = __ldg(indices + t), j1 = __ldg(indices + t + 1);
+    T b0[DB * DB], b1[DB * DB];
+    load_block<T, DB>(vals, t, b0);
+    load_block<T, DB>(vals, t + 1, b1);
+    T x0[DB][V], x1[DB][V];
+    if (on) {
+#pragma unroll
+      for (int q = 0; q < DB; ++q) {
+        vload(X + ((size_t)j0 * DB + q) * ld + col, x0[q]);
+        vload(X + ((size_t)j1 * DB + q) * ld + col, x1[q]);
+      }
+#pragma unroll
+      for (int q = 0; q < DB; ++q)
+#pragma unroll
+        for (int p = 0; p < DB; ++p)
+#pragma unroll
+          for (int v = 0; v < V; ++v) {
+            acc[p][v] = fma(b0[p * DB + q], x0[q][v], acc[p][v]);
+            acc[p][v] = fma(b1[p * DB + q], x1[q][v], acc[p][v]);
+          }
+    }
+  }
+  if (t < e) {
+    const int j = __ldg(indices + t);
+    T blk[DB * DB];
+    load_block<T, DB>(vals, t, blk);
+    if (on)
+#pragma unroll
+      for (int q = 0; q < DB; ++q) {
+        T x[V];
+        vload(X + ((size_t)j * DB + q) * ld + col, x);
+#pragma unroll
+        for (int p = 0; p < DB; ++p)
+#pragma unroll
+          for (int v = 0; v < V; ++v) acc[p][v] = fma(blk[p * DB + q], x[v], acc[p][v]);
+      }
+  }
+  if (!on) return;
+#pragma unroll
+  for (int p = 0; p < DB; ++p) {
+    const size_t row = ((size_t)i * DB + p) * ld + col;
+    T out[V], x[V];
+#pragma unroll
+    for (int v = 0; v < V; ++v) out[v] = alpha * acc[p][v];
+    if (beta != T(0)) {
+      vload(X + row, x);
+#pragma unroll
+      for (int v = 0; v < V; ++v) out[v] = fma(beta, x[v], out[v]);
+    }
+    if (Z && gamma != T(0)) {
+      vload(Z + row, x);
+#pragma unroll
+      for (int v = 0; v < V; ++v) out[v] = fma(gamma, x[v], out[v]);
+    }
+    vstore(Y + row, out);
+  }
+}
+
+template <typename T>
+int launch_chunked(int n, int DB, const int* indptr, const int* indices, const T* vals, const T* X, T* Y, const T* Z,
+                   int b, int ld, T alpha, T beta, T gamma, cudaStream_t st) {
+  constexpr int V = Vec<T>::V;
+  const int nch = ceil_div(b / V, 32);
+  const long long warps = (long long)n * nch;
+  const int grid = ceil_div(warps * 32, 256);
+  rvgp::note_launch();
+#define RVGP_SPMM_C(DBv) \
+  bspmm_chunked_kernel<T, DBv><<<grid, 256, 0, st>>>(n, nch, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma)
+  switch (DB) {
+    case 1: RVGP_SPMM_C(1); break;
+    case 2: RVGP_SPMM_C(2); break;
+    case 3: RVGP_SPMM_C(3); break;
+    default: RVGP_SPMM_C(4);
+  }
+#undef RVGP_SPMM_C
+  RVGP_LAUNCH_CHECK("rvgp_bspmm");
+  return RVGP_OK;
+}
+
+// Column groups above which the chunked kernel runs (RVGP_SPMM_CHUNK_MIN
+// overrides it; 0 = always, a large value = never).
+int chunk_min_groups() {
+  static int v = -1;
+  if (v < 0) {
+    const char* e = getenv("RVGP_SPMM_CHUNK_MIN");
+    v = e ? atoi(e) : 33;
+  }
+  return v;
+}
+
 template <typename T>
 int launch(int n, int DB, const int* indptr, const int* indices, const T* vals, const T* X, T* Y, const T* Z, int b,
            int ld, T alpha, T beta, T gamma, cudaStream_t st) {
@@ -146,6 +266,8 @@ int launch(int n, int DB, const int* indptr, const int* indices, const T* vals, 
   const int G = groups <= 32 ? 1 : groups <= 64 ? 2 : groups <= 128 ? 4 : groups <= 256 ? 8 : 16;
   RVGP_CHECK_ARG(groups <= 32 * 16, "rvgp_bspmm: block width b=%d too large", b);
   RVGP_CHECK_ARG(DB >= 1 && DB <= 4, "rvgp_bspmm: block size %d not supported (1..4)", DB);
+  if (groups >= chunk_min_groups())
+    return launch_chunked<T>(n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
   int wshift = 5;
   while (wshift > 0 && (1 << (wshift - 1)) >= groups) --wshift;
   const long long warps = ((long long)n + (32 >> wshift) - 1) / (32 >> wshift);

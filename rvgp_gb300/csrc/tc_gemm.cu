@@ -98,6 +98,7 @@ __device__ __forceinline__ void epilogue(uint32_t tmem, int nacc, int Npad, floa
   }
 }
 
+// bar[0..1]: MMA completion per stage; bar[2]: drain barrier of the failure path
 __device__ __forceinline__ void setup(uint64_t* bar, uint32_t* tmem_slot, int* s_fail) {
   if ((threadIdx.x >> 5) == 0) {
     tc::tmem_alloc(tmem_slot, kTmemCols);
@@ -106,6 +107,7 @@ __device__ __forceinline__ void setup(uint64_t* bar, uint32_t* tmem_slot, int* s
   if (threadIdx.x == 0) {
     tc::mbar_init(&bar[0], 1);
     tc::mbar_init(&bar[1], 1);
+    tc::mbar_init(&bar[2], 1);
     tc::fence_mbar_init();
     *s_fail = 0;
   }
@@ -114,7 +116,26 @@ __device__ __forceinline__ void setup(uint64_t* bar, uint32_t* tmem_slot, int* s
   tc::fence_after_sync();
 }
 
-__device__ __forceinline__ void teardown(uint32_t tmem, const int* s_fail, int* err) {
+// Every thread learns whether a pipeline wait timed out; the epilogue runs
+// only if none did.
+__device__ __forceinline__ bool pipeline_ok(const int* s_fail) {
+  __syncthreads();
+  return *s_fail == 0;
+}
+
+// After a timed-out wait, thread 0 (the MMA issuer) commits once more and
+// waits (bounded) until every MMA it issued has completed, so TMEM is freed
+// only when nothing writes it any more; `full` / `nfull` / `last` name the
+// bulk-copy barriers and the parity of the last copy issued into each, which
+// are waited on likewise before the CTA's shared memory is released.
+__device__ __forceinline__ void teardown(uint32_t tmem, uint64_t* bar, const int* s_fail, int* err,
+                                         uint64_t* full = nullptr, int nfull = 0, const int* last = nullptr) {
+  if (*s_fail && threadIdx.x == 0) {
+    tc::mma_commit(&bar[2]);
+    tc::mbar_wait(&bar[2], 0, kWaitLimit);
+    for (int k = 0; k < nfull; ++k)
+      if (last[k] >= 0) tc::mbar_wait(&full[k], (uint32_t)last[k], kWaitLimit);
+  }
   tc::fence_before_sync();
   __syncthreads();
   if ((threadIdx.x >> 5) == 0) tc::tmem_dealloc(tmem, kTmemCols);
@@ -138,7 +159,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     tc_gram_kernel(const float* __restrict__ A, int lda, const float* __restrict__ B, int ldb, long long N, int p,
                    int q, int Npad, int Brows, long long rows_per, float* __restrict__ part, int* __restrict__ err) {
   extern __shared__ uint8_t smem_raw[];
-  __shared__ uint64_t bar[2];
+  __shared__ uint64_t bar[3];
   __shared__ uint32_t tmem_slot;
   __shared__ int s_fail;
   uint8_t* smem = align1024(smem_raw);
@@ -215,8 +236,8 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
   if (nslabs > 0 && !tc::mbar_wait(&bar[(nslabs - 1) & 1], ((nslabs - 1) >> 1) & 1, kWaitLimit)) s_fail = 1;
   tc::fence_after_sync();
-  epilogue(tmem, min(nslabs, 2), Npad, part + ((size_t)blockIdx.y * p + i0) * q, q, p - i0, q);
-  teardown(tmem, &s_fail, err);
+  if (pipeline_ok(&s_fail)) epilogue(tmem, min(nslabs, 2), Npad, part + ((size_t)blockIdx.y * p + i0) * q, q, p - i0, q);
+  teardown(tmem, bar, &s_fail, err);
 }
 
 // ---------------------------------------------------------------- C = A Bm
@@ -255,7 +276,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     tc_gemm_kernel(const float* __restrict__ A, int lda, long long N, int K, const uint8_t* __restrict__ img, int Npad,
                    int q, float* __restrict__ C, int ldc, int* __restrict__ err) {
   extern __shared__ uint8_t smem_raw[];
-  __shared__ uint64_t bar[2], full[2];
+  __shared__ uint64_t bar[3], full[2];
   __shared__ uint32_t tmem_slot;
   __shared__ int s_fail;
   uint8_t* smem = align1024(smem_raw);
@@ -333,8 +354,14 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (kslabs > 0 && !tc::mbar_wait(&bar[(kslabs - 1) & 1], ((kslabs - 1) >> 1) & 1, kWaitLimit)) s_fail = 1;
   tc::fence_after_sync();
   const int nrows = (int)min((long long)kTileM, N - row0);
-  epilogue(tmem, min(kslabs, 2), Npad, C + row0 * ldc, ldc, nrows, q);
-  teardown(tmem, &s_fail, err);
+  if (pipeline_ok(&s_fail)) epilogue(tmem, min(kslabs, 2), Npad, C + row0 * ldc, ldc, nrows, q);
+  // the last B-image copy into each stage: slab s uses full[s % 2], phase s / 2
+  int last[2];
+  for (int k = 0; k < 2; ++k) {
+    const int sl = kslabs - 1 - ((kslabs - 1 - k) % 2 + 2) % 2;
+    last[k] = sl >= 0 ? (sl >> 1) & 1 : -1;
+  }
+  teardown(tmem, bar, &s_fail, err, full, 2, last);
 }
 
 // ---------------------------------------------------------------- C = Aᵀ A, bulk-copied row slabs
@@ -346,7 +373,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     tc_gram_bulk_kernel(const float* __restrict__ A, int lda, long long N, int p, int Npad, int Brows,
                         long long rows_per, int raw_pad, float* __restrict__ part, int* __restrict__ err) {
   extern __shared__ uint8_t smem_raw[];
-  __shared__ uint64_t bar[2], full[3];
+  __shared__ uint64_t bar[3], full[3];
   __shared__ uint32_t tmem_slot;
   __shared__ int s_fail;
   uint8_t* smem = align1024(smem_raw);
@@ -403,8 +430,14 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
   if (nslabs > 0 && !tc::mbar_wait(&bar[(nslabs - 1) & 1], ((nslabs - 1) >> 1) & 1, kWaitLimit)) s_fail = 1;
   tc::fence_after_sync();
-  epilogue(tmem, min(nslabs, 2), Npad, part + ((size_t)blockIdx.y * p + i0) * p, p, p - i0, p);
-  teardown(tmem, &s_fail, err);
+  if (pipeline_ok(&s_fail)) epilogue(tmem, min(nslabs, 2), Npad, part + ((size_t)blockIdx.y * p + i0) * p, p, p - i0, p);
+  // the last raw copy into each ring slot: slab s uses full[s % 3], phase s / 3
+  int last[3];
+  for (int k = 0; k < 3; ++k) {
+    const int sl = nslabs - 1 - ((nslabs - 1 - k) % 3 + 3) % 3;
+    last[k] = sl >= 0 ? (sl / 3) & 1 : -1;
+  }
+  teardown(tmem, bar, &s_fail, err, full, 3, last);
 }
 
 int pad16(int q) { return (q + 15) / 16 * 16; }
@@ -433,7 +466,7 @@ struct GramPlan {
 GramPlan gram_plan(long long N, int p) {
   GramPlan g;
   g.mtiles = ceil_div(p, kTileM);
-  const int want = std::max(1, kNumSMs / g.mtiles);
+  const int want = std::max(1, num_sms() / g.mtiles);
   long long rows = (N + want - 1) / want;
   rows = std::max<long long>(kSlab, (rows + kSlab - 1) / kSlab * kSlab);
   g.rows_per = rows;

@@ -46,3 +46,6 @@ def test_argument_errors_without_gpu():
     assert st == -1
     assert b"" != lib.rvgp_last_error()
     assert lib.rvgp_knn_workspace(100, 3, 10) > 100 * 3 * 4
+    # unsupported shapes report no workspace (rvgp_knn itself rejects them)
+    assert lib.rvgp_knn_workspace(100, 129, 10) == 0
+    assert lib.rvgp_knn_workspace(100, 3, 100) == 0

@@ -136,8 +136,11 @@ def test_connections_and_lc(core, name):
 @pytest.mark.parametrize("d,dtype,b", [(1, torch.float64, 6), (2, torch.float64, 40), (2, torch.float32, 64),
                                        (3, torch.float32, 8), (1, torch.float32, 12), (1, torch.float32, 4),
                                        (2, torch.float32, 228), (2, torch.float64, 228), (4, torch.float32, 20),
-                                       (3, torch.float64, 130), (1, torch.float32, 1040)])
+                                       (3, torch.float64, 130), (1, torch.float32, 1040), (2, torch.float32, 564),
+                                       (2, torch.float64, 564), (1, torch.float32, 564), (2, torch.float32, 132)])
 def test_bspmm(core, d, dtype, b):
+    # widths above 32 column groups (128 FP32 / 64 FP64 columns) run the
+    # column-chunked kernel, narrower ones the row-per-warp kernel
     rng = np.random.default_rng(d * 100 + b)
     n = 700
     A = sp.random(n, n, density=0.02, random_state=1, format="csr") + sp.eye(n)

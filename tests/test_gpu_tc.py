@@ -28,7 +28,9 @@ def test_tc_gram(core, N, p, q, same):
     ref = A.double().T @ B.double()
     scale = torch.outer(A.double().norm(dim=0), B.double().norm(dim=0))
     err = ((C - ref).abs() / scale).max().item()
-    assert err < 3e-6, err
+    # FP32 accumulation inside a CTA: wide products get fewer row splits per
+    # CTA tile (longer FP32 sums), hence the looser bound above 256 columns
+    assert err < (3e-6 if max(p, q) <= 256 else 1e-5), err
 
 
 @pytest.mark.parametrize("N,K,q", [(40000, 228, 228), (1000, 50, 30), (129, 256, 256), (5, 3, 17), (20000, 228, 200),
