@@ -246,6 +246,20 @@ size_t rvgp_gp_predict_local_workspace(int nt, int d, int m, int mode);
 int rvgp_gp_predict_local(const double* T, int n, int D, int ld, int d, const double* U, int m, const int* idx,
                           int nt, int mode, const double* state, double* mean, double* var, void* workspace,
                           size_t ws_bytes, void* stream);
+/* R independent mixed-form Adam fits of one problem from R starts (theta0,
+ * device R x 4), each the optimisation of RVGP/main.py:87-95 from its own
+ * initial parameters, then the FP64 LML of every fit at its final parameters
+ * and the best fit: the multi-start hyperparameter search of a batch of fields
+ * (no counterpart in the reference, which fits once from its defaults).
+ * lower / mask on the device; theta_out (R x 4), hist (R x steps, optional),
+ * lml (R; -inf for a stopped fit), status (R), outs (R x 5 scratch: LML and
+ * gradient per fit), best (1 int), theta_best (4).  No host synchronisation. */
+size_t rvgp_gp_fit_restarts_workspace(int m, int R);
+int rvgp_gp_fit_restarts(const double* C, const double* b, const double* yy, long long N, int m, const double* evals,
+                         double n_rows, int typ, const double* theta0, const double* lower, const int* mask, int R,
+                         int steps, double lr, double beta1, double beta2, double eps, double* theta_out,
+                         double* hist, double* lml, int* status, double* outs, int* best, double* theta_best,
+                         void* workspace, size_t ws_bytes, void* stream);
 /* predict_f(full_cov=False) mean and variance at Nte rows (RVGP/main.py:102-116). */
 size_t rvgp_gp_predict_workspace(long long Nte, int m, int mode);
 int rvgp_gp_predict(const double* Phi_star, const float* Phi_star32, long long Nte, int m, int mode,

@@ -56,6 +56,9 @@ SIGNATURES = {
                                               c_size_t, P]),
     "rvgp_gp_predict_workspace": (c_size_t, [ctypes.c_longlong, c_int, c_int]),
     "rvgp_gp_predict": (c_int, [P, P, ctypes.c_longlong, c_int, c_int, P, P, P, P, c_size_t, P]),
+    "rvgp_gp_fit_restarts_workspace": (c_size_t, [c_int, c_int]),
+    "rvgp_gp_fit_restarts": (c_int, [P, P, P, ctypes.c_longlong, c_int, P, c_double, c_int, P, P, P, c_int, c_int,
+                                     c_double, c_double, c_double, c_double, P, P, P, P, P, P, P, P, c_size_t, P]),
     "rvgp_gp_prepare_local_workspace": (c_size_t, [c_int, c_int, c_int, c_int]),
     "rvgp_gp_prepare_local": (c_int, [P, c_int, c_int, c_int, c_int, P, c_int, P, c_int, P, c_int, P, P, P, P,
                                       c_size_t, P]),
@@ -672,6 +675,36 @@ def gp_fit_adam_mixed(C, b, yy, N, evals, n_rows, theta0, lower, mask, steps, lr
                                           ctypes.byref(status), ptr(ws), ws.numel(), stream()),
           "rvgp_gp_fit_adam_mixed")
     return theta, work.out, hist, work, status.value == 0
+
+
+def gp_fit_restarts(C, b, yy, N, evals, n_rows, theta0s, lower, mask, steps, lr=0.05, betas=(0.9, 0.999), eps=1e-8,
+                    typ="matern", history=False, out=None):
+    """R mixed-form Adam fits from the starts theta0s (R, 4), their FP64 LMLs
+    and the best (rvgp_gp_fit_restarts); lower (4,) float64 and mask (4,)
+    int32 are device tensors.  Only enqueues (capturable in a CUDA graph):
+    returns a dict of device tensors theta (R, 4), lml (R,), status (R,),
+    best (1,), theta_best (4,), hist (R, steps) or None.  ``out``: a dict from
+    an earlier call with the same shapes, reused in place."""
+    theta0s = _dev(theta0s, torch.float64, "theta0s")
+    R = theta0s.shape[0]
+    m = evals.numel()
+    dev = evals.device
+    if out is None:
+        L = lib()
+        out = dict(theta=torch.empty((R, 4), dtype=torch.float64, device=dev),
+                   lml=torch.empty(R, dtype=torch.float64, device=dev),
+                   status=torch.empty(R, dtype=torch.int32, device=dev),
+                   outs=torch.empty((R, 5), dtype=torch.float64, device=dev),
+                   best=torch.empty(1, dtype=torch.int32, device=dev),
+                   theta_best=torch.empty(4, dtype=torch.float64, device=dev),
+                   hist=torch.empty((R, max(steps, 1)), dtype=torch.float64, device=dev) if history else None,
+                   ws=workspace(L.rvgp_gp_fit_restarts_workspace(m, R), dev))
+    check(lib().rvgp_gp_fit_restarts(ptr(C), ptr(b), ptr(yy), int(N), m, ptr(evals), float(n_rows), KERNEL_TYPES[typ],
+                                     ptr(theta0s), ptr(lower), ptr(mask), R, int(steps), float(lr), float(betas[0]),
+                                     float(betas[1]), float(eps), ptr(out["theta"]), ptr(out["hist"]), ptr(out["lml"]),
+                                     ptr(out["status"]), ptr(out["outs"]), ptr(out["best"]), ptr(out["theta_best"]),
+                                     ptr(out["ws"]), out["ws"].numel(), stream()), "rvgp_gp_fit_restarts")
+    return out
 
 
 def gp_predict(Phi_star, state, m, Phi_star32=None, mode="fp64"):

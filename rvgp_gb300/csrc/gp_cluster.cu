@@ -364,10 +364,17 @@ __global__ void __launch_bounds__(kNT, 1)
                    const double* __restrict__ yy_p, long long N, int m, const double* __restrict__ evals,
                    double n_rows, int typ, const double* __restrict__ theta0, const double* __restrict__ lower,
                    const int* __restrict__ mask, int steps, double lr, double beta1, double beta2, double eps,
-                   double* __restrict__ theta_out, double* __restrict__ hist, int* __restrict__ status) {
+                   double* __restrict__ theta_out, double* __restrict__ hist, int* __restrict__ status,
+                   int restarts_mode) {
   cg::cluster_group cl = cg::this_cluster();
   const int rank = (int)cl.block_rank();
   const int nb = (int)cl.num_blocks();
+  // cluster c of the grid runs restart c (independent fits from their own start)
+  const int rs = blockIdx.x / nb;
+  theta0 += 4 * rs;
+  theta_out += 4 * rs;
+  if (hist) hist += (size_t)steps * rs;
+  status += rs;
   const int mp = nb * FB, ld = ld_rows(mp), i0 = rank * FB;
   extern __shared__ __align__(16) unsigned char sm[];
   const CLayout Ly = clayout(m, nb);
@@ -670,7 +677,7 @@ __global__ void __launch_bounds__(kNT, 1)
     __syncthreads();
   }
   if (rank == 0 && tid == 0) {
-    if (!flag[0])
+    if (!flag[0] || restarts_mode)
       for (int q = 0; q < 4; ++q) theta_out[q] = th[q];
     *status = flag[0];
   }
@@ -727,7 +734,8 @@ int gp_fit_cluster_max_m() {
 int gp_fit_cluster_launch(const float* C32, const double* C, const double* b, const double* yy, long long N, int m,
                           const double* evals, double n_rows, int typ, const double* theta0, const double* lower_dev,
                           const int* mask_dev, int steps, double lr, double beta1, double beta2, double eps,
-                          double* theta_out, double* hist, int* status, cudaStream_t st) {
+                          double* theta_out, double* hist, int* status, cudaStream_t st, int restarts,
+                          int restarts_mode) {
   const int nb = (m + FB - 1) / FB;
   if (nb < 2 || nb > kMaxCluster || m > gp_fit_cluster_max_m()) {
     set_error("gp_fit_cluster: m=%d outside the cluster fit's range", m);
@@ -739,7 +747,7 @@ int gp_fit_cluster_launch(const float* C32, const double* C, const double* b, co
     return RVGP_ELAUNCH;
   }
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(nb);
+  cfg.gridDim = dim3(nb * restarts);  // one cluster per fit
   cfg.blockDim = dim3(kNT);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = st;
@@ -753,7 +761,7 @@ int gp_fit_cluster_launch(const float* C32, const double* C, const double* b, co
   rvgp::note_launch();
   const cudaError_t e = cudaLaunchKernelEx(&cfg, gp_fit_cluster, C32, C, b, yy, N, m, evals, n_rows, typ, theta0,
                                            lower_dev, mask_dev, steps, lr, beta1, beta2, eps, theta_out, hist,
-                                           status);
+                                           status, restarts_mode);
   if (e != cudaSuccess) {
     set_error("gp_fit_cluster: launch failed: %s", cudaGetErrorString(e));
     return RVGP_ELAUNCH;

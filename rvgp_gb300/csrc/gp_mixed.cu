@@ -232,8 +232,14 @@ __global__ void __launch_bounds__(kThreads, 1)
                const double* __restrict__ yy_p, long long N, int m, const double* __restrict__ evals, double n_rows,
                int typ, const double* __restrict__ theta0, const double* __restrict__ lower,
                const int* __restrict__ mask, int steps, double lr, double beta1, double beta2, double eps,
-               double* __restrict__ theta_out, double* __restrict__ hist, int* __restrict__ status) {
+               double* __restrict__ theta_out, double* __restrict__ hist, int* __restrict__ status,
+               int restarts_mode) {
   extern __shared__ __align__(16) unsigned char sm[];
+  // CTA r runs restart r (independent fits of the same problem from their own start)
+  theta0 += 4 * blockIdx.x;
+  theta_out += 4 * blockIdx.x;
+  if (hist) hist += (size_t)steps * blockIdx.x;
+  status += blockIdx.x;
   const Layout Ly = layout(m);
   double* S = reinterpret_cast<double*>(sm + Ly.S);
   double* dS = reinterpret_cast<double*>(sm + Ly.dS);
@@ -475,7 +481,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     __syncthreads();
   }
   if (tid == 0) {
-    if (!s_bad)
+    if (!s_bad || restarts_mode)
       for (int q = 0; q < 4; ++q) theta_out[q] = th[q];
     *status = s_bad;
   }
@@ -496,10 +502,12 @@ int gp_fit_cluster_max_m();
 int gp_fit_cluster_launch(const float* C32, const double* C, const double* b, const double* yy, long long N, int m,
                           const double* evals, double n_rows, int typ, const double* theta0, const double* lower_dev,
                           const int* mask_dev, int steps, double lr, double beta1, double beta2, double eps,
-                          double* theta_out, double* hist, int* status, cudaStream_t st);
+                          double* theta_out, double* hist, int* status, cudaStream_t st, int restarts = 1,
+                          int restarts_mode = 0);
 }  // namespace rvgp
 
 extern "C" size_t rvgp_gp_lml_workspace(int m);
+extern "C" size_t rvgp_gp_state_size(int m);
 extern "C" int rvgp_gp_lml(const double* C, const double* b, const double* yy, long long N, int m,
                            const double* evals, double n_rows, int typ, const double* theta, double* out,
                            double* state, void* workspace, size_t ws_bytes, void* stream);
@@ -580,7 +588,7 @@ RVGP_API int rvgp_gp_fit_adam_mixed_launch(const double* C, const double* b, con
   }
   rvgp::note_launch();
   gp_fit_f32<<<1, kThreads, smem, st>>>(f.C32, C, b, yy, N, m, evals, n_rows, typ, theta0, f.dl, f.dm, steps, lr,
-                                        beta1, beta2, eps, theta_out, hist, f.dstat);
+                                        beta1, beta2, eps, theta_out, hist, f.dstat, 0);
   RVGP_LAUNCH_CHECK("rvgp_gp_fit_adam_mixed");
   return RVGP_OK;
 }
@@ -621,4 +629,91 @@ RVGP_API int rvgp_gp_fit_adam_mixed(const double* C, const double* b, const doub
   if (rc != RVGP_OK) return rc;
   return rvgp_gp_fit_adam_mixed_finish(C, b, yy, N, m, evals, n_rows, typ, theta_out, out, state, status, workspace,
                                        ws_bytes, stream);
+}
+
+// ------------------------------------------------------------------ many starts at once
+// R independent mixed-form Adam fits of one problem from R starting points
+// (the multi-start hyperparameter search of a batch of fields), then the FP64
+// likelihood of every fit at its final parameters and the best of them, all
+// enqueued without any host synchronisation (a stream capture may hold it).
+//   theta0 (device, R x 4) starts; lower (device, 4) and mask (device, 4 ints)
+//   as rvgp_gp_fit_adam; theta_out (device, R x 4) final parameters; hist
+//   (device, R x steps, optional) FP32 LML before each step; lml (device, R)
+//   FP64 LML at theta_out (-inf for a fit stopped by a non-positive FP32 pivot
+//   or invalid parameters, status (device, R) = 1 for those); best (device, 1
+//   int) index of the largest LML (lowest index on ties); theta_best
+//   (device, 4) = its parameters.
+// m <= rvgp_gp_fit_mixed_max_m(); one CTA per fit up to the one-SM limit,
+// one thread-block cluster per fit above it.
+RVGP_API size_t rvgp_gp_fit_restarts_workspace(int m, int R) {
+  return rvgp_gp_lml_workspace(m) + sizeof(float) * (size_t)m * m + (size_t)rvgp_gp_state_size(m) * sizeof(double) +
+         8 * sizeof(double) + 4 * 256;
+}
+
+namespace rvgp {
+namespace {
+__global__ void restarts_select(const double* __restrict__ outs, int R, const int* __restrict__ status,
+                                const double* __restrict__ theta_out, double* __restrict__ lml, int* __restrict__ best,
+                                double* __restrict__ theta_best) {
+  if (threadIdx.x != 0) return;
+  int bi = -1;
+  double bv = -INFINITY;
+  for (int r = 0; r < R; ++r) {
+    const double v = (status[r] == 0 && isfinite(outs[5 * r])) ? outs[5 * r] : -INFINITY;
+    lml[r] = v;
+    if (bi < 0 || v > bv) {
+      bi = r;
+      bv = v;
+    }
+  }
+  *best = bi;
+  for (int q = 0; q < 4; ++q) theta_best[q] = theta_out[4 * bi + q];
+}
+}  // namespace
+}  // namespace rvgp
+
+RVGP_API int rvgp_gp_fit_restarts(const double* C, const double* b, const double* yy, long long N, int m,
+                                  const double* evals, double n_rows, int typ, const double* theta0,
+                                  const double* lower, const int* mask, int R, int steps, double lr, double beta1,
+                                  double beta2, double eps, double* theta_out, double* hist, double* lml,
+                                  int* status, double* outs, int* best, double* theta_best, void* workspace,
+                                  size_t ws_bytes, void* stream) {
+  RVGP_CHECK_ARG(C && b && yy && evals && theta0 && lower && mask && theta_out && lml && status && outs && best &&
+                     theta_best,
+                 "rvgp_gp_fit_restarts: null pointer");
+  RVGP_CHECK_ARG(typ == 0 || typ == 1, "rvgp_gp_fit_restarts: typ must be 0 (matern) or 1 (se)");
+  RVGP_CHECK_ARG(R >= 1 && R <= 1024 && steps >= 0, "rvgp_gp_fit_restarts: bad R=%d or steps", R);
+  RVGP_CHECK_ARG(workspace && ws_bytes >= rvgp_gp_fit_restarts_workspace(m, R), "rvgp_gp_fit_restarts: workspace");
+  const int mmax = rvgp_gp_fit_mixed_max_m();
+  RVGP_CHECK_ARG(m >= 1 && m <= mmax, "rvgp_gp_fit_restarts: m=%d exceeds the mixed fit's limit %d", m, mmax);
+  cudaStream_t st = as_stream(stream);
+  Workspace ws(workspace, ws_bytes);
+  void* lml_ws = ws.take<char>(rvgp_gp_lml_workspace(m));
+  float* C32 = ws.take<float>((size_t)m * m);
+  double* state = ws.take<double>(rvgp_gp_state_size(m));
+  rvgp::note_launch();
+  to_f32<<<ceil_div((long long)m * m, 256), 256, 0, st>>>(C, (long long)m * m, C32);
+  if (m > one_cta_max_m()) {
+    TRY_RC(gp_fit_cluster_launch(C32, C, b, yy, N, m, evals, n_rows, typ, theta0, lower, mask, steps, lr, beta1,
+                                 beta2, eps, theta_out, hist, status, st, R, 1));
+  } else {
+    const size_t smem = layout(m).total;
+    if (cudaFuncSetAttribute(gp_fit_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+      set_error("rvgp_gp_fit_restarts: cannot reserve %zu bytes of shared memory", smem);
+      return RVGP_ELAUNCH;
+    }
+    rvgp::note_launch();
+    gp_fit_f32<<<R, kThreads, smem, st>>>(C32, C, b, yy, N, m, evals, n_rows, typ, theta0, lower, mask, steps, lr,
+                                          beta1, beta2, eps, theta_out, hist, status, 1);
+  }
+  RVGP_LAUNCH_CHECK("rvgp_gp_fit_restarts");
+  // FP64 likelihood of every fit at its final parameters (the fits stopped
+  // early keep finite parameters; their LML is discarded by the selection)
+  for (int r = 0; r < R; ++r)
+    TRY_RC(rvgp_gp_lml(C, b, yy, N, m, evals, n_rows, typ, theta_out + 4 * r, outs + 5 * r, state, lml_ws,
+                       rvgp_gp_lml_workspace(m), stream));
+  rvgp::note_launch();
+  restarts_select<<<1, 32, 0, st>>>(outs, R, status, theta_out, lml, best, theta_best);
+  RVGP_LAUNCH_CHECK("rvgp_gp_fit_restarts");
+  return RVGP_OK;
 }

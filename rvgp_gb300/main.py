@@ -205,6 +205,47 @@ class manifold_GPR:
         self._eval_key, self._eval_out = self._theta_key(), out.cpu().numpy()
         return vals
 
+    # ------------------------------------------------------------------ many starts
+    def _device_bounds(self):
+        """Lower bounds and trainable flags of [nu, kappa, sigma_f, noise] as device tensors."""
+        slots = self._slots()
+        lower = torch.tensor([p.lower if p is not None else 0.0 for p in slots], dtype=torch.float64,
+                             device=self.kernel.device)
+        mask = torch.tensor([int(p is not None and p.trainable) for p in slots], dtype=torch.int32,
+                            device=self.kernel.device)
+        return lower, mask
+
+    def restart_starts(self, n_restarts, kappa_range=(0.5, 50.0), seed=0):
+        """Starting parameters of a multi-start search: the model's current
+        values with log-uniform initial lengthscales kappa in kappa_range
+        (seeded), as an (n_restarts, 4) device tensor."""
+        rng = np.random.default_rng(seed)
+        th = self.theta().cpu().numpy()
+        out = np.tile(th, (int(n_restarts), 1))
+        lo, hi = np.log(kappa_range[0]), np.log(kappa_range[1])
+        out[:, 1] = np.exp(rng.uniform(lo, hi, int(n_restarts)))
+        return torch.as_tensor(out, device=self.kernel.device)
+
+    def fit_restarts(self, theta0s, epochs=200, lr=0.05, history=False):
+        """Multi-start hyperparameter search on the device: one mixed-form
+        Adam fit of ``epochs`` steps from every row of theta0s (R, 4) at once
+        (rvgp_gp_fit_restarts: R CTAs or R thread-block clusters in one
+        launch), the FP64 log marginal likelihood of each, and the best; the
+        model takes the best fit's parameters.  Returns the dict of device
+        tensors of _core.gp_fit_restarts (theta, lml, status, best, ...)."""
+        if self.m > _core.gp_fit_mixed_max_m():
+            raise ValueError(f"fit_restarts: m={self.m} exceeds the mixed fit's limit {_core.gp_fit_mixed_max_m()}")
+        lower, mask = self._device_bounds()
+        out = _core.gp_fit_restarts(self.C, self.b, self.yy, self.N, self.kernel.eigenvalues,
+                                    self.kernel.num_verticies, theta0s, lower, mask, epochs, lr=lr,
+                                    typ=self.kernel.typ, history=history)
+        for p, v in zip(self._slots(), out["theta_best"].cpu().numpy()):
+            if p is not None and p.trainable:
+                p.assign(float(v))
+        self.n_evals += (epochs + 1) * theta0s.shape[0]
+        self.fit_form = "mixed (restarts)"
+        return out
+
     # ------------------------------------------------------------------ prediction
     def _predict_rows(self, Phi_star):
         self._evaluate()  # posterior state at the current parameters
@@ -264,6 +305,74 @@ class manifold_GPR:
         mean, var = self.predict_f(np.asarray(test_ind, dtype=np.float64))
         n = len(test_ind)
         return mean.numpy().reshape(n, -1), var.numpy().reshape(n, -1)
+
+
+class ManyFieldsSolve:
+    """Device sequence of the many-fields workload (B time-sample fields on one
+    manifold observed at the same training points, RVGP's one-fit-per-sample
+    use of eeg_utils.py:26-35): R restarts of the hyperparameter fit on the
+    model's own field, the FP64 posterior state at the best fit's parameters,
+    and the posterior means and LMLs of all B fields with those parameters.
+
+    ``enqueue()`` issues only stream-ordered device work: no host
+    synchronisation, and no allocation after the first call (the buffers are
+    kept), so the sequence can be captured in a CUDA graph (``capture()``) and
+    replayed (``replay()``).  ``gp`` is a manifold_GPR fitted (or prepared with
+    epochs=0) on the field the restarts optimise; ``fields`` (B, n, D) on the
+    device; ``points`` the prediction points; ``theta0s`` (R, 4) the starts."""
+
+    def __init__(self, gp, fields, points, theta0s, epochs=200, lr=0.05):
+        self.gp = gp
+        self.epochs, self.lr = int(epochs), float(lr)
+        dev = gp.kernel.device
+        F = fields.to(dev, torch.float64) if isinstance(fields, torch.Tensor) else torch.as_tensor(
+            np.ascontiguousarray(fields, dtype=np.float64), device=dev)
+        self.B = F.shape[0]
+        self.Y = F[:, gp._train_idx.long(), :].reshape(self.B, -1).t().contiguous()
+        self.Phi, _, _ = _core.gather_rows(gp.kernel.eigenvectors, gp.D, gp._train_idx)
+        idx = torch.as_tensor(np.asarray(points, dtype=np.int32), device=dev)
+        self.Phi_star, _, _ = _core.gather_rows(gp.kernel.eigenvectors, gp.D, idx)
+        self.n_points = int(idx.numel())
+        self.theta0s = theta0s.to(dev, torch.float64).contiguous()
+        self.lower, self.mask = gp._device_bounds()
+        self.fit = None
+        self.mean = torch.empty((self.Phi_star.shape[0], self.B), dtype=torch.float64, device=dev)
+        self.lml = torch.empty(self.B, dtype=torch.float64, device=dev)
+        L = _core.lib()
+        self.ws = _core.workspace(L.rvgp_gp_posterior_batch_workspace(gp.m, self.B), dev)
+        self.graph = None
+
+    def enqueue(self):
+        gp = self.gp
+        self.fit = _core.gp_fit_restarts(gp.C, gp.b, gp.yy, gp.N, gp.kernel.eigenvalues, gp.kernel.num_verticies,
+                                         self.theta0s, self.lower, self.mask, self.epochs, lr=self.lr,
+                                         typ=gp.kernel.typ, out=self.fit)
+        _core.gp_lml(gp.C, gp.b, gp.yy, gp.N, gp.kernel.eigenvalues, gp.kernel.num_verticies, self.fit["theta_best"],
+                     gp.kernel.typ, gp.work)
+        L = _core.lib()
+        _core.check(L.rvgp_gp_posterior_batch(_core.ptr(self.Phi), self.Phi.shape[0], gp.m, _core.ptr(self.Y), self.B,
+                                              _core.ptr(self.fit["theta_best"]), _core.ptr(gp.work.state),
+                                              _core.ptr(self.Phi_star), self.Phi_star.shape[0], _core.ptr(self.mean),
+                                              _core.ptr(self.lml), _core.ptr(self.ws), self.ws.numel(),
+                                              _core.stream()), "rvgp_gp_posterior_batch")
+
+    def capture(self):
+        """Record enqueue() in a CUDA graph (after one eager call, which sets
+        up every kernel and buffer)."""
+        if self.fit is None:
+            self.enqueue()
+        torch.cuda.synchronize()
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            self.enqueue()
+        return self.graph
+
+    def replay(self):
+        self.graph.replay()
+
+    def means(self):
+        """Posterior means (B, len(points), D) of the last run."""
+        return self.mean.t().reshape(self.B, self.n_points, self.gp.D)
 
 
 class InducingPoints:
@@ -403,6 +512,13 @@ class manifold_SGPR(manifold_GPR):
     def _predict_rows(self, Phi_star):
         self._evaluate()  # posterior state at the current parameters
         return _core.sgpr_predict(Phi_star, self.work.state, self.m)
+
+    def predict_points(self, points):
+        """Posterior mean and variance at manifold points (indices), each (len, D), on the device."""
+        idx = torch.as_tensor(np.asarray(points, dtype=np.int32), device=self.kernel.device)
+        Phi, _, _ = _core.gather_rows(self.kernel.eigenvectors, self.D, idx)
+        mean, var = self._predict_rows(Phi)
+        return mean.reshape(-1, self.D), var.reshape(-1, self.D)
 
 
 class rbf_GPR(manifold_GPR):

@@ -55,3 +55,30 @@ def test_load_mesh_errors(tmp_path):
     (tmp_path / "bad.obj").write_text("v 0 0\n")
     with pytest.raises(IndexError):
         load_mesh("bad", folder=str(tmp_path))
+
+
+def test_ptu_dijkstra_drop_in_errors_and_expansion():
+    """The drop-in for the reference's native module raises the reference's
+    errors before any device work (RVGP/lib/ptu_dijkstra.pyx:68-82,152-156)
+    and expands edge indices as pyx:202-214 does."""
+    import scipy.sparse as sp
+    from rvgp_gb300 import ptu_dijkstra as P
+    X = np.zeros((10, 3))
+    A = sp.eye(10, format="csr")
+    with pytest.raises(ValueError, match="less than the total number"):
+        P.tangent_frames(X, A, 2, 10)
+    with pytest.raises(ValueError, match="larger or equal to the embedding"):
+        P.tangent_frames(X, A, 3, 2)
+    with pytest.raises(ValueError, match="less or equal to the ambient"):
+        P.tangent_frames(X, A, 4, 5)
+    with pytest.raises(ValueError, match="less or equal to the ambient"):
+        P.connections(np.zeros((10, 3, 2)), A, 4)
+    with pytest.raises(ValueError, match="unit edge weights"):
+        P.tangent_frames(X, 2.0 * A, 2, 5)
+    ei = np.array([[0, 1, 2], [1, 2, 0]])
+    # the reference's construction: every (i, j) of range(dim)², edge-major
+    dim = 2
+    ind = [np.array([i, j]) for i in range(dim) for j in range(dim)]
+    ref = np.stack([ei * dim + i[:, None] for i in ind], axis=2).reshape(2, 3 * len(ind))
+    np.testing.assert_array_equal(P.expand_edge_index(ei, dim), ref)
+    np.testing.assert_array_equal(P.expand_edge_index(ei, 1), ei)
