@@ -47,6 +47,14 @@ WORKLOADS = {
                                          t_smooth=50.0, adam=200, rotational=False, dim=2),
     "torus_n20000_k20_m200": dict(kind="torus", n=20000, D=3, k=20, m=200, train_frac=0.3, t_smooth=50.0, adam=200,
                                   rotational=True),
+    # scale-up: a bumpy sphere of 500 000 points, furthest-point sampled on
+    # the GPU to 250 000 inside the step, then k = 20, m = 1000, 20 % train
+    "bumpy_sphere_n500000_fps250000_k20_m1000": dict(kind="bumpy_sphere", n=250000, n_raw=500000, D=3, k=20,
+                                                     m=1000, train_frac=0.2, t_smooth=50.0, adam=200,
+                                                     rotational=False, dim=2),
+    # the Swiss roll at half size (profiling captures of the wide kernels)
+    "swissroll64_n50000_k15_m500": dict(kind="swissroll64", n=50000, D=64, k=15, m=500, train_frac=0.2,
+                                        t_smooth=50.0, adam=200, rotational=False, dim=2),
     "sphere_n2000_k10_m50": dict(kind="sphere", n=2000, D=3, k=10, m=50, train_frac=0.5, t_smooth=100.0, adam=200,
                                  rotational=False),
 }
@@ -55,10 +63,25 @@ METRIC = "RVGP fit+predict wall s (mixed vs FP64 GPU, equal pred. error); HBM GB
 
 
 def make_inputs(wl, seed=0):
+    """Points (the raw cloud when the step samples it first), train / test
+    indices into the points the pipeline runs on."""
     from rvgp_gb300.workloads import make_points, rotational_field, split
-    X = make_points(wl["kind"], wl["n"], seed=seed)
+    X = make_points(wl["kind"], wl.get("n_raw", wl["n"]), seed=seed)
     train, test = split(wl["n"], wl["train_frac"], seed=seed)
     return X, train, test
+
+
+def sample_points(X, wl):
+    """The step's furthest-point sample (RVGP/geometry.py:126-162) when the
+    workload starts from a larger cloud: the first wl['n'] points of the FPS
+    order from point 0, on the device."""
+    if "n_raw" not in wl:
+        return X
+    import torch
+    from rvgp_gb300 import _core
+    Xd = X if isinstance(X, torch.Tensor) else torch.as_tensor(X, device="cuda")
+    perm, _ = _core.fps(Xd, N=wl["n"], start_idx=0)
+    return Xd[perm.long()].contiguous()
 
 
 def dim_kwargs(wl):
@@ -78,6 +101,7 @@ def make_field(X, wl, seed=0):
     field (+ the rotational field on the torus)."""
     import rvgp_gb300 as RVGP
     from rvgp_gb300.workloads import rotational_field
+    X = sample_points(X, wl)
     d = RVGP.create_data_object(X, n_neighbors=wl["k"], n_eigenpairs=wl["m"], verbose=False, **dim_kwargs(wl))
     d.random_vector_field(seed=seed)
     d.smooth_vector_field(t=wl["t_smooth"])
@@ -98,6 +122,14 @@ def pipeline(X, V, train, test, wl, precision, timings=None, keep=None):
     (with ``keep`` a dict, also the data object and the fitted model)."""
     import torch
     import rvgp_gb300 as RVGP
+    if "n_raw" in wl:
+        e_fps = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        e_fps[0].record()
+        X = sample_points(X, wl)
+        e_fps[1].record()
+        if timings is not None:
+            torch.cuda.synchronize()
+            timings["fps"] = e_fps[0].elapsed_time(e_fps[1]) / 1e3
     d = RVGP.create_data_object(X, n_neighbors=wl["k"], n_eigenpairs=wl["m"], precision=precision, verbose=False,
                                 timings=timings, **dim_kwargs(wl))
     d.vectors = V
@@ -363,7 +395,12 @@ def run_ours(args):
             import rvgp_gb300 as RVGP
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            d = RVGP.create_data_object(X, n_neighbors=wl["k"], n_eigenpairs=wl["m"], verbose=False, **dim_kwargs(wl))
+            Xh = X
+            if "n_raw" in wl:  # the public furthest-point sampling on the host array
+                from rvgp_gb300.geometry import furthest_point_sampling
+                perm_h, _ = furthest_point_sampling(X, N=wl["n"])
+                Xh = X[perm_h]
+            d = RVGP.create_data_object(Xh, n_neighbors=wl["k"], n_eigenpairs=wl["m"], verbose=False, **dim_kwargs(wl))
             d.vectors = V
             gp = RVGP.fit(d, train_ind=train, epochs=wl["adam"], optimizer="adam", lr=0.05, verbose=False)
             mean_h, var_h = gp.transform(d, test)
@@ -371,7 +408,8 @@ def run_ours(args):
             torch.cuda.synchronize()
             e2e_times.append(time.perf_counter() - t0)
         peaks, src = measured_peaks()
-        d = __import__("rvgp_gb300").create_data_object(Xd, n_neighbors=wl["k"], n_eigenpairs=wl["m"], verbose=False,
+        Xs = sample_points(Xd, wl)  # the points the pipeline runs on
+        d = __import__("rvgp_gb300").create_data_object(Xs, n_neighbors=wl["k"], n_eigenpairs=wl["m"], verbose=False,
                                                         **dim_kwargs(wl))
         roof = spmm_roofline(d, wl, peaks, flush)
         d.wait()
@@ -402,14 +440,14 @@ def run_ours(args):
             # the queries, the SVDs of a share of the points, capped eigsh, the
             # dense GP at a few thousand rows; the later stages start from this
             # step's graph and gauges
-            d_in = __import__("rvgp_gb300").create_data_object(Xd, n_neighbors=wl["k"], n_eigenpairs=wl["m"],
+            d_in = __import__("rvgp_gb300").create_data_object(Xs, n_neighbors=wl["k"], n_eigenpairs=wl["m"],
                                                                verbose=False, **dim_kwargs(wl))
             inputs = gpu_inputs(d_in)
             d_in.wait()
             del d_in
             small = wl["n"] > 50000
             out["cpu_baseline"] = cpu_baseline(
-                wl, X, V, train, test, inputs=inputs,
+                wl, Xs.cpu().numpy(), V, train, test, inputs=inputs,
                 caps=dict(eigsh=args.cpu_eigsh_cap / 6, knn_rows=5000 if small else None,
                           frame_rows=10000 if small else None, gp_rows=8192))
         print(json.dumps(out), flush=True)

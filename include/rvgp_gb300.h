@@ -126,6 +126,14 @@ int rvgp_eigsh_ordered(const int* indptr, const int* indices, const double* vals
 
 /* ---- tensor-core tall products ----------------------------------------- */
 
+/* Launch-variant autotuner of this library (no counterpart in the reference):
+ * kernels with several equivalent launch forms (the block SpMM: row per warp,
+ * column-chunked with 2 or 4 neighbours per iteration, all giving the same
+ * bits) time them once per shape class and keep the fastest in an on-disk
+ * cache ($RVGP_AUTOTUNE_CACHE, else ~/.cache/rvgp_gb300/autotune.txt).
+ * cache_path: the file in use; lookup: the cached variant of a key, or -1. */
+const char* rvgp_autotune_cache_path(void);
+int rvgp_autotune_lookup(const char* key);
 /* The eigensolver's FP32 tall products on the tcgen05 tensor cores with
  * split-TF32 operands (x = tf32(x) + remainder; three TF32 products per
  * term, FP32-level accuracy), p, q, K <= 2048 (outputs wider than 256
@@ -358,6 +366,16 @@ size_t rvgp_fps_workspace(int n);
 int rvgp_fps(const double* X, int n, int D, int N_max, int start, const double* diam, double spacing, int* perm,
              double* lambdas, int* count, void* workspace, size_t ws_bytes, void* stream);
 /* Largest pairwise exact distance (D.max() at RVGP/geometry.py:143). */
+/* The same furthest-point sampling in one cooperative launch (D <= 8): a
+ * bounded grid barrier per selection, the new distances screened in FP32
+ * with a certified error bound and computed exactly in FP64 only where the
+ * running minimum can change, so perm / lambdas equal rvgp_fps's
+ * (RVGP/geometry.py:126-162).  exact_evals (device, optional): exact
+ * distances evaluated.  Synchronises the stream (barrier status). */
+size_t rvgp_fps_persistent_workspace(int n);
+int rvgp_fps_persistent(const double* X, int n, int D, int N_max, int start, const double* diam, double spacing,
+                        int* perm, double* lambdas, int* count, long long* exact_evals, void* workspace,
+                        size_t ws_bytes, void* stream);
 size_t rvgp_diameter_workspace(int n);
 int rvgp_diameter(const double* X, int n, int D, double* out, void* workspace, size_t ws_bytes, void* stream);
 

@@ -56,6 +56,10 @@ SIGNATURES = {
                                               c_size_t, P]),
     "rvgp_gp_predict_workspace": (c_size_t, [ctypes.c_longlong, c_int, c_int]),
     "rvgp_gp_predict": (c_int, [P, P, ctypes.c_longlong, c_int, c_int, P, P, P, P, c_size_t, P]),
+    "rvgp_fps_persistent_workspace": (c_size_t, [c_int]),
+    "rvgp_fps_persistent": (c_int, [P, c_int, c_int, c_int, c_int, P, c_double, P, P, P, P, P, c_size_t, P]),
+    "rvgp_autotune_cache_path": (ctypes.c_char_p, []),
+    "rvgp_autotune_lookup": (c_int, [ctypes.c_char_p]),
     "rvgp_gp_fit_restarts_workspace": (c_size_t, [c_int, c_int]),
     "rvgp_gp_fit_restarts": (c_int, [P, P, P, ctypes.c_longlong, c_int, P, c_double, c_int, P, P, P, c_int, c_int,
                                      c_double, c_double, c_double, c_double, P, P, P, P, P, P, P, P, c_size_t, P]),
@@ -815,8 +819,12 @@ def diameter(X):
     return out
 
 
-def fps(X, N=None, spacing=0.1, start_idx=0):
-    """(perm int32, lambdas f64) on the device: RVGP/geometry.py:126-162."""
+def fps(X, N=None, spacing=0.1, start_idx=0, persistent=None, stats=None):
+    """(perm int32, lambdas f64) on the device: RVGP/geometry.py:126-162.
+    persistent (default: D <= 8): one cooperative launch for all selections
+    (rvgp_fps_persistent) instead of one launch per selection (rvgp_fps);
+    the same result.  ``stats`` (dict, optional) receives the number of exact
+    FP64 distances the persistent form evaluated."""
     X = _dev(X, torch.float64, "X")
     n, D = X.shape
     N_max = n if N is None else int(N)
@@ -826,9 +834,20 @@ def fps(X, N=None, spacing=0.1, start_idx=0):
     count = torch.empty(1, dtype=torch.int32, device=dev)
     diam = diameter(X) if N is None else None
     L = lib()
-    ws = workspace(L.rvgp_fps_workspace(n), dev)
-    check(L.rvgp_fps(ptr(X), n, D, N_max, int(start_idx), ptr(diam), float(spacing), ptr(perm), ptr(lam),
-                     ptr(count), ptr(ws), ws.numel(), stream()), "rvgp_fps")
+    if persistent is None:
+        persistent = D <= 8
+    if persistent:
+        ev = torch.zeros(1, dtype=torch.int64, device=dev)
+        ws = workspace(L.rvgp_fps_persistent_workspace(n), dev)
+        check(L.rvgp_fps_persistent(ptr(X), n, D, N_max, int(start_idx), ptr(diam), float(spacing), ptr(perm),
+                                    ptr(lam), ptr(count), ptr(ev), ptr(ws), ws.numel(), stream()),
+              "rvgp_fps_persistent")
+        if stats is not None:
+            stats["exact_evals"] = int(ev.item())
+    else:
+        ws = workspace(L.rvgp_fps_workspace(n), dev)
+        check(L.rvgp_fps(ptr(X), n, D, N_max, int(start_idx), ptr(diam), float(spacing), ptr(perm), ptr(lam),
+                         ptr(count), ptr(ws), ws.numel(), stream()), "rvgp_fps")
     c = int(count.item())
     if c >= 0:
         perm, lam = perm[:c], lam[:c]

@@ -24,6 +24,7 @@
 #include "common.cuh"
 #include "linalg.cuh"
 #include <math.h>
+#include <string.h>
 #include <float.h>
 #include <vector>
 #include <algorithm>
@@ -101,6 +102,33 @@ template <typename T>
 __global__ void copy_to(const double* __restrict__ A, long long cnt, T* __restrict__ B) {
   const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (e < cnt) B[e] = (T)A[e];
+}
+
+// Second Cholesky QR pass for blocks wider than the one-CTA FP32 path: with
+// D = diag(G)^-½ and E = D G D - I, *emax = max |E| (as the bits of a
+// non-negative float, which order like the values; zeroed by the caller).
+__global__ void first_order_emax(const double* __restrict__ G, int p, unsigned* __restrict__ emax) {
+  float em = 0.f;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < (long long)p * p;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(e / p), j = (int)(e % p);
+    if (j >= i) continue;
+    const double v = G[e] * rsqrt(G[(size_t)i * p + i]) * rsqrt(G[(size_t)j * p + j]);
+    em = fmaxf(em, (float)fabs(v));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) em = fmaxf(em, __shfl_xor_sync(0xffffffffu, em, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(emax, __float_as_uint(em));
+}
+
+// B = D (I - E/2) (p x p, row-major, FP32): V B is orthonormal to O(|E|²)
+__global__ void first_order_B(const double* __restrict__ G, int p, float* __restrict__ B) {
+  const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e >= (long long)p * p) return;
+  const int i = (int)(e / p), j = (int)(e % p);
+  const double di = rsqrt(G[(size_t)i * p + i]);
+  const double Eij = (i == j) ? 0.0 : G[e] * di * rsqrt(G[(size_t)j * p + j]);
+  B[e] = (float)(di * ((i == j ? 1.0 : 0.0) - 0.5 * Eij));
 }
 
 // add shift * trace(G)/p to the diagonal (rescue for a numerically singular Gram)
@@ -352,6 +380,26 @@ int orthonormalise(const Problem& P, Block<T>& B, Small& s, Stats& stt, cudaStre
         continue;
       }
       // a failed FP32 pivot: the same pass in FP64 on the explicitly scaled block
+    } else if (sizeof(T) == 4 && pass == 1) {
+      // wide FP32 block: the second pass is usually a first-order correction
+      // (one tensor-core block product) as in the one-CTA path above
+      TRY(gram_any(B.V, B.V, N, p, s.G, s, st));
+      cudaMemsetAsync(s.info + 1, 0, sizeof(unsigned), st);
+      rvgp::note_launch();
+      first_order_emax<<<std::min(4 * num_sms(), ceil_div((long long)p * p, 256)), 256, 0, st>>>(
+          s.G, p, reinterpret_cast<unsigned*>(s.info + 1));
+      unsigned bits = 0;
+      if (read_back(&bits, s.info + 1, sizeof(unsigned), st) != cudaSuccess) return check_launch("orthonormalise");
+      float emax;
+      memcpy(&emax, &bits, sizeof(float));
+      if (emax <= kFirstOrderTol) {
+        rvgp::note_launch();
+        first_order_B<<<ceil_div((long long)p * p, 256), 256, 0, st>>>(s.G, p, s.Bf);
+        TRY(block_product(reinterpret_cast<const float*>(B.V), s.Bf, N, p, reinterpret_cast<float*>(B.T1), s, st));
+        std::swap(B.V, B.T1);
+        continue;
+      }
+      // not near orthonormal: the full pass below (its Gram is recomputed on the scaled block)
     }
     TRY(col_norms<T>(B.V, p, N, p, nrm<T>(s), s.cn_ws, s.cn_bytes, st));
     TRY(scale_cols<T>(B.V, p, N, p, nrm<T>(s), true, st));

@@ -21,6 +21,8 @@
 // (neighbouring rows share neighbours) raise the L1 hit rate.
 // HBM traffic per product ≈ E*(DB²*sv + 4) + 2*n*DB*b*sx (+ Z).
 #include "common.cuh"
+#include "autotune.cuh"
+#include <stdio.h>
 #include <stdlib.h>
 
 namespace rvgp {
@@ -137,13 +139,15 @@ __global__ void __launch_bounds__(256) bspmm_kernel(int n, const int* __restrict
     }
 }
 
-// Wide blocks (more than 32 column groups): warp w takes block row
-// i = w / nch and the 32 column groups of chunk c = w % nch, one group per
-// lane, so the accumulators stay at DB x V registers and every SM holds its
-// full complement of warps; the chunks of a row are consecutive warps of one
-// CTA (its indices and blocks are fetched from L1 after the first).  Two
-// neighbours per iteration keep four gathers in flight per lane.
-template <typename T, int DB>
+// Column-chunked form: warp w takes block row i = w / nch and the 32 column
+// groups of chunk c = w % nch, one group per lane, so the accumulators stay at
+// DB x V registers and every SM holds its full complement of warps; the chunks
+// of a row are consecutive warps of one CTA (its indices and blocks come from
+// L1 after the first).  U neighbours per iteration: all their loads are
+// issued first, then the products in the row kernel's order (neighbour by
+// neighbour, block column by block column), so every variant gives the same
+// bits.
+template <typename T, int DB, int U>
 __global__ void __launch_bounds__(256) bspmm_chunked_kernel(int n, int nch, const int* __restrict__ indptr,
                                                             const int* __restrict__ indices,
                                                             const T* __restrict__ vals, const T* __restrict__ X,
@@ -165,30 +169,27 @@ __global__ void __launch_bounds__(256) bspmm_chunked_kernel(int n, int nch, cons
     for (int v = 0; v < V; ++v) acc[p][v] = T(0);
   const int s = __ldg(indptr + i), e = __ldg(indptr + i + 1);
   int t = s;
-  for (; t + 1 < e; t += 2) {
-    const int j0 = __ldg(indices + t), j1 = __ldg(indices + t + 1);
-    T b0[DB * DB], b1[DB * DB];
-    load_block<T, DB>(vals, t, b0);
-    load_block<T, DB>(vals, t + 1, b1);
-    T x0[DB][V], x1[DB][V];
-    if (on) {
+  for (; t + U <= e; t += U) {
+    T blk[U][DB * DB], x[U][DB][V];
 #pragma unroll
-      for (int q = 0; q < DB; ++q) {
-        vload(X + ((size_t)j0 * DB + q) * ld + col, x0[q]);
-        vload(X + ((size_t)j1 * DB + q) * ld + col, x1[q]);
-      }
+    for (int u = 0; u < U; ++u) {
+      const int j = __ldg(indices + t + u);
+      load_block<T, DB>(vals, t + u, blk[u]);
+      if (on)
 #pragma unroll
-      for (int q = 0; q < DB; ++q)
-#pragma unroll
-        for (int p = 0; p < DB; ++p)
-#pragma unroll
-          for (int v = 0; v < V; ++v) {
-            acc[p][v] = fma(b0[p * DB + q], x0[q][v], acc[p][v]);
-            acc[p][v] = fma(b1[p * DB + q], x1[q][v], acc[p][v]);
-          }
+        for (int q = 0; q < DB; ++q) vload(X + ((size_t)j * DB + q) * ld + col, x[u][q]);
     }
+    if (on)
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+#pragma unroll
+        for (int q = 0; q < DB; ++q)
+#pragma unroll
+          for (int p = 0; p < DB; ++p)
+#pragma unroll
+            for (int v = 0; v < V; ++v) acc[p][v] = fma(blk[u][p * DB + q], x[u][q][v], acc[p][v]);
   }
-  if (t < e) {
+  for (; t < e; ++t) {
     const int j = __ldg(indices + t);
     T blk[DB * DB];
     load_block<T, DB>(vals, t, blk);
@@ -224,7 +225,7 @@ __global__ void __launch_bounds__(256) bspmm_chunked_kernel(int n, int nch, cons
   }
 }
 
-template <typename T>
+template <typename T, int U>
 int launch_chunked(int n, int DB, const int* indptr, const int* indices, const T* vals, const T* X, T* Y, const T* Z,
                    int b, int ld, T alpha, T beta, T gamma, cudaStream_t st) {
   constexpr int V = Vec<T>::V;
@@ -233,7 +234,7 @@ int launch_chunked(int n, int DB, const int* indptr, const int* indices, const T
   const int grid = ceil_div(warps * 32, 256);
   rvgp::note_launch();
 #define RVGP_SPMM_C(DBv) \
-  bspmm_chunked_kernel<T, DBv><<<grid, 256, 0, st>>>(n, nch, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma)
+  bspmm_chunked_kernel<T, DBv, U><<<grid, 256, 0, st>>>(n, nch, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma)
   switch (DB) {
     case 1: RVGP_SPMM_C(1); break;
     case 2: RVGP_SPMM_C(2); break;
@@ -241,33 +242,15 @@ int launch_chunked(int n, int DB, const int* indptr, const int* indices, const T
     default: RVGP_SPMM_C(4);
   }
 #undef RVGP_SPMM_C
-  RVGP_LAUNCH_CHECK("rvgp_bspmm");
-  return RVGP_OK;
-}
-
-// Column groups above which the chunked kernel runs (RVGP_SPMM_CHUNK_MIN
-// overrides it; 0 = always, a large value = never).
-int chunk_min_groups() {
-  static int v = -1;
-  if (v < 0) {
-    const char* e = getenv("RVGP_SPMM_CHUNK_MIN");
-    v = e ? atoi(e) : 33;
-  }
-  return v;
+  return check_launch("rvgp_bspmm");
 }
 
 template <typename T>
-int launch(int n, int DB, const int* indptr, const int* indices, const T* vals, const T* X, T* Y, const T* Z, int b,
-           int ld, T alpha, T beta, T gamma, cudaStream_t st) {
+int launch_rows(int n, int DB, const int* indptr, const int* indices, const T* vals, const T* X, T* Y, const T* Z,
+                int b, int ld, T alpha, T beta, T gamma, cudaStream_t st) {
   constexpr int V = Vec<T>::V;
-  RVGP_CHECK_ARG(b % V == 0 && ld % V == 0 && b <= ld, "rvgp_bspmm: b=%d and ld=%d must be multiples of %d", b, ld, V);
-  RVGP_CHECK_ARG(((uintptr_t)X | (uintptr_t)Y | (uintptr_t)(Z ? Z : X)) % 16 == 0, "rvgp_bspmm: 16-byte alignment");
   const int groups = b / V;
   const int G = groups <= 32 ? 1 : groups <= 64 ? 2 : groups <= 128 ? 4 : groups <= 256 ? 8 : 16;
-  RVGP_CHECK_ARG(groups <= 32 * 16, "rvgp_bspmm: block width b=%d too large", b);
-  RVGP_CHECK_ARG(DB >= 1 && DB <= 4, "rvgp_bspmm: block size %d not supported (1..4)", DB);
-  if (groups >= chunk_min_groups())
-    return launch_chunked<T>(n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
   int wshift = 5;
   while (wshift > 0 && (1 << (wshift - 1)) >= groups) --wshift;
   const long long warps = ((long long)n + (32 >> wshift) - 1) / (32 >> wshift);
@@ -291,8 +274,58 @@ int launch(int n, int DB, const int* indptr, const int* indices, const T* vals, 
   }
 #undef RVGP_SPMM_DB
 #undef RVGP_SPMM_G
-  RVGP_LAUNCH_CHECK("rvgp_bspmm");
-  return RVGP_OK;
+  return check_launch("rvgp_bspmm");
+}
+
+// Column groups from which the chunked form is the default variant
+// (RVGP_SPMM_CHUNK_MIN overrides it and turns the tuner off: 0 = always
+// chunked, a large value = always row per warp).
+int chunk_min_groups() {
+  static int v = -1;
+  if (v < 0) {
+    const char* e = getenv("RVGP_SPMM_CHUNK_MIN");
+    v = e ? atoi(e) : 33;
+  }
+  return v;
+}
+
+bool overlaps(const void* a, const void* b, size_t bytes) {
+  const char *x = static_cast<const char*>(a), *y = static_cast<const char*>(b);
+  return x < y + bytes && y < x + bytes;
+}
+
+// Variants: 0 = row per warp (G groups per lane), 1 / 2 = column-chunked with
+// 2 / 4 neighbours per iteration.  The tuner (autotune.cuh) picks one per
+// shape class; the same bits come out of all three.
+template <typename T>
+int launch(int n, int DB, const int* indptr, const int* indices, const T* vals, const T* X, T* Y, const T* Z, int b,
+           int ld, T alpha, T beta, T gamma, cudaStream_t st) {
+  constexpr int V = Vec<T>::V;
+  RVGP_CHECK_ARG(b % V == 0 && ld % V == 0 && b <= ld, "rvgp_bspmm: b=%d and ld=%d must be multiples of %d", b, ld, V);
+  RVGP_CHECK_ARG(((uintptr_t)X | (uintptr_t)Y | (uintptr_t)(Z ? Z : X)) % 16 == 0, "rvgp_bspmm: 16-byte alignment");
+  const int groups = b / V;
+  RVGP_CHECK_ARG(groups <= 32 * 16, "rvgp_bspmm: block width b=%d too large", b);
+  RVGP_CHECK_ARG(DB >= 1 && DB <= 4, "rvgp_bspmm: block size %d not supported (1..4)", DB);
+  auto run = [&](int v) -> int {
+    switch (v) {
+      case 0: return launch_rows<T>(n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
+      case 1: return launch_chunked<T, 2>(n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
+      default: return launch_chunked<T, 4>(n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
+    }
+  };
+  int def = groups >= chunk_min_groups() ? 1 : 0;
+  // tuning runs the product several times into Y: only when Y overlaps neither input
+  const size_t bytes = (size_t)n * DB * ld * sizeof(T);
+  const bool independent = !overlaps(Y, X, bytes) && !(Z && overlaps(Y, Z, bytes));
+  int v = def;
+  if (independent && getenv("RVGP_SPMM_CHUNK_MIN") == nullptr) {
+    char key[160];
+    snprintf(key, sizeof(key), "bspmm %s DB%d b%d n2^%d", sizeof(T) == 4 ? "f32" : "f64", DB, b,
+             autotune::log2_bucket(n));
+    v = autotune::tune(key, 3, def, st, 3, run);
+    if (v < 0) return v;
+  }
+  return run(v);
 }
 
 }  // namespace
