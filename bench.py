@@ -117,7 +117,7 @@ def make_field(X, wl, seed=0):
 
 
 # ------------------------------------------------------------------------------ our arm
-def pipeline(X, V, train, test, wl, precision, timings=None, keep=None):
+def pipeline(X, V, train, test, wl, precision, timings=None, keep=None, nvtx=None):
     """One step through the public API; returns (mean, var) on the device
     (with ``keep`` a dict, also the data object and the fitted model)."""
     import torch
@@ -131,7 +131,7 @@ def pipeline(X, V, train, test, wl, precision, timings=None, keep=None):
             torch.cuda.synchronize()
             timings["fps"] = e_fps[0].elapsed_time(e_fps[1]) / 1e3
     d = RVGP.create_data_object(X, n_neighbors=wl["k"], n_eigenpairs=wl["m"], precision=precision, verbose=False,
-                                timings=timings, **dim_kwargs(wl))
+                                timings=timings, nvtx=nvtx, **dim_kwargs(wl))
     d.vectors = V
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
     ev[0].record()
@@ -154,8 +154,9 @@ def pipeline(X, V, train, test, wl, precision, timings=None, keep=None):
 
 def error_statements(mixed, fp64, mean_mixed, mean64):
     """The mixed form's results against the FP64 form's on the same inputs:
-    eigenvalue relative error (Lc and L; relative to max(|λ|, 1e-9 λ_max), as
-    the null eigenvalue of L is 0), the largest principal-angle sine
+    eigenvalue relative error (Lc and L; over the eigenvalues above 1e-6 of the
+    largest, as the null eigenvalue of L is 0, with the largest absolute
+    error over the largest eigenvalue beside it), the largest principal-angle sine
     between eigen-subspaces per cluster of numerically equal eigenvalues (the
     eigenvectors inside a cluster are arbitrary) and over the whole m-space,
     the relative L2 error of the posterior mean, and |ΔLML| at each form's
@@ -182,10 +183,15 @@ def error_statements(mixed, fp64, mean_mixed, mean64):
     out = {}
     for tag, ea, eb, Ua, Ub in (("Lc", da.evals_Lc, db.evals_Lc, da.evecs_Lc_local, db.evecs_Lc_local),
                                 ("L", da.evals_L, db.evals_L, da.evecs_L, db.evecs_L)):
-        # relative to each eigenvalue, floored at 1e-9 of the largest (L's first is 0)
-        rel = float(((ea - eb).abs() / eb.abs().clamp_min(1e-9 * float(eb.abs().max()))).max())
+        # relative error over the eigenvalues above 1e-6 of the largest (the
+        # null eigenvalue of L is 0 up to rounding), and the largest absolute
+        # error in units of the largest returned eigenvalue
+        big = eb.abs() >= 1e-6 * float(eb.abs().max())
+        rel = float(((ea - eb).abs()[big] / eb.abs()[big]).max())
+        absn = float((ea - eb).abs().max() / eb.abs().max())
         cl, whole = sines(Ua, Ub, eb)
         out[f"eigenvalue_rel_err_{tag}"] = rel
+        out[f"eigenvalue_abs_err_over_max_{tag}"] = absn
         out[f"principal_angle_sin_max_per_cluster_{tag}"] = cl
         out[f"principal_angle_sin_whole_space_{tag}"] = whole
     out["posterior_mean_rel_err"] = float(torch.linalg.vector_norm(mean_mixed - mean64) /
@@ -350,7 +356,7 @@ def run_ours(args):
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             torch.cuda.nvtx.range_push("timed_step")  # lets a profiler select exactly these launches
             e0.record(stream)
-            mean_mixed, _ = pipeline(Xd, Vd, train, test, wl, "mixed")
+            mean_mixed, _ = pipeline(Xd, Vd, train, test, wl, "mixed", nvtx="timed_step")
             e1.record(stream)
             torch.cuda.nvtx.range_pop()
             barrier()

@@ -693,7 +693,8 @@ RVGP_API int rvgp_gp_fit_restarts(const double* C, const double* b, const double
   double* state = ws.take<double>(rvgp_gp_state_size(m));
   rvgp::note_launch();
   to_f32<<<ceil_div((long long)m * m, 256), 256, 0, st>>>(C, (long long)m * m, C32);
-  if (m > one_cta_max_m()) {
+  const char* force = getenv("RVGP_GP_FIT_CLUSTER");  // as for the single fit (tests)
+  if (m > one_cta_max_m() || (force && force[0] == '1' && m > 32 && m <= gp_fit_cluster_max_m())) {
     TRY_RC(gp_fit_cluster_launch(C32, C, b, yy, N, m, evals, n_rows, typ, theta0, lower, mask, steps, lr, beta1,
                                  beta2, eps, theta_out, hist, status, st, R, 1));
   } else {
