@@ -502,8 +502,9 @@ int gp_fit_cluster_max_m();
 int gp_fit_cluster_launch(const float* C32, const double* C, const double* b, const double* yy, long long N, int m,
                           const double* evals, double n_rows, int typ, const double* theta0, const double* lower_dev,
                           const int* mask_dev, int steps, double lr, double beta1, double beta2, double eps,
-                          double* theta_out, double* hist, int* status, cudaStream_t st, int restarts = 1,
-                          int restarts_mode = 0);
+                          double* theta_out, double* hist, int* status, cudaStream_t st, int restarts,
+                          int restarts_mode, double* scratch);
+size_t gp_fit_cluster_scratch(int m, int restarts);
 }  // namespace rvgp
 
 extern "C" size_t rvgp_gp_lml_workspace(int m);
@@ -527,7 +528,8 @@ static int one_cta_max_m() {
 RVGP_API int rvgp_gp_fit_mixed_max_m(void) { return std::max(one_cta_max_m(), gp_fit_cluster_max_m()); }
 
 RVGP_API size_t rvgp_gp_fit_mixed_workspace(int m) {
-  return rvgp_gp_lml_workspace(m) + sizeof(float) * (size_t)m * m + 4 * sizeof(double) + 3 * 256 + 64;
+  return rvgp_gp_lml_workspace(m) + sizeof(float) * (size_t)m * m + 4 * sizeof(double) +
+         gp_fit_cluster_scratch(m, 1) + 6 * 256 + 64;
 }
 
 namespace {
@@ -537,6 +539,7 @@ struct FitBufs {
   double* dl;
   int* dm;
   int* dstat;
+  double* scratch;  // the wide cluster fit's FP64 arrays (m > 512)
 };
 FitBufs carve_fit(void* workspace, size_t ws_bytes, int m) {
   Workspace ws(workspace, ws_bytes);
@@ -546,6 +549,7 @@ FitBufs carve_fit(void* workspace, size_t ws_bytes, int m) {
   f.dl = ws.take<double>(4);
   f.dm = ws.take<int>(4);
   f.dstat = ws.take<int>(1);
+  f.scratch = gp_fit_cluster_scratch(m, 1) ? ws.take<double>(gp_fit_cluster_scratch(m, 1) / sizeof(double)) : nullptr;
   return f;
 }
 }  // namespace
@@ -576,7 +580,7 @@ RVGP_API int rvgp_gp_fit_adam_mixed_launch(const double* C, const double* b, con
   const bool cluster = m > one_cta_max_m() || (force && force[0] == '1' && m > 32 && m <= gp_fit_cluster_max_m());
   if (cluster) {
     const int rc = gp_fit_cluster_launch(f.C32, C, b, yy, N, m, evals, n_rows, typ, theta0, f.dl, f.dm, steps, lr,
-                                         beta1, beta2, eps, theta_out, hist, f.dstat, st);
+                                         beta1, beta2, eps, theta_out, hist, f.dstat, st, 1, 0, f.scratch);
     if (rc != RVGP_OK) return rc;
     RVGP_LAUNCH_CHECK("rvgp_gp_fit_adam_mixed");
     return RVGP_OK;
@@ -647,7 +651,7 @@ RVGP_API int rvgp_gp_fit_adam_mixed(const double* C, const double* b, const doub
 // one thread-block cluster per fit above it.
 RVGP_API size_t rvgp_gp_fit_restarts_workspace(int m, int R) {
   return rvgp_gp_lml_workspace(m) + sizeof(float) * (size_t)m * m + (size_t)rvgp_gp_state_size(m) * sizeof(double) +
-         8 * sizeof(double) + 4 * 256;
+         gp_fit_cluster_scratch(m, R) + 8 * sizeof(double) + 5 * 256;
 }
 
 namespace rvgp {
@@ -691,12 +695,14 @@ RVGP_API int rvgp_gp_fit_restarts(const double* C, const double* b, const double
   void* lml_ws = ws.take<char>(rvgp_gp_lml_workspace(m));
   float* C32 = ws.take<float>((size_t)m * m);
   double* state = ws.take<double>(rvgp_gp_state_size(m));
+  const size_t scr = gp_fit_cluster_scratch(m, R);
+  double* scratch = scr ? ws.take<double>(scr / sizeof(double)) : nullptr;
   rvgp::note_launch();
   to_f32<<<ceil_div((long long)m * m, 256), 256, 0, st>>>(C, (long long)m * m, C32);
   const char* force = getenv("RVGP_GP_FIT_CLUSTER");  // as for the single fit (tests)
   if (m > one_cta_max_m() || (force && force[0] == '1' && m > 32 && m <= gp_fit_cluster_max_m())) {
     TRY_RC(gp_fit_cluster_launch(C32, C, b, yy, N, m, evals, n_rows, typ, theta0, lower, mask, steps, lr, beta1,
-                                 beta2, eps, theta_out, hist, status, st, R, 1));
+                                 beta2, eps, theta_out, hist, status, st, R, 1, scratch));
   } else {
     const size_t smem = layout(m).total;
     if (cudaFuncSetAttribute(gp_fit_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {

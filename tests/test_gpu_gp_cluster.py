@@ -1,13 +1,15 @@
 """GPU: the mixed-precision Adam fit on one thread-block cluster (the m x m
 capacitance algebra spread over the shared memory of up to 16 CTAs) against the
-FP64 device fit (rvgp_gp_fit_adam) and the one-CTA mixed fit.
+FP64 device fit (rvgp_gp_fit_adam) and the one-CTA mixed fit.  m up to 512
+runs on a cluster of m/32 CTAs holding one block row each; m from 513 to 1024
+on 16 CTAs holding two block rows each (the wide form).
 
 Same tolerances as the one-CTA fit: parameters 1e-4 relative, posterior means
 1e-6 relative, the returned out / state the FP64 likelihood at the returned
 parameters (1e-12); the LML history to 1e-4 of its largest magnitude up to
 m = 200 and 3e-4 above (the history follows the parameters, which still move
 fast at the last steps, so a parameter difference of 1e-4 shows in it at
-~|∂LML/∂log θ| · 1e-4)."""
+~|∂LML/∂log θ| · 1e-4), 1e-3 above 512, where the FP32 pivots lose more."""
 import os
 
 import numpy as np
@@ -51,7 +53,8 @@ def fit_mixed(core, force_cluster, *args, **kw):
 
 
 @pytest.mark.parametrize("m,N,typ", [(40, 600, "matern"), (97, 1500, "se"), (200, 4000, "matern"),
-                                     (300, 5000, "matern"), (500, 8000, "matern")])
+                                     (300, 5000, "matern"), (500, 8000, "matern"), (700, 10000, "se"),
+                                     (1000, 15000, "matern")])
 def test_cluster_fit_matches_fp64_fit(core, m, N, typ):
     if m > core.gp_fit_mixed_max_m():
         pytest.skip(f"clusters for m={m} cannot be launched on this device")
@@ -68,7 +71,7 @@ def test_cluster_fit_matches_fp64_fit(core, m, N, typ):
     assert ok
     np.testing.assert_allclose(th32.cpu().numpy(), th64.cpu().numpy(), rtol=1e-4)
     h64n = h64.cpu().numpy()
-    htol = 1e-4 if m <= 200 else 3e-4
+    htol = 1e-4 if m <= 200 else 3e-4 if m <= 512 else 1e-3
     np.testing.assert_allclose(h32.cpu().numpy(), h64n, rtol=0, atol=htol * np.abs(h64n).max())
     mean32, _ = core.gp_predict(cu(Phi[:300]), w32.state, m)
     err = (torch.linalg.vector_norm(mean32 - mean64) / torch.linalg.vector_norm(mean64)).item()

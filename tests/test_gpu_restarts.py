@@ -37,7 +37,8 @@ def structured(seed, N, m):
     return Phi, Phi @ coef + 0.05 * rng.standard_normal(N), lam
 
 
-@pytest.mark.parametrize("m,N,R,force_cluster", [(60, 900, 5, False), (60, 900, 3, True), (300, 5000, 3, False)])
+@pytest.mark.parametrize("m,N,R,force_cluster", [(60, 900, 5, False), (60, 900, 3, True), (300, 5000, 3, False),
+                                                      (600, 9000, 2, False)])
 def test_restarts_equal_single_fits(core, m, N, R, force_cluster):
     if m > core.gp_fit_mixed_max_m():
         pytest.skip("m beyond the mixed fit on this device")
