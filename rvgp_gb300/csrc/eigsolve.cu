@@ -408,16 +408,24 @@ int orthonormalise(const Problem& P, Block<T>& B, Small& s, Stats& stt, cudaStre
     int info = 0;
     if (read_back(&info, s.info, sizeof(int), st) != cudaSuccess) return check_launch("orthonormalise");
     if (info != 0) {
-      // numerically rank-deficient block: shifted Cholesky QR on a fresh Gram
+      // Numerically singular Gram (rounding of an ill-conditioned block made
+      // it indefinite): shifted Cholesky QR on a fresh Gram, the shift raised
+      // until the factorisation holds (10 u p ||V||² in FP32 terms is ~1e-4
+      // at p = 1000); the shifted factor leaves a block of condition ~s^-½,
+      // which two plain passes then orthonormalise.
       ++stt.chol_rescues;
       if (++rescues > 3) {
         set_error("eigensolver: Cholesky QR failed repeatedly (block lost rank)");
         return 1;
       }
-      TRY(gram_any(B.V, B.V, N, p, s.G, s, st));
-      rvgp::note_launch(); shift_diag<<<1, 256, 0, st>>>(s.G, p, 1e-6);
-      TRY(cholesky<double>(s.G, p, p, s.info, st));
-      if (read_back(&info, s.info, sizeof(int), st) != cudaSuccess) return check_launch("orthonormalise");
+      const double shifts[] = {sizeof(T) == 4 ? 1e-5 : 1e-12, 1e-4, 1e-3, 1e-2};
+      for (double sh : shifts) {
+        TRY(gram_any(B.V, B.V, N, p, s.G, s, st));
+        rvgp::note_launch(); shift_diag<<<1, 256, 0, st>>>(s.G, p, sh);
+        TRY(cholesky<double>(s.G, p, p, s.info, st));
+        if (read_back(&info, s.info, sizeof(int), st) != cudaSuccess) return check_launch("orthonormalise");
+        if (info == 0) break;
+      }
       if (info != 0) {
         set_error("eigensolver: Cholesky QR failed (block lost rank)");
         return 1;
@@ -480,13 +488,23 @@ int rayleigh_ritz(const Problem& P, Block<T>& B, Small& s, Stats& stt, int max_s
   return check_launch("rayleigh_ritz");
 }
 
-int choose_degree(const std::vector<double>& th, int m, double a, double b, double range, int cap) {
+// Degree of the next filter on [a, b]: the m-th Ritz direction grows by about
+// 2e4 against the edge a, the lowest one by at most `range` times the m-th and
+// by at most `amp` in all.  `amp` bounds the spread of the filtered block's
+// column norms along the Ritz directions, hence its condition number: an FP32
+// block whose lowest directions outgrow the guard directions by much more
+// than ~1e5 (with a Ritz basis only partly rotated) has a Gram matrix that
+// its own rounding makes indefinite.
+constexpr double kAmp32 = 1e5;  // largest filter gain of the FP32 stage
+
+int choose_degree(const std::vector<double>& th, int m, double a, double b, double range, int cap, double amp) {
   const double e = (b - a) / 2, c = (b + a) / 2;
   const double xm = std::max(1.0 + 1e-6, (c - th[m - 1]) / e);
   const double x0 = std::max(xm, (c - std::min(th[0], th[m - 1])) / e);
   int deg = (int)ceil(log(2e4) / acosh(xm));
   const double gap = acosh(x0) - acosh(xm);
   if (gap > 0) deg = std::min(deg, (int)floor(log(range) / gap));
+  deg = std::min(deg, (int)floor(acosh(amp) / acosh(x0)));
   return std::max(4, std::min(deg, cap));
 }
 
@@ -502,7 +520,7 @@ int iterate(const Problem& P, Block<T>& B, Small& s, Stats& stt, double bup, dou
   if (have_ritz) {
     a = theta[p - 1];
     a0 = std::min(theta[0], 0.0) - 1e-3 * bup;
-    deg = choose_degree(theta, m, a, bup, range, sizeof(T) == 4 ? 60 : 250);
+    deg = choose_degree(theta, m, a, bup, range, sizeof(T) == 4 ? 60 : 250, sizeof(T) == 4 ? kAmp32 : 1e300);
   } else {
     a = bup * std::min(0.5, std::max(4.0 * p / (double)P.N, 0.01));
     a0 = -1e-3 * bup;
@@ -535,7 +553,7 @@ int iterate(const Problem& P, Block<T>& B, Small& s, Stats& stt, double bup, dou
     }
     a = theta[p - 1];
     a0 = std::min(theta[0], 0.0) - 1e-3 * bup;
-    deg = choose_degree(theta, m, a, bup, range, sizeof(T) == 4 ? 60 : 250);
+    deg = choose_degree(theta, m, a, bup, range, sizeof(T) == 4 ? 60 : 250, sizeof(T) == 4 ? kAmp32 : 1e300);
   }
   *nconv_out = nconv;
   return RVGP_OK;
