@@ -270,18 +270,19 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of an ncu capture of
-# the launches timed below (Morton-renumbered Lc, torus n=20000, k=20, p=228, L2
-# flushed before each) on GB300: 82.34 MB read (exactly the algorithmic reads)
-# + 10.61 MB written by the end of the launch (the rest of Y is still in L2).
-SPMM_TRAFFIC_BYTES = 92_953_088
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of the
+# tiled Chebyshev-step SpMM from ncu captures, keyed by (n, d, p, stored
+# blocks) of the workload's Lc; filled from the captures under profiles/.
+SPMM_TRAFFIC = {}
 
 
 def spmm_roofline(d, wl, peaks, flush, reps=20):
     """Achieved HBM bandwidth of the eigensolver's Chebyshev-step SpMM (FP32,
     block width p) on this workload's connection Laplacian: each launch timed
     alone with CUDA events on the launching stream, L2 flushed before it.  The
-    matrix is the Morton-renumbered one the eigensolver multiplies by."""
+    matrix is the Morton-renumbered one the eigensolver multiplies by, through
+    the tiled plan the eigensolver builds (the untiled product is timed beside
+    it for reference)."""
     import torch
     from rvgp_gb300 import _core
     dev = d._dev
@@ -289,33 +290,40 @@ def spmm_roofline(d, wl, peaks, flush, reps=20):
     n, k = d.n, d.dim_man
     N = n * k
     p = _core.block_size(wl["m"], N)
+    plan = _core.spmm_plan(ip, ix, k)
     torch.cuda.nvtx.range_push("spmm_roofline")  # lets a profiler select exactly these launches
     X = torch.randn((N, p), dtype=torch.float32, device="cuda")
     Z = torch.randn_like(X)
     Y = torch.empty_like(X)
-    for _ in range(3):
-        _core.bspmm(ip, ix, v32, X, Y, Z, 0.1, -0.2, 0.3)
     s = torch.cuda.current_stream()
-    times = []
-    for _ in range(reps):
-        flush_l2(flush)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(s)
-        _core.bspmm(ip, ix, v32, X, Y, Z, 0.1, -0.2, 0.3)
-        e1.record(s)
-        torch.cuda.synchronize()
-        times.append(e0.elapsed_time(e1) / 1e3)
+
+    def timed(pl):
+        for _ in range(3):
+            _core.bspmm(ip, ix, v32, X, Y, Z, 0.1, -0.2, 0.3, plan=pl)
+        times = []
+        for _ in range(reps):
+            flush_l2(flush)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(s)
+            _core.bspmm(ip, ix, v32, X, Y, Z, 0.1, -0.2, 0.3, plan=pl)
+            e1.record(s)
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1) / 1e3)
+        return float(np.mean(times))
+
+    t = timed(plan)
     torch.cuda.nvtx.range_pop()
-    t = float(np.mean(times))
+    t_untiled = timed(None)
     E = dev.indices.numel()
-    alg = E * (k * k * 4 + 4) + (n + 1) * 4 + 3 * N * p * 4  # values + indices + read X, read Z, write Y
+    # values + local column indices (2 bytes) + row pointers + read X, read Z, write Y
+    alg = E * (k * k * 4 + 2) + (n + 1) * 4 + 3 * N * p * 4
     achieved = alg / t / 1e9
-    same_shape = (n, k, p, E) == (20000, 2, 228, 460824)
-    return {"kernel": "bspmm_kernel<float,2> (Chebyshev step, Lc x block)", "bound": "hbm",
+    return {"kernel": f"bspmm_tiled_kernel<float,{k},2> (Chebyshev step, Lc x block, tiled plan)", "bound": "hbm",
             "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
             "frac": round(achieved / peaks["hbm_gbs"], 4),
-            "traffic": SPMM_TRAFFIC_BYTES if same_shape else None, "algorithmic_bytes": int(alg),
-            "avg_launch_us": round(t * 1e6, 2), "block_width": p, "l2": "flushed before every timed launch"}
+            "traffic": SPMM_TRAFFIC.get((n, k, p, E)), "algorithmic_bytes": int(alg),
+            "avg_launch_us": round(t * 1e6, 2), "untiled_avg_launch_us": round(t_untiled * 1e6, 2),
+            "block_width": p, "l2": "flushed before every timed launch"}
 
 
 def run_ours(args):

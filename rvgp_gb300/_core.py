@@ -47,6 +47,12 @@ SIGNATURES = {
     "rvgp_gp_fit_adam": (c_int, [P, P, P, ctypes.c_longlong, c_int, P, c_double, c_int, P, P, P, c_int, c_double,
                                  c_double, c_double, c_double, P, P, P, P, P, c_size_t, P]),
     "rvgp_gp_fit_mixed_max_m": (c_int, []),
+    "rvgp_spmm_plan_bytes": (ctypes.c_size_t, [c_int, c_int, ctypes.c_longlong]),
+    "rvgp_spmm_plan_build": (c_int, [c_int, c_int, P, P, ctypes.c_longlong, P, ctypes.c_size_t, P]),
+    "rvgp_bspmm_planned_f32": (c_int, [P, ctypes.c_size_t, c_int, c_int, ctypes.c_longlong, P, P, P, P, P, P, c_int,
+                                       c_int, ctypes.c_float, ctypes.c_float, ctypes.c_float, P]),
+    "rvgp_bspmm_planned_f64": (c_int, [P, ctypes.c_size_t, c_int, c_int, ctypes.c_longlong, P, P, P, P, P, P, c_int,
+                                       c_int, c_double, c_double, c_double, P]),
     "rvgp_gp_fit_mixed_workspace": (c_size_t, [c_int]),
     "rvgp_gp_fit_adam_mixed": (c_int, [P, P, P, ctypes.c_longlong, c_int, P, c_double, c_int, P, P, P, c_int,
                                        c_double, c_double, c_double, c_double, P, P, P, P, P, P, c_size_t, P]),
@@ -250,15 +256,36 @@ def connections(T, d, indptr, indices, want_R=True, want64=True, want32=True):
 
 
 # ---------------------------------------------------------------------------- products
-def bspmm(indptr, indices, vals, X, Y=None, Z=None, alpha=1.0, beta=0.0, gamma=0.0):
-    """Y = alpha*(A X) + beta*X + gamma*Z for block-CSR A with square blocks."""
+def spmm_plan(indptr, indices, DB=1):
+    """The tiled product's plan of a block-CSR matrix (a byte tensor): per tile
+    of 32 block rows its halo of distinct columns and every entry's position
+    in it.  Build once per matrix, pass to ``bspmm(..., plan=)``."""
+    n = indptr.numel() - 1
+    nnz = indices.numel()
+    L = lib()
+    nbytes = L.rvgp_spmm_plan_bytes(n, DB, nnz)
+    plan = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=indptr.device)
+    check(L.rvgp_spmm_plan_build(n, DB, ptr(indptr), ptr(indices), nnz, ptr(plan), nbytes, stream()),
+          "rvgp_spmm_plan_build")
+    return plan
+
+
+def bspmm(indptr, indices, vals, X, Y=None, Z=None, alpha=1.0, beta=0.0, gamma=0.0, plan=None):
+    """Y = alpha*(A X) + beta*X + gamma*Z for block-CSR A with square blocks
+    (tiled through ``plan`` when given: the same bits)."""
     n = indptr.numel() - 1
     DB = 1 if vals.dim() == 1 else vals.shape[-1]
     rows, b = X.shape
     if rows != n * DB:
         raise ValueError("X rows must equal n * block size")
     Y = torch.empty_like(X) if Y is None else Y
-    f = lib().rvgp_bspmm_f32 if X.dtype == torch.float32 else lib().rvgp_bspmm_f64
+    L = lib()
+    if plan is not None:
+        f = L.rvgp_bspmm_planned_f32 if X.dtype == torch.float32 else L.rvgp_bspmm_planned_f64
+        check(f(ptr(plan), plan.numel(), n, DB, indices.numel(), ptr(indptr), ptr(indices), ptr(vals), ptr(X),
+                ptr(Y), ptr(Z), b, X.stride(0), alpha, beta, gamma, stream()), "rvgp_bspmm_planned")
+        return Y
+    f = L.rvgp_bspmm_f32 if X.dtype == torch.float32 else L.rvgp_bspmm_f64
     check(f(n, DB, ptr(indptr), ptr(indices), ptr(vals), ptr(X), ptr(Y), ptr(Z), b, X.stride(0), alpha, beta, gamma,
             stream()), "rvgp_bspmm")
     return Y
@@ -297,7 +324,9 @@ def eigsh(indptr, indices, vals64, vals32=None, m=10, mode="mixed", tol=None, to
     if tol is None:  # mixed: stop at the FP32 stage's accuracy; fp64: ARPACK-level residuals
         tol = tol32 if imode == 1 else 1e-11
     L = lib()
-    ws = workspace(L.rvgp_eigsh_workspace(n, DB, m, p, imode), dev)
+    # + the tiled product's plan (built inside, once per solve)
+    ws = workspace(L.rvgp_eigsh_workspace(n, DB, m, p, imode) + 256 +
+                   L.rvgp_spmm_plan_bytes(n, DB, indices.numel()), dev)
     sc = 1.0 if scale is None else float(scale)
     if perm is None:
         st = L.rvgp_eigsh(ptr(indptr), ptr(indices), ptr(vals64), ptr(vals32), n, DB, m, p, imode, tol, tol32,
@@ -308,7 +337,7 @@ def eigsh(indptr, indices, vals64, vals32=None, m=10, mode="mixed", tol=None, to
                                   tol32, max_iter, seed, ptr(perm), ptr(evals), ptr(evecs), m, sc, stats, ptr(ws),
                                   ws.numel(), stream())
     info = dict(iters=stats[0], spmm=stats[1], sweeps=stats[2], converged=stats[3], refine_iters=stats[4],
-                chol_rescues=stats[5], tensor_cores=bool(stats[6]), p=p, filter_ms=stats[8] / 1e3, orth_ms=stats[9] / 1e3,
+                chol_rescues=stats[5], tensor_cores=bool(stats[6]), tiled_spmm=bool(stats[7]), p=p, filter_ms=stats[8] / 1e3, orth_ms=stats[9] / 1e3,
                 rr_ms=stats[10] / 1e3, jacobi_ms=stats[11] / 1e3)
     if st < 0:
         check(st, "rvgp_eigsh")

@@ -30,20 +30,33 @@
 #include <algorithm>
 
 namespace rvgp {
-int bspmm_f32(int n, int DB, const int* indptr, const int* indices, const float* vals, const float* X, float* Y,
-              const float* Z, int b, int ld, float alpha, float beta, float gamma, cudaStream_t st);
-int bspmm_f64(int n, int DB, const int* indptr, const int* indices, const double* vals, const double* X, double* Y,
-              const double* Z, int b, int ld, double alpha, double beta, double gamma, cudaStream_t st);
+int bspmm_planned_f32(const void* plan, size_t plan_bytes, int n, int DB, long long nnz, const int* indptr,
+                      const int* indices, const float* vals, const float* X, float* Y, const float* Z, int b, int ld,
+                      float alpha, float beta, float gamma, cudaStream_t st);
+int bspmm_planned_f64(const void* plan, size_t plan_bytes, int n, int DB, long long nnz, const int* indptr,
+                      const int* indices, const double* vals, const double* X, double* Y, const double* Z, int b,
+                      int ld, double alpha, double beta, double gamma, cudaStream_t st);
+size_t spmm_plan_bytes(int n, int DB, long long nnz);
+int spmm_plan_build(int n, int DB, const int* indptr, const int* indices, long long nnz, void* plan,
+                    size_t plan_bytes, cudaStream_t st);
 
 namespace {
 
-inline int spmm(int n, int DB, const int* ip, const int* ix, const float* v, const float* X, float* Y, const float* Z,
-                int b, int ld, double al, double be, double ga, cudaStream_t st) {
-  return bspmm_f32(n, DB, ip, ix, v, X, Y, Z, b, ld, (float)al, (float)be, (float)ga, st);
+// the tiled product's plan of the matrix (null: untiled variants)
+struct SpmmPlan {
+  const void* plan = nullptr;
+  size_t bytes = 0;
+  long long nnz = 0;
+};
+
+inline int spmm(const SpmmPlan& pl, int n, int DB, const int* ip, const int* ix, const float* v, const float* X,
+                float* Y, const float* Z, int b, int ld, double al, double be, double ga, cudaStream_t st) {
+  return bspmm_planned_f32(pl.plan, pl.bytes, n, DB, pl.nnz, ip, ix, v, X, Y, Z, b, ld, (float)al, (float)be,
+                           (float)ga, st);
 }
-inline int spmm(int n, int DB, const int* ip, const int* ix, const double* v, const double* X, double* Y,
-                const double* Z, int b, int ld, double al, double be, double ga, cudaStream_t st) {
-  return bspmm_f64(n, DB, ip, ix, v, X, Y, Z, b, ld, al, be, ga, st);
+inline int spmm(const SpmmPlan& pl, int n, int DB, const int* ip, const int* ix, const double* v, const double* X,
+                double* Y, const double* Z, int b, int ld, double al, double be, double ga, cudaStream_t st) {
+  return bspmm_planned_f64(pl.plan, pl.bytes, n, DB, pl.nnz, ip, ix, v, X, Y, Z, b, ld, al, be, ga, st);
 }
 
 __global__ void gershgorin_kernel(int n, int DB, const int* __restrict__ indptr, const double* __restrict__ vals,
@@ -252,6 +265,7 @@ struct Problem {
   const double* v64;
   const float* v32;
   int m, p;
+  SpmmPlan plan;
 };
 
 template <typename T>
@@ -333,11 +347,11 @@ int filter(const Problem& P, Block<T>& B, int deg, double a, double b, double a0
   const double tau = 2.0 / sigma;
   T *X = B.V, *Y = B.T1, *Z = B.T2;
   const T* vals = vals_of<T>(P);
-  TRY(spmm(P.n, P.DB, P.indptr, P.indices, vals, X, Y, (const T*)nullptr, P.p, P.p, sigma / e, -c * sigma / e, 0.0, st));
+  TRY(spmm(P.plan, P.n, P.DB, P.indptr, P.indices, vals, X, Y, (const T*)nullptr, P.p, P.p, sigma / e, -c * sigma / e, 0.0, st));
   ++stt.spmm;
   for (int i = 2; i <= deg; ++i) {
     const double sn = 1.0 / (tau - sigma);
-    TRY(spmm(P.n, P.DB, P.indptr, P.indices, vals, Y, Z, X, P.p, P.p, 2 * sn / e, -2 * c * sn / e, -sigma * sn, st));
+    TRY(spmm(P.plan, P.n, P.DB, P.indptr, P.indices, vals, Y, Z, X, P.p, P.p, 2 * sn / e, -2 * c * sn / e, -sigma * sn, st));
     ++stt.spmm;
     T* t = X;
     X = Y;
@@ -446,7 +460,7 @@ int rayleigh_ritz(const Problem& P, Block<T>& B, Small& s, Stats& stt, int max_s
                   std::vector<double>& res, PhaseEvents& ev, cudaStream_t st) {
   const long long N = P.N;
   const int p = P.p;
-  TRY(spmm(P.n, P.DB, P.indptr, P.indices, vals_of<T>(P), B.V, B.W, (const T*)nullptr, p, p, 1.0, 0.0, 0.0, st));
+  TRY(spmm(P.plan, P.n, P.DB, P.indptr, P.indices, vals_of<T>(P), B.V, B.W, (const T*)nullptr, p, p, 1.0, 0.0, 0.0, st));
   ++stt.spmm;
   TRY(gram_any(B.V, B.W, N, p, s.H, s, st));
   int used = 0;
@@ -655,8 +669,23 @@ static int eigsh_impl(const int* indptr, const int* indices, const double* vals6
   s.jac32 = (mode == 1 && p % 2 == 0 && p <= jacobi32_max_p()) ? 1 : 0;
   s.tc = (mode == 1 && s.tc_bytes > 0 && tc_enabled() && tc_supported(p, p)) ? 1 : 0;
   cudaMemsetAsync(s.tc_err, 0, sizeof(int), st);
-  Problem P{n, DB, N, indptr, indices, vals64, vals32, m, p};
+  Problem P{n, DB, N, indptr, indices, vals64, vals32, m, p, SpmmPlan{}};
   Stats stt;
+  // the tiled product's plan, in the workspace beyond `need` when the caller
+  // sized it for one (rvgp_spmm_plan_bytes); RVGP_SPMM_TILED=0 turns it off
+  {
+    const char* e = getenv("RVGP_SPMM_TILED");
+    int nnz = 0;
+    if (!(e && e[0] == '0') && ws_bytes > need) {
+      if (read_back(&nnz, indptr + n, sizeof(int), st) != cudaSuccess) return check_launch("rvgp_eigsh");
+      const size_t pb = spmm_plan_bytes(n, DB, nnz);
+      if (pb > 0 && ws.used + 256 + pb <= ws_bytes) {
+        void* plan = ws.take<char>(pb);
+        TRY(spmm_plan_build(n, DB, indptr, indices, nnz, plan, pb, st));
+        P.plan = SpmmPlan{plan, pb, (long long)nnz};
+      }
+    }
+  }
 
   // spectrum upper bound (Gershgorin)
   const int gb = std::min(num_sms() * 2, ceil_div(N, 256));
@@ -698,6 +727,7 @@ static int eigsh_impl(const int* indptr, const int* indices, const double* vals6
     stats[4] = stt.refine_iters;
     stats[5] = stt.chol_rescues;
     stats[6] = s.tc;
+    stats[7] = P.plan.plan != nullptr;
     for (int q = 0; q < 4; ++q) stats[8 + q] = (int)(stt.ms[q] * 1000.f);  // microseconds per phase
   }
   RVGP_LAUNCH_CHECK("rvgp_eigsh");

@@ -22,6 +22,7 @@
 // HBM traffic per product ≈ E*(DB²*sv + 4) + 2*n*DB*b*sx (+ Z).
 #include "common.cuh"
 #include "autotune.cuh"
+#include <limits.h>
 #include <stdio.h>
 #include <stdlib.h>
 
@@ -328,6 +329,274 @@ int launch(int n, int DB, const int* indptr, const int* indices, const T* vals, 
   return run(v);
 }
 
+// ------------------------------------------------------------ tiled form
+// The product over one matrix is repeated hundreds of times (Chebyshev
+// filter), so a plan built once per matrix pays: block rows are cut into
+// tiles of kTileRows consecutive rows (in the locality-preserving order, a
+// compact patch), and for every tile the sorted set of distinct block rows
+// its entries reference (its halo, ~4x fewer than the references at k = 15
+// on a surface) and, per entry, the position of its column in that set.
+// CTA (tile, chunk) copies the halo's rows, one 128-byte column chunk of
+// them, into shared memory (cp.async) and forms the tile's output rows from
+// there; the grid runs chunk by chunk, so one chunk of X (n*DB*128 bytes)
+// stays in L2 while the tiles that gather from it run, and X is read from
+// HBM about once per product.  Tiles whose halo or entry count exceeds the
+// shared-memory budget are marked (halo size -1) and gather from global
+// memory.  Each output row accumulates neighbour by neighbour and block
+// column by block column as the other variants do: the same bits.
+constexpr int kTileRows = 32;
+constexpr int kHaloRows = 576;      // halo rows x DB per tile (72 KB of 128-byte chunks)
+constexpr int kPlanMaxEntries = 2048;
+constexpr int kSegBytes = 128;
+
+__host__ __device__ inline int plan_hmax(int DB) { return kHaloRows / DB; }
+inline int plan_tiles(int n) { return (n + kTileRows - 1) / kTileRows; }
+
+struct PlanView {
+  int* tile_h;
+  int* halo;
+  unsigned short* lidx;
+};
+
+PlanView plan_view(void* plan, size_t bytes, int n, int DB, long long nnz) {
+  Workspace ws(plan, bytes);
+  PlanView v;
+  v.tile_h = ws.take<int>(plan_tiles(n));
+  v.halo = ws.take<int>((size_t)plan_tiles(n) * plan_hmax(DB));
+  v.lidx = ws.take<unsigned short>((size_t)nnz);
+  return v;
+}
+
+__global__ void __launch_bounds__(256) spmm_plan_kernel(int n, int hmax, const int* __restrict__ indptr,
+                                                        const int* __restrict__ indices, int* __restrict__ tile_h,
+                                                        int* __restrict__ halo, unsigned short* __restrict__ lidx) {
+  __shared__ int keys[kPlanMaxEntries];
+  __shared__ int uniq[kPlanMaxEntries];
+  __shared__ int wsum[8];
+  const int tile = blockIdx.x, tid = threadIdx.x;
+  const int i0 = tile * kTileRows, i1 = min(n, i0 + kTileRows);
+  const int e0 = indptr[i0], ne = indptr[i1] - e0;
+  if (ne > kPlanMaxEntries) {
+    if (tid == 0) tile_h[tile] = -1;
+    return;
+  }
+  int P2 = 1;
+  while (P2 < ne) P2 <<= 1;
+  for (int k = tid; k < P2; k += 256) keys[k] = k < ne ? indices[e0 + k] : INT_MAX;
+  __syncthreads();
+  for (int size = 2; size <= P2; size <<= 1)
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int k = tid; k < P2 / 2; k += 256) {
+        const int lo = 2 * stride * (k / stride) + (k % stride), hi = lo + stride;
+        const bool asc = (lo & size) == 0;
+        const int a = keys[lo], b = keys[hi];
+        if ((a > b) == asc) {
+          keys[lo] = b;
+          keys[hi] = a;
+        }
+      }
+      __syncthreads();
+    }
+  // distinct keys: exclusive scan of the first-occurrence flags, runs of
+  // kPlanMaxEntries / 256 = 8 consecutive keys per thread
+  constexpr int RUN = kPlanMaxEntries / 256;
+  int flags[RUN], cnt = 0;
+#pragma unroll
+  for (int r = 0; r < RUN; ++r) {
+    const int k = tid * RUN + r;
+    flags[r] = (k < ne && (k == 0 || keys[k] != keys[k - 1])) ? 1 : 0;
+    cnt += flags[r];
+  }
+  const int lane = tid & 31, warp = tid >> 5;
+  int incl = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += v;
+  }
+  if (lane == 31) wsum[warp] = incl;
+  __syncthreads();
+  int base = 0, total = 0;
+  for (int w = 0; w < 8; ++w) {
+    if (w < warp) base += wsum[w];
+    total += wsum[w];
+  }
+  int pos = base + incl - cnt;
+#pragma unroll
+  for (int r = 0; r < RUN; ++r)
+    if (flags[r]) uniq[pos++] = keys[tid * RUN + r];
+  __syncthreads();
+  if (total > hmax) {
+    if (tid == 0) tile_h[tile] = -1;
+    return;
+  }
+  for (int k = tid; k < total; k += 256) halo[(size_t)tile * hmax + k] = uniq[k];
+  for (int k = tid; k < ne; k += 256) {
+    const int c = indices[e0 + k];
+    int lo = 0, hi = total - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (uniq[mid] < c)
+        lo = mid + 1;
+      else
+        hi = mid;
+    }
+    lidx[e0 + k] = (unsigned short)lo;
+  }
+  if (tid == 0) tile_h[tile] = total;
+}
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+template <typename T, int DB, int U>
+__global__ void __launch_bounds__(256) bspmm_tiled_kernel(int n, int n_tiles, const int* __restrict__ tile_h,
+                                                          const int* __restrict__ halo,
+                                                          const unsigned short* __restrict__ lidx,
+                                                          const int* __restrict__ indptr,
+                                                          const int* __restrict__ indices,
+                                                          const T* __restrict__ vals, const T* __restrict__ X,
+                                                          T* __restrict__ Y, const T* __restrict__ Z, int b, int ld,
+                                                          T alpha, T beta, T gamma) {
+  constexpr int V = Vec<T>::V;
+  constexpr int SEG = kSegBytes / (int)sizeof(T);  // chunk width in elements
+  constexpr int G = SEG / V;                       // lanes per row (8)
+  constexpr int HM = kHaloRows / DB;
+  extern __shared__ __align__(16) unsigned char tiled_smem[];
+  T* xs = reinterpret_cast<T*>(tiled_smem);
+  const int tile = blockIdx.x % n_tiles, chunk = blockIdx.x / n_tiles;
+  const int c0 = chunk * SEG;
+  const int groups = min(G, (b - c0) / V);
+  const int h = __ldg(tile_h + tile);
+  if (h > 0) {
+    const int* hl = halo + (size_t)tile * HM;
+    for (int e = threadIdx.x; e < h * DB * G; e += 256) {
+      const int r = e / G, g = e % G;  // r = halo row * DB + q
+      if (g < groups) {
+        const int j = __ldg(hl + r / DB), q = r % DB;
+        cp_async16(xs + (size_t)r * SEG + g * V, X + ((size_t)j * DB + q) * ld + c0 + g * V);
+      }
+    }
+    cp_async_wait_all();
+    __syncthreads();
+  }
+  const int slot = threadIdx.x / G, g = threadIdx.x % G;
+  const int i = tile * kTileRows + slot;
+  if (i >= n) return;  // no barrier below
+  const bool on = g < groups;
+  const bool staged = h >= 0;
+  const int col = c0 + g * V;
+  T acc[DB][V];
+#pragma unroll
+  for (int p = 0; p < DB; ++p)
+#pragma unroll
+    for (int v = 0; v < V; ++v) acc[p][v] = T(0);
+  const int s = __ldg(indptr + i), e = __ldg(indptr + i + 1);
+  int t = s;
+  for (; t + U <= e; t += U) {
+    T blk[U][DB * DB], x[U][DB][V];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      load_block<T, DB>(vals, t + u, blk[u]);
+      if (on) {
+        if (staged) {
+          const int li = __ldg(lidx + t + u);
+#pragma unroll
+          for (int q = 0; q < DB; ++q) vload(xs + (size_t)(li * DB + q) * SEG + g * V, x[u][q]);
+        } else {
+          const int j = __ldg(indices + t + u);
+#pragma unroll
+          for (int q = 0; q < DB; ++q) vload(X + ((size_t)j * DB + q) * ld + col, x[u][q]);
+        }
+      }
+    }
+    if (on)
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+#pragma unroll
+        for (int q = 0; q < DB; ++q)
+#pragma unroll
+          for (int p = 0; p < DB; ++p)
+#pragma unroll
+            for (int v = 0; v < V; ++v) acc[p][v] = fma(blk[u][p * DB + q], x[u][q][v], acc[p][v]);
+  }
+  for (; t < e; ++t) {
+    T blk[DB * DB], x[DB][V];
+    load_block<T, DB>(vals, t, blk);
+    if (on) {
+      if (staged) {
+        const int li = __ldg(lidx + t);
+#pragma unroll
+        for (int q = 0; q < DB; ++q) vload(xs + (size_t)(li * DB + q) * SEG + g * V, x[q]);
+      } else {
+        const int j = __ldg(indices + t);
+#pragma unroll
+        for (int q = 0; q < DB; ++q) vload(X + ((size_t)j * DB + q) * ld + col, x[q]);
+      }
+#pragma unroll
+      for (int q = 0; q < DB; ++q)
+#pragma unroll
+        for (int p = 0; p < DB; ++p)
+#pragma unroll
+          for (int v = 0; v < V; ++v) acc[p][v] = fma(blk[p * DB + q], x[q][v], acc[p][v]);
+    }
+  }
+  if (!on) return;
+#pragma unroll
+  for (int p = 0; p < DB; ++p) {
+    const size_t row = ((size_t)i * DB + p) * ld + col;
+    T out[V], x[V];
+#pragma unroll
+    for (int v = 0; v < V; ++v) out[v] = alpha * acc[p][v];
+    if (beta != T(0)) {
+      vload(X + row, x);
+#pragma unroll
+      for (int v = 0; v < V; ++v) out[v] = fma(beta, x[v], out[v]);
+    }
+    if (Z && gamma != T(0)) {
+      vload(Z + row, x);
+#pragma unroll
+      for (int v = 0; v < V; ++v) out[v] = fma(gamma, x[v], out[v]);
+    }
+    vstore(Y + row, out);
+  }
+}
+
+template <typename T, int DB>
+int launch_tiled_db(int n, const PlanView& pv, const int* indptr, const int* indices, const T* vals, const T* X, T* Y,
+                    const T* Z, int b, int ld, T alpha, T beta, T gamma, cudaStream_t st) {
+  constexpr int SEG = kSegBytes / (int)sizeof(T);
+  const int nt = plan_tiles(n), nch = ceil_div(b, SEG);
+  const size_t smem = (size_t)kHaloRows / DB * DB * kSegBytes;
+  if (cudaFuncSetAttribute(bspmm_tiled_kernel<T, DB, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+      cudaSuccess)
+    return check_launch("rvgp_bspmm (tiled)");
+  rvgp::note_launch();
+  bspmm_tiled_kernel<T, DB, 2><<<(unsigned)((long long)nt * nch), 256, smem, st>>>(
+      n, nt, pv.tile_h, pv.halo, pv.lidx, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma);
+  return check_launch("rvgp_bspmm (tiled)");
+}
+
+template <typename T>
+int launch_tiled(const void* plan, size_t plan_bytes, int n, int DB, long long nnz, const int* indptr,
+                 const int* indices, const T* vals, const T* X, T* Y, const T* Z, int b, int ld, T alpha, T beta,
+                 T gamma, cudaStream_t st) {
+  constexpr int V = Vec<T>::V;
+  RVGP_CHECK_ARG(b % V == 0 && ld % V == 0 && b <= ld, "rvgp_bspmm: b=%d and ld=%d must be multiples of %d", b, ld, V);
+  RVGP_CHECK_ARG(((uintptr_t)X | (uintptr_t)Y | (uintptr_t)(Z ? Z : X)) % 16 == 0, "rvgp_bspmm: 16-byte alignment");
+  RVGP_CHECK_ARG(DB >= 1 && DB <= 4, "rvgp_bspmm: block size %d not supported (1..4)", DB);
+  const PlanView pv = plan_view(const_cast<void*>(plan), plan_bytes, n, DB, nnz);
+  switch (DB) {
+    case 1: return launch_tiled_db<T, 1>(n, pv, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
+    case 2: return launch_tiled_db<T, 2>(n, pv, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
+    case 3: return launch_tiled_db<T, 3>(n, pv, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
+    default: return launch_tiled_db<T, 4>(n, pv, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
+  }
+}
+
 }  // namespace
 
 int bspmm_f32(int n, int DB, const int* indptr, const int* indices, const float* vals, const float* X, float* Y,
@@ -337,6 +606,42 @@ int bspmm_f32(int n, int DB, const int* indptr, const int* indices, const float*
 int bspmm_f64(int n, int DB, const int* indptr, const int* indices, const double* vals, const double* X, double* Y,
               const double* Z, int b, int ld, double alpha, double beta, double gamma, cudaStream_t st) {
   return launch<double>(n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
+}
+
+size_t spmm_plan_bytes(int n, int DB, long long nnz) {
+  if (n < 1 || DB < 1 || DB > 4 || nnz < 0) return 0;
+  Workspace ws(nullptr, 0);
+  ws.take<int>(plan_tiles(n));
+  ws.take<int>((size_t)plan_tiles(n) * plan_hmax(DB));
+  ws.take<unsigned short>((size_t)nnz);
+  return ws.used;
+}
+
+int spmm_plan_build(int n, int DB, const int* indptr, const int* indices, long long nnz, void* plan,
+                    size_t plan_bytes, cudaStream_t st) {
+  RVGP_CHECK_ARG(indptr && indices && plan, "rvgp_spmm_plan_build: null pointer");
+  RVGP_CHECK_ARG(n >= 1 && DB >= 1 && DB <= 4 && nnz >= 0, "rvgp_spmm_plan_build: bad n=%d or DB=%d", n, DB);
+  RVGP_CHECK_ARG(plan_bytes >= spmm_plan_bytes(n, DB, nnz), "rvgp_spmm_plan_build: plan of %zu bytes needed",
+                 spmm_plan_bytes(n, DB, nnz));
+  const PlanView pv = plan_view(plan, plan_bytes, n, DB, nnz);
+  rvgp::note_launch();
+  spmm_plan_kernel<<<plan_tiles(n), 256, 0, st>>>(n, plan_hmax(DB), indptr, indices, pv.tile_h, pv.halo, pv.lidx);
+  return check_launch("rvgp_spmm_plan_build");
+}
+
+int bspmm_planned_f32(const void* plan, size_t plan_bytes, int n, int DB, long long nnz, const int* indptr,
+                      const int* indices, const float* vals, const float* X, float* Y, const float* Z, int b, int ld,
+                      float alpha, float beta, float gamma, cudaStream_t st) {
+  if (!plan) return launch<float>(n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
+  return launch_tiled<float>(plan, plan_bytes, n, DB, nnz, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma,
+                             st);
+}
+int bspmm_planned_f64(const void* plan, size_t plan_bytes, int n, int DB, long long nnz, const int* indptr,
+                      const int* indices, const double* vals, const double* X, double* Y, const double* Z, int b,
+                      int ld, double alpha, double beta, double gamma, cudaStream_t st) {
+  if (!plan) return launch<double>(n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
+  return launch_tiled<double>(plan, plan_bytes, n, DB, nnz, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta,
+                              gamma, st);
 }
 
 }  // namespace rvgp
@@ -351,4 +656,32 @@ RVGP_API int rvgp_bspmm_f64(int n, int DB, const int* indptr, const int* indices
                             const double* X, double* Y, const double* Z, int b, int ld, double alpha, double beta,
                             double gamma, void* stream) {
   return rvgp::bspmm_f64(n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, rvgp::as_stream(stream));
+}
+
+// Bytes of the tiled product's plan for a block-CSR matrix of n block rows
+// (DB x DB blocks) and nnz stored blocks.
+RVGP_API size_t rvgp_spmm_plan_bytes(int n, int DB, long long nnz) { return rvgp::spmm_plan_bytes(n, DB, nnz); }
+
+// Builds the plan (per tile of 32 block rows: its halo of distinct columns
+// and the local column of every entry) into caller memory.  Stream-ordered.
+RVGP_API int rvgp_spmm_plan_build(int n, int DB, const int* indptr, const int* indices, long long nnz, void* plan,
+                                  size_t plan_bytes, void* stream) {
+  return rvgp::spmm_plan_build(n, DB, indptr, indices, nnz, plan, plan_bytes, rvgp::as_stream(stream));
+}
+
+// rvgp_bspmm_f32 / _f64 through a plan of the same matrix (null plan: the
+// untiled variants).  The same bits as rvgp_bspmm_*.
+RVGP_API int rvgp_bspmm_planned_f32(const void* plan, size_t plan_bytes, int n, int DB, long long nnz,
+                                    const int* indptr, const int* indices, const float* vals, const float* X,
+                                    float* Y, const float* Z, int b, int ld, float alpha, float beta, float gamma,
+                                    void* stream) {
+  return rvgp::bspmm_planned_f32(plan, plan_bytes, n, DB, nnz, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta,
+                                 gamma, rvgp::as_stream(stream));
+}
+RVGP_API int rvgp_bspmm_planned_f64(const void* plan, size_t plan_bytes, int n, int DB, long long nnz,
+                                    const int* indptr, const int* indices, const double* vals, const double* X,
+                                    double* Y, const double* Z, int b, int ld, double alpha, double beta,
+                                    double gamma, void* stream) {
+  return rvgp::bspmm_planned_f64(plan, plan_bytes, n, DB, nnz, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta,
+                                 gamma, rvgp::as_stream(stream));
 }

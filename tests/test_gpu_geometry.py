@@ -155,3 +155,38 @@ def test_bspmm(core, d, dtype, b):
                    alpha=0.7, beta=-0.3, gamma=1.9)
     tol = 1e-12 if dtype == torch.float64 else 2e-5
     np.testing.assert_allclose(Y.cpu().double().numpy(), ref, atol=tol * np.abs(ref).max())
+
+
+@pytest.mark.parametrize("d,dtype,b", [(1, torch.float32, 564), (2, torch.float32, 564), (2, torch.float64, 130),
+                                       (3, torch.float32, 40), (4, torch.float64, 8), (1, torch.float64, 6),
+                                       (2, torch.float32, 4)])
+def test_bspmm_planned_same_bits(core, d, dtype, b):
+    """The tiled product (a plan per matrix, halo rows staged in shared memory)
+    gives the bits of the untiled product: tiles of 32 rows with ragged last
+    column chunks, empty rows, a tile whose halo exceeds the shared-memory
+    budget and one with more than 2048 entries (both gather from global
+    memory), and a last tile of fewer than 32 rows."""
+    rng = np.random.default_rng(7 * d + b)
+    n = 1000 + 17
+    A = sp.random(n, n, density=0.012, random_state=3, format="lil")
+    A[40:72, :] = 0.0                      # tile 1: rows 40..63 empty, ...
+    A[70, rng.choice(n, 900, replace=False)] = 1.0   # ... tile 2: halo above every budget
+    A[128:160, :] = sp.random(32, n, density=0.08, random_state=4).tolil()  # tile 4: > 2048 entries
+    A = (A.tocsr() + sp.eye(n)).tocsr()
+    A.sort_indices()
+    blocks = rng.standard_normal((A.nnz, d, d))
+    X = rng.standard_normal((n * d, b))
+    Z = rng.standard_normal((n * d, b))
+    vals = cu(blocks if d > 1 else blocks[:, 0, 0], dtype)
+    ip, ix = cu(A.indptr, torch.int32), cu(A.indices, torch.int32)
+    plan = core.spmm_plan(ip, ix, d)
+    for beta, Zt in ((-0.3, cu(Z, dtype)), (0.0, None)):
+        ref = core.bspmm(ip, ix, vals, cu(X, dtype), Z=Zt, alpha=0.7, beta=beta, gamma=1.9)
+        got = core.bspmm(ip, ix, vals, cu(X, dtype), Z=Zt, alpha=0.7, beta=beta, gamma=1.9, plan=plan)
+        torch.cuda.synchronize()
+        assert torch.equal(got, ref)
+    M = sp.bsr_matrix((blocks, A.indices, A.indptr), shape=(n * d, n * d))
+    want = 0.7 * (M @ X) - 0.3 * X + 1.9 * Z
+    got = core.bspmm(ip, ix, vals, cu(X, dtype), Z=cu(Z, dtype), alpha=0.7, beta=-0.3, gamma=1.9, plan=plan)
+    tol = 1e-12 if dtype == torch.float64 else 2e-5
+    np.testing.assert_allclose(got.cpu().double().numpy(), want, atol=tol * np.abs(want).max())
