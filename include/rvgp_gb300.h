@@ -393,6 +393,18 @@ size_t rvgp_fps_persistent_workspace(int n);
 int rvgp_fps_persistent(const double* X, int n, int D, int N_max, int start, const double* diam, double spacing,
                         int* perm, double* lambdas, int* count, long long* exact_evals, void* workspace,
                         size_t ws_bytes, void* stream);
+
+/* The same selections by spatial pruning (D <= 8, n <= rvgp_fps_spatial_max_n(D)):
+ * points renumbered along a Morton curve into blocks of 32 and superblocks of
+ * 1024 with FP64 bounding boxes and running maxima; each selection updates
+ * only the blocks whose box comes closer to the new point than their maximum,
+ * in one CTA (no grid-wide barrier).  Same arguments and results as
+ * rvgp_fps_persistent (RVGP/geometry.py:126-162). */
+int rvgp_fps_spatial_max_n(int D);
+size_t rvgp_fps_spatial_workspace(int n, int D);
+int rvgp_fps_spatial(const double* X, int n, int D, int N_max, int start, const double* diam, double spacing,
+                     int* perm, double* lambdas, int* count, long long* exact_evals, void* workspace, size_t ws_bytes,
+                     void* stream);
 size_t rvgp_diameter_workspace(int n);
 int rvgp_diameter(const double* X, int n, int D, double* out, void* workspace, size_t ws_bytes, void* stream);
 

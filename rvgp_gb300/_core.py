@@ -47,6 +47,9 @@ SIGNATURES = {
     "rvgp_gp_fit_adam": (c_int, [P, P, P, ctypes.c_longlong, c_int, P, c_double, c_int, P, P, P, c_int, c_double,
                                  c_double, c_double, c_double, P, P, P, P, P, c_size_t, P]),
     "rvgp_gp_fit_mixed_max_m": (c_int, []),
+    "rvgp_fps_spatial_max_n": (c_int, [c_int]),
+    "rvgp_fps_spatial_workspace": (c_size_t, [c_int, c_int]),
+    "rvgp_fps_spatial": (c_int, [P, c_int, c_int, c_int, c_int, P, c_double, P, P, P, P, P, c_size_t, P]),
     "rvgp_spmm_plan_bytes": (ctypes.c_size_t, [c_int, c_int, ctypes.c_longlong]),
     "rvgp_spmm_plan_build": (c_int, [c_int, c_int, P, P, ctypes.c_longlong, P, ctypes.c_size_t, P]),
     "rvgp_bspmm_planned_f32": (c_int, [P, ctypes.c_size_t, c_int, c_int, ctypes.c_longlong, P, P, P, P, P, P, c_int,
@@ -848,12 +851,14 @@ def diameter(X):
     return out
 
 
-def fps(X, N=None, spacing=0.1, start_idx=0, persistent=None, stats=None):
+def fps(X, N=None, spacing=0.1, start_idx=0, persistent=None, stats=None, method=None):
     """(perm int32, lambdas f64) on the device: RVGP/geometry.py:126-162.
-    persistent (default: D <= 8): one cooperative launch for all selections
-    (rvgp_fps_persistent) instead of one launch per selection (rvgp_fps);
-    the same result.  ``stats`` (dict, optional) receives the number of exact
-    FP64 distances the persistent form evaluated."""
+    method: "spatial" (default for D <= 8 up to rvgp_fps_spatial_max_n: one
+    CTA visits only the blocks of points the new selection can change),
+    "persistent" (one cooperative launch over all points per selection) or
+    "steps" (one launch per selection); the same result.  persistent=True /
+    False are the older names of "persistent" / "steps".  ``stats`` (dict,
+    optional) receives the number of exact FP64 distances evaluated."""
     X = _dev(X, torch.float64, "X")
     n, D = X.shape
     N_max = n if N is None else int(N)
@@ -863,9 +868,23 @@ def fps(X, N=None, spacing=0.1, start_idx=0, persistent=None, stats=None):
     count = torch.empty(1, dtype=torch.int32, device=dev)
     diam = diameter(X) if N is None else None
     L = lib()
-    if persistent is None:
-        persistent = D <= 8
-    if persistent:
+    if method is None:
+        if persistent is not None:
+            method = "persistent" if persistent else "steps"
+        elif D <= 8 and n <= L.rvgp_fps_spatial_max_n(D):
+            method = "spatial"
+        else:
+            method = "persistent" if D <= 8 else "steps"
+    if method not in ("spatial", "persistent", "steps"):
+        raise ValueError(f"fps: unknown method {method!r}")
+    if method == "spatial":
+        ev = torch.zeros(1, dtype=torch.int64, device=dev)
+        ws = workspace(L.rvgp_fps_spatial_workspace(n, D), dev)
+        check(L.rvgp_fps_spatial(ptr(X), n, D, N_max, int(start_idx), ptr(diam), float(spacing), ptr(perm),
+                                 ptr(lam), ptr(count), ptr(ev), ptr(ws), ws.numel(), stream()), "rvgp_fps_spatial")
+        if stats is not None:
+            stats["exact_evals"] = int(ev.item())
+    elif method == "persistent":
         ev = torch.zeros(1, dtype=torch.int64, device=dev)
         ws = workspace(L.rvgp_fps_persistent_workspace(n), dev)
         check(L.rvgp_fps_persistent(ptr(X), n, D, N_max, int(start_idx), ptr(diam), float(spacing), ptr(perm),

@@ -14,6 +14,7 @@
 #include "gridsync.cuh"
 #include <float.h>
 #include <limits.h>
+#include <algorithm>
 
 namespace rvgp {
 namespace {
@@ -374,5 +375,352 @@ RVGP_API int rvgp_diameter(const double* X, int n, int D, double* out, void* wor
   rvgp::note_launch(); diameter_tiles<<<num_sms() * 4, kThreads, 0, st>>>(X, n, D, part);
   rvgp::note_launch(); max_reduce<<<1, kThreads, 0, st>>>(part, num_sms() * 4, out);
   RVGP_LAUNCH_CHECK("rvgp_diameter");
+  return RVGP_OK;
+}
+
+// ------------------------------------------------------------ spatial form
+// The same selections with the update confined to where it can change
+// anything.  Selecting p with value r = max_x ds[x] lowers ds[x] only where
+// d(p, x) < ds[x] <= r.  Points are renumbered along a Morton curve
+// (rvgp_locality_order) and cut into blocks of 32 and superblocks of 32
+// blocks, each with its FP64 bounding box and the maximum of ds over it
+// (value, then lowest original index).  A block is visited only when the
+// distance from p to its box is below its maximum (times 1 - 2e-12, which
+// covers the rounding of both sides, so the skipped points are exactly those
+// whose minimum keeps its value), and the next point is the maximum over the
+// superblock maxima.  Late in a long run the ball of radius r holds a
+// handful of blocks: each selection is a few dependent L2 round trips in one
+// CTA of 1024 threads, with no grid barrier.  Distances as in the other
+// forms (exact_dist), so the three forms select the same points.
+namespace rvgp {
+namespace {
+constexpr int kSpThreads = 1024;
+constexpr int kBlk = 32;           // points per block
+constexpr int kSup = 32;           // blocks per superblock
+constexpr double kPruneMargin = 1.0 - 2e-12;
+
+struct Max3 {
+  double v;
+  int orig, pos;
+};
+
+__device__ __forceinline__ Max3 warp_max3(Max3 a) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    Max3 b{__shfl_xor_sync(0xffffffffu, a.v, o), __shfl_xor_sync(0xffffffffu, a.orig, o),
+           __shfl_xor_sync(0xffffffffu, a.pos, o)};
+    if (better(b.v, b.orig, a.v, a.orig)) a = b;
+  }
+  return a;
+}
+
+// squared distance from p to the box [lo, hi] (0 inside)
+__device__ __forceinline__ double box_dist2(const double* p, const double* lo, const double* hi, int D) {
+  double s = 0.0;
+  for (int j = 0; j < D; ++j) {
+    const double e = fmax(0.0, fmax(lo[j] - p[j], p[j] - hi[j]));
+    s += e * e;
+  }
+  return s;
+}
+
+// Points in Morton order, ds from the start point, per-block boxes and maxima
+// (warp per block).
+__global__ void fps_sp_blocks(const double* __restrict__ X, const int* __restrict__ order, int n, int D, int start,
+                              double* __restrict__ Xs, double* __restrict__ ds, double* __restrict__ box,
+                              double* __restrict__ bmax, int* __restrict__ borig, int* __restrict__ bpos) {
+  const int warp = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+  const int nb = (n + kBlk - 1) / kBlk;
+  if (warp >= nb) return;
+  const int q = warp * kBlk + lane;
+  const bool on = q < n;
+  const int o = on ? order[q] : 0;
+  Max3 m{-DBL_MAX, INT_MAX, 0};
+  if (on) {
+    for (int j = 0; j < D; ++j) Xs[(size_t)q * D + j] = X[(size_t)o * D + j];
+    const double d = exact_dist(X, D, start, o);
+    ds[q] = d;
+    m = Max3{d, o, q};
+  }
+  m = warp_max3(m);
+  for (int j = 0; j < D; ++j) {
+    double lo = on ? X[(size_t)o * D + j] : DBL_MAX, hi = on ? X[(size_t)o * D + j] : -DBL_MAX;
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) {
+      lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, s));
+      hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, s));
+    }
+    if (lane == 0) {
+      box[(size_t)warp * 2 * D + j] = lo;
+      box[(size_t)warp * 2 * D + D + j] = hi;
+    }
+  }
+  if (lane == 0) {
+    bmax[warp] = m.v;
+    borig[warp] = m.orig;
+    bpos[warp] = m.pos;
+  }
+}
+
+// Superblock boxes and maxima (warp per superblock).
+__global__ void fps_sp_super(int nb, int D, const double* __restrict__ box, const double* __restrict__ bmax,
+                             const int* __restrict__ borig, const int* __restrict__ bpos, double* __restrict__ sbox,
+                             double* __restrict__ smax, int* __restrict__ sorig, int* __restrict__ spos) {
+  const int warp = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+  const int ns = (nb + kSup - 1) / kSup;
+  if (warp >= ns) return;
+  const int b = warp * kSup + lane;
+  const bool on = b < nb;
+  Max3 m = on ? Max3{bmax[b], borig[b], bpos[b]} : Max3{-DBL_MAX, INT_MAX, 0};
+  m = warp_max3(m);
+  for (int j = 0; j < D; ++j) {
+    double lo = on ? box[(size_t)b * 2 * D + j] : DBL_MAX, hi = on ? box[(size_t)b * 2 * D + D + j] : -DBL_MAX;
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) {
+      lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, s));
+      hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, s));
+    }
+    if (lane == 0) {
+      sbox[(size_t)warp * 2 * D + j] = lo;
+      sbox[(size_t)warp * 2 * D + D + j] = hi;
+    }
+  }
+  if (lane == 0) {
+    smax[warp] = m.v;
+    sorig[warp] = m.orig;
+    spos[warp] = m.pos;
+  }
+}
+
+// Selections 1 .. N_max-1 in one CTA.  Shared memory: the superblock boxes
+// and maxima, the lists of superblocks and blocks to visit.
+__global__ void __launch_bounds__(kSpThreads, 1)
+    fps_sp_select(const double* __restrict__ Xs, const int* __restrict__ order, int n, int D, int N_max,
+                  double* __restrict__ ds, const double* __restrict__ box, double* __restrict__ bmax,
+                  int* __restrict__ borig, int* __restrict__ bpos, const double* __restrict__ sbox_g,
+                  const double* __restrict__ smax_g, const int* __restrict__ sorig_g, const int* __restrict__ spos_g,
+                  int* __restrict__ perm, double* __restrict__ lambdas, int* __restrict__ count,
+                  const double* __restrict__ diam, double spacing, int* __restrict__ blist_g,
+                  long long* __restrict__ exact_evals) {
+  extern __shared__ __align__(16) unsigned char fsm[];
+  const int nb = (n + kBlk - 1) / kBlk, ns = (nb + kSup - 1) / kSup;
+  double* sbox = reinterpret_cast<double*>(fsm);        // ns x 2D
+  double* smax = sbox + (size_t)ns * 2 * D;             // ns
+  int* sorig = reinterpret_cast<int*>(smax + ns);       // ns
+  int* spos = sorig + ns;                                // ns
+  int* slist = spos + ns;                                // ns
+  __shared__ double s_p[8];
+  __shared__ double s_wv[32];
+  __shared__ int s_wo[32], s_wp[32];
+  __shared__ int s_ns, s_nb, s_stop;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int s = tid; s < ns; s += kSpThreads) {
+    for (int j = 0; j < 2 * D; ++j) sbox[(size_t)s * 2 * D + j] = sbox_g[(size_t)s * 2 * D + j];
+    smax[s] = smax_g[s];
+    sorig[s] = sorig_g[s];
+    spos[s] = spos_g[s];
+  }
+  long long exact = 0;
+  __syncthreads();
+  for (int it = 1; it < N_max; ++it) {
+    // ---- A. the next point: maximum over the superblock maxima
+    Max3 m{-DBL_MAX, INT_MAX, 0};
+    for (int s = tid; s < ns; s += kSpThreads)
+      if (better(smax[s], sorig[s], m.v, m.orig)) m = Max3{smax[s], sorig[s], spos[s]};
+    m = warp_max3(m);
+    if (lane == 0) {
+      s_wv[warp] = m.v;
+      s_wo[warp] = m.orig;
+      s_wp[warp] = m.pos;
+    }
+    __syncthreads();
+    if (warp == 0) {
+      Max3 w{s_wv[lane], s_wo[lane], s_wp[lane]};
+      w = warp_max3(w);
+      if (lane == 0) {
+        s_stop = 0;
+        s_ns = 0;
+        s_nb = 0;
+        if (diam && w.v / diam[0] < spacing) {
+          s_stop = 1;
+          *count = it;
+        } else {
+          perm[it] = w.orig;
+          lambdas[it] = w.v;
+        }
+      }
+      __syncwarp();
+      if (lane < D) s_p[lane] = Xs[(size_t)__shfl_sync(0xffffffffu, w.pos, 0) * D + lane];
+    }
+    __syncthreads();
+    if (s_stop) break;
+    // ---- B. superblocks whose box comes closer to p than their maximum
+    for (int s = tid; s < ns; s += kSpThreads) {
+      const double d2 = box_dist2(s_p, sbox + (size_t)s * 2 * D, sbox + (size_t)s * 2 * D + D, D);
+      if (d2 * kPruneMargin <= smax[s] * smax[s]) slist[atomicAdd(&s_ns, 1)] = s;
+    }
+    __syncthreads();
+    // ---- C. their blocks, the same test (warp per superblock, lane per block)
+    const int nsl = s_ns;
+    for (int e = warp; e < nsl; e += kSpThreads / 32) {
+      const int b = slist[e] * kSup + lane;
+      if (b < nb) {
+        const double bm = bmax[b];
+        const double d2 = box_dist2(s_p, box + (size_t)b * 2 * D, box + (size_t)b * 2 * D + D, D);
+        if (d2 * kPruneMargin <= bm * bm) blist_g[atomicAdd(&s_nb, 1)] = b;
+      }
+    }
+    __syncthreads();
+    // ---- D. their points (warp per block, lane per point), new block maxima
+    const int nbl = s_nb;
+    for (int e = warp; e < nbl; e += kSpThreads / 32) {
+      const int b = blist_g[e];
+      const int q = b * kBlk + lane;
+      Max3 mm{-DBL_MAX, INT_MAX, 0};
+      if (q < n) {
+        double cur = ds[q];
+        if (cur > 0.0) {
+          double acc = 0.0;
+          for (int j = 0; j < D; ++j) {
+            const double df = __dsub_rn(s_p[j], Xs[(size_t)q * D + j]);
+            acc = __dadd_rn(acc, __dmul_rn(df, df));
+          }
+          const double d = sqrt(acc);
+          ++exact;
+          if (d < cur) {
+            cur = d;
+            ds[q] = d;
+          }
+        }
+        mm = Max3{cur, order[q], q};
+      }
+      mm = warp_max3(mm);
+      if (lane == 0) {
+        bmax[b] = mm.v;
+        borig[b] = mm.orig;
+        bpos[b] = mm.pos;
+      }
+    }
+    __syncthreads();
+    // ---- E. new maxima of the visited superblocks (warp per superblock)
+    for (int e = warp; e < nsl; e += kSpThreads / 32) {
+      const int s = slist[e];
+      const int b = s * kSup + lane;
+      Max3 mm = b < nb ? Max3{bmax[b], borig[b], bpos[b]} : Max3{-DBL_MAX, INT_MAX, 0};
+      mm = warp_max3(mm);
+      if (lane == 0) {
+        smax[s] = mm.v;
+        sorig[s] = mm.orig;
+        spos[s] = mm.pos;
+      }
+    }
+    __syncthreads();
+  }
+  if (exact_evals) atomicAdd((unsigned long long*)exact_evals, (unsigned long long)exact);
+}
+
+__global__ void write_first(int* perm, double* lambdas, int start) {
+  if (threadIdx.x == 0) {
+    perm[0] = start;
+    lambdas[0] = 0.0;
+  }
+}
+
+__global__ void add_ll(long long* p, long long v) { *p += v; }
+
+size_t fps_sp_smem(int n, int D) {
+  const int nb = (n + kBlk - 1) / kBlk, ns = (nb + kSup - 1) / kSup;
+  return (size_t)ns * (2 * D * sizeof(double) + sizeof(double) + 3 * sizeof(int));
+}
+}  // namespace
+}  // namespace rvgp
+
+extern "C" size_t rvgp_locality_order_workspace(int n, int D);
+extern "C" int rvgp_locality_order(const double* X, int n, int D, int* perm, int* rank, void* workspace,
+                                   size_t ws_bytes, void* stream);
+
+// Largest n the spatial form takes for dimension D (its superblock table
+// must fit one SM's shared memory), 0 when D is outside 1..8.
+RVGP_API int rvgp_fps_spatial_max_n(int D) {
+  if (D < 1 || D > 8) return 0;
+  int dev = 0, optin = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
+    return 0;
+  const size_t per = 2 * D * sizeof(double) + sizeof(double) + 3 * sizeof(int);
+  const long long ns = ((long long)optin - 2048) / (long long)per;
+  return (int)std::min<long long>(INT_MAX / 2, ns * kBlk * kSup);
+}
+
+RVGP_API size_t rvgp_fps_spatial_workspace(int n, int D) {
+  const int nb = (n + kBlk - 1) / kBlk, ns = (nb + kSup - 1) / kSup;
+  Workspace ws(nullptr, 0);
+  ws.take<int>(n);                          // order
+  ws.take<int>(n);                          // rank
+  ws.take<double>((size_t)n * D);           // Xs
+  ws.take<double>(n);                       // ds
+  ws.take<double>((size_t)nb * 2 * D);      // box
+  ws.take<double>(nb);                      // bmax
+  ws.take<int>(2 * (size_t)nb);             // borig, bpos
+  ws.take<int>(nb);                         // block list
+  ws.take<double>((size_t)ns * (2 * D + 1));  // sbox, smax
+  ws.take<int>(2 * (size_t)ns);             // sorig, spos
+  ws.take<char>(rvgp_locality_order_workspace(n, D));
+  return ws.used;
+}
+
+// Same arguments and results as rvgp_fps_persistent; n <= rvgp_fps_spatial_max_n(D).
+RVGP_API int rvgp_fps_spatial(const double* X, int n, int D, int N_max, int start, const double* diam,
+                              double spacing, int* perm, double* lambdas, int* count, long long* exact_evals,
+                              void* workspace, size_t ws_bytes, void* stream) {
+  RVGP_CHECK_ARG(X && perm && lambdas && count && n >= 1 && D >= 1 && D <= 8, "rvgp_fps_spatial: bad arguments");
+  RVGP_CHECK_ARG(N_max >= 1 && N_max <= n && start >= 0 && start < n, "rvgp_fps_spatial: bad N=%d or start=%d",
+                 N_max, start);
+  RVGP_CHECK_ARG(n <= rvgp_fps_spatial_max_n(D), "rvgp_fps_spatial: n=%d above the limit %d for D=%d", n,
+                 rvgp_fps_spatial_max_n(D), D);
+  RVGP_CHECK_ARG(workspace && ws_bytes >= rvgp_fps_spatial_workspace(n, D), "rvgp_fps_spatial: workspace");
+  cudaStream_t st = as_stream(stream);
+  const int nb = (n + kBlk - 1) / kBlk, ns = (nb + kSup - 1) / kSup;
+  Workspace ws(workspace, ws_bytes);
+  int* order = ws.take<int>(n);
+  int* rank = ws.take<int>(n);
+  double* Xs = ws.take<double>((size_t)n * D);
+  double* ds = ws.take<double>(n);
+  double* box = ws.take<double>((size_t)nb * 2 * D);
+  double* bmax = ws.take<double>(nb);
+  int* borig = ws.take<int>(nb);
+  int* bpos = ws.take<int>(nb);
+  int* blist = ws.take<int>(nb);
+  double* sbox = ws.take<double>((size_t)ns * 2 * D);
+  double* smax = ws.take<double>(ns);
+  int* sorig = ws.take<int>(ns);
+  int* spos = ws.take<int>(ns);
+  const size_t lo_bytes = rvgp_locality_order_workspace(n, D);
+  void* lo_ws = ws.take<char>(lo_bytes);
+  TRY_RC(rvgp_locality_order(X, n, D, order, rank, lo_ws, lo_bytes, stream));
+  cudaMemsetAsync(count, 0xFF, sizeof(int), st);  // -1: all N_max taken unless the spacing stop fires
+  if (exact_evals) cudaMemsetAsync(exact_evals, 0, sizeof(long long), st);
+  rvgp::note_launch();
+  fps_sp_blocks<<<ceil_div((long long)nb * 32, 256), 256, 0, st>>>(X, order, n, D, start, Xs, ds, box, bmax, borig,
+                                                                    bpos);
+  rvgp::note_launch();
+  fps_sp_super<<<ceil_div((long long)ns * 32, 256), 256, 0, st>>>(nb, D, box, bmax, borig, bpos, sbox, smax, sorig,
+                                                                   spos);
+  rvgp::note_launch();
+  write_first<<<1, 32, 0, st>>>(perm, lambdas, start);
+  if (N_max > 1) {
+    const size_t smem = fps_sp_smem(n, D);
+    if (cudaFuncSetAttribute(fps_sp_select, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+      return check_launch("rvgp_fps_spatial");
+    rvgp::note_launch();
+    fps_sp_select<<<1, kSpThreads, smem, st>>>(Xs, order, n, D, N_max, ds, box, bmax, borig, bpos, sbox, smax, sorig,
+                                               spos, perm, lambdas, count, diam, spacing, blist, exact_evals);
+  }
+  RVGP_LAUNCH_CHECK("rvgp_fps_spatial");
+  if (exact_evals) {
+    // the n distances from the start point
+    rvgp::note_launch();
+    add_ll<<<1, 1, 0, st>>>(exact_evals, (long long)n);
+  }
   return RVGP_OK;
 }
