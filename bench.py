@@ -280,9 +280,9 @@ def spmm_roofline(d, wl, peaks, flush, reps=20):
     """Achieved HBM bandwidth of the eigensolver's Chebyshev-step SpMM (FP32,
     block width p) on this workload's connection Laplacian: each launch timed
     alone with CUDA events on the launching stream, L2 flushed before it.  The
-    matrix is the Morton-renumbered one the eigensolver multiplies by, through
-    the tiled plan the eigensolver builds (the untiled product is timed beside
-    it for reference)."""
+    matrix is the Morton-renumbered one the eigensolver multiplies by, and the
+    product the launch tuner's variant (what the eigensolver runs); the
+    shared-memory tiled plan is timed beside it for reference."""
     import torch
     from rvgp_gb300 import _core
     dev = d._dev
@@ -311,18 +311,23 @@ def spmm_roofline(d, wl, peaks, flush, reps=20):
             times.append(e0.elapsed_time(e1) / 1e3)
         return float(np.mean(times))
 
-    t = timed(plan)
+    t = timed(None)  # the variant the launch tuner picked for this shape (what the eigensolver runs)
     torch.cuda.nvtx.range_pop()
-    t_untiled = timed(None)
+    t_plan = timed(plan)
+    key = f"bspmm f32 DB{k} b{p} n2^{int(n).bit_length() - 1}".encode()
+    variant = int(_core.lib().rvgp_autotune_lookup(key))
     E = dev.indices.numel()
-    # values + local column indices (2 bytes) + row pointers + read X, read Z, write Y
-    alg = E * (k * k * 4 + 2) + (n + 1) * 4 + 3 * N * p * 4
+    # values + column indices + row pointers + read X, read Z, write Y
+    alg = E * (k * k * 4 + 4) + (n + 1) * 4 + 3 * N * p * 4
     achieved = alg / t / 1e9
-    return {"kernel": f"bspmm_tiled_kernel<float,{k},2> (Chebyshev step, Lc x block, tiled plan)", "bound": "hbm",
-            "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
+    names = {0: f"bspmm_kernel<float,{k},G>", 1: f"bspmm_chunked_kernel<float,{k},2>",
+             2: f"bspmm_chunked_kernel<float,{k},4>", 3: f"bspmm_tile_kernel<float,{k},2>",
+             4: f"bspmm_tile_kernel<float,{k},4>"}
+    return {"kernel": f"{names.get(variant, '?')} (Chebyshev step, Lc x block; launch tuner's variant {variant})",
+            "bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
             "frac": round(achieved / peaks["hbm_gbs"], 4),
             "traffic": SPMM_TRAFFIC.get((n, k, p, E)), "algorithmic_bytes": int(alg),
-            "avg_launch_us": round(t * 1e6, 2), "untiled_avg_launch_us": round(t_untiled * 1e6, 2),
+            "avg_launch_us": round(t * 1e6, 2), "smem_plan_avg_launch_us": round(t_plan * 1e6, 2),
             "block_width": p, "l2": "flushed before every timed launch"}
 
 

@@ -112,6 +112,17 @@ int rvgp_bspmm_planned_f64(const void* plan, size_t plan_bytes, int n, int DB, l
                            const int* indices, const double* vals, const double* X, double* Y, const double* Z, int b,
                            int ld, double alpha, double beta, double gamma, void* stream);
 
+/* Eigendecomposition of a symmetric FP32 matrix (the Rayleigh-Ritz step of the
+ * eigensolver; ARPACK's inside scipy's eigsh, RVGP/geometry.py:73): H (p x p,
+ * read only) -> w ascending, V (p x p) eigenvectors by column, after at most
+ * max_sweeps Jacobi sweeps, stopping at off(H) <= tol ||H||_F; *sweeps_used
+ * (host, may be null).  method 0: block Jacobi (32-wide block pairs, two grid
+ * barriers per round) for p >= 64, else scalar; 1: scalar parallel Jacobi;
+ * 2: block.  Synchronises. */
+size_t rvgp_symeig_f32_workspace(int p);
+int rvgp_symeig_f32(const float* H, int p, float* w, float* V, int max_sweeps, double tol, int* sweeps_used,
+                    int method, void* workspace, size_t ws_bytes, void* stream);
+
 /* ---- eigensolver ------------------------------------------------------ */
 
 /* m smallest eigenpairs of a symmetric PSD block-CSR matrix by Chebyshev-

@@ -47,6 +47,8 @@ SIGNATURES = {
     "rvgp_gp_fit_adam": (c_int, [P, P, P, ctypes.c_longlong, c_int, P, c_double, c_int, P, P, P, c_int, c_double,
                                  c_double, c_double, c_double, P, P, P, P, P, c_size_t, P]),
     "rvgp_gp_fit_mixed_max_m": (c_int, []),
+    "rvgp_symeig_f32_workspace": (c_size_t, [c_int]),
+    "rvgp_symeig_f32": (c_int, [P, c_int, P, P, c_int, c_double, P, c_int, P, c_size_t, P]),
     "rvgp_fps_spatial_max_n": (c_int, [c_int]),
     "rvgp_fps_spatial_workspace": (c_size_t, [c_int, c_int]),
     "rvgp_fps_spatial": (c_int, [P, c_int, c_int, c_int, c_int, P, c_double, P, P, P, P, P, c_size_t, P]),
@@ -347,6 +349,22 @@ def eigsh(indptr, indices, vals64, vals32=None, m=10, mode="mixed", tol=None, to
     if st > 0:
         raise RuntimeError(f"ARPACK-equivalent no convergence: {lib().rvgp_last_error().decode()}")
     return evals, evecs, info
+
+
+def symeig_f32(H, max_sweeps=60, tol=4e-6, method=0):
+    """Eigendecomposition of a symmetric FP32 matrix on the device by Jacobi
+    (the eigensolver's Rayleigh-Ritz step): (w ascending, V by column, sweeps).
+    method 0: block Jacobi for p >= 64, 1: scalar, 2: block."""
+    H = _dev(H, torch.float32, "H")
+    p = H.shape[0]
+    w = torch.empty(p, dtype=torch.float32, device=H.device)
+    V = torch.empty((p, p), dtype=torch.float32, device=H.device)
+    used = ctypes.c_int(0)
+    L = lib()
+    ws = workspace(L.rvgp_symeig_f32_workspace(p), H.device)
+    check(L.rvgp_symeig_f32(ptr(H), p, ptr(w), ptr(V), int(max_sweeps), float(tol), ctypes.byref(used), int(method),
+                            ptr(ws), ws.numel(), stream()), "rvgp_symeig_f32")
+    return w, V, used.value
 
 
 def tc_gram(A, B=None):

@@ -248,6 +248,7 @@ struct Small {
   float* d32;         // its column scaling diag(VᵀV)^-½
   int cholqr32;       // p fits the one-CTA FP32 Cholesky QR
   int jac32;          // p fits the one-CTA FP32 Jacobi
+  int jacb;           // FP32 block Jacobi (wider p)
   void* jac32_ws;
   size_t jac32_bytes;
   float* nf;
@@ -470,7 +471,10 @@ int rayleigh_ritz(const Problem& P, Block<T>& B, Small& s, Stats& stt, int max_s
     // rotation costs ~64x an FP32 one on GB300).  Stop at off(H) <= 4e-6 ||H||_F,
     // below the FP32 stage's residual tolerance and above FP32 rounding.
     TRY(convert_f64_to_f32(s.H, p, s.Hf, p, p, p, st));
-    if (s.jac32)
+    if (s.jacb)
+      TRY(jacobi_block_eigh(s.Hf, p, s.thf, s.Bf, std::min(max_sweeps, kFp32Sweeps), 4e-6, &used, s.jac_ws,
+                            s.jac_bytes, st));
+    else if (s.jac32)
       TRY(jacobi32_eigh(s.Hf, p, s.thf, s.Bf, std::min(max_sweeps, kFp32Sweeps), 4e-6, &used, s.jac32_ws,
                         s.jac32_bytes, st));
     else
@@ -615,6 +619,7 @@ Layout carve(Workspace& ws, long long N, int p, int mode) {
   s.d32 = ws.take<float>(p);
   s.cholqr32 = 0;
   s.jac32 = 0;
+  s.jacb = 0;
   s.jac32_bytes = jacobi32_workspace(p, kFp32Sweeps);
   s.jac32_ws = ws.take<char>(s.jac32_bytes);
   s.gram_bytes = std::max(gram_workspace<float>(N, p, p), gram_workspace<double>(N, p, p));
@@ -667,16 +672,25 @@ static int eigsh_impl(const int* indptr, const int* indices, const double* vals6
   Small& s = L.s;
   s.cholqr32 = (mode == 1 && p <= cholqr32_max_p()) ? 1 : 0;
   s.jac32 = (mode == 1 && p % 2 == 0 && p <= jacobi32_max_p()) ? 1 : 0;
+  {
+    // block Jacobi above the one-CTA size (RVGP_JACOBI_BLOCK=0: the scalar kernel)
+    const char* e = getenv("RVGP_JACOBI_BLOCK");
+    s.jacb = (mode == 1 && !s.jac32 && p >= 128 && jacobi_block_workspace(p) <= s.jac_bytes && !(e && e[0] == '0'))
+                 ? 1
+                 : 0;
+  }
   s.tc = (mode == 1 && s.tc_bytes > 0 && tc_enabled() && tc_supported(p, p)) ? 1 : 0;
   cudaMemsetAsync(s.tc_err, 0, sizeof(int), st);
   Problem P{n, DB, N, indptr, indices, vals64, vals32, m, p, SpmmPlan{}};
   Stats stt;
-  // the tiled product's plan, in the workspace beyond `need` when the caller
-  // sized it for one (rvgp_spmm_plan_bytes); RVGP_SPMM_TILED=0 turns it off
+  // the shared-memory tiled product's plan, in the workspace beyond `need`
+  // when the caller sized it for one (rvgp_spmm_plan_bytes), on request
+  // (RVGP_SPMM_TILED=1): on GB300 its staging costs more than the L1 reuse
+  // of the tile-mapped variant the tuner can pick
   {
     const char* e = getenv("RVGP_SPMM_TILED");
     int nnz = 0;
-    if (!(e && e[0] == '0') && ws_bytes > need) {
+    if (e && e[0] == '1' && ws_bytes > need) {
       if (read_back(&nnz, indptr + n, sizeof(int), st) != cudaSuccess) return check_launch("rvgp_eigsh");
       const size_t pb = spmm_plan_bytes(n, DB, nnz);
       if (pb > 0 && ws.used + 256 + pb <= ws_bytes) {

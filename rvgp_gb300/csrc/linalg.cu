@@ -536,24 +536,24 @@ __global__ void __launch_bounds__(1024) offnorm_kernel(const T* __restrict__ H, 
 // sort the diagonal ascending (ties by index) and permute the columns of V (one CTA)
 template <typename T>
 __device__ void sort_eig_block(const T* __restrict__ H, const T* __restrict__ V, int p, T* __restrict__ w,
-                               T* __restrict__ Vout, unsigned char* smem);
+                               T* __restrict__ Vout, unsigned char* smem, int ld);
 
 template <typename T>
 __global__ void __launch_bounds__(1024) sort_eig(const T* __restrict__ H, const T* __restrict__ V, int p,
                                                  T* __restrict__ w, T* __restrict__ Vout) {
   extern __shared__ unsigned char smem[];
-  sort_eig_block<T>(H, V, p, w, Vout, smem);
+  sort_eig_block<T>(H, V, p, w, Vout, smem, p);
 }
 
 template <typename T>
 __device__ void sort_eig_block(const T* __restrict__ H, const T* __restrict__ V, int p, T* __restrict__ w,
-                               T* __restrict__ Vout, unsigned char* smem) {
+                               T* __restrict__ Vout, unsigned char* smem, int ld) {
   T* key = reinterpret_cast<T*>(smem);
   int* idx = reinterpret_cast<int*>(key + 2048);
   int P2 = 1;
   while (P2 < p) P2 <<= 1;
   for (int t = threadIdx.x; t < P2; t += blockDim.x) {
-    key[t] = t < p ? H[(size_t)t * p + t] : T(0);
+    key[t] = t < p ? H[(size_t)t * ld + t] : T(0);
     idx[t] = t < p ? t : INT_MAX;
   }
   __syncthreads();
@@ -583,7 +583,7 @@ __device__ void sort_eig_block(const T* __restrict__ H, const T* __restrict__ V,
   for (int t = threadIdx.x; t < p; t += blockDim.x) w[t] = key[t];
   for (long long e = threadIdx.x; e < (long long)p * p; e += blockDim.x) {
     const int r = (int)(e / p), c = (int)(e % p);
-    Vout[e] = V[(size_t)r * p + idx[c]];
+    Vout[e] = V[(size_t)r * ld + idx[c]];
   }
 }
 
@@ -697,7 +697,277 @@ __global__ void __launch_bounds__(256) jacobi_persistent(T* H, T* Hb, T* Va, T* 
     ++used;
   }
   if (blockIdx.x == 0) {
-    sort_eig_block<T>(h0, v0, p, w, Vout, smem);
+    sort_eig_block<T>(h0, v0, p, w, Vout, smem, p);
+    if (threadIdx.x == 0) *sweeps_out = used;
+  }
+}
+
+// ------------------------------------------------------------------ block Jacobi (FP32)
+// The same eigendecomposition with far fewer grid-wide barriers: the index
+// range (padded with zero rows and columns to P, a multiple of 64) is cut
+// into blocks of 32, and a sweep pairs the blocks by the circle method (nb - 1
+// rounds of nb / 2 disjoint pairs).  In a round, CTA k diagonalises the 64 x
+// 64 principal submatrix of pair k by cyclic Jacobi in shared memory (the
+// same rotation formula as the scalar kernel, 63 rounds of 32 rotations per
+// inner sweep, until its off-diagonal part is below the outer tolerance) and
+// publishes its orthogonal factor Q_k; then every 64 x 64 tile of H becomes
+// Q_aᵀ H_ab Q_b and every 64-row tile of V becomes V Q_b, each tile read and
+// written by one task (in place).  Two grid barriers per round: 2(nb - 1) per
+// sweep instead of p - 1.  Zero padding never couples to the real indices, so
+// V's leading p x p block holds the eigenvectors.
+constexpr int kJB = 32;
+constexpr int kJP = 2 * kJB;   // pair width
+constexpr int kJLd = kJP + 1;  // shared-memory row stride
+constexpr int kJbThreads = 256;
+constexpr int kJbMaxInner = 6;
+
+__device__ __forceinline__ void jrot32(float a, float b, float c, float& cs, float& sn) {
+  cs = 1.f;
+  sn = 0.f;
+  const double tiny = Eps<float>::v * 1e-3;
+  if (c != 0.f && (double)c * (double)c > tiny * tiny * fabs((double)a) * fabs((double)b)) {
+    const float theta = (b - a) * rcp_nr(2.f * c);
+    float t;
+    if (fabs((double)theta) > 1e15) {
+      t = 0.5f * rcp_nr(theta);
+    } else {
+      const float q = fmaf(theta, theta, 1.f);
+      const float root = q * rsqrt_nr(q);
+      t = (theta >= 0.f ? 1.f : -1.f) * rcp_nr(fabsf(theta) + root);
+    }
+    cs = rsqrt_nr(fmaf(t, t, 1.f));
+    sn = t * cs;
+  }
+}
+
+// pair k of round r of the circle schedule over n (even) items
+__device__ __forceinline__ int2 circle_pair(int n, int r, int k) {
+  if (k == 0) return make_int2(min(r, n - 1), max(r, n - 1));
+  const int a = (r + k) % (n - 1), b = (r - k + (n - 1)) % (n - 1);
+  return make_int2(min(a, b), max(a, b));
+}
+
+// global index of local index l (0..63) of the pair of blocks (I, J)
+__device__ __forceinline__ int pair_index(int I, int J, int l) { return l < kJB ? I * kJB + l : J * kJB + l - kJB; }
+
+// sum over the CTA in a fixed order (warp shuffles, then warp 0)
+__device__ __forceinline__ double cta_sum(double v, double* red) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double t = 0.0;
+  for (int w = 0; w < kJbThreads / 32; ++w) t += red[w];
+  return t;
+}
+
+// Diagonalise the 64 x 64 principal submatrix of the pair (I, J); Q (64 x 64, global) <- its factor.
+__device__ void jb_pair_solve(const float* __restrict__ H, int P, int I, int J, float* __restrict__ Qg, double tol2,
+                              float* sm, double* red) {
+  float* S = sm;
+  float* S2 = S + kJP * kJLd;
+  float* Q = S2 + kJP * kJLd;
+  float* Q2 = Q + kJP * kJLd;
+  float* cf = Q2 + kJP * kJLd;                    // per local index: c1, c2
+  int* pq = reinterpret_cast<int*>(cf + 2 * kJP);  // per local index: P, Q, partner
+  const int tid = threadIdx.x;
+  for (int e = tid; e < kJP * kJP; e += kJbThreads) {
+    const int r = e / kJP, c = e % kJP;
+    const int gi = pair_index(I, J, r), gj = pair_index(I, J, c);
+    S[r * kJLd + c] = 0.5f * (H[(size_t)gi * P + gj] + H[(size_t)gj * P + gi]);
+    Q[r * kJLd + c] = r == c ? 1.f : 0.f;
+  }
+  __syncthreads();
+  for (int sweep = 0; sweep < kJbMaxInner; ++sweep) {
+    double off = 0.0, tot = 0.0;
+    for (int e = tid; e < kJP * kJP; e += kJbThreads) {
+      const double v = S[(e / kJP) * kJLd + e % kJP];
+      tot += v * v;
+      if (e / kJP != e % kJP) off += v * v;
+    }
+    off = cta_sum(off, red);
+    tot = cta_sum(tot, red);
+    if (!(off > tol2 * tot)) break;  // the same decision in every thread
+    for (int rr = 0; rr < kJP - 1; ++rr) {
+      if (tid < kJP / 2) {
+        const int2 pr = circle_pair(kJP, rr, tid);
+        float cs, sn;
+        jrot32(S[pr.x * kJLd + pr.x], S[pr.y * kJLd + pr.y], S[pr.x * kJLd + pr.y], cs, sn);
+        cf[2 * pr.x] = cs;
+        cf[2 * pr.x + 1] = -sn;
+        cf[2 * pr.y] = sn;
+        cf[2 * pr.y + 1] = cs;
+        pq[3 * pr.x] = pr.x;
+        pq[3 * pr.x + 1] = pr.y;
+        pq[3 * pr.x + 2] = pr.y;
+        pq[3 * pr.y] = pr.x;
+        pq[3 * pr.y + 1] = pr.y;
+        pq[3 * pr.y + 2] = pr.x;
+      }
+      __syncthreads();
+      for (int e = tid; e < kJP * kJP; e += kJbThreads) {
+        const int i = e / kJP, j = e % kJP;
+        const float ci1 = cf[2 * i], ci2 = cf[2 * i + 1], cj1 = cf[2 * j], cj2 = cf[2 * j + 1];
+        const int aP = pq[3 * i], aQ = pq[3 * i + 1], bP = pq[3 * j], bQ = pq[3 * j + 1];
+        float v;
+        if (i != j && pq[3 * i + 2] == j) {
+          v = 0.f;
+        } else {
+          v = ci1 * (cj1 * S[aP * kJLd + bP] + cj2 * S[aP * kJLd + bQ]);
+          v += ci2 * (cj1 * S[aQ * kJLd + bP] + cj2 * S[aQ * kJLd + bQ]);
+        }
+        S2[i * kJLd + j] = v;
+        Q2[i * kJLd + j] = cj1 * Q[i * kJLd + bP] + cj2 * Q[i * kJLd + bQ];
+      }
+      __syncthreads();
+      float* t = S;
+      S = S2;
+      S2 = t;
+      t = Q;
+      Q = Q2;
+      Q2 = t;
+    }
+  }
+  for (int e = tid; e < kJP * kJP; e += kJbThreads) Qg[e] = Q[(e / kJP) * kJLd + e % kJP];
+}
+
+// X (64 x 64 tile: rows ri(l), columns ci(l) of a matrix with leading
+// dimension P) <- Qaᵀ X Qb (Qa null: X Qb).  Each thread forms a 4 x 4 block.
+__device__ void jb_apply_tile(float* __restrict__ X, int P, int rI, int rJ, int rows_contig, int cI, int cJ,
+                              const float* __restrict__ Qa, const float* __restrict__ Qb, float* sm) {
+  float* Xs = sm;
+  float* A = Xs + kJP * kJLd;
+  float* B = A + kJP * kJLd;
+  float* T = B + kJP * kJLd;
+  const int tid = threadIdx.x;
+  auto grow = [&](int l) { return rows_contig >= 0 ? rows_contig + l : pair_index(rI, rJ, l); };
+  for (int e = tid; e < kJP * kJP; e += kJbThreads) {
+    const int r = e / kJP, c = e % kJP;
+    Xs[r * kJLd + c] = X[(size_t)grow(r) * P + pair_index(cI, cJ, c)];
+    B[r * kJLd + c] = Qb[e];
+    if (Qa) A[r * kJLd + c] = Qa[e];
+  }
+  __syncthreads();
+  const int i0 = 4 * (tid / 16), j0 = 4 * (tid % 16);
+  float acc[4][4];
+  const float* src = Xs;
+  if (Qa) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) acc[u][v] = 0.f;
+    for (int k = 0; k < kJP; ++k) {
+      float a[4], x[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) a[u] = A[k * kJLd + i0 + u];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) x[v] = Xs[k * kJLd + j0 + v];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) acc[u][v] = fmaf(a[u], x[v], acc[u][v]);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) T[(i0 + u) * kJLd + j0 + v] = acc[u][v];
+    __syncthreads();
+    src = T;
+  }
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) acc[u][v] = 0.f;
+  for (int k = 0; k < kJP; ++k) {
+    float a[4], b[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) a[u] = src[(i0 + u) * kJLd + k];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) b[v] = B[k * kJLd + j0 + v];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) acc[u][v] = fmaf(a[u], b[v], acc[u][v]);
+  }
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) X[(size_t)grow(i0 + u) * P + pair_index(cI, cJ, j0 + v)] = acc[u][v];
+  __syncthreads();  // the shared buffers are reused by the next task
+}
+
+__global__ void __launch_bounds__(kJbThreads) jacobi_block32(const float* __restrict__ H, int p, int P, float* Hp,
+                                                             float* Vp, float* Qbuf, double* part, int max_sweeps,
+                                                             double tol2, unsigned int* bar, int* err,
+                                                             int* sweeps_out, float* w, float* Vout) {
+  extern __shared__ __align__(16) unsigned char jsm[];
+  __shared__ double red[kJbThreads / 32];
+  __shared__ double s_off, s_tot;
+  float* sm = reinterpret_cast<float*>(jsm);
+  const unsigned G = gridDim.x;
+  const int nb = P / kJB, npair = nb / 2;
+  const long long PP = (long long)P * P;
+  const long long gtid = blockIdx.x * (long long)blockDim.x + threadIdx.x, gsz = (long long)G * blockDim.x;
+  for (long long e = gtid; e < PP; e += gsz) {
+    const int i = (int)(e / P), j = (int)(e % P);
+    Hp[e] = (i < p && j < p) ? 0.5f * (H[(size_t)i * p + j] + H[(size_t)j * p + i]) : 0.f;
+    Vp[e] = i == j ? 1.f : 0.f;
+  }
+  if (!grid_barrier(bar, err, G)) return;
+  int used = 0;
+  const int ntask = npair * npair + (P / kJP) * npair;
+  for (int sweep = 0; sweep < max_sweeps; ++sweep) {
+    double off = 0.0, tot = 0.0;
+    for (long long e = gtid; e < PP; e += gsz) {
+      const double v = (double)Hp[e];
+      tot += v * v;
+      if (e / P != e % P) off += v * v;
+    }
+    off = cta_sum(off, red);
+    tot = cta_sum(tot, red);
+    if (threadIdx.x == 0) {
+      part[2 * blockIdx.x] = off;
+      part[2 * blockIdx.x + 1] = tot;
+    }
+    if (!grid_barrier(bar, err, G)) return;
+    if (threadIdx.x == 0) {
+      double a = 0.0, b = 0.0;
+      for (unsigned q = 0; q < G; ++q) {
+        a += part[2 * q];
+        b += part[2 * q + 1];
+      }
+      s_off = a;
+      s_tot = b;
+    }
+    __syncthreads();
+    if (!(s_off > tol2 * s_tot)) break;
+    for (int r = 0; r < nb - 1; ++r) {
+      for (int k = blockIdx.x; k < npair; k += G) {
+        const int2 pr = circle_pair(nb, r, k);
+        jb_pair_solve(Hp, P, pr.x, pr.y, Qbuf + (size_t)k * kJP * kJP, tol2, sm, red);
+        __syncthreads();
+      }
+      if (!grid_barrier(bar, err, G)) return;
+      for (int t = blockIdx.x; t < ntask; t += G) {
+        if (t < npair * npair) {
+          const int a = t / npair, b = t % npair;
+          const int2 pa = circle_pair(nb, r, a), pb = circle_pair(nb, r, b);
+          jb_apply_tile(Hp, P, pa.x, pa.y, -1, pb.x, pb.y, Qbuf + (size_t)a * kJP * kJP,
+                        Qbuf + (size_t)b * kJP * kJP, sm);
+        } else {
+          const int u = t - npair * npair;
+          const int R = u / npair, b = u % npair;
+          const int2 pb = circle_pair(nb, r, b);
+          jb_apply_tile(Vp, P, 0, 0, R * kJP, pb.x, pb.y, nullptr, Qbuf + (size_t)b * kJP * kJP, sm);
+        }
+      }
+      if (!grid_barrier(bar, err, G)) return;
+    }
+    ++used;
+  }
+  if (blockIdx.x == 0) {
+    sort_eig_block<float>(Hp, Vp, p, w, Vout, jsm, P);
     if (threadIdx.x == 0) *sweeps_out = used;
   }
 }
@@ -949,6 +1219,78 @@ int jacobi_eigh(T* H, int p, T* w, T* V, int max_sweeps, double tol, int* sweeps
   return check_launch("jacobi_eigh");
 }
 
+size_t jacobi_block_smem() {
+  return std::max<size_t>(4 * sizeof(float) * kJP * kJLd + 2 * kJP * sizeof(float) + 3 * kJP * sizeof(int),
+                          2048 * sizeof(float) + 2048 * sizeof(int));
+}
+
+size_t jacobi_block_workspace(int p) {
+  const int P = (p + kJP - 1) / kJP * kJP;
+  Workspace W(nullptr, 0);
+  W.take<float>((size_t)P * P);
+  W.take<float>((size_t)P * P);
+  W.take<float>((size_t)(P / kJP) * kJP * kJP);
+  W.take<double>(2 * (size_t)kMaxCoopGrid);
+  W.take<unsigned int>(kMaxCoopGrid + 1);
+  W.take<int>(2);
+  return W.used;
+}
+
+// FP32 eigendecomposition by block Jacobi (see jacobi_block32): w ascending,
+// V (p x p) the eigenvectors by column.  H is read only.  Returns
+// RVGP_ENOTSUP when the cooperative launch cannot hold a CTA per block pair.
+int jacobi_block_eigh(const float* H, int p, float* w, float* V, int max_sweeps, double tol, int* sweeps_used,
+                      void* ws, size_t ws_bytes, cudaStream_t st) {
+  if (p < kJP || p > 2048) {
+    set_error("jacobi_block_eigh: p=%d out of range", p);
+    return RVGP_ENOTSUP;
+  }
+  if (ws_bytes < jacobi_block_workspace(p)) {
+    set_error("jacobi_block_eigh: workspace too small");
+    return RVGP_EWORKSPACE;
+  }
+  const int P = (p + kJP - 1) / kJP * kJP;
+  Workspace W(ws, ws_bytes);
+  float* Hp = W.take<float>((size_t)P * P);
+  float* Vp = W.take<float>((size_t)P * P);
+  float* Qb = W.take<float>((size_t)(P / kJP) * kJP * kJP);
+  double* part = W.take<double>(2 * (size_t)kMaxCoopGrid);
+  unsigned int* bar = W.take<unsigned int>(kMaxCoopGrid + 1);
+  int* flags = W.take<int>(2);
+  const size_t smem = jacobi_block_smem();
+  if (cudaFuncSetAttribute(jacobi_block32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return check_launch("jacobi_block_eigh");
+  const int npair = P / kJP;
+  const int ntask = npair * npair + (P / kJP) * npair;
+  int G = std::min(std::min(cooperative_grid(jacobi_block32, kJbThreads, smem), kMaxCoopGrid), num_sms());
+  G = std::min(G, ntask);
+  if (G < npair) {
+    set_error("jacobi_block_eigh: %d resident CTAs for %d block pairs", G, npair);
+    return RVGP_ENOTSUP;
+  }
+  cudaMemsetAsync(bar, 0, (G + 1) * sizeof(unsigned int), st);
+  cudaMemsetAsync(flags, 0, 2 * sizeof(int), st);
+  int pv = p, Pv = P, ms = max_sweeps;
+  double t2 = tol * tol;
+  int* err_dev = flags;
+  int* sweeps_dev = flags + 1;
+  void* args[] = {(void*)&H, &pv, &Pv, &Hp, &Vp, &Qb, &part, &ms, &t2, &bar, &err_dev, &sweeps_dev, &w, &V};
+  rvgp::note_launch();
+  cudaError_t e = cudaLaunchCooperativeKernel((const void*)jacobi_block32, dim3(G), dim3(kJbThreads), args, smem, st);
+  if (e != cudaSuccess) {
+    set_error("jacobi_block_eigh: cooperative launch failed: %s", cudaGetErrorString(e));
+    return RVGP_ELAUNCH;
+  }
+  int hv[2] = {0, 0};
+  if (read_back(hv, flags, sizeof(hv), st) != cudaSuccess) return check_launch("jacobi_block_eigh");
+  if (hv[0] != 0) {
+    set_error("jacobi_block_eigh: a grid barrier timed out");
+    return RVGP_ELAUNCH;
+  }
+  if (sweeps_used) *sweeps_used = hv[1];
+  return check_launch("jacobi_block_eigh");
+}
+
 template <typename T>
 size_t col_norms_workspace(long long N, int b) {
   return sizeof(T) * (size_t)col_chunks(N) * b + 256;
@@ -999,3 +1341,35 @@ INST(double)
 #undef INST
 
 }  // namespace rvgp
+
+using namespace rvgp;
+
+RVGP_API size_t rvgp_symeig_f32_workspace(int p) {
+  if (p < 1 || p > 2048) return 0;
+  return sizeof(float) * (size_t)p * p + 256 + std::max(jacobi_workspace<float>(p), jacobi_block_workspace(p));
+}
+
+// Eigendecomposition of a symmetric FP32 matrix H (p x p, read only; the
+// Rayleigh-Ritz step of the eigensolver, whose reference is ARPACK inside
+// scipy's eigsh, RVGP/geometry.py:73): w ascending, V (p x p) eigenvectors by
+// column, up to max_sweeps sweeps until off(H) <= tol ||H||_F.  method 0:
+// block Jacobi for p >= 64, else scalar; 1: scalar parallel Jacobi (one grid
+// barrier per rotation round); 2: block Jacobi.  *sweeps_used (host, may be
+// null).  Synchronises.
+RVGP_API int rvgp_symeig_f32(const float* H, int p, float* w, float* V, int max_sweeps, double tol,
+                             int* sweeps_used, int method, void* workspace, size_t ws_bytes, void* stream) {
+  RVGP_CHECK_ARG(H && w && V && p >= 1 && p <= 2048 && max_sweeps >= 0, "rvgp_symeig_f32: bad arguments");
+  RVGP_CHECK_ARG(method >= 0 && method <= 2, "rvgp_symeig_f32: method %d", method);
+  RVGP_CHECK_ARG(workspace && ws_bytes >= rvgp_symeig_f32_workspace(p), "rvgp_symeig_f32: workspace");
+  cudaStream_t st = as_stream(stream);
+  const bool block = method == 2 || (method == 0 && p >= kJP);
+  RVGP_CHECK_ARG(!block || p >= kJP, "rvgp_symeig_f32: the block form needs p >= %d", kJP);
+  Workspace W(workspace, ws_bytes);
+  float* Hc = W.take<float>((size_t)p * p);
+  const size_t rest = ws_bytes - W.used;
+  void* jws = W.take<char>(rest - 256);
+  if (block) return jacobi_block_eigh(H, p, w, V, max_sweeps, tol, sweeps_used, jws, rest - 256, st);
+  cudaMemcpyAsync(Hc, H, sizeof(float) * (size_t)p * p, cudaMemcpyDeviceToDevice, st);
+  return jacobi_eigh<float>(Hc, p, w, V, max_sweeps, tol, sweeps_used, jws, rest - 256, st);
+}
+

@@ -96,6 +96,12 @@ template <typename T>
 int jacobi_eigh(T* H, int p, T* w, T* V, int max_sweeps, double tol, int* sweeps_used, void* ws, size_t ws_bytes,
                 cudaStream_t st);
 
+// FP32 block Jacobi (64 <= p <= 2048): the eigendecomposition of jacobi_eigh
+// (H read only) with two grid barriers per round of 32-wide block pairs.
+size_t jacobi_block_workspace(int p);
+int jacobi_block_eigh(const float* H, int p, float* w, float* V, int max_sweeps, double tol, int* sweeps_used,
+                      void* ws, size_t ws_bytes, cudaStream_t st);
+
 // Column utilities on X (N x b, ld).
 template <typename T>
 int col_norms(const T* X, int ld, long long N, int b, T* out, void* ws, size_t ws_bytes, cudaStream_t st);

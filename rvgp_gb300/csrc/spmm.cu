@@ -23,6 +23,7 @@
 #include "common.cuh"
 #include "autotune.cuh"
 #include <limits.h>
+#include <algorithm>
 #include <stdio.h>
 #include <stdlib.h>
 
@@ -226,6 +227,111 @@ __global__ void __launch_bounds__(256) bspmm_chunked_kernel(int n, int nch, cons
   }
 }
 
+// Tile-mapped form without staging: CTA (tile of 32 consecutive rows, one
+// 128-byte column chunk), 8 lanes per row, chunk-major grid.  The rows of a
+// tile share most of their neighbours (~131 distinct rows for ~570
+// references at k = 15 on a surface, in the locality order), so after the
+// first touch the gathered chunks come from L1, and no shared memory caps
+// the occupancy.  Same accumulation order as the other variants.
+template <typename T, int DB, int U>
+__global__ void __launch_bounds__(256) bspmm_tile_kernel(int n, int n_tiles, const int* __restrict__ indptr,
+                                                         const int* __restrict__ indices, const T* __restrict__ vals,
+                                                         const T* __restrict__ X, T* __restrict__ Y,
+                                                         const T* __restrict__ Z, int b, int ld, T alpha, T beta,
+                                                         T gamma) {
+  constexpr int V = Vec<T>::V;
+  constexpr int SEG = 128 / (int)sizeof(T);
+  constexpr int G = SEG / V;  // 8 lanes per row
+  const int tile = blockIdx.x % n_tiles, chunk = blockIdx.x / n_tiles;
+  const int c0 = chunk * SEG;
+  const int groups = min(G, (b - c0) / V);
+  const int slot = threadIdx.x / G, g = threadIdx.x % G;
+  const int i = tile * 32 + slot;
+  if (i >= n) return;
+  const bool on = g < groups;
+  const int col = c0 + g * V;
+  T acc[DB][V];
+#pragma unroll
+  for (int p = 0; p < DB; ++p)
+#pragma unroll
+    for (int v = 0; v < V; ++v) acc[p][v] = T(0);
+  const int s = __ldg(indptr + i), e = __ldg(indptr + i + 1);
+  int t = s;
+  for (; t + U <= e; t += U) {
+    T blk[U][DB * DB], x[U][DB][V];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int j = __ldg(indices + t + u);
+      load_block<T, DB>(vals, t + u, blk[u]);
+      if (on)
+#pragma unroll
+        for (int q = 0; q < DB; ++q) vload(X + ((size_t)j * DB + q) * ld + col, x[u][q]);
+    }
+    if (on)
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+#pragma unroll
+        for (int q = 0; q < DB; ++q)
+#pragma unroll
+          for (int p = 0; p < DB; ++p)
+#pragma unroll
+            for (int v = 0; v < V; ++v) acc[p][v] = fma(blk[u][p * DB + q], x[u][q][v], acc[p][v]);
+  }
+  for (; t < e; ++t) {
+    const int j = __ldg(indices + t);
+    T blk[DB * DB];
+    load_block<T, DB>(vals, t, blk);
+    if (on)
+#pragma unroll
+      for (int q = 0; q < DB; ++q) {
+        T x[V];
+        vload(X + ((size_t)j * DB + q) * ld + col, x);
+#pragma unroll
+        for (int p = 0; p < DB; ++p)
+#pragma unroll
+          for (int v = 0; v < V; ++v) acc[p][v] = fma(blk[p * DB + q], x[v], acc[p][v]);
+      }
+  }
+  if (!on) return;
+#pragma unroll
+  for (int p = 0; p < DB; ++p) {
+    const size_t row = ((size_t)i * DB + p) * ld + col;
+    T out[V], x[V];
+#pragma unroll
+    for (int v = 0; v < V; ++v) out[v] = alpha * acc[p][v];
+    if (beta != T(0)) {
+      vload(X + row, x);
+#pragma unroll
+      for (int v = 0; v < V; ++v) out[v] = fma(beta, x[v], out[v]);
+    }
+    if (Z && gamma != T(0)) {
+      vload(Z + row, x);
+#pragma unroll
+      for (int v = 0; v < V; ++v) out[v] = fma(gamma, x[v], out[v]);
+    }
+    vstore(Y + row, out);
+  }
+}
+
+template <typename T, int U>
+int launch_tile(int n, int DB, const int* indptr, const int* indices, const T* vals, const T* X, T* Y, const T* Z,
+                int b, int ld, T alpha, T beta, T gamma, cudaStream_t st) {
+  constexpr int SEG = 128 / (int)sizeof(T);
+  const int nt = (n + 31) / 32, nch = ceil_div(b, SEG);
+  rvgp::note_launch();
+#define RVGP_SPMM_T(DBv)                                                                                          \
+  bspmm_tile_kernel<T, DBv, U><<<(unsigned)((long long)nt * nch), 256, 0, st>>>(n, nt, indptr, indices, vals, X, Y, \
+                                                                                 Z, b, ld, alpha, beta, gamma)
+  switch (DB) {
+    case 1: RVGP_SPMM_T(1); break;
+    case 2: RVGP_SPMM_T(2); break;
+    case 3: RVGP_SPMM_T(3); break;
+    default: RVGP_SPMM_T(4);
+  }
+#undef RVGP_SPMM_T
+  return check_launch("rvgp_bspmm");
+}
+
 template <typename T, int U>
 int launch_chunked(int n, int DB, const int* indptr, const int* indices, const T* vals, const T* X, T* Y, const T* Z,
                    int b, int ld, T alpha, T beta, T gamma, cudaStream_t st) {
@@ -296,8 +402,9 @@ bool overlaps(const void* a, const void* b, size_t bytes) {
 }
 
 // Variants: 0 = row per warp (G groups per lane), 1 / 2 = column-chunked with
-// 2 / 4 neighbours per iteration.  The tuner (autotune.cuh) picks one per
-// shape class; the same bits come out of all three.
+// 2 / 4 neighbours per iteration, 3 / 4 = tile-mapped with 2 / 4.  The tuner
+// (autotune.cuh) picks one per shape class (RVGP_SPMM_VARIANT=v forces one);
+// the same bits come out of all five.
 template <typename T>
 int launch(int n, int DB, const int* indptr, const int* indices, const T* vals, const T* X, T* Y, const T* Z, int b,
            int ld, T alpha, T beta, T gamma, cudaStream_t st) {
@@ -311,19 +418,22 @@ int launch(int n, int DB, const int* indptr, const int* indices, const T* vals, 
     switch (v) {
       case 0: return launch_rows<T>(n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
       case 1: return launch_chunked<T, 2>(n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
-      default: return launch_chunked<T, 4>(n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
+      case 2: return launch_chunked<T, 4>(n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
+      case 3: return launch_tile<T, 2>(n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
+      default: return launch_tile<T, 4>(n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
     }
   };
   int def = groups >= chunk_min_groups() ? 1 : 0;
+  if (const char* fv = getenv("RVGP_SPMM_VARIANT")) def = std::min(4, std::max(0, atoi(fv)));  // tests: one variant
   // tuning runs the product several times into Y: only when Y overlaps neither input
   const size_t bytes = (size_t)n * DB * ld * sizeof(T);
   const bool independent = !overlaps(Y, X, bytes) && !(Z && overlaps(Y, Z, bytes));
   int v = def;
-  if (independent && getenv("RVGP_SPMM_CHUNK_MIN") == nullptr) {
+  if (independent && getenv("RVGP_SPMM_CHUNK_MIN") == nullptr && getenv("RVGP_SPMM_VARIANT") == nullptr) {
     char key[160];
     snprintf(key, sizeof(key), "bspmm %s DB%d b%d n2^%d", sizeof(T) == 4 ? "f32" : "f64", DB, b,
              autotune::log2_bucket(n));
-    v = autotune::tune(key, 3, def, st, 3, run);
+    v = autotune::tune(key, 5, def, st, 3, run);
     if (v < 0) return v;
   }
   return run(v);

@@ -1,0 +1,67 @@
+"""GPU: the FP32 Jacobi eigendecompositions of the eigensolver's
+Rayleigh-Ritz step (rvgp_symeig_f32): the block form (32-wide block pairs,
+64 x 64 subproblems solved in shared memory) and the scalar parallel form
+against numpy's FP64 eigh on the same FP32 input.  Tolerances for FP32:
+eigenvalues within 2e-5 ||H||, residual ||H V - V diag(w)|| and departure
+from orthonormality ||VᵀV - I|| within 2e-4 (Frobenius, relative to ||H||_F
+and sqrt(p)); p not a multiple of 64 (zero padding), clustered and repeated
+eigenvalues, a nearly diagonal matrix (the later Rayleigh-Ritz steps)."""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def core():
+    from rvgp_gb300 import _core
+    _core.require_cuda()
+    return _core
+
+
+def make(kind, p, seed):
+    rng = np.random.default_rng(seed)
+    Q, _ = np.linalg.qr(rng.standard_normal((p, p)))
+    if kind == "random":
+        lam = rng.uniform(0.0, 3.0, p)
+    elif kind == "clustered":
+        lam = np.repeat(rng.uniform(0.0, 2.0, p // 8 + 1), 8)[:p] + 1e-6 * rng.standard_normal(p)
+    elif kind == "repeated":
+        lam = np.sort(np.concatenate([np.zeros(p // 3), np.ones(p - p // 3)]))
+    else:  # nearly diagonal
+        H = np.diag(np.linspace(0.0, 2.0, p)) + 1e-3 * rng.standard_normal((p, p))
+        return (H + H.T) / 2
+    return (Q * lam) @ Q.T
+
+
+@pytest.mark.parametrize("method", [2, 1])
+@pytest.mark.parametrize("kind,p", [("random", 64), ("random", 130), ("clustered", 564), ("repeated", 300),
+                                    ("near_diagonal", 564), ("random", 1128)])
+def test_symeig_f32(core, method, kind, p):
+    if method == 1 and p > 600:
+        pytest.skip("the scalar form is slow at this size")
+    H = make(kind, p, p + method).astype(np.float32)
+    w, V, sweeps = core.symeig_f32(torch.as_tensor(H, device="cuda"), max_sweeps=60, tol=4e-6, method=method)
+    w, V = w.cpu().double().numpy(), V.cpu().double().numpy()
+    Hd = H.astype(np.float64)
+    ref = np.linalg.eigvalsh(Hd)
+    nH = np.linalg.norm(Hd)
+    assert np.all(np.diff(w) >= 0)
+    assert np.abs(w - ref).max() <= 2e-5 * nH
+    assert np.linalg.norm(Hd @ V - V * w) <= 2e-4 * nH
+    assert np.linalg.norm(V.T @ V - np.eye(p)) <= 2e-4 * np.sqrt(p)
+    assert 1 <= sweeps <= 60
+
+
+def test_symeig_block_one_sweep_reduces_off_norm(core):
+    """A single sweep (the intermediate Rayleigh-Ritz steps) leaves a basis in
+    which H is much closer to diagonal than the start."""
+    p = 564
+    H = make("random", p, 3).astype(np.float32)
+    w, V, sweeps = core.symeig_f32(torch.as_tensor(H, device="cuda"), max_sweeps=1, tol=4e-6, method=2)
+    V = V.cpu().double().numpy()
+    B = V.T @ H.astype(np.float64) @ V
+    off = np.linalg.norm(B - np.diag(np.diag(B)))
+    off0 = np.linalg.norm(H - np.diag(np.diag(H)))
+    assert sweeps == 1 and off < 0.2 * off0
