@@ -549,8 +549,8 @@ __global__ void __launch_bounds__(kSpThreads, 1)
           lambdas[it] = w.v;
         }
       }
-      __syncwarp();
-      if (lane < D) s_p[lane] = Xs[(size_t)__shfl_sync(0xffffffffu, w.pos, 0) * D + lane];
+      // w is the same in every lane (butterfly reduction)
+      if (lane < D) s_p[lane] = Xs[(size_t)w.pos * D + lane];
     }
     __syncthreads();
     if (s_stop) break;

@@ -917,6 +917,7 @@ __global__ void __launch_bounds__(kJbThreads) jacobi_block32(const float* __rest
   if (!grid_barrier(bar, err, G)) return;
   int used = 0;
   const int ntask = npair * npair + (P / kJP) * npair;
+  double prev_off = -1.0;
   for (int sweep = 0; sweep < max_sweeps; ++sweep) {
     double off = 0.0, tot = 0.0;
     for (long long e = gtid; e < PP; e += gsz) {
@@ -942,6 +943,10 @@ __global__ void __launch_bounds__(kJbThreads) jacobi_block32(const float* __rest
     }
     __syncthreads();
     if (!(s_off > tol2 * s_tot)) break;
+    // the tile products leave an off-diagonal floor of ~64u||H|| (FP32 sums of
+    // 64 terms) near the tolerance: a sweep that did not halve off(H) stops
+    if (prev_off >= 0.0 && s_off > 0.25 * prev_off) break;
+    prev_off = s_off;
     for (int r = 0; r < nb - 1; ++r) {
       for (int k = blockIdx.x; k < npair; k += G) {
         const int2 pr = circle_pair(nb, r, k);
