@@ -394,7 +394,7 @@ RVGP_API int rvgp_diameter(const double* X, int n, int D, double* out, void* wor
 // forms (exact_dist), so the three forms select the same points.
 namespace rvgp {
 namespace {
-constexpr int kSpThreads = 1024;
+constexpr int kSpThreads = 512;
 constexpr int kBlk = 32;           // points per block
 constexpr int kSup = 32;           // blocks per superblock
 constexpr double kPruneMargin = 1.0 - 2e-12;
@@ -462,10 +462,12 @@ __global__ void fps_sp_blocks(const double* __restrict__ X, const int* __restric
   }
 }
 
-// Superblock boxes and maxima (warp per superblock).
-__global__ void fps_sp_super(int nb, int D, const double* __restrict__ box, const double* __restrict__ bmax,
-                             const int* __restrict__ borig, const int* __restrict__ bpos, double* __restrict__ sbox,
-                             double* __restrict__ smax, int* __restrict__ sorig, int* __restrict__ spos) {
+// Superblock boxes and maxima, and the coordinates of each superblock's
+// maximising point (warp per superblock).
+__global__ void fps_sp_super(int nb, int D, const double* __restrict__ Xs, const double* __restrict__ box,
+                             const double* __restrict__ bmax, const int* __restrict__ borig,
+                             const int* __restrict__ bpos, double* __restrict__ sbox, double* __restrict__ smax,
+                             int* __restrict__ sorig, int* __restrict__ spos, double* __restrict__ sxy) {
   const int warp = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
   const int ns = (nb + kSup - 1) / kSup;
   if (warp >= ns) return;
@@ -490,32 +492,44 @@ __global__ void fps_sp_super(int nb, int D, const double* __restrict__ box, cons
     sorig[warp] = m.orig;
     spos[warp] = m.pos;
   }
+  if (lane < D) sxy[(size_t)warp * D + lane] = Xs[(size_t)m.pos * D + lane];
 }
 
-// Selections 1 .. N_max-1 in one CTA.  Shared memory: the superblock boxes
-// and maxima, the lists of superblocks and blocks to visit.
+// Selections 1 .. N_max-1 in one CTA.  Shared memory: the superblock boxes,
+// maxima and the coordinates of their maximising points, the list of
+// superblocks to visit.  A warp owns a listed superblock from the block test
+// to its new maximum: it tests the 32 blocks (lane per block), updates the
+// points of the blocks that pass (lane per point, four blocks' loads in
+// flight), keeps the blocks' maxima in the lanes' registers and reduces them
+// to the superblock's.  Per selection: three CTA barriers and three
+// dependent L2 round trips (block data, points, the new maximising point).
+template <int D>
 __global__ void __launch_bounds__(kSpThreads, 1)
-    fps_sp_select(const double* __restrict__ Xs, const int* __restrict__ order, int n, int D, int N_max,
+    fps_sp_select(const double* __restrict__ Xs, const int* __restrict__ order, int n, int N_max,
                   double* __restrict__ ds, const double* __restrict__ box, double* __restrict__ bmax,
                   int* __restrict__ borig, int* __restrict__ bpos, const double* __restrict__ sbox_g,
                   const double* __restrict__ smax_g, const int* __restrict__ sorig_g, const int* __restrict__ spos_g,
-                  int* __restrict__ perm, double* __restrict__ lambdas, int* __restrict__ count,
-                  const double* __restrict__ diam, double spacing, int* __restrict__ blist_g,
+                  const double* __restrict__ sxy_g, int* __restrict__ perm, double* __restrict__ lambdas,
+                  int* __restrict__ count, const double* __restrict__ diam, double spacing,
                   long long* __restrict__ exact_evals) {
+  constexpr int GB = D <= 4 ? 4 : 2;  // blocks whose points are loaded together
   extern __shared__ __align__(16) unsigned char fsm[];
   const int nb = (n + kBlk - 1) / kBlk, ns = (nb + kSup - 1) / kSup;
-  double* sbox = reinterpret_cast<double*>(fsm);        // ns x 2D
-  double* smax = sbox + (size_t)ns * 2 * D;             // ns
-  int* sorig = reinterpret_cast<int*>(smax + ns);       // ns
-  int* spos = sorig + ns;                                // ns
-  int* slist = spos + ns;                                // ns
-  __shared__ double s_p[8];
-  __shared__ double s_wv[32];
-  __shared__ int s_wo[32], s_wp[32];
-  __shared__ int s_ns, s_nb, s_stop;
+  double* sbox = reinterpret_cast<double*>(fsm);  // ns x 2D
+  double* sxy = sbox + (size_t)ns * 2 * D;        // ns x D
+  double* smax = sxy + (size_t)ns * D;            // ns
+  int* sorig = reinterpret_cast<int*>(smax + ns);  // ns
+  int* spos = sorig + ns;                          // ns
+  int* slist = spos + ns;                          // ns
+  __shared__ double s_p[D];
+  __shared__ double s_wv[kSpThreads / 32];
+  __shared__ int s_wo[kSpThreads / 32], s_ws[kSpThreads / 32];
+  __shared__ int s_ns, s_stop;
+  constexpr int NW = kSpThreads / 32;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   for (int s = tid; s < ns; s += kSpThreads) {
     for (int j = 0; j < 2 * D; ++j) sbox[(size_t)s * 2 * D + j] = sbox_g[(size_t)s * 2 * D + j];
+    for (int j = 0; j < D; ++j) sxy[(size_t)s * D + j] = sxy_g[(size_t)s * D + j];
     smax[s] = smax_g[s];
     sorig[s] = sorig_g[s];
     spos[s] = spos_g[s];
@@ -523,24 +537,23 @@ __global__ void __launch_bounds__(kSpThreads, 1)
   long long exact = 0;
   __syncthreads();
   for (int it = 1; it < N_max; ++it) {
-    // ---- A. the next point: maximum over the superblock maxima
+    // ---- A. the next point: maximum over the superblock maxima (pos = superblock)
     Max3 m{-DBL_MAX, INT_MAX, 0};
     for (int s = tid; s < ns; s += kSpThreads)
-      if (better(smax[s], sorig[s], m.v, m.orig)) m = Max3{smax[s], sorig[s], spos[s]};
+      if (better(smax[s], sorig[s], m.v, m.orig)) m = Max3{smax[s], sorig[s], s};
     m = warp_max3(m);
     if (lane == 0) {
       s_wv[warp] = m.v;
       s_wo[warp] = m.orig;
-      s_wp[warp] = m.pos;
+      s_ws[warp] = m.pos;
     }
     __syncthreads();
     if (warp == 0) {
-      Max3 w{s_wv[lane], s_wo[lane], s_wp[lane]};
-      w = warp_max3(w);
+      Max3 w = lane < NW ? Max3{s_wv[lane], s_wo[lane], s_ws[lane]} : Max3{-DBL_MAX, INT_MAX, 0};
+      w = warp_max3(w);  // the same in every lane
       if (lane == 0) {
         s_stop = 0;
         s_ns = 0;
-        s_nb = 0;
         if (diam && w.v / diam[0] < spacing) {
           s_stop = 1;
           *count = it;
@@ -549,70 +562,96 @@ __global__ void __launch_bounds__(kSpThreads, 1)
           lambdas[it] = w.v;
         }
       }
-      // w is the same in every lane (butterfly reduction)
-      if (lane < D) s_p[lane] = Xs[(size_t)w.pos * D + lane];
+      if (lane < D) s_p[lane] = sxy[(size_t)w.pos * D + lane];
     }
     __syncthreads();
     if (s_stop) break;
+    double p[D];
+#pragma unroll
+    for (int j = 0; j < D; ++j) p[j] = s_p[j];
     // ---- B. superblocks whose box comes closer to p than their maximum
     for (int s = tid; s < ns; s += kSpThreads) {
-      const double d2 = box_dist2(s_p, sbox + (size_t)s * 2 * D, sbox + (size_t)s * 2 * D + D, D);
+      const double d2 = box_dist2(p, sbox + (size_t)s * 2 * D, sbox + (size_t)s * 2 * D + D, D);
       if (d2 * kPruneMargin <= smax[s] * smax[s]) slist[atomicAdd(&s_ns, 1)] = s;
     }
     __syncthreads();
-    // ---- C. their blocks, the same test (warp per superblock, lane per block)
+    // ---- C. each listed superblock by one warp
     const int nsl = s_ns;
-    for (int e = warp; e < nsl; e += kSpThreads / 32) {
-      const int b = slist[e] * kSup + lane;
-      if (b < nb) {
-        const double bm = bmax[b];
-        const double d2 = box_dist2(s_p, box + (size_t)b * 2 * D, box + (size_t)b * 2 * D + D, D);
-        if (d2 * kPruneMargin <= bm * bm) blist_g[atomicAdd(&s_nb, 1)] = b;
+    for (int e = warp; e < nsl; e += NW) {
+      const int sb = slist[e];
+      const int b = sb * kSup + lane;
+      const bool valid = b < nb;
+      Max3 bm{-DBL_MAX, INT_MAX, 0};
+      bool need = false;
+      if (valid) {
+        bm = Max3{bmax[b], borig[b], bpos[b]};
+        const double d2 = box_dist2(p, box + (size_t)b * 2 * D, box + (size_t)b * 2 * D + D, D);
+        need = d2 * kPruneMargin <= bm.v * bm.v;
       }
-    }
-    __syncthreads();
-    // ---- D. their points (warp per block, lane per point), new block maxima
-    const int nbl = s_nb;
-    for (int e = warp; e < nbl; e += kSpThreads / 32) {
-      const int b = blist_g[e];
-      const int q = b * kBlk + lane;
-      Max3 mm{-DBL_MAX, INT_MAX, 0};
-      if (q < n) {
-        double cur = ds[q];
-        if (cur > 0.0) {
-          double acc = 0.0;
-          for (int j = 0; j < D; ++j) {
-            const double df = __dsub_rn(s_p[j], Xs[(size_t)q * D + j]);
-            acc = __dadd_rn(acc, __dmul_rn(df, df));
-          }
-          const double d = sqrt(acc);
-          ++exact;
-          if (d < cur) {
-            cur = d;
-            ds[q] = d;
+      unsigned mask = __ballot_sync(0xffffffffu, need);
+      while (mask) {  // warp-uniform
+        int bl[GB], cnt = 0;
+#pragma unroll
+        for (int u = 0; u < GB; ++u) {
+          bl[u] = -1;
+          if (mask) {
+            bl[u] = __ffs(mask) - 1;
+            mask &= mask - 1;
+            ++cnt;
           }
         }
-        mm = Max3{cur, order[q], q};
+        double cur[GB], x[GB][D];
+        int q[GB], o[GB];
+#pragma unroll
+        for (int u = 0; u < GB; ++u) {
+          q[u] = bl[u] >= 0 ? (sb * kSup + bl[u]) * kBlk + lane : n;
+          if (q[u] < n) {
+            cur[u] = ds[q[u]];
+            o[u] = order[q[u]];
+#pragma unroll
+            for (int j = 0; j < D; ++j) x[u][j] = Xs[(size_t)q[u] * D + j];
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < GB; ++u) {
+          if (bl[u] < 0) break;  // warp-uniform
+          Max3 mm{-DBL_MAX, INT_MAX, 0};
+          if (q[u] < n) {
+            double c = cur[u];
+            if (c > 0.0) {
+              double acc = 0.0;
+#pragma unroll
+              for (int j = 0; j < D; ++j) {
+                const double df = __dsub_rn(p[j], x[u][j]);
+                acc = __dadd_rn(acc, __dmul_rn(df, df));
+              }
+              const double d = sqrt(acc);
+              ++exact;
+              if (d < c) {
+                c = d;
+                ds[q[u]] = d;
+              }
+            }
+            mm = Max3{c, o[u], q[u]};
+          }
+          mm = warp_max3(mm);
+          const int bb = sb * kSup + bl[u];
+          if (lane == bl[u]) bm = mm;
+          if (lane == 0) {
+            bmax[bb] = mm.v;
+            borig[bb] = mm.orig;
+            bpos[bb] = mm.pos;
+          }
+        }
+        (void)cnt;
       }
-      mm = warp_max3(mm);
+      Max3 sm = warp_max3(bm);
       if (lane == 0) {
-        bmax[b] = mm.v;
-        borig[b] = mm.orig;
-        bpos[b] = mm.pos;
+        smax[sb] = sm.v;
+        sorig[sb] = sm.orig;
+        spos[sb] = sm.pos;
       }
-    }
-    __syncthreads();
-    // ---- E. new maxima of the visited superblocks (warp per superblock)
-    for (int e = warp; e < nsl; e += kSpThreads / 32) {
-      const int s = slist[e];
-      const int b = s * kSup + lane;
-      Max3 mm = b < nb ? Max3{bmax[b], borig[b], bpos[b]} : Max3{-DBL_MAX, INT_MAX, 0};
-      mm = warp_max3(mm);
-      if (lane == 0) {
-        smax[s] = mm.v;
-        sorig[s] = mm.orig;
-        spos[s] = mm.pos;
-      }
+      if (lane < D) sxy[(size_t)sb * D + lane] = Xs[(size_t)sm.pos * D + lane];
     }
     __syncthreads();
   }
@@ -630,7 +669,7 @@ __global__ void add_ll(long long* p, long long v) { *p += v; }
 
 size_t fps_sp_smem(int n, int D) {
   const int nb = (n + kBlk - 1) / kBlk, ns = (nb + kSup - 1) / kSup;
-  return (size_t)ns * (2 * D * sizeof(double) + sizeof(double) + 3 * sizeof(int));
+  return (size_t)ns * (3 * D * sizeof(double) + sizeof(double) + 3 * sizeof(int));
 }
 }  // namespace
 }  // namespace rvgp
@@ -647,25 +686,45 @@ RVGP_API int rvgp_fps_spatial_max_n(int D) {
   if (cudaGetDevice(&dev) != cudaSuccess ||
       cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
     return 0;
-  const size_t per = 2 * D * sizeof(double) + sizeof(double) + 3 * sizeof(int);
+  const size_t per = 3 * D * sizeof(double) + sizeof(double) + 3 * sizeof(int);
   const long long ns = ((long long)optin - 2048) / (long long)per;
   return (int)std::min<long long>(INT_MAX / 2, ns * kBlk * kSup);
 }
 
-RVGP_API size_t rvgp_fps_spatial_workspace(int n, int D) {
+namespace {
+struct SpBufs {
+  int *order, *rank, *borig, *bpos, *sorig, *spos;
+  double *Xs, *ds, *box, *bmax, *sbox, *sxy, *smax;
+  void* lo_ws;
+  size_t lo_bytes;
+};
+// one carve for the size query and the call
+SpBufs carve_sp(Workspace& ws, int n, int D) {
   const int nb = (n + kBlk - 1) / kBlk, ns = (nb + kSup - 1) / kSup;
+  SpBufs b;
+  b.order = ws.take<int>(n);
+  b.rank = ws.take<int>(n);
+  b.Xs = ws.take<double>((size_t)n * D);
+  b.ds = ws.take<double>(n);
+  b.box = ws.take<double>((size_t)nb * 2 * D);
+  b.bmax = ws.take<double>(nb);
+  b.borig = ws.take<int>(nb);
+  b.bpos = ws.take<int>(nb);
+  b.sbox = ws.take<double>((size_t)ns * 2 * D);
+  b.sxy = ws.take<double>((size_t)ns * D);
+  b.smax = ws.take<double>(ns);
+  b.sorig = ws.take<int>(ns);
+  b.spos = ws.take<int>(ns);
+  b.lo_bytes = rvgp_locality_order_workspace(n, D);
+  b.lo_ws = ws.take<char>(b.lo_bytes);
+  return b;
+}
+}  // namespace
+
+RVGP_API size_t rvgp_fps_spatial_workspace(int n, int D) {
+  if (n < 1 || D < 1 || D > 8) return 0;
   Workspace ws(nullptr, 0);
-  ws.take<int>(n);                          // order
-  ws.take<int>(n);                          // rank
-  ws.take<double>((size_t)n * D);           // Xs
-  ws.take<double>(n);                       // ds
-  ws.take<double>((size_t)nb * 2 * D);      // box
-  ws.take<double>(nb);                      // bmax
-  ws.take<int>(2 * (size_t)nb);             // borig, bpos
-  ws.take<int>(nb);                         // block list
-  ws.take<double>((size_t)ns * (2 * D + 1));  // sbox, smax
-  ws.take<int>(2 * (size_t)ns);             // sorig, spos
-  ws.take<char>(rvgp_locality_order_workspace(n, D));
+  carve_sp(ws, n, D);
   return ws.used;
 }
 
@@ -682,21 +741,11 @@ RVGP_API int rvgp_fps_spatial(const double* X, int n, int D, int N_max, int star
   cudaStream_t st = as_stream(stream);
   const int nb = (n + kBlk - 1) / kBlk, ns = (nb + kSup - 1) / kSup;
   Workspace ws(workspace, ws_bytes);
-  int* order = ws.take<int>(n);
-  int* rank = ws.take<int>(n);
-  double* Xs = ws.take<double>((size_t)n * D);
-  double* ds = ws.take<double>(n);
-  double* box = ws.take<double>((size_t)nb * 2 * D);
-  double* bmax = ws.take<double>(nb);
-  int* borig = ws.take<int>(nb);
-  int* bpos = ws.take<int>(nb);
-  int* blist = ws.take<int>(nb);
-  double* sbox = ws.take<double>((size_t)ns * 2 * D);
-  double* smax = ws.take<double>(ns);
-  int* sorig = ws.take<int>(ns);
-  int* spos = ws.take<int>(ns);
-  const size_t lo_bytes = rvgp_locality_order_workspace(n, D);
-  void* lo_ws = ws.take<char>(lo_bytes);
+  const SpBufs B = carve_sp(ws, n, D);
+  int *order = B.order, *rank = B.rank, *borig = B.borig, *bpos = B.bpos, *sorig = B.sorig, *spos = B.spos;
+  double *Xs = B.Xs, *ds = B.ds, *box = B.box, *bmax = B.bmax, *sbox = B.sbox, *sxy = B.sxy, *smax = B.smax;
+  void* lo_ws = B.lo_ws;
+  const size_t lo_bytes = B.lo_bytes;
   TRY_RC(rvgp_locality_order(X, n, D, order, rank, lo_ws, lo_bytes, stream));
   cudaMemsetAsync(count, 0xFF, sizeof(int), st);  // -1: all N_max taken unless the spacing stop fires
   if (exact_evals) cudaMemsetAsync(exact_evals, 0, sizeof(long long), st);
@@ -704,17 +753,34 @@ RVGP_API int rvgp_fps_spatial(const double* X, int n, int D, int N_max, int star
   fps_sp_blocks<<<ceil_div((long long)nb * 32, 256), 256, 0, st>>>(X, order, n, D, start, Xs, ds, box, bmax, borig,
                                                                     bpos);
   rvgp::note_launch();
-  fps_sp_super<<<ceil_div((long long)ns * 32, 256), 256, 0, st>>>(nb, D, box, bmax, borig, bpos, sbox, smax, sorig,
-                                                                   spos);
+  fps_sp_super<<<ceil_div((long long)ns * 32, 256), 256, 0, st>>>(nb, D, Xs, box, bmax, borig, bpos, sbox, smax,
+                                                                   sorig, spos, sxy);
   rvgp::note_launch();
   write_first<<<1, 32, 0, st>>>(perm, lambdas, start);
   if (N_max > 1) {
     const size_t smem = fps_sp_smem(n, D);
-    if (cudaFuncSetAttribute(fps_sp_select, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-      return check_launch("rvgp_fps_spatial");
-    rvgp::note_launch();
-    fps_sp_select<<<1, kSpThreads, smem, st>>>(Xs, order, n, D, N_max, ds, box, bmax, borig, bpos, sbox, smax, sorig,
-                                               spos, perm, lambdas, count, diam, spacing, blist, exact_evals);
+#define RVGP_FPS_SP(Dv)                                                                                          \
+  case Dv: {                                                                                                     \
+    if (cudaFuncSetAttribute(fps_sp_select<Dv>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=      \
+        cudaSuccess)                                                                                             \
+      return check_launch("rvgp_fps_spatial");                                                                   \
+    rvgp::note_launch();                                                                                         \
+    fps_sp_select<Dv><<<1, kSpThreads, smem, st>>>(Xs, order, n, N_max, ds, box, bmax, borig, bpos, sbox, smax,  \
+                                                   sorig, spos, sxy, perm, lambdas, count, diam, spacing,        \
+                                                   exact_evals);                                                  \
+    break;                                                                                                       \
+  }
+    switch (D) {
+      RVGP_FPS_SP(1)
+      RVGP_FPS_SP(2)
+      RVGP_FPS_SP(3)
+      RVGP_FPS_SP(4)
+      RVGP_FPS_SP(5)
+      RVGP_FPS_SP(6)
+      RVGP_FPS_SP(7)
+      default: RVGP_FPS_SP(8)
+    }
+#undef RVGP_FPS_SP
   }
   RVGP_LAUNCH_CHECK("rvgp_fps_spatial");
   if (exact_evals) {

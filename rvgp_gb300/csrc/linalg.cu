@@ -718,8 +718,8 @@ __global__ void __launch_bounds__(256) jacobi_persistent(T* H, T* Hb, T* Va, T* 
 constexpr int kJB = 32;
 constexpr int kJP = 2 * kJB;   // pair width
 constexpr int kJLd = kJP + 1;  // shared-memory row stride
-constexpr int kJbThreads = 256;
-constexpr int kJbMaxInner = 6;
+constexpr int kJbThreads = 1024;
+constexpr int kJbMaxInner = 2;
 
 __device__ __forceinline__ void jrot32(float a, float b, float c, float& cs, float& sn) {
   cs = 1.f;
@@ -833,7 +833,7 @@ __device__ void jb_pair_solve(const float* __restrict__ H, int P, int I, int J, 
 }
 
 // X (64 x 64 tile: rows ri(l), columns ci(l) of a matrix with leading
-// dimension P) <- Qaᵀ X Qb (Qa null: X Qb).  Each thread forms a 4 x 4 block.
+// dimension P) <- Qaᵀ X Qb (Qa null: X Qb).  Each thread forms a 2 x 2 block.
 __device__ void jb_apply_tile(float* __restrict__ X, int P, int rI, int rJ, int rows_contig, int cI, int cJ,
                               const float* __restrict__ Qa, const float* __restrict__ Qb, float* sm) {
   float* Xs = sm;
@@ -849,51 +849,52 @@ __device__ void jb_apply_tile(float* __restrict__ X, int P, int rI, int rJ, int 
     if (Qa) A[r * kJLd + c] = Qa[e];
   }
   __syncthreads();
-  const int i0 = 4 * (tid / 16), j0 = 4 * (tid % 16);
-  float acc[4][4];
+  constexpr int TB = 2;  // output block per thread
+  const int i0 = TB * (tid / (kJP / TB)), j0 = TB * (tid % (kJP / TB));
+  float acc[TB][TB];
   const float* src = Xs;
   if (Qa) {
 #pragma unroll
-    for (int u = 0; u < 4; ++u)
+    for (int u = 0; u < TB; ++u)
 #pragma unroll
-      for (int v = 0; v < 4; ++v) acc[u][v] = 0.f;
+      for (int v = 0; v < TB; ++v) acc[u][v] = 0.f;
     for (int k = 0; k < kJP; ++k) {
-      float a[4], x[4];
+      float a[TB], x[TB];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) a[u] = A[k * kJLd + i0 + u];
+      for (int u = 0; u < TB; ++u) a[u] = A[k * kJLd + i0 + u];
 #pragma unroll
-      for (int v = 0; v < 4; ++v) x[v] = Xs[k * kJLd + j0 + v];
+      for (int v = 0; v < TB; ++v) x[v] = Xs[k * kJLd + j0 + v];
 #pragma unroll
-      for (int u = 0; u < 4; ++u)
+      for (int u = 0; u < TB; ++u)
 #pragma unroll
-        for (int v = 0; v < 4; ++v) acc[u][v] = fmaf(a[u], x[v], acc[u][v]);
+        for (int v = 0; v < TB; ++v) acc[u][v] = fmaf(a[u], x[v], acc[u][v]);
     }
 #pragma unroll
-    for (int u = 0; u < 4; ++u)
+    for (int u = 0; u < TB; ++u)
 #pragma unroll
-      for (int v = 0; v < 4; ++v) T[(i0 + u) * kJLd + j0 + v] = acc[u][v];
+      for (int v = 0; v < TB; ++v) T[(i0 + u) * kJLd + j0 + v] = acc[u][v];
     __syncthreads();
     src = T;
   }
 #pragma unroll
-  for (int u = 0; u < 4; ++u)
+  for (int u = 0; u < TB; ++u)
 #pragma unroll
-    for (int v = 0; v < 4; ++v) acc[u][v] = 0.f;
+    for (int v = 0; v < TB; ++v) acc[u][v] = 0.f;
   for (int k = 0; k < kJP; ++k) {
-    float a[4], b[4];
+    float a[TB], b[TB];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) a[u] = src[(i0 + u) * kJLd + k];
+    for (int u = 0; u < TB; ++u) a[u] = src[(i0 + u) * kJLd + k];
 #pragma unroll
-    for (int v = 0; v < 4; ++v) b[v] = B[k * kJLd + j0 + v];
+    for (int v = 0; v < TB; ++v) b[v] = B[k * kJLd + j0 + v];
 #pragma unroll
-    for (int u = 0; u < 4; ++u)
+    for (int u = 0; u < TB; ++u)
 #pragma unroll
-      for (int v = 0; v < 4; ++v) acc[u][v] = fmaf(a[u], b[v], acc[u][v]);
+      for (int v = 0; v < TB; ++v) acc[u][v] = fmaf(a[u], b[v], acc[u][v]);
   }
 #pragma unroll
-  for (int u = 0; u < 4; ++u)
+  for (int u = 0; u < TB; ++u)
 #pragma unroll
-    for (int v = 0; v < 4; ++v) X[(size_t)grow(i0 + u) * P + pair_index(cI, cJ, j0 + v)] = acc[u][v];
+    for (int v = 0; v < TB; ++v) X[(size_t)grow(i0 + u) * P + pair_index(cI, cJ, j0 + v)] = acc[u][v];
   __syncthreads();  // the shared buffers are reused by the next task
 }
 
@@ -944,8 +945,9 @@ __global__ void __launch_bounds__(kJbThreads) jacobi_block32(const float* __rest
     __syncthreads();
     if (!(s_off > tol2 * s_tot)) break;
     // the tile products leave an off-diagonal floor of ~64u||H|| (FP32 sums of
-    // 64 terms) near the tolerance: a sweep that did not halve off(H) stops
-    if (prev_off >= 0.0 && s_off > 0.25 * prev_off) break;
+    // 64 terms) near the tolerance: from the third sweep on, one that did not
+    // halve off(H)² stops (early sweeps reduce it by far more)
+    if (sweep >= 2 && s_off > 0.5 * prev_off) break;
     prev_off = s_off;
     for (int r = 0; r < nb - 1; ++r) {
       for (int k = blockIdx.x; k < npair; k += G) {
