@@ -204,6 +204,55 @@ __global__ void __launch_bounds__(256) resid_partial(const T* __restrict__ W, co
   }
 }
 
+// Rayleigh quotients of the FP32 Ritz vectors: vᵀw and vᵀv per column (FP32
+// products summed in FP64 per row chunk), then theta = vᵀw / vᵀv.  The FP32
+// Jacobi's diagonal drifts with its rounding (~1e-4 relative at p ~ 500,
+// growing with the rotations per index); the quotient's error is of the order
+// of the squared residual.
+__global__ void __launch_bounds__(256) rq_partial(const float* __restrict__ W, const float* __restrict__ V, int ld,
+                                                  long long N, int b, long long chunk, double* __restrict__ part) {
+  __shared__ double sh[2][8][32];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int j = blockIdx.y * 32 + lane;
+  const long long r0 = blockIdx.x * chunk, r1 = min(N, r0 + chunk);
+  double vw = 0.0, vv = 0.0;
+  if (j < b) {
+    for (long long r = r0 + warp; r < r1;) {
+      float a0 = 0.f, a1 = 0.f;  // FP32 sums of at most 16 rows, then FP64
+      for (int k = 0; k < 16 && r < r1; ++k, r += 8) {
+        const float v = V[r * ld + j];
+        a0 = fmaf(v, W[r * ld + j], a0);
+        a1 = fmaf(v, v, a1);
+      }
+      vw += a0;
+      vv += a1;
+    }
+  }
+  sh[0][warp][lane] = vw;
+  sh[1][warp][lane] = vv;
+  __syncthreads();
+  if (warp == 0 && j < b) {
+    double t0 = 0.0, t1 = 0.0;
+    for (int w = 0; w < 8; ++w) {
+      t0 += sh[0][w][lane];
+      t1 += sh[1][w][lane];
+    }
+    part[(size_t)blockIdx.x * 2 * b + j] = t0;
+    part[(size_t)blockIdx.x * 2 * b + b + j] = t1;
+  }
+}
+
+__global__ void rq_final(const double* __restrict__ part, int nchunk, int b, double* __restrict__ theta) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= b) return;
+  double vw = 0.0, vv = 0.0;
+  for (int c = 0; c < nchunk; ++c) {
+    vw += part[(size_t)c * 2 * b + j];
+    vv += part[(size_t)c * 2 * b + b + j];
+  }
+  if (vv > 0.0) theta[j] = vw / vv;
+}
+
 __global__ void resid_final(const double* __restrict__ part, int nchunk, int b, double* __restrict__ out) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= b) return;
@@ -471,9 +520,12 @@ int rayleigh_ritz(const Problem& P, Block<T>& B, Small& s, Stats& stt, int max_s
     // rotation costs ~64x an FP32 one on GB300).  Stop at off(H) <= 4e-6 ||H||_F,
     // below the FP32 stage's residual tolerance and above FP32 rounding.
     TRY(convert_f64_to_f32(s.H, p, s.Hf, p, p, p, st));
-    if (s.jacb)
-      TRY(jacobi_block_eigh(s.Hf, p, s.thf, s.Bf, std::min(max_sweeps, kFp32Sweeps), 4e-6, &used, s.jac_ws,
-                            s.jac_bytes, st));
+    // the one-sweep intermediate steps by block Jacobi (3.7x faster per sweep at
+    // p = 1128; its FP32 rounding floor, ~5e-4 of ||H||, is irrelevant there and
+    // the Ritz values are recomputed as Rayleigh quotients below); the full
+    // step by the scalar kernel, whose floor is lower
+    if (s.jacb && max_sweeps <= 1)
+      TRY(jacobi_block_eigh(s.Hf, p, s.thf, s.Bf, max_sweeps, 4e-6, &used, s.jac_ws, s.jac_bytes, st));
     else if (s.jac32)
       TRY(jacobi32_eigh(s.Hf, p, s.thf, s.Bf, std::min(max_sweeps, kFp32Sweeps), 4e-6, &used, s.jac32_ws,
                         s.jac32_bytes, st));
@@ -493,6 +545,13 @@ int rayleigh_ritz(const Problem& P, Block<T>& B, Small& s, Stats& stt, int max_s
   std::swap(B.W, B.T2);
   const int nc = resid_chunks(N);
   const long long chunk = (N + nc - 1) / nc;
+  if (sizeof(T) == 4) {
+    rvgp::note_launch();
+    rq_partial<<<dim3(nc, ceil_div(p, 32)), 256, 0, st>>>(reinterpret_cast<const float*>(B.W),
+                                                          reinterpret_cast<const float*>(B.V), p, N, p, chunk,
+                                                          s.resid_part);
+    rvgp::note_launch(); rq_final<<<ceil_div(p, 256), 256, 0, st>>>(s.resid_part, nc, p, s.theta);
+  }
   rvgp::note_launch();
   resid_partial<T><<<dim3(nc, ceil_div(p, 32)), 256, 0, st>>>(B.W, B.V, s.theta, p, N, p, chunk, s.resid_part);
   rvgp::note_launch(); resid_final<<<ceil_div(p, 256), 256, 0, st>>>(s.resid_part, nc, p, s.res);
@@ -606,7 +665,7 @@ Layout carve(Workspace& ws, long long N, int p, int mode) {
   s.res = ws.take<double>(p);
   s.norms64 = ws.take<double>(p);
   s.gersh = ws.take<double>(num_sms() * 2);
-  s.resid_part = ws.take<double>((size_t)resid_chunks(N) * p);
+  s.resid_part = ws.take<double>((size_t)resid_chunks(N) * 2 * p);  // [vᵀw | vᵀv] partials, then the residual's
   s.info = ws.take<int>(4);
   s.Bf = ws.take<float>(pp);
   s.Bd = ws.take<double>(pp);
