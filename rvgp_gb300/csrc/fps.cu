@@ -383,66 +383,94 @@ RVGP_API int rvgp_diameter(const double* X, int n, int D, double* out, void* wor
 // anything.  Selecting p with value r = max_x ds[x] lowers ds[x] only where
 // d(p, x) < ds[x] <= r.  Points are renumbered along a Morton curve
 // (rvgp_locality_order) and cut into blocks of 32 and superblocks of 32
-// blocks, each with its FP64 bounding box and the maximum of ds over it
-// (value, then lowest original index).  A block is visited only when the
-// distance from p to its box is below its maximum (times 1 - 2e-12, which
-// covers the rounding of both sides, so the skipped points are exactly those
-// whose minimum keeps its value), and the next point is the maximum over the
-// superblock maxima.  Late in a long run the ball of radius r holds a
-// handful of blocks: each selection is a few dependent L2 round trips in one
-// CTA of 1024 threads, with no grid barrier.  Distances as in the other
-// forms (exact_dist), so the three forms select the same points.
+// blocks, each with its bounding box (FP32, rounded outwards, so it contains
+// the FP64 points) and the maximum of ds over it (value, then lowest
+// original index).  One CTA runs all selections with no grid barrier:
+//  A. the next point is the maximum over the superblock maxima (shared
+//     memory), compared as integer keys: the bits of a non-negative double
+//     order like its value, then the original index;
+//  B. superblocks whose box may come closer to p than their maximum are
+//     listed: the FP32 box distance lb32 with the certified margin
+//     δ = 4u(2R√D + (D+2)·lb32) (u = 2^-24, R the largest point norm: the
+//     roundings of p, of the differences, squares, sum and square root), so a
+//     superblock is skipped only when lb32 − δ > its maximum for certain;
+//  C. a warp owns each listed superblock: the same test per block, then the
+//     points of the blocks that pass (lane per point, loads of several
+//     blocks in flight) get the FP32 distance with the same margin and, only
+//     where it cannot exclude a new minimum, the exact FP64 distance
+//     (exact_dist's order); the blocks' maxima stay in the lanes' registers
+//     and reduce to the superblock's, whose maximising point's coordinates go
+//     to shared memory for step A.
+// The stored minima are bit-identical to the other forms', so the three
+// forms select the same points with the same lambdas.
 namespace rvgp {
 namespace {
 constexpr int kSpThreads = 512;
-constexpr int kBlk = 32;           // points per block
-constexpr int kSup = 32;           // blocks per superblock
-constexpr double kPruneMargin = 1.0 - 2e-12;
+constexpr int kBlk = 32;  // points per block
+constexpr int kSup = 32;  // blocks per superblock
 
-struct Max3 {
-  double v;
+// (value bits, original index, position): value >= 0, so its bits order like it
+struct Key {
+  unsigned long long v;
   int orig, pos;
 };
-
-__device__ __forceinline__ Max3 warp_max3(Max3 a) {
+__device__ __forceinline__ bool kbetter(const Key& a, const Key& b) {
+  return a.v > b.v || (a.v == b.v && a.orig < b.orig);
+}
+__device__ __forceinline__ Key kpad() { return Key{0ull, INT_MAX, 0}; }
+__device__ __forceinline__ Key kof(double v, int orig, int pos) {
+  return Key{(unsigned long long)__double_as_longlong(v), orig, pos};
+}
+__device__ __forceinline__ Key warp_maxk(Key a) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    Max3 b{__shfl_xor_sync(0xffffffffu, a.v, o), __shfl_xor_sync(0xffffffffu, a.orig, o),
-           __shfl_xor_sync(0xffffffffu, a.pos, o)};
-    if (better(b.v, b.orig, a.v, a.orig)) a = b;
+    Key b{__shfl_xor_sync(0xffffffffu, a.v, o), __shfl_xor_sync(0xffffffffu, a.orig, o),
+          __shfl_xor_sync(0xffffffffu, a.pos, o)};
+    if (kbetter(b, a)) a = b;
   }
   return a;
 }
 
-// squared distance from p to the box [lo, hi] (0 inside)
-__device__ __forceinline__ double box_dist2(const double* p, const double* lo, const double* hi, int D) {
-  double s = 0.0;
+// FP32 distance from p to the box [lo, hi] and its certified error bound
+template <int D>
+__device__ __forceinline__ float box_lb32(const float* p, const float* lo, const float* hi) {
+  float s = 0.f;
+#pragma unroll
   for (int j = 0; j < D; ++j) {
-    const double e = fmax(0.0, fmax(lo[j] - p[j], p[j] - hi[j]));
-    s += e * e;
+    const float e = fmaxf(0.f, fmaxf(lo[j] - p[j], p[j] - hi[j]));
+    s = fmaf(e, e, s);
   }
-  return s;
+  return sqrtf(s);
 }
 
-// Points in Morton order, ds from the start point, per-block boxes and maxima
-// (warp per block).
+// Points in Morton order (FP64 and FP32), ds from the start point, per-block
+// FP32 boxes (outward) and maxima (warp per block); the largest squared norm.
 __global__ void fps_sp_blocks(const double* __restrict__ X, const int* __restrict__ order, int n, int D, int start,
-                              double* __restrict__ Xs, double* __restrict__ ds, double* __restrict__ box,
-                              double* __restrict__ bmax, int* __restrict__ borig, int* __restrict__ bpos) {
+                              double* __restrict__ Xs, float* __restrict__ Xs32, double* __restrict__ ds,
+                              float* __restrict__ box, double* __restrict__ bmax, int* __restrict__ borig,
+                              int* __restrict__ bpos, unsigned long long* __restrict__ r2max) {
   const int warp = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
   const int nb = (n + kBlk - 1) / kBlk;
   if (warp >= nb) return;
   const int q = warp * kBlk + lane;
   const bool on = q < n;
   const int o = on ? order[q] : 0;
-  Max3 m{-DBL_MAX, INT_MAX, 0};
+  Key m = kpad();
+  double r2 = 0.0;
   if (on) {
-    for (int j = 0; j < D; ++j) Xs[(size_t)q * D + j] = X[(size_t)o * D + j];
+    for (int j = 0; j < D; ++j) {
+      const double x = X[(size_t)o * D + j];
+      Xs[(size_t)q * D + j] = x;
+      Xs32[(size_t)q * D + j] = (float)x;
+      r2 += x * x;
+    }
     const double d = exact_dist(X, D, start, o);
     ds[q] = d;
-    m = Max3{d, o, q};
+    m = kof(d, o, q);
   }
-  m = warp_max3(m);
+  m = warp_maxk(m);
+#pragma unroll
+  for (int s = 16; s > 0; s >>= 1) r2 = fmax(r2, __shfl_xor_sync(0xffffffffu, r2, s));
   for (int j = 0; j < D; ++j) {
     double lo = on ? X[(size_t)o * D + j] : DBL_MAX, hi = on ? X[(size_t)o * D + j] : -DBL_MAX;
 #pragma unroll
@@ -451,36 +479,37 @@ __global__ void fps_sp_blocks(const double* __restrict__ X, const int* __restric
       hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, s));
     }
     if (lane == 0) {
-      box[(size_t)warp * 2 * D + j] = lo;
-      box[(size_t)warp * 2 * D + D + j] = hi;
+      box[(size_t)warp * 2 * D + j] = __double2float_rd(lo);
+      box[(size_t)warp * 2 * D + D + j] = __double2float_ru(hi);
     }
   }
   if (lane == 0) {
-    bmax[warp] = m.v;
+    bmax[warp] = __longlong_as_double((long long)m.v);
     borig[warp] = m.orig;
     bpos[warp] = m.pos;
+    atomicMax(r2max, (unsigned long long)__double_as_longlong(r2));
   }
 }
 
 // Superblock boxes and maxima, and the coordinates of each superblock's
 // maximising point (warp per superblock).
-__global__ void fps_sp_super(int nb, int D, const double* __restrict__ Xs, const double* __restrict__ box,
+__global__ void fps_sp_super(int nb, int D, const double* __restrict__ Xs, const float* __restrict__ box,
                              const double* __restrict__ bmax, const int* __restrict__ borig,
-                             const int* __restrict__ bpos, double* __restrict__ sbox, double* __restrict__ smax,
+                             const int* __restrict__ bpos, float* __restrict__ sbox, double* __restrict__ smax,
                              int* __restrict__ sorig, int* __restrict__ spos, double* __restrict__ sxy) {
   const int warp = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
   const int ns = (nb + kSup - 1) / kSup;
   if (warp >= ns) return;
   const int b = warp * kSup + lane;
   const bool on = b < nb;
-  Max3 m = on ? Max3{bmax[b], borig[b], bpos[b]} : Max3{-DBL_MAX, INT_MAX, 0};
-  m = warp_max3(m);
+  Key m = on ? kof(bmax[b], borig[b], bpos[b]) : kpad();
+  m = warp_maxk(m);
   for (int j = 0; j < D; ++j) {
-    double lo = on ? box[(size_t)b * 2 * D + j] : DBL_MAX, hi = on ? box[(size_t)b * 2 * D + D + j] : -DBL_MAX;
+    float lo = on ? box[(size_t)b * 2 * D + j] : FLT_MAX, hi = on ? box[(size_t)b * 2 * D + D + j] : -FLT_MAX;
 #pragma unroll
     for (int s = 16; s > 0; s >>= 1) {
-      lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, s));
-      hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, s));
+      lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, s));
+      hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, s));
     }
     if (lane == 0) {
       sbox[(size_t)warp * 2 * D + j] = lo;
@@ -488,44 +517,37 @@ __global__ void fps_sp_super(int nb, int D, const double* __restrict__ Xs, const
     }
   }
   if (lane == 0) {
-    smax[warp] = m.v;
+    smax[warp] = __longlong_as_double((long long)m.v);
     sorig[warp] = m.orig;
     spos[warp] = m.pos;
   }
   if (lane < D) sxy[(size_t)warp * D + lane] = Xs[(size_t)m.pos * D + lane];
 }
 
-// Selections 1 .. N_max-1 in one CTA.  Shared memory: the superblock boxes,
-// maxima and the coordinates of their maximising points, the list of
-// superblocks to visit.  A warp owns a listed superblock from the block test
-// to its new maximum: it tests the 32 blocks (lane per block), updates the
-// points of the blocks that pass (lane per point, four blocks' loads in
-// flight), keeps the blocks' maxima in the lanes' registers and reduces them
-// to the superblock's.  Per selection: three CTA barriers and three
-// dependent L2 round trips (block data, points, the new maximising point).
 template <int D>
 __global__ void __launch_bounds__(kSpThreads, 1)
-    fps_sp_select(const double* __restrict__ Xs, const int* __restrict__ order, int n, int N_max,
-                  double* __restrict__ ds, const double* __restrict__ box, double* __restrict__ bmax,
-                  int* __restrict__ borig, int* __restrict__ bpos, const double* __restrict__ sbox_g,
-                  const double* __restrict__ smax_g, const int* __restrict__ sorig_g, const int* __restrict__ spos_g,
-                  const double* __restrict__ sxy_g, int* __restrict__ perm, double* __restrict__ lambdas,
-                  int* __restrict__ count, const double* __restrict__ diam, double spacing,
-                  long long* __restrict__ exact_evals) {
+    fps_sp_select(const double* __restrict__ Xs, const float* __restrict__ Xs32, const int* __restrict__ order,
+                  int n, int N_max, double* __restrict__ ds, const float* __restrict__ box,
+                  double* __restrict__ bmax, int* __restrict__ borig, int* __restrict__ bpos,
+                  const float* __restrict__ sbox_g, const double* __restrict__ smax_g,
+                  const int* __restrict__ sorig_g, const int* __restrict__ spos_g, const double* __restrict__ sxy_g,
+                  const unsigned long long* __restrict__ r2max, int* __restrict__ perm,
+                  double* __restrict__ lambdas, int* __restrict__ count, const double* __restrict__ diam,
+                  double spacing, long long* __restrict__ exact_evals) {
   constexpr int GB = D <= 4 ? 4 : 2;  // blocks whose points are loaded together
+  constexpr int NW = kSpThreads / 32;
   extern __shared__ __align__(16) unsigned char fsm[];
   const int nb = (n + kBlk - 1) / kBlk, ns = (nb + kSup - 1) / kSup;
-  double* sbox = reinterpret_cast<double*>(fsm);  // ns x 2D
-  double* sxy = sbox + (size_t)ns * 2 * D;        // ns x D
-  double* smax = sxy + (size_t)ns * D;            // ns
-  int* sorig = reinterpret_cast<int*>(smax + ns);  // ns
-  int* spos = sorig + ns;                          // ns
-  int* slist = spos + ns;                          // ns
+  double* sxy = reinterpret_cast<double*>(fsm);          // ns x D
+  double* smax = sxy + (size_t)ns * D;                    // ns
+  float* sbox = reinterpret_cast<float*>(smax + ns);      // ns x 2D
+  int* sorig = reinterpret_cast<int*>(sbox + (size_t)ns * 2 * D);  // ns
+  int* spos = sorig + ns;                                  // ns
+  int* slist = spos + ns;                                  // ns
   __shared__ double s_p[D];
-  __shared__ double s_wv[kSpThreads / 32];
-  __shared__ int s_wo[kSpThreads / 32], s_ws[kSpThreads / 32];
+  __shared__ unsigned long long s_wv[NW];
+  __shared__ int s_wo[NW], s_ws[NW];
   __shared__ int s_ns, s_stop;
-  constexpr int NW = kSpThreads / 32;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   for (int s = tid; s < ns; s += kSpThreads) {
     for (int j = 0; j < 2 * D; ++j) sbox[(size_t)s * 2 * D + j] = sbox_g[(size_t)s * 2 * D + j];
@@ -534,14 +556,21 @@ __global__ void __launch_bounds__(kSpThreads, 1)
     sorig[s] = sorig_g[s];
     spos[s] = spos_g[s];
   }
+  const double R = sqrt(__longlong_as_double((long long)*r2max));
+  const float u = 5.9604644775390625e-8f;  // 2^-24
+  const float c0 = (float)(4.0 * 5.9604644775390625e-8 * 2.0 * R * sqrt((double)D) * (1.0 + 1e-6));
+  const float c1 = (float)(4.0 * 5.9604644775390625e-8 * (D + 2) * (1.0 + 1e-6));
+  (void)u;
   long long exact = 0;
   __syncthreads();
   for (int it = 1; it < N_max; ++it) {
     // ---- A. the next point: maximum over the superblock maxima (pos = superblock)
-    Max3 m{-DBL_MAX, INT_MAX, 0};
-    for (int s = tid; s < ns; s += kSpThreads)
-      if (better(smax[s], sorig[s], m.v, m.orig)) m = Max3{smax[s], sorig[s], s};
-    m = warp_max3(m);
+    Key m = kpad();
+    for (int s = tid; s < ns; s += kSpThreads) {
+      const Key c = kof(smax[s], sorig[s], s);
+      if (kbetter(c, m)) m = c;
+    }
+    m = warp_maxk(m);
     if (lane == 0) {
       s_wv[warp] = m.v;
       s_wo[warp] = m.orig;
@@ -549,17 +578,18 @@ __global__ void __launch_bounds__(kSpThreads, 1)
     }
     __syncthreads();
     if (warp == 0) {
-      Max3 w = lane < NW ? Max3{s_wv[lane], s_wo[lane], s_ws[lane]} : Max3{-DBL_MAX, INT_MAX, 0};
-      w = warp_max3(w);  // the same in every lane
+      Key w = lane < NW ? Key{s_wv[lane], s_wo[lane], s_ws[lane]} : kpad();
+      w = warp_maxk(w);  // the same in every lane
       if (lane == 0) {
+        const double v = __longlong_as_double((long long)w.v);
         s_stop = 0;
         s_ns = 0;
-        if (diam && w.v / diam[0] < spacing) {
+        if (diam && v / diam[0] < spacing) {
           s_stop = 1;
           *count = it;
         } else {
           perm[it] = w.orig;
-          lambdas[it] = w.v;
+          lambdas[it] = v;
         }
       }
       if (lane < D) s_p[lane] = sxy[(size_t)w.pos * D + lane];
@@ -567,12 +597,16 @@ __global__ void __launch_bounds__(kSpThreads, 1)
     __syncthreads();
     if (s_stop) break;
     double p[D];
+    float p32[D];
 #pragma unroll
-    for (int j = 0; j < D; ++j) p[j] = s_p[j];
-    // ---- B. superblocks whose box comes closer to p than their maximum
+    for (int j = 0; j < D; ++j) {
+      p[j] = s_p[j];
+      p32[j] = (float)p[j];
+    }
+    // ---- B. superblocks that may hold a point whose minimum p can lower
     for (int s = tid; s < ns; s += kSpThreads) {
-      const double d2 = box_dist2(p, sbox + (size_t)s * 2 * D, sbox + (size_t)s * 2 * D + D, D);
-      if (d2 * kPruneMargin <= smax[s] * smax[s]) slist[atomicAdd(&s_ns, 1)] = s;
+      const float lb = box_lb32<D>(p32, sbox + (size_t)s * 2 * D, sbox + (size_t)s * 2 * D + D);
+      if (!((double)(lb - (c0 + c1 * lb)) > smax[s])) slist[atomicAdd(&s_ns, 1)] = s;
     }
     __syncthreads();
     // ---- C. each listed superblock by one warp
@@ -581,73 +615,82 @@ __global__ void __launch_bounds__(kSpThreads, 1)
       const int sb = slist[e];
       const int b = sb * kSup + lane;
       const bool valid = b < nb;
-      Max3 bm{-DBL_MAX, INT_MAX, 0};
+      Key bm = kpad();
       bool need = false;
       if (valid) {
-        bm = Max3{bmax[b], borig[b], bpos[b]};
-        const double d2 = box_dist2(p, box + (size_t)b * 2 * D, box + (size_t)b * 2 * D + D, D);
-        need = d2 * kPruneMargin <= bm.v * bm.v;
+        const double bv = bmax[b];
+        bm = kof(bv, borig[b], bpos[b]);
+        const float lb = box_lb32<D>(p32, box + (size_t)b * 2 * D, box + (size_t)b * 2 * D + D);
+        need = !((double)(lb - (c0 + c1 * lb)) > bv);
       }
       unsigned mask = __ballot_sync(0xffffffffu, need);
       while (mask) {  // warp-uniform
-        int bl[GB], cnt = 0;
+        int bl[GB];
 #pragma unroll
-        for (int u = 0; u < GB; ++u) {
-          bl[u] = -1;
+        for (int t = 0; t < GB; ++t) {
+          bl[t] = -1;
           if (mask) {
-            bl[u] = __ffs(mask) - 1;
+            bl[t] = __ffs(mask) - 1;
             mask &= mask - 1;
-            ++cnt;
           }
         }
-        double cur[GB], x[GB][D];
+        double cur[GB];
+        float x[GB][D];
         int q[GB], o[GB];
 #pragma unroll
-        for (int u = 0; u < GB; ++u) {
-          q[u] = bl[u] >= 0 ? (sb * kSup + bl[u]) * kBlk + lane : n;
-          if (q[u] < n) {
-            cur[u] = ds[q[u]];
-            o[u] = order[q[u]];
+        for (int t = 0; t < GB; ++t) {
+          q[t] = bl[t] >= 0 ? (sb * kSup + bl[t]) * kBlk + lane : n;
+          if (q[t] < n) {
+            cur[t] = ds[q[t]];
+            o[t] = order[q[t]];
 #pragma unroll
-            for (int j = 0; j < D; ++j) x[u][j] = Xs[(size_t)q[u] * D + j];
+            for (int j = 0; j < D; ++j) x[t][j] = Xs32[(size_t)q[t] * D + j];
           }
         }
 #pragma unroll
-        for (int u = 0; u < GB; ++u) {
-          if (bl[u] < 0) break;  // warp-uniform
-          Max3 mm{-DBL_MAX, INT_MAX, 0};
-          if (q[u] < n) {
-            double c = cur[u];
+        for (int t = 0; t < GB; ++t) {
+          if (bl[t] < 0) break;  // warp-uniform
+          Key mm = kpad();
+          if (q[t] < n) {
+            double c = cur[t];
             if (c > 0.0) {
-              double acc = 0.0;
+              float s2 = 0.f;
 #pragma unroll
               for (int j = 0; j < D; ++j) {
-                const double df = __dsub_rn(p[j], x[u][j]);
-                acc = __dadd_rn(acc, __dmul_rn(df, df));
+                const float df = p32[j] - x[t][j];
+                s2 = fmaf(df, df, s2);
               }
-              const double d = sqrt(acc);
-              ++exact;
-              if (d < c) {
-                c = d;
-                ds[q[u]] = d;
+              const float d32 = sqrtf(s2);
+              if (!((double)(d32 - (c0 + c1 * d32)) > c)) {  // cannot rule out a new minimum
+                double acc = 0.0;
+#pragma unroll
+                for (int j = 0; j < D; ++j) {
+                  const double df = __dsub_rn(p[j], Xs[(size_t)q[t] * D + j]);
+                  acc = __dadd_rn(acc, __dmul_rn(df, df));
+                }
+                const double d = sqrt(acc);
+                ++exact;
+                if (d < c) {
+                  c = d;
+                  ds[q[t]] = d;
+                }
               }
             }
-            mm = Max3{c, o[u], q[u]};
+            mm = kof(c, o[t], q[t]);
           }
-          mm = warp_max3(mm);
-          const int bb = sb * kSup + bl[u];
-          if (lane == bl[u]) bm = mm;
+          mm = warp_maxk(mm);
+          const int bb = sb * kSup + bl[t];
+          if (lane == bl[t]) bm = mm;
           if (lane == 0) {
-            bmax[bb] = mm.v;
+            bmax[bb] = __longlong_as_double((long long)mm.v);
             borig[bb] = mm.orig;
             bpos[bb] = mm.pos;
           }
         }
-        (void)cnt;
       }
-      Max3 sm = warp_max3(bm);
+      const Key sm = warp_maxk(bm);
       if (lane == 0) {
-        smax[sb] = sm.v;
+        smax[sb] = __longlong_as_double((long long)sm.v);
         sorig[sb] = sm.orig;
         spos[sb] = sm.pos;
       }
@@ -669,14 +712,50 @@ __global__ void add_ll(long long* p, long long v) { *p += v; }
 
 size_t fps_sp_smem(int n, int D) {
   const int nb = (n + kBlk - 1) / kBlk, ns = (nb + kSup - 1) / kSup;
-  return (size_t)ns * (3 * D * sizeof(double) + sizeof(double) + 3 * sizeof(int));
+  return (size_t)ns * (D * sizeof(double) + sizeof(double) + 2 * D * sizeof(float) + 3 * sizeof(int));
 }
+
+struct SpBufs {
+  int *order, *rank, *borig, *bpos, *sorig, *spos;
+  double *Xs, *ds, *bmax, *smax, *sxy;
+  float *Xs32, *box, *sbox;
+  unsigned long long* r2max;
+  void* lo_ws;
+  size_t lo_bytes;
+};
 }  // namespace
 }  // namespace rvgp
 
 extern "C" size_t rvgp_locality_order_workspace(int n, int D);
 extern "C" int rvgp_locality_order(const double* X, int n, int D, int* perm, int* rank, void* workspace,
                                    size_t ws_bytes, void* stream);
+
+namespace {
+// one carve for the size query and the call
+rvgp::SpBufs carve_sp(Workspace& ws, int n, int D) {
+  using namespace rvgp;
+  const int nb = (n + kBlk - 1) / kBlk, ns = (nb + kSup - 1) / kSup;
+  SpBufs b;
+  b.order = ws.take<int>(n);
+  b.rank = ws.take<int>(n);
+  b.Xs = ws.take<double>((size_t)n * D);
+  b.Xs32 = ws.take<float>((size_t)n * D);
+  b.ds = ws.take<double>(n);
+  b.box = ws.take<float>((size_t)nb * 2 * D);
+  b.bmax = ws.take<double>(nb);
+  b.borig = ws.take<int>(nb);
+  b.bpos = ws.take<int>(nb);
+  b.sbox = ws.take<float>((size_t)ns * 2 * D);
+  b.sxy = ws.take<double>((size_t)ns * D);
+  b.smax = ws.take<double>(ns);
+  b.sorig = ws.take<int>(ns);
+  b.spos = ws.take<int>(ns);
+  b.r2max = ws.take<unsigned long long>(1);
+  b.lo_bytes = rvgp_locality_order_workspace(n, D);
+  b.lo_ws = ws.take<char>(b.lo_bytes);
+  return b;
+}
+}  // namespace
 
 // Largest n the spatial form takes for dimension D (its superblock table
 // must fit one SM's shared memory), 0 when D is outside 1..8.
@@ -686,40 +765,10 @@ RVGP_API int rvgp_fps_spatial_max_n(int D) {
   if (cudaGetDevice(&dev) != cudaSuccess ||
       cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
     return 0;
-  const size_t per = 3 * D * sizeof(double) + sizeof(double) + 3 * sizeof(int);
+  const size_t per = D * sizeof(double) + sizeof(double) + 2 * D * sizeof(float) + 3 * sizeof(int);
   const long long ns = ((long long)optin - 2048) / (long long)per;
-  return (int)std::min<long long>(INT_MAX / 2, ns * kBlk * kSup);
+  return (int)std::min<long long>(INT_MAX / 2, ns * rvgp::kBlk * rvgp::kSup);
 }
-
-namespace {
-struct SpBufs {
-  int *order, *rank, *borig, *bpos, *sorig, *spos;
-  double *Xs, *ds, *box, *bmax, *sbox, *sxy, *smax;
-  void* lo_ws;
-  size_t lo_bytes;
-};
-// one carve for the size query and the call
-SpBufs carve_sp(Workspace& ws, int n, int D) {
-  const int nb = (n + kBlk - 1) / kBlk, ns = (nb + kSup - 1) / kSup;
-  SpBufs b;
-  b.order = ws.take<int>(n);
-  b.rank = ws.take<int>(n);
-  b.Xs = ws.take<double>((size_t)n * D);
-  b.ds = ws.take<double>(n);
-  b.box = ws.take<double>((size_t)nb * 2 * D);
-  b.bmax = ws.take<double>(nb);
-  b.borig = ws.take<int>(nb);
-  b.bpos = ws.take<int>(nb);
-  b.sbox = ws.take<double>((size_t)ns * 2 * D);
-  b.sxy = ws.take<double>((size_t)ns * D);
-  b.smax = ws.take<double>(ns);
-  b.sorig = ws.take<int>(ns);
-  b.spos = ws.take<int>(ns);
-  b.lo_bytes = rvgp_locality_order_workspace(n, D);
-  b.lo_ws = ws.take<char>(b.lo_bytes);
-  return b;
-}
-}  // namespace
 
 RVGP_API size_t rvgp_fps_spatial_workspace(int n, int D) {
   if (n < 1 || D < 1 || D > 8) return 0;
@@ -738,37 +787,35 @@ RVGP_API int rvgp_fps_spatial(const double* X, int n, int D, int N_max, int star
   RVGP_CHECK_ARG(n <= rvgp_fps_spatial_max_n(D), "rvgp_fps_spatial: n=%d above the limit %d for D=%d", n,
                  rvgp_fps_spatial_max_n(D), D);
   RVGP_CHECK_ARG(workspace && ws_bytes >= rvgp_fps_spatial_workspace(n, D), "rvgp_fps_spatial: workspace");
+  using namespace rvgp;
   cudaStream_t st = as_stream(stream);
   const int nb = (n + kBlk - 1) / kBlk, ns = (nb + kSup - 1) / kSup;
   Workspace ws(workspace, ws_bytes);
   const SpBufs B = carve_sp(ws, n, D);
-  int *order = B.order, *rank = B.rank, *borig = B.borig, *bpos = B.bpos, *sorig = B.sorig, *spos = B.spos;
-  double *Xs = B.Xs, *ds = B.ds, *box = B.box, *bmax = B.bmax, *sbox = B.sbox, *sxy = B.sxy, *smax = B.smax;
-  void* lo_ws = B.lo_ws;
-  const size_t lo_bytes = B.lo_bytes;
-  TRY_RC(rvgp_locality_order(X, n, D, order, rank, lo_ws, lo_bytes, stream));
+  TRY_RC(rvgp_locality_order(X, n, D, B.order, B.rank, B.lo_ws, B.lo_bytes, stream));
   cudaMemsetAsync(count, 0xFF, sizeof(int), st);  // -1: all N_max taken unless the spacing stop fires
+  cudaMemsetAsync(B.r2max, 0, sizeof(unsigned long long), st);
   if (exact_evals) cudaMemsetAsync(exact_evals, 0, sizeof(long long), st);
   rvgp::note_launch();
-  fps_sp_blocks<<<ceil_div((long long)nb * 32, 256), 256, 0, st>>>(X, order, n, D, start, Xs, ds, box, bmax, borig,
-                                                                    bpos);
+  fps_sp_blocks<<<ceil_div((long long)nb * 32, 256), 256, 0, st>>>(X, B.order, n, D, start, B.Xs, B.Xs32, B.ds,
+                                                                    B.box, B.bmax, B.borig, B.bpos, B.r2max);
   rvgp::note_launch();
-  fps_sp_super<<<ceil_div((long long)ns * 32, 256), 256, 0, st>>>(nb, D, Xs, box, bmax, borig, bpos, sbox, smax,
-                                                                   sorig, spos, sxy);
+  fps_sp_super<<<ceil_div((long long)ns * 32, 256), 256, 0, st>>>(nb, D, B.Xs, B.box, B.bmax, B.borig, B.bpos,
+                                                                   B.sbox, B.smax, B.sorig, B.spos, B.sxy);
   rvgp::note_launch();
   write_first<<<1, 32, 0, st>>>(perm, lambdas, start);
   if (N_max > 1) {
     const size_t smem = fps_sp_smem(n, D);
-#define RVGP_FPS_SP(Dv)                                                                                          \
-  case Dv: {                                                                                                     \
-    if (cudaFuncSetAttribute(fps_sp_select<Dv>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=      \
-        cudaSuccess)                                                                                             \
-      return check_launch("rvgp_fps_spatial");                                                                   \
-    rvgp::note_launch();                                                                                         \
-    fps_sp_select<Dv><<<1, kSpThreads, smem, st>>>(Xs, order, n, N_max, ds, box, bmax, borig, bpos, sbox, smax,  \
-                                                   sorig, spos, sxy, perm, lambdas, count, diam, spacing,        \
-                                                   exact_evals);                                                  \
-    break;                                                                                                       \
+#define RVGP_FPS_SP(Dv)                                                                                        \
+  case Dv: {                                                                                                   \
+    if (cudaFuncSetAttribute(fps_sp_select<Dv>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=    \
+        cudaSuccess)                                                                                           \
+      return check_launch("rvgp_fps_spatial");                                                                 \
+    rvgp::note_launch();                                                                                       \
+    fps_sp_select<Dv><<<1, kSpThreads, smem, st>>>(B.Xs, B.Xs32, B.order, n, N_max, B.ds, B.box, B.bmax,       \
+                                                   B.borig, B.bpos, B.sbox, B.smax, B.sorig, B.spos, B.sxy,    \
+                                                   B.r2max, perm, lambdas, count, diam, spacing, exact_evals); \
+    break;                                                                                                     \
   }
     switch (D) {
       RVGP_FPS_SP(1)
