@@ -263,13 +263,13 @@ __global__ void resid_final(const double* __restrict__ part, int nchunk, int b, 
 
 template <typename T>
 __global__ void write_output(const T* __restrict__ V, int ldv, long long N, int m, double scale, double* __restrict__ out,
-                             int ldo, const int* __restrict__ perm, int DB) {
+                             int ldo, const int* __restrict__ perm, int DB, const int* __restrict__ colmap) {
   const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (e >= N * m) return;
   const long long r = e / m;
   const int j = (int)(e % m);
   const long long ro = perm ? (long long)perm[r / DB] * DB + r % DB : r;
-  out[ro * ldo + j] = scale * (double)V[r * ldv + j];
+  out[ro * ldo + j] = scale * (double)V[r * ldv + colmap[j]];
 }
 
 int resid_chunks(long long N) { return (int)std::max<long long>(1, std::min<long long>(512, (N + 1023) / 1024)); }
@@ -284,6 +284,7 @@ struct Small {
   double *G, *H, *Q, *Linv, *theta, *res, *norms64;
   double *gersh, *resid_part;
   int* info;
+  int* colmap;  // output column -> block column (Ritz values sorted)
   void* gram_ws;
   size_t gram_bytes;
   void* jac_ws;
@@ -667,6 +668,7 @@ Layout carve(Workspace& ws, long long N, int p, int mode) {
   s.gersh = ws.take<double>(num_sms() * 2);
   s.resid_part = ws.take<double>((size_t)resid_chunks(N) * 2 * p);  // [vᵀw | vᵀv] partials, then the residual's
   s.info = ws.take<int>(4);
+  s.colmap = ws.take<int>(p);
   s.Bf = ws.take<float>(pp);
   s.Bd = ws.take<double>(pp);
   s.nf = ws.take<float>(p);
@@ -790,8 +792,18 @@ static int eigsh_impl(const int* indptr, const int* indices, const double* vals6
     TRY(iterate<double>(P, L.d, s, stt, bup, tol, max_iter, first_deg, 1e10, theta, res, false, &nconv, st));
   }
   stt.conv = nconv;
-  cudaMemcpyAsync(evals, s.theta, sizeof(double) * m, cudaMemcpyDeviceToDevice, st);
-  rvgp::note_launch(); write_output<double><<<ceil_div(N * m, 256), 256, 0, st>>>(L.d.V, p, N, m, scale, evecs, ld_evecs, perm, DB);
+  // the m lowest Ritz values ascending (Rayleigh quotients can swap nearly
+  // equal neighbours), ties by block column; their vectors by a column map
+  std::vector<int> order(p);
+  for (int j = 0; j < p; ++j) order[j] = j;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return theta[a] < theta[b]; });
+  std::vector<double> ev(m);
+  for (int j = 0; j < m; ++j) ev[j] = theta[order[j]];
+  cudaMemcpyAsync(evals, ev.data(), sizeof(double) * m, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(s.colmap, order.data(), sizeof(int) * m, cudaMemcpyHostToDevice, st);
+  rvgp::note_launch(); write_output<double><<<ceil_div(N * m, 256), 256, 0, st>>>(L.d.V, p, N, m, scale, evecs, ld_evecs, perm, DB, s.colmap);
+  // the host vectors must outlive the copies from pageable memory
+  if (cudaStreamSynchronize(st) != cudaSuccess) return check_launch("rvgp_eigsh");
   if (stats) {
     stats[0] = stt.iters;
     stats[1] = stt.spmm;
