@@ -136,8 +136,10 @@ int rvgp_symeig_f32(const float* H, int p, float* w, float* V, int max_sweeps, d
  * SpMMs, Jacobi sweeps, converged, refinement iterations, Cholesky rescues,
  * 1 when the FP32 Grams and block products ran on the tensor cores (mode 1,
  * p <= 256; RVGP_TENSOR_CORES=0 in the environment selects the CUDA-core
- * kernels), -, then microseconds spent in filter / orthonormalisation /
- * Rayleigh-Ritz tall products / Jacobi).  When tol >= tol32 (mode 1) no FP64 iteration runs.
+ * kernels), 1 when the shared-memory tiled SpMM ran, then microseconds spent
+ * in filter / orthonormalisation / Rayleigh-Ritz tall products / Jacobi,
+ * then the number of vectors the FP32 stage locked).  When tol >= tol32
+ * (mode 1) no FP64 iteration runs.
  * Returns 0, or the number of unconverged pairs.  Synchronises the stream. */
 size_t rvgp_eigsh_workspace(int n, int DB, int m, int p, int mode);
 int rvgp_eigsh(const int* indptr, const int* indices, const double* vals64, const float* vals32, int n, int DB, int m,

@@ -304,7 +304,7 @@ def block_size(m, N):
     return min(p, N - N % 4)
 
 
-def eigsh(indptr, indices, vals64, vals32=None, m=10, mode="mixed", tol=None, tol32=2e-5, max_iter=60, seed=0,
+def eigsh(indptr, indices, vals64, vals32=None, m=10, mode="mixed", tol=None, tol32=1e-5, max_iter=60, seed=0,
           scale=None, p=None, perm=None):
     """m smallest eigenpairs of the block-CSR matrix: (evals (m,), evecs (N, m), stats dict).
 
@@ -342,7 +342,7 @@ def eigsh(indptr, indices, vals64, vals32=None, m=10, mode="mixed", tol=None, to
                                   tol32, max_iter, seed, ptr(perm), ptr(evals), ptr(evecs), m, sc, stats, ptr(ws),
                                   ws.numel(), stream())
     info = dict(iters=stats[0], spmm=stats[1], sweeps=stats[2], converged=stats[3], refine_iters=stats[4],
-                chol_rescues=stats[5], tensor_cores=bool(stats[6]), tiled_spmm=bool(stats[7]), p=p, filter_ms=stats[8] / 1e3, orth_ms=stats[9] / 1e3,
+                chol_rescues=stats[5], tensor_cores=bool(stats[6]), tiled_spmm=bool(stats[7]), locked=stats[12], p=p, filter_ms=stats[8] / 1e3, orth_ms=stats[9] / 1e3,
                 rr_ms=stats[10] / 1e3, jacobi_ms=stats[11] / 1e3)
     if st < 0:
         check(st, "rvgp_eigsh")

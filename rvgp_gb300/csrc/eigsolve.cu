@@ -272,6 +272,32 @@ __global__ void write_output(const T* __restrict__ V, int ldv, long long N, int 
   out[ro * ldo + j] = scale * (double)V[r * ldv + colmap[j]];
 }
 
+// dst[r, d0 + j] = src[r, c0 + j], j < ncols (all column offsets and leading
+// dimensions multiples of 4: float4 moves)
+__global__ void copy_cols4(const float* __restrict__ src, int lds, int c0, float* __restrict__ dst, int ldd, int d0,
+                           long long N, int ncols) {
+  const int g = ncols / 4;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < N * g;
+       e += (long long)gridDim.x * blockDim.x) {
+    const long long r = e / g;
+    const int j = 4 * (int)(e % g);
+    *reinterpret_cast<float4*>(dst + r * ldd + d0 + j) = *reinterpret_cast<const float4*>(src + r * lds + c0 + j);
+  }
+}
+
+__global__ void sub_f32x4(float* __restrict__ X, const float* __restrict__ Y, long long n4) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n4;
+       e += (long long)gridDim.x * blockDim.x) {
+    float4 a = reinterpret_cast<float4*>(X)[e];
+    const float4 b = reinterpret_cast<const float4*>(Y)[e];
+    a.x -= b.x;
+    a.y -= b.y;
+    a.z -= b.z;
+    a.w -= b.w;
+    reinterpret_cast<float4*>(X)[e] = a;
+  }
+}
+
 int resid_chunks(long long N) { return (int)std::max<long long>(1, std::min<long long>(512, (N + 1023) / 1024)); }
 
 // ------------------------------------------------------------------------------ solver state
@@ -367,7 +393,7 @@ constexpr float kFirstOrderTol = 1e-3f;  // FP32 Jacobi sweeps are capped: off(H
   } while (0)
 
 struct Stats {
-  int iters = 0, spmm = 0, sweeps = 0, conv = 0, refine_iters = 0, chol_rescues = 0;
+  int iters = 0, spmm = 0, sweeps = 0, conv = 0, refine_iters = 0, chol_rescues = 0, locked = 0;
   float ms[4] = {0, 0, 0, 0};  // filter, orthonormalise, Rayleigh-Ritz tall products, Jacobi
 };
 
@@ -637,6 +663,140 @@ int iterate(const Problem& P, Block<T>& B, Small& s, Stats& stt, double bup, dou
   return RVGP_OK;
 }
 
+// The one-SM kernels of the FP32 stage by block width (the active width
+// shrinks as eigenpairs are locked): Cholesky QR and Jacobi in one CTA when
+// the width fits, block Jacobi above (RVGP_JACOBI_BLOCK=0: the scalar kernel).
+void set_width_flags(Small& s, int w, int mode) {
+  s.cholqr32 = (mode == 1 && w <= cholqr32_max_p()) ? 1 : 0;
+  s.jac32 = (mode == 1 && w % 2 == 0 && w <= jacobi32_max_p()) ? 1 : 0;
+  const char* e = getenv("RVGP_JACOBI_BLOCK");
+  s.jacb = (mode == 1 && !s.jac32 && w >= 128 && jacobi_block_workspace(w) <= s.jac_bytes && !(e && e[0] == '0'))
+               ? 1
+               : 0;
+}
+
+// Va (N x pa) -= Vl (Vlᵀ Va), Vl the nl locked columns (ld ldl): one
+// classical Gram-Schmidt pass against the locked vectors (tensor cores when
+// the block products use them).  Tmp: N x pa scratch.
+int project_out(const float* Vl, int ldl, int nl, float* Va, int pa, long long N, float* Tmp, Small& s,
+                cudaStream_t st) {
+  if (s.tc)
+    TRY(tc_gram_f32_out64(Vl, ldl, Va, pa, N, nl, pa, s.G, pa, s.tc_err, s.tc_ws, s.tc_bytes, st));
+  else
+    TRY(gram_f32_out64(Vl, ldl, Va, pa, N, nl, pa, s.G, pa, 1.0, 0.0, s.gram_ws, s.gram_bytes, st));
+  TRY(convert_f64_to_f32(s.G, pa, s.Bf, pa, nl, pa, st));
+  if (s.tc) {
+    TRY(tc_gemm_f32(Vl, ldl, N, nl, s.Bf, pa, pa, Tmp, pa, s.tc_err, s.tc_ws, s.tc_bytes, st));
+    const long long n4 = N * pa / 4;
+    rvgp::note_launch();
+    sub_f32x4<<<(unsigned)std::min<long long>(8LL * num_sms(), ceil_div(n4, 256)), 256, 0, st>>>(Va, Tmp, n4);
+    return check_launch("project_out");
+  }
+  return gemm_nn<float>(Vl, ldl, s.Bf, pa, N, nl, pa, Va, pa, -1.f, 1.f, st);
+}
+
+int copy_cols(const float* src, int lds, int c0, float* dst, int ldd, int d0, long long N, int ncols,
+              cudaStream_t st) {
+  if (ncols <= 0) return RVGP_OK;
+  const long long g = N * (ncols / 4);
+  rvgp::note_launch();
+  copy_cols4<<<(unsigned)std::min<long long>(8LL * num_sms(), ceil_div(g, 256)), 256, 0, st>>>(src, lds, c0, dst, ldd,
+                                                                                               d0, N, ncols);
+  return check_launch("copy_cols");
+}
+
+// The FP32 stage with locking.  After each Rayleigh-Ritz step the leading
+// active Ritz vectors whose residual passes (in multiples of 4, never beyond
+// m) move to Vl and leave the iteration: the filter, the orthonormalisation,
+// the Rayleigh-Ritz products and the Jacobi then run on the p - nl active
+// columns, kept compact (ld = p - nl) so every kernel sees a plain block.
+// After each filter the active block is projected against Vl twice
+// (classical Gram-Schmidt twice: the filter amplifies the residual
+// components along the locked directions most) before its Cholesky QR.  The
+// filter degree still bounds the gain of the lowest Ritz value overall
+// (locked or not), as without locking.  On return B.V is the N x p block
+// [locked | active] (ld p), theta / res the matching values.
+int iterate_locked(const Problem& P, Block<float>& B, float* Vl, int ldl, Small& s, Stats& stt, double bup,
+                   double tol, int max_iter, int first_deg, double range, std::vector<double>& theta,
+                   std::vector<double>& res, int* nconv_out, cudaStream_t st) {
+  const int m = P.m, p = P.p;
+  const long long N = P.N;
+  const char* le = getenv("RVGP_EIG_LOCK");
+  const bool lock_on = !(le && le[0] == '0');
+  int nl = 0;
+  std::vector<double> th_l, res_l;
+  Problem A = P;
+  int nconv = 0;
+  double a = bup * std::min(0.5, std::max(4.0 * p / (double)N, 0.01)), a0 = -1e-3 * bup;
+  int deg = first_deg;
+  PhaseEvents ev;
+  constexpr int kPartialSweeps = 1, kFullSweeps = 60;
+  for (int it = 0; it < max_iter; ++it) {
+    const int pa = p - nl, ma = m - nl;
+    A.p = pa;
+    A.m = ma;
+    set_width_flags(s, pa, 1);
+    if (a >= bup * 0.999) a = bup * 0.5;
+    cudaEventRecord(ev.e[0], st);
+    TRY(filter<float>(A, B, deg, a, bup, a0, stt, st));
+    cudaEventRecord(ev.e[1], st);
+    for (int pass = 0; pass < 2 && nl > 0; ++pass) TRY(project_out(Vl, ldl, nl, B.V, pa, N, B.T1, s, st));
+    TRY(orthonormalise<float>(A, B, s, stt, st));
+    cudaEventRecord(ev.e[2], st);
+    TRY(rayleigh_ritz<float>(A, B, s, stt, kPartialSweeps, theta, res, ev, st));
+    ++stt.iters;
+    nconv = 0;
+    for (int j = 0; j < ma; ++j)
+      if (res[j] <= tol * bup) ++nconv;
+    if (nconv == ma) {
+      for (int q = 0; q < 3; ++q) cudaEventRecord(ev.e[q], st);  // no filter / orthonormalisation time here
+      TRY(rayleigh_ritz<float>(A, B, s, stt, kFullSweeps, theta, res, ev, st));
+      nconv = 0;
+      for (int j = 0; j < ma; ++j)
+        if (res[j] <= tol * bup) ++nconv;
+      if (nconv == ma) break;
+    }
+    if (lock_on) {
+      int k = 0;
+      while (k < ma && res[k] <= tol * bup) ++k;
+      k = k / 4 * 4;
+      if (k >= 8) {
+        TRY(copy_cols(B.V, pa, 0, Vl, ldl, nl, N, k, st));
+        TRY(copy_cols(B.V, pa, k, B.T1, pa - k, 0, N, pa - k, st));
+        std::swap(B.V, B.T1);
+        th_l.insert(th_l.end(), theta.begin(), theta.begin() + k);
+        res_l.insert(res_l.end(), res.begin(), res.begin() + k);
+        theta.erase(theta.begin(), theta.begin() + k);
+        res.erase(res.begin(), res.begin() + k);
+        nl += k;
+        stt.locked = nl;
+      }
+    }
+    const int pn = p - nl;
+    const double lowest = nl > 0 ? std::min(th_l.front(), theta[0]) : theta[0];
+    a = theta[pn - 1];
+    a0 = std::min(lowest, 0.0) - 1e-3 * bup;
+    std::vector<double> thd(theta);
+    thd[0] = std::min(thd[0], lowest);
+    deg = choose_degree(thd, m - nl, a, bup, range, 60, kAmp32);
+  }
+  if (nl > 0) {
+    TRY(copy_cols(Vl, ldl, 0, B.T1, p, 0, N, nl, st));
+    TRY(copy_cols(B.V, p - nl, 0, B.T1, p, nl, N, p - nl, st));
+    std::swap(B.V, B.T1);
+    th_l.insert(th_l.end(), theta.begin(), theta.end());
+    res_l.insert(res_l.end(), res.begin(), res.end());
+    theta.swap(th_l);
+    res.swap(res_l);
+  }
+  set_width_flags(s, p, 1);
+  nconv = 0;
+  for (int j = 0; j < m; ++j)
+    if (res[j] <= tol * bup) ++nconv;
+  *nconv_out = nconv;
+  return RVGP_OK;
+}
+
 struct Layout {
   Block<float> f;
   Block<double> d;
@@ -712,7 +872,7 @@ RVGP_API size_t rvgp_eigsh_workspace(int n, int DB, int m, int p, int mode) {
 // mode 1.  p: block size (m < p <= N, p % 4 == 0).  mode: 0 plain FP64, 1 mixed.
 // tol: FP64 residual tolerance relative to the Gershgorin bound; tol32 the
 // FP32 stage's.  evals: m doubles ascending; evecs: N x m (ld_evecs) times
-// `scale`.  stats (host, 8 ints, may be null): iterations, SpMM count, Jacobi
+// `scale`.  stats (host, 16 ints, may be null): iterations, SpMM count, Jacobi
 // sweeps, converged, FP64 refinement iterations, Cholesky rescues.
 // Returns 0, or the number of unconverged eigenpairs (> 0).  Synchronises.
 static int eigsh_impl(const int* indptr, const int* indices, const double* vals64, const float* vals32, int n,
@@ -731,15 +891,7 @@ static int eigsh_impl(const int* indptr, const int* indices, const double* vals6
   Workspace ws(workspace, ws_bytes);
   Layout L = carve(ws, N, p, mode);
   Small& s = L.s;
-  s.cholqr32 = (mode == 1 && p <= cholqr32_max_p()) ? 1 : 0;
-  s.jac32 = (mode == 1 && p % 2 == 0 && p <= jacobi32_max_p()) ? 1 : 0;
-  {
-    // block Jacobi above the one-CTA size (RVGP_JACOBI_BLOCK=0: the scalar kernel)
-    const char* e = getenv("RVGP_JACOBI_BLOCK");
-    s.jacb = (mode == 1 && !s.jac32 && p >= 128 && jacobi_block_workspace(p) <= s.jac_bytes && !(e && e[0] == '0'))
-                 ? 1
-                 : 0;
-  }
+  set_width_flags(s, p, mode);
   s.tc = (mode == 1 && s.tc_bytes > 0 && tc_enabled() && tc_supported(p, p)) ? 1 : 0;
   cudaMemsetAsync(s.tc_err, 0, sizeof(int), st);
   Problem P{n, DB, N, indptr, indices, vals64, vals32, m, p, SpmmPlan{}};
@@ -776,13 +928,17 @@ static int eigsh_impl(const int* indptr, const int* indices, const double* vals6
   const int first_deg = 12;
   if (mode == 1) {
     rvgp::note_launch(); random_block<float><<<ceil_div(N * p, 256), 256, 0, st>>>(L.f.V, N, p, p, seed, perm, DB);
-    TRY(iterate<float>(P, L.f, s, stt, bup, tol32, max_iter, first_deg, 1e4, theta, res, false, &nconv, st));
+    // locked vectors live in the FP64 scratch block, unused until the refinement
+    const int ldl = (m + 3) / 4 * 4;
+    TRY(iterate_locked(P, L.f, reinterpret_cast<float*>(L.d.T2), ldl, s, stt, bup, tol32, max_iter, first_deg, 1e4,
+                       theta, res, &nconv, st));
     // FP64 refinement from the FP32 subspace
     TRY(convert_f32_to_f64(L.f.V, p, L.d.V, p, N, p, st));
     nconv = 0;
     for (int j = 0; j < m; ++j)
       if (res[j] <= tol * bup) ++nconv;
     if (nconv < m) {
+      std::sort(theta.begin(), theta.end());  // locked and active values: the degree rule wants them ordered
       const int before = stt.iters;
       TRY(iterate<double>(P, L.d, s, stt, bup, tol, max_iter, 4, 1e10, theta, res, true, &nconv, st));
       stt.refine_iters = stt.iters - before;
@@ -813,6 +969,7 @@ static int eigsh_impl(const int* indptr, const int* indices, const double* vals6
     stats[5] = stt.chol_rescues;
     stats[6] = s.tc;
     stats[7] = P.plan.plan != nullptr;
+    stats[12] = stt.locked;
     for (int q = 0; q < 4; ++q) stats[8 + q] = (int)(stt.ms[q] * 1000.f);  // microseconds per phase
   }
   RVGP_LAUNCH_CHECK("rvgp_eigsh");

@@ -87,3 +87,42 @@ def test_eigsh_rejects_too_many(core):
     ix = cu(np.arange(10), torch.int32)
     with pytest.raises(ValueError):
         core.eigsh(ip, ix, cu(np.ones(10)), m=9)
+
+
+def test_eigsh_locking(core):
+    """The FP32 stage locks converged Ritz vectors (the filter, the
+    orthonormalisation and the Rayleigh-Ritz step then run on the active
+    columns only): the eigenpairs agree with scipy's and with the solve
+    without locking (RVGP_EIG_LOCK=0) to the mixed form's accuracy, and at
+    this size some vectors are locked."""
+    import os
+    from rvgp_gb300.workloads import make_points
+    n, k, m = 8000, 10, 160
+    X = make_points("sphere", n, seed=2)
+    nn = O.knn(X, k)
+    ip, ix = O.symmetrised_csr(nn, n)
+    L = O.laplacian(ip, ix, n)
+    ev_ref, V_ref = O.spectrum_shift_invert(L, m)
+    args = (cu(ip, torch.int32), cu(ix, torch.int32), cu(L.data))
+    ev, V, info = core.eigsh(*args, m=m, mode="mixed", scale=1.0)
+    old = os.environ.get("RVGP_EIG_LOCK")
+    os.environ["RVGP_EIG_LOCK"] = "0"
+    try:
+        ev0, V0, info0 = core.eigsh(*args, m=m, mode="mixed", scale=1.0)
+    finally:
+        if old is None:
+            del os.environ["RVGP_EIG_LOCK"]
+        else:
+            os.environ["RVGP_EIG_LOCK"] = old
+    assert info["locked"] > 0 and info0["locked"] == 0
+    assert info["converged"] == m and info0["converged"] == m
+    top = ev_ref.max()
+    for e, Vv in ((ev, V), (ev0, V0)):
+        e = e.cpu().numpy()
+        assert np.all(np.diff(e) >= 0)
+        assert np.abs(e - ev_ref).max() <= 1e-5 * top
+        Vv = Vv.cpu().numpy()
+        assert np.abs(Vv.T @ Vv - np.eye(m)).max() <= 1e-4
+        for sl in cluster_slices(ev_ref, rtol=1e-4):
+            if sl.stop < m and sl.stop - sl.start < 8:
+                assert subspace_sin(Vv[:, sl], V_ref[:, sl]) < 3e-2
