@@ -117,12 +117,17 @@ def test_eigsh_locking(core):
     assert info["locked"] > 0 and info0["locked"] == 0
     assert info["converged"] == m and info0["converged"] == m
     top = ev_ref.max()
+    bup = float(abs(L).sum(axis=1).max())  # the Gershgorin bound the tolerance refers to
+    # the invariant subspace below the widest spectral gap in the upper half
+    # (well determined: its angle is at most ~ residual / gap)
+    gaps = np.diff(ev_ref[m // 2 - 1:m])
+    cut = m // 2 + int(np.argmax(gaps))
     for e, Vv in ((ev, V), (ev0, V0)):
         e = e.cpu().numpy()
         assert np.all(np.diff(e) >= 0)
         assert np.abs(e - ev_ref).max() <= 1e-5 * top
         Vv = Vv.cpu().numpy()
         assert np.abs(Vv.T @ Vv - np.eye(m)).max() <= 1e-4
-        for sl in cluster_slices(ev_ref, rtol=1e-4):
-            if sl.stop < m and sl.stop - sl.start < 8:
-                assert subspace_sin(Vv[:, sl], V_ref[:, sl]) < 3e-2
+        resid = np.linalg.norm(L @ Vv - Vv * e, axis=0)
+        assert resid.max() <= 5e-5 * bup  # the FP32 stage stops at 1e-5 of the bound
+        assert subspace_sin(Vv[:, :cut], V_ref[:, :cut]) < 1e-2
