@@ -844,6 +844,9 @@ Layout carve(Workspace& ws, long long N, int p, int mode) {
   s.jac32_bytes = jacobi32_workspace(p, kFp32Sweeps);
   s.jac32_ws = ws.take<char>(s.jac32_bytes);
   s.gram_bytes = std::max(gram_workspace<float>(N, p, p), gram_workspace<double>(N, p, p));
+  // the locking projection's Grams are nl x (p - nl): their split counts grow
+  // as nl shrinks, so size for every width the iteration can reach
+  for (int w = 4; w < p; w += 4) s.gram_bytes = std::max(s.gram_bytes, gram_workspace<float>(N, w, p - w));
   s.gram_ws = ws.take<char>(s.gram_bytes);
   s.jac_bytes = jacobi_workspace<double>(p);
   s.jac_ws = ws.take<char>(s.jac_bytes);
@@ -852,6 +855,9 @@ Layout carve(Workspace& ws, long long N, int p, int mode) {
   s.tc = 0;
   s.tc_err = ws.take<int>(1);
   s.tc_bytes = mode == 1 ? std::max(tc_gram_workspace(N, p, p), tc_gemm_workspace(p, p)) : 0;
+  if (mode == 1)
+    for (int w = 4; w < p; w += 4)
+      s.tc_bytes = std::max(s.tc_bytes, std::max(tc_gram_workspace(N, w, p - w), tc_gemm_workspace(w, p - w)));
   s.tc_ws = ws.take<char>(s.tc_bytes);
   return L;
 }

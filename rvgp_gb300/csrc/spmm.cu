@@ -43,6 +43,24 @@ __device__ __forceinline__ void vload(const T* p, T* out) {
   for (int q = 0; q < Vec<T>::V; ++q) out[q] = s[q];
 }
 
+// the same load cached in L2 only (no L1 allocation)
+template <typename T>
+__device__ __forceinline__ void vload_cg(const T* p, T* out) {
+  using VT = typename Vec<T>::type;
+  VT v = __ldcg(reinterpret_cast<const VT*>(p));
+  const T* s = reinterpret_cast<const T*>(&v);
+#pragma unroll
+  for (int q = 0; q < Vec<T>::V; ++q) out[q] = s[q];
+}
+
+template <typename T, bool CG>
+__device__ __forceinline__ void vgather(const T* p, T* out) {
+  if constexpr (CG)
+    vload_cg(p, out);
+  else
+    vload(p, out);
+}
+
 template <typename T>
 __device__ __forceinline__ void vstore(T* p, const T* in) {
   using VT = typename Vec<T>::type;
@@ -149,7 +167,7 @@ __global__ void __launch_bounds__(256) bspmm_kernel(int n, const int* __restrict
 // issued first, then the products in the row kernel's order (neighbour by
 // neighbour, block column by block column), so every variant gives the same
 // bits.
-template <typename T, int DB, int U>
+template <typename T, int DB, int U, bool CG = false>
 __global__ void __launch_bounds__(256) bspmm_chunked_kernel(int n, int nch, const int* __restrict__ indptr,
                                                             const int* __restrict__ indices,
                                                             const T* __restrict__ vals, const T* __restrict__ X,
@@ -179,7 +197,7 @@ __global__ void __launch_bounds__(256) bspmm_chunked_kernel(int n, int nch, cons
       load_block<T, DB>(vals, t + u, blk[u]);
       if (on)
 #pragma unroll
-        for (int q = 0; q < DB; ++q) vload(X + ((size_t)j * DB + q) * ld + col, x[u][q]);
+        for (int q = 0; q < DB; ++q) vgather<T, CG>(X + ((size_t)j * DB + q) * ld + col, x[u][q]);
     }
     if (on)
 #pragma unroll
@@ -199,7 +217,7 @@ __global__ void __launch_bounds__(256) bspmm_chunked_kernel(int n, int nch, cons
 #pragma unroll
       for (int q = 0; q < DB; ++q) {
         T x[V];
-        vload(X + ((size_t)j * DB + q) * ld + col, x);
+        vgather<T, CG>(X + ((size_t)j * DB + q) * ld + col, x);
 #pragma unroll
         for (int p = 0; p < DB; ++p)
 #pragma unroll
@@ -233,7 +251,7 @@ __global__ void __launch_bounds__(256) bspmm_chunked_kernel(int n, int nch, cons
 // references at k = 15 on a surface, in the locality order), so after the
 // first touch the gathered chunks come from L1, and no shared memory caps
 // the occupancy.  Same accumulation order as the other variants.
-template <typename T, int DB, int U>
+template <typename T, int DB, int U, bool CG = false>
 __global__ void __launch_bounds__(256) bspmm_tile_kernel(int n, int n_tiles, const int* __restrict__ indptr,
                                                          const int* __restrict__ indices, const T* __restrict__ vals,
                                                          const T* __restrict__ X, T* __restrict__ Y,
@@ -265,7 +283,7 @@ __global__ void __launch_bounds__(256) bspmm_tile_kernel(int n, int n_tiles, con
       load_block<T, DB>(vals, t + u, blk[u]);
       if (on)
 #pragma unroll
-        for (int q = 0; q < DB; ++q) vload(X + ((size_t)j * DB + q) * ld + col, x[u][q]);
+        for (int q = 0; q < DB; ++q) vgather<T, CG>(X + ((size_t)j * DB + q) * ld + col, x[u][q]);
     }
     if (on)
 #pragma unroll
@@ -285,7 +303,7 @@ __global__ void __launch_bounds__(256) bspmm_tile_kernel(int n, int n_tiles, con
 #pragma unroll
       for (int q = 0; q < DB; ++q) {
         T x[V];
-        vload(X + ((size_t)j * DB + q) * ld + col, x);
+        vgather<T, CG>(X + ((size_t)j * DB + q) * ld + col, x);
 #pragma unroll
         for (int p = 0; p < DB; ++p)
 #pragma unroll
@@ -313,14 +331,14 @@ __global__ void __launch_bounds__(256) bspmm_tile_kernel(int n, int n_tiles, con
   }
 }
 
-template <typename T, int U>
+template <typename T, int U, bool CG = false>
 int launch_tile(int n, int DB, const int* indptr, const int* indices, const T* vals, const T* X, T* Y, const T* Z,
                 int b, int ld, T alpha, T beta, T gamma, cudaStream_t st) {
   constexpr int SEG = 128 / (int)sizeof(T);
   const int nt = (n + 31) / 32, nch = ceil_div(b, SEG);
   rvgp::note_launch();
 #define RVGP_SPMM_T(DBv)                                                                                          \
-  bspmm_tile_kernel<T, DBv, U><<<(unsigned)((long long)nt * nch), 256, 0, st>>>(n, nt, indptr, indices, vals, X, Y, \
+  bspmm_tile_kernel<T, DBv, U, CG><<<(unsigned)((long long)nt * nch), 256, 0, st>>>(n, nt, indptr, indices, vals, X, Y, \
                                                                                  Z, b, ld, alpha, beta, gamma)
   switch (DB) {
     case 1: RVGP_SPMM_T(1); break;
@@ -332,7 +350,7 @@ int launch_tile(int n, int DB, const int* indptr, const int* indices, const T* v
   return check_launch("rvgp_bspmm");
 }
 
-template <typename T, int U>
+template <typename T, int U, bool CG = false>
 int launch_chunked(int n, int DB, const int* indptr, const int* indices, const T* vals, const T* X, T* Y, const T* Z,
                    int b, int ld, T alpha, T beta, T gamma, cudaStream_t st) {
   constexpr int V = Vec<T>::V;
@@ -341,7 +359,7 @@ int launch_chunked(int n, int DB, const int* indptr, const int* indices, const T
   const int grid = ceil_div(warps * 32, 256);
   rvgp::note_launch();
 #define RVGP_SPMM_C(DBv) \
-  bspmm_chunked_kernel<T, DBv, U><<<grid, 256, 0, st>>>(n, nch, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma)
+  bspmm_chunked_kernel<T, DBv, U, CG><<<grid, 256, 0, st>>>(n, nch, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma)
   switch (DB) {
     case 1: RVGP_SPMM_C(1); break;
     case 2: RVGP_SPMM_C(2); break;
@@ -402,9 +420,11 @@ bool overlaps(const void* a, const void* b, size_t bytes) {
 }
 
 // Variants: 0 = row per warp (G groups per lane), 1 / 2 = column-chunked with
-// 2 / 4 neighbours per iteration, 3 / 4 = tile-mapped with 2 / 4.  The tuner
-// (autotune.cuh) picks one per shape class (RVGP_SPMM_VARIANT=v forces one);
-// the same bits come out of all five.
+// 2 / 4 neighbours per iteration, 3 / 4 = tile-mapped with 2 / 4, 5 / 6 =
+// chunked / tile-mapped (2 neighbours) with the neighbour gathers cached in
+// L2 only (a gather that misses L1 costs the L1 data path a fill and a read;
+// L2 has headroom).  The tuner (autotune.cuh) picks one per shape class
+// (RVGP_SPMM_VARIANT=v forces one); the same bits come out of all seven.
 template <typename T>
 int launch(int n, int DB, const int* indptr, const int* indices, const T* vals, const T* X, T* Y, const T* Z, int b,
            int ld, T alpha, T beta, T gamma, cudaStream_t st) {
@@ -420,11 +440,13 @@ int launch(int n, int DB, const int* indptr, const int* indices, const T* vals, 
       case 1: return launch_chunked<T, 2>(n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
       case 2: return launch_chunked<T, 4>(n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
       case 3: return launch_tile<T, 2>(n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
-      default: return launch_tile<T, 4>(n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
+      case 4: return launch_tile<T, 4>(n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
+      case 5: return launch_chunked<T, 2, true>(n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
+      default: return launch_tile<T, 2, true>(n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
     }
   };
   int def = groups >= chunk_min_groups() ? 1 : 0;
-  if (const char* fv = getenv("RVGP_SPMM_VARIANT")) def = std::min(4, std::max(0, atoi(fv)));  // tests: one variant
+  if (const char* fv = getenv("RVGP_SPMM_VARIANT")) def = std::min(6, std::max(0, atoi(fv)));  // tests: one variant
   // tuning runs the product several times into Y: only when Y overlaps neither input
   const size_t bytes = (size_t)n * DB * ld * sizeof(T);
   const bool independent = !overlaps(Y, X, bytes) && !(Z && overlaps(Y, Z, bytes));
@@ -433,7 +455,7 @@ int launch(int n, int DB, const int* indptr, const int* indices, const T* vals, 
     char key[160];
     snprintf(key, sizeof(key), "bspmm %s DB%d b%d n2^%d", sizeof(T) == 4 ? "f32" : "f64", DB, b,
              autotune::log2_bucket(n));
-    v = autotune::tune(key, 5, def, st, 3, run);
+    v = autotune::tune(key, 7, def, st, 3, run);
     if (v < 0) return v;
   }
   return run(v);
