@@ -323,7 +323,7 @@ def spmm_roofline(d, wl, peaks, flush, reps=20):
     names = {0: f"bspmm_kernel<float,{k},G>", 1: f"bspmm_chunked_kernel<float,{k},2>",
              2: f"bspmm_chunked_kernel<float,{k},4>", 3: f"bspmm_tile_kernel<float,{k},2>",
              4: f"bspmm_tile_kernel<float,{k},4>", 5: f"bspmm_chunked_kernel<float,{k},2,L2>",
-             6: f"bspmm_tile_kernel<float,{k},2,L2>"}
+             6: f"bspmm_tile_kernel<float,{k},2,L2>", 7: f"bspmm_chunked_kernel<float,{k},2,rowblocks>"}
     return {"kernel": f"{names.get(variant, '?')} (Chebyshev step, Lc x block; launch tuner's variant {variant})",
             "bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
             "frac": round(achieved / peaks["hbm_gbs"], 4),

@@ -304,7 +304,7 @@ def block_size(m, N):
     return min(p, N - N % 4)
 
 
-def eigsh(indptr, indices, vals64, vals32=None, m=10, mode="mixed", tol=None, tol32=1e-5, max_iter=60, seed=0,
+def eigsh(indptr, indices, vals64, vals32=None, m=10, mode="mixed", tol=None, tol32=None, max_iter=60, seed=0,
           scale=None, p=None, perm=None):
     """m smallest eigenpairs of the block-CSR matrix: (evals (m,), evecs (N, m), stats dict).
 
@@ -326,6 +326,8 @@ def eigsh(indptr, indices, vals64, vals32=None, m=10, mode="mixed", tol=None, to
     evals = torch.empty(m, dtype=torch.float64, device=dev)
     evecs = torch.empty((N, m), dtype=torch.float64, device=dev)
     stats = (ctypes.c_int * 16)()
+    if tol32 is None:  # the FP32 stage's residual tolerance (relative to the Gershgorin bound)
+        tol32 = float(os.environ.get("RVGP_EIG_TOL32", "1e-5"))
     if tol is None:  # mixed: stop at the FP32 stage's accuracy; fp64: ARPACK-level residuals
         tol = tol32 if imode == 1 else 1e-11
     L = lib()

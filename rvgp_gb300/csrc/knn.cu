@@ -22,6 +22,7 @@
 //                 queued.
 //   4. fallback : exact FP64 scan of the queued rows (one CTA per row).
 #include "common.cuh"
+#include "knn_top.cuh"
 #include <float.h>
 #include <limits.h>
 #include <mutex>
@@ -103,39 +104,6 @@ __global__ void prep_radius(const double* __restrict__ part_r2, int nblk, double
   // sqrt of an FP64 sum: inflate by a relative 1e-12 so R is an upper bound
   *radius = sqrt(m) * (1.0 + 1e-12);
 }
-
-// The KC smallest (value, index) pairs seen, ascending, held in registers:
-// every position is a compile-time index, so nothing spills to local memory.
-// Empty slots hold (FLT_MAX, -1).
-template <int KC>
-struct RegTop {
-  float d[KC];
-  int i[KC];
-  __device__ __forceinline__ void init() {
-#pragma unroll
-    for (int r = 0; r < KC; ++r) {
-      d[r] = FLT_MAX;
-      i[r] = -1;
-    }
-  }
-  __device__ __forceinline__ float worst() const { return d[KC - 1]; }
-  // Insert keeping the order (equal values stay in arrival order); call only
-  // when v < worst().  Each position decides from the old values of itself and
-  // its predecessor, so the KC selects are independent of one another.
-  __device__ __forceinline__ void insert(float v, int idx) {
-#pragma unroll
-    for (int r = KC - 1; r > 0; --r) {
-      const bool shift = d[r - 1] > v;
-      const bool here = d[r] > v;
-      d[r] = shift ? d[r - 1] : (here ? v : d[r]);
-      i[r] = shift ? i[r - 1] : (here ? idx : i[r]);
-    }
-    if (d[0] > v) {
-      d[0] = v;
-      i[0] = idx;
-    }
-  }
-};
 
 template <int DP, int KC>
 __global__ void __launch_bounds__(kQB) knn_screen(const float* __restrict__ Xf, int n, int nsplit,
@@ -222,10 +190,14 @@ struct TopList {
   }
 };
 
+// r2q (optional): the tensor-core screen's |x'|² per query (knn_tc.cu): its
+// certificate replaces the SIMT screen's; tcerr (optional): a raised flag of
+// that screen sends every row to the exact scan.
 __global__ void knn_finish(const double* __restrict__ X, int n, int D, int DP, int k, int kc, int nsplit,
                            const float* __restrict__ part_d, const int* __restrict__ part_i,
                            const double* __restrict__ radius, int* __restrict__ out_idx,
-                           int* __restrict__ nflag, int* __restrict__ flag_list) {
+                           int* __restrict__ nflag, int* __restrict__ flag_list, const float* __restrict__ r2q,
+                           const int* __restrict__ tcerr) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n) return;
   TopList L;
@@ -260,12 +232,24 @@ __global__ void knn_finish(const double* __restrict__ X, int n, int D, int DP, i
   } else {
     // here some slice kept a full list, so total >= kc and cnt == kc
     const double u = 5.9604644775390625e-08;  // 2^-24
-    const double g = DP * u / (1.0 - DP * u);
-    const double f = sqrt((double)L.worst);
-    double lb = (f / (1.0 + g) - 4.01 * u * radius[0]) / (1.0 + u);
+    double lb;
+    if (r2q) {
+      // tensor-core screen: d'² >= (f² - 3 eps |x'|²) / (1 + 2 eps) on the
+      // block-centred FP32 values, eps = 1e-4 (knn_tc.cu), then their own
+      // rounding (u (|x'| + |y'|) <= u (2|x'| + d')) and the FP32 copy's
+      const double eps = 1e-4, rq = (double)r2q[q] * (1.0 + 1e-6);
+      const double lb2 = ((double)L.worst - 3.0 * eps * rq) / (1.0 + 2.0 * eps);
+      const double dp = sqrt(fmax(lb2, 0.0));
+      lb = (dp * (1.0 - u) - 2.0 * u * sqrt(rq) - 4.01 * u * radius[0]) / (1.0 + u);
+    } else {
+      const double g = DP * u / (1.0 - DP * u);
+      const double f = sqrt((double)L.worst);
+      lb = (f / (1.0 + g) - 4.01 * u * radius[0]) / (1.0 + u);
+    }
     lb *= (1.0 - 1e-12);
     certified = lb > 0.0 && lb * lb > d2[k - 1] * (1.0 + 1e-12);
   }
+  if (tcerr && *tcerr) certified = false;
   for (int r = 0; r < k; ++r) out_idx[(size_t)q * k + r] = r < cnt ? id[r] : -1;
   if (!certified) {
     int slot = atomicAdd(nflag, 1);
@@ -354,26 +338,53 @@ void launch_screen(int DP, dim3 grid, cudaStream_t st, const float* Xf, int n, i
 
 struct KnnPlan {
   int DP, kc, nsplit, nblk_prep;
+  bool tc;  // tensor-core screen (knn_tc.cu)
 };
 
-KnnPlan plan(int n, int D, int k) {
+// The tensor-core screen for 16 < D <= 64 (RVGP_KNN_TC=0, or
+// RVGP_TENSOR_CORES=0, selects the SIMT screen); the allocation-free entry
+// point keeps the SIMT screen (its scratch is fixed).
+bool knn_tc_enabled(int D) {
+  const char* e = getenv("RVGP_KNN_TC");
+  const char* t = getenv("RVGP_TENSOR_CORES");
+  return D > 16 && D <= 64 && !(e && e[0] == '0') && !(t && t[0] == '0');
+}
+
+KnnPlan plan(int n, int D, int k, bool allow_tc = true) {
   KnnPlan p;
   p.DP = padded_dim(D);
   p.kc = kc_bucket(k);
+  p.tc = allow_tc && knn_tc_enabled(D);
   int qblocks = ceil_div(n, kQB);
-  p.nsplit = max(1, min(16, ceil_div(4 * num_sms(), qblocks)));
+  p.nsplit = max(1, min(16, ceil_div((p.tc ? 1 : 4) * num_sms(), qblocks)));
   p.nblk_prep = min(num_sms() * 2, max(1, ceil_div(n, 256)));
   return p;
 }
 
 struct KnnBufs {
   double *part_mm, *centre, *part_r2, *radius;
-  float *Xf, *part_d;
-  int *part_i, *nflag, *flag_list;
+  float *Xf, *part_d, *r2q;
+  int *part_i, *nflag, *flag_list, *order, *rank, *tcerr;
+  void* lo_ws;
+  size_t lo_bytes;
 };
+
+}  // namespace
+}  // namespace rvgp
+extern "C" size_t rvgp_locality_order_workspace(int n, int D);
+extern "C" int rvgp_locality_order(const double* X, int n, int D, int* perm, int* rank, void* workspace,
+                                   size_t ws_bytes, void* stream);
+namespace rvgp {
+int knn_tc_screen_launch(int DP, int kc, const float* Xf, int n, const int* order, int nsplit, float* part_d,
+                         int* part_i, float* r2q, int* err, cudaStream_t st);
+namespace {
 
 KnnBufs carve(Workspace& ws, const KnnPlan& p, int n, int D) {
   KnnBufs b;
+  b.r2q = nullptr;
+  b.order = b.rank = b.tcerr = nullptr;
+  b.lo_ws = nullptr;
+  b.lo_bytes = 0;
   b.part_mm = ws.take<double>((size_t)p.nblk_prep * D * 2);
   b.centre = ws.take<double>(D);
   b.part_r2 = ws.take<double>(p.nblk_prep);
@@ -383,12 +394,20 @@ KnnBufs carve(Workspace& ws, const KnnPlan& p, int n, int D) {
   b.part_i = ws.take<int>((size_t)n * p.nsplit * p.kc);
   b.nflag = ws.take<int>(1);
   b.flag_list = ws.take<int>(n);
+  if (p.tc) {
+    b.r2q = ws.take<float>(n);
+    b.order = ws.take<int>(n);
+    b.rank = ws.take<int>(n);
+    b.tcerr = ws.take<int>(1);
+    b.lo_bytes = rvgp_locality_order_workspace(n, D);
+    b.lo_ws = ws.take<char>(b.lo_bytes);
+  }
   return b;
 }
 
-size_t workspace_bytes(int n, int D, int k) {
+size_t workspace_bytes(int n, int D, int k, bool allow_tc = true) {
   Workspace ws(nullptr, 0);
-  carve(ws, plan(n, D, k), n, D);
+  carve(ws, plan(n, D, k, allow_tc), n, D);
   return ws.used;
 }
 
@@ -404,17 +423,25 @@ RVGP_API size_t rvgp_knn_workspace(int n, int D, int k) {
   return workspace_bytes(n, D, k);
 }
 
+static int knn_impl(const double* X, int n, int D, int k, int* idx, void* workspace, size_t ws_bytes, void* stream,
+                    bool allow_tc);
+
 RVGP_API int rvgp_knn(const double* X, int n, int D, int k, int* idx, void* workspace, size_t ws_bytes,
                       void* stream) {
+  return knn_impl(X, n, D, k, idx, workspace, ws_bytes, stream, true);
+}
+
+static int knn_impl(const double* X, int n, int D, int k, int* idx, void* workspace, size_t ws_bytes, void* stream,
+                    bool allow_tc) {
   RVGP_CHECK_ARG(X && idx, "rvgp_knn: null pointer");
   RVGP_CHECK_ARG(n >= 2, "rvgp_knn: need at least 2 points, got %d", n);
   RVGP_CHECK_ARG(k >= 1 && k < n, "Expected n_neighbors < n_samples, got %d >= %d", k, n);
   RVGP_CHECK_ARG(k + kExtra <= kMaxKC, "rvgp_knn: k=%d exceeds the supported maximum %d", k, kMaxKC - kExtra);
   RVGP_CHECK_ARG(padded_dim(D) > 0, "rvgp_knn: ambient dimension %d > 128 is not supported", D);
-  size_t need = workspace_bytes(n, D, k);
+  size_t need = workspace_bytes(n, D, k, allow_tc);
   RVGP_CHECK_ARG(workspace && ws_bytes >= need, "rvgp_knn: workspace of %zu bytes needed", need);
   cudaStream_t st = as_stream(stream);
-  KnnPlan p = plan(n, D, k);
+  KnnPlan p = plan(n, D, k, allow_tc);
   Workspace ws(workspace, ws_bytes);
   KnnBufs b = carve(ws, p, n, D);
   rvgp::note_launch(); prep_minmax<<<p.nblk_prep, 256, 2 * 256 * sizeof(double), st>>>(X, n, D, b.part_mm);
@@ -422,16 +449,23 @@ RVGP_API int rvgp_knn(const double* X, int n, int D, int k, int* idx, void* work
   rvgp::note_launch(); prep_copy<<<p.nblk_prep, 256, 0, st>>>(X, n, D, p.DP, b.centre, b.Xf, b.part_r2);
   rvgp::note_launch(); prep_radius<<<1, 32, 0, st>>>(b.part_r2, p.nblk_prep, b.radius);
   cudaMemsetAsync(b.nflag, 0, sizeof(int), st);
-  dim3 grid(ceil_div(n, kQB), p.nsplit);
-  rvgp::note_launch();
-  switch (p.kc) {
-    case 16: launch_screen<16>(p.DP, grid, st, b.Xf, n, p.nsplit, b.part_d, b.part_i); break;
-    case 32: launch_screen<32>(p.DP, grid, st, b.Xf, n, p.nsplit, b.part_d, b.part_i); break;
-    case 48: launch_screen<48>(p.DP, grid, st, b.Xf, n, p.nsplit, b.part_d, b.part_i); break;
-    default: launch_screen<72>(p.DP, grid, st, b.Xf, n, p.nsplit, b.part_d, b.part_i); break;
+  if (p.tc) {
+    // queries in the locality order: a block of 128 is a compact patch
+    TRY_RC(rvgp_locality_order(X, n, D, b.order, b.rank, b.lo_ws, b.lo_bytes, stream));
+    cudaMemsetAsync(b.tcerr, 0, sizeof(int), st);
+    TRY_RC(knn_tc_screen_launch(p.DP, p.kc, b.Xf, n, b.order, p.nsplit, b.part_d, b.part_i, b.r2q, b.tcerr, st));
+  } else {
+    dim3 grid(ceil_div(n, kQB), p.nsplit);
+    rvgp::note_launch();
+    switch (p.kc) {
+      case 16: launch_screen<16>(p.DP, grid, st, b.Xf, n, p.nsplit, b.part_d, b.part_i); break;
+      case 32: launch_screen<32>(p.DP, grid, st, b.Xf, n, p.nsplit, b.part_d, b.part_i); break;
+      case 48: launch_screen<48>(p.DP, grid, st, b.Xf, n, p.nsplit, b.part_d, b.part_i); break;
+      default: launch_screen<72>(p.DP, grid, st, b.Xf, n, p.nsplit, b.part_d, b.part_i); break;
+    }
   }
   rvgp::note_launch(); knn_finish<<<ceil_div(n, 128), 128, 0, st>>>(X, n, D, p.DP, k, p.kc, p.nsplit, b.part_d, b.part_i,
-                                                                 b.radius, idx, b.nflag, b.flag_list);
+                                                                 b.radius, idx, b.nflag, b.flag_list, b.r2q, b.tcerr);
   rvgp::note_launch(); knn_fallback<<<num_sms(), kFbThreads, 0, st>>>(X, n, D, k, b.nflag, b.flag_list, idx);
   RVGP_LAUNCH_CHECK("rvgp_knn");
   return RVGP_OK;
@@ -474,9 +508,10 @@ void* g_scratch_ptr[kMaxDevices] = {};
 
 RVGP_API int rvgp_knn_noalloc(const double* X, int n, int D, int k, int* idx, void* stream) {
   RVGP_CHECK_ARG(n >= 2 && k >= 1 && k < n && D >= 1, "rvgp_knn_noalloc: bad sizes n=%d D=%d k=%d", n, D, k);
-  const size_t need = rvgp_knn_workspace(n, D, k);
-  RVGP_CHECK_ARG(need > 0, "rvgp_knn_noalloc: unsupported shape n=%d, D=%d, k=%d (D must be <= 128, k <= %d)", n,
-                 D, k, kMaxKC - kExtra);
+  RVGP_CHECK_ARG(rvgp_knn_workspace(n, D, k) > 0,
+                 "rvgp_knn_noalloc: unsupported shape n=%d, D=%d, k=%d (D must be <= 128, k <= %d)", n, D, k,
+                 kMaxKC - kExtra);
+  const size_t need = workspace_bytes(n, D, k, false);  // the SIMT screen: its scratch is the fixed buffer's
   RVGP_CHECK_ARG(need <= kNoAllocScratchBytes,
                  "rvgp_knn_noalloc: n=%d, D=%d, k=%d needs %zu bytes of scratch, more than the fixed %zu-byte "
                  "buffer; use rvgp_knn with a caller-provided workspace",
@@ -501,7 +536,7 @@ RVGP_API int rvgp_knn_noalloc(const double* X, int n, int D, int k, int* idx, vo
     }
     scratch = g_scratch_ptr[dev];
   }
-  return rvgp_knn(X, n, D, k, idx, scratch, kNoAllocScratchBytes, stream);
+  return knn_impl(X, n, D, k, idx, scratch, kNoAllocScratchBytes, stream, false);
 }
 
 // Number of rows the last rvgp_knn call on this workspace sent to the exact

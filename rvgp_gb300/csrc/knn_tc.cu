@@ -1,0 +1,309 @@
+// Tensor-core screen of the exact kNN search (knn.cu, step 2) for ambient
+// dimensions 17..64 (padded to DP = 32 or 64): the squared distances of a
+// block of 128 queries to tiles of 128 candidates as
+//     f² = |x'|² + |y'|² − 2 x'·y'
+// with x', y' the FP32 coordinates minus the block's own centre c (the mean
+// of its 128 queries), and x'·y' from split-TF32 tcgen05 MMAs (x' = hi + lo,
+// A B ≈ Ahi Bhi + Ahi Blo + Alo Bhi, FP32 accumulators in TMEM).  Queries are
+// taken in the locality (Morton) order, so a block is a compact patch and
+// |x'| is its radius scale.
+//
+// Error bound (per pair, on the FP32 centred values): the dropped lo·lo term
+// and the TF32 truncation of lo, ≤ 1.2e-6 |x'||y'|; at most 3·64 FP32
+// accumulation roundings (truncation assumed), ≤ 2.3e-5 |x'||y'|; the two
+// FP32 norms, ≤ 64u each; the final sums, 4u — in all |f² − d'²| ≤
+// 2.9e-5 (|x'|² + |y'|²).  With ε = 1e-4 and |y'|² ≤ 2d'² + 2|x'|²:
+//     d'² ≥ (f² − 3ε|x'|²) / (1 + 2ε),
+// monotone in f², so the kc-th survivor's f² bounds every non-survivor; the
+// finish kernel turns it into a certificate with the FP32 copy's own rounding
+// (4.01 u R, as for the SIMT screen) and per-query |x'|² (r2q).
+//
+// CTA: 288 threads.  Warps 0-3: epilogue, thread i owns query row i = TMEM
+// lane i and its register top-kc list; warps 4-7: producers, thread r stages
+// candidate row r of a tile (centred, split, 128-byte-swizzled K-major) and
+// its squared norm; warp 8: one thread issues the MMAs.  Two candidate
+// buffers and two TMEM accumulators; mbarriers: staged[b] (4 producer
+// warps), full[b] (MMA commit), free[b] (4 epilogue warps).  Every wait is
+// bounded; on a timeout the CTA raises the error flag, drains its MMAs and
+// frees its TMEM.
+#include "common.cuh"
+#include "knn_top.cuh"
+#include "tcgen05.cuh"
+#include <float.h>
+
+namespace rvgp {
+namespace {
+
+constexpr int kTQ = 128;             // queries per CTA (MMA M)
+constexpr int kTC = 128;             // candidates per tile (MMA N)
+constexpr int kTThreads = 288;
+constexpr uint32_t kTTmemCols = 256;  // two 128-column accumulators
+constexpr long long kTWait = 1ll << 22;
+constexpr int kSlabBytes = kTQ * 128;  // one 32-element K slab of a 128-row operand
+
+__device__ __forceinline__ uint8_t* align1k(uint8_t* p) {
+  const uint32_t a = tc::smem_u32(p);
+  return p + (((a + 1023u) & ~1023u) - a);
+}
+
+// hi / lo TF32 parts of 4 consecutive K elements (chunk kc of slab s) of row r
+__device__ __forceinline__ void put4(uint8_t* hi, uint8_t* lo, int r, int s, int kc, float4 v) {
+  float4 h, l;
+  h.x = tc::to_tf32(v.x);
+  h.y = tc::to_tf32(v.y);
+  h.z = tc::to_tf32(v.z);
+  h.w = tc::to_tf32(v.w);
+  l.x = v.x - h.x;
+  l.y = v.y - h.y;
+  l.z = v.z - h.z;
+  l.w = v.w - h.w;
+  const int off = s * kSlabBytes + r * 128 + ((kc ^ (r & 7)) << 4);
+  *reinterpret_cast<float4*>(hi + off) = h;
+  *reinterpret_cast<float4*>(lo + off) = l;
+}
+
+template <int DP, int KC>
+__global__ void __launch_bounds__(kTThreads, 1)
+    knn_tc_screen(const float* __restrict__ Xf, int n, const int* __restrict__ order, int nsplit,
+                  float* __restrict__ part_d, int* __restrict__ part_i, float* __restrict__ r2q,
+                  int* __restrict__ err) {
+  constexpr int NS = DP / 32;                 // K slabs
+  constexpr int OPB = NS * kSlabBytes;        // one split (hi or lo) of a 128-row operand
+  extern __shared__ uint8_t smem_raw[];
+  __shared__ uint64_t bar[7];                 // staged[2], full[2], free[2], drain
+  __shared__ uint32_t tmem_slot;
+  __shared__ int s_fail;
+  __shared__ float cen[DP];
+  __shared__ float cn[2][kTC];
+  uint8_t* smem = align1k(smem_raw);
+  uint8_t* Ahi = smem;
+  uint8_t* Alo = Ahi + OPB;
+  uint8_t* Bb = Alo + OPB;                    // buffer b: hi at Bb + 2 b OPB, lo after it
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int qb = blockIdx.x, split = blockIdx.y;
+  const int q0 = qb * kTQ, nq = min(kTQ, n - q0);
+  const long long chunk = ((long long)n + nsplit - 1) / nsplit;
+  const int c0 = (int)min((long long)n, split * chunk), c1 = (int)min((long long)n, c0 + chunk);
+  const int ntiles = (c1 - c0 + kTC - 1) / kTC;
+
+  if (warp == 0) {
+    tc::tmem_alloc(&tmem_slot, kTTmemCols);
+    tc::tmem_relinquish();
+  }
+  if (tid == 0) {
+    for (int b = 0; b < 2; ++b) {
+      tc::mbar_init(&bar[b], 4);
+      tc::mbar_init(&bar[2 + b], 1);
+      tc::mbar_init(&bar[4 + b], 4);
+    }
+    tc::mbar_init(&bar[6], 1);
+    tc::fence_mbar_init();
+    s_fail = 0;
+  }
+  // the block's centre: mean of its queries (fixed order)
+  for (int j = tid; j < DP; j += kTThreads) {
+    float s = 0.f;
+    for (int i = 0; i < nq; ++i) s += Xf[(size_t)order[q0 + i] * DP + j];
+    cen[j] = s / (float)nq;
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = tmem_slot;
+  // A operand (query rows, centred) and each query's |x'|², by the epilogue threads
+  float qn = 0.f;
+  int q = -1;
+  if (warp < 4) {
+    const int i = tid;
+    const bool on = i < nq;
+    q = on ? order[q0 + i] : -1;
+#pragma unroll
+    for (int s = 0; s < NS; ++s)
+#pragma unroll
+      for (int kc = 0; kc < 8; ++kc) {
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (on) {
+          const float4 x = *reinterpret_cast<const float4*>(Xf + (size_t)q * DP + s * 32 + kc * 4);
+          const int j = s * 32 + kc * 4;
+          v = make_float4(x.x - cen[j], x.y - cen[j + 1], x.z - cen[j + 2], x.w - cen[j + 3]);
+          qn = fmaf(v.x, v.x, qn);
+          qn = fmaf(v.y, v.y, qn);
+          qn = fmaf(v.z, v.z, qn);
+          qn = fmaf(v.w, v.w, qn);
+        }
+        put4(Ahi, Alo, i, s, kc, v);
+      }
+    if (on && split == 0) r2q[q] = qn;
+  }
+  tc::fence_async_smem();
+  __syncthreads();
+
+  if (warp < 4) {
+    // ---- epilogue: thread i = TMEM lane i
+    RegTop<KC> L;
+    L.init();
+    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+    for (int t = 0; t < ntiles; ++t) {
+      const int b = t & 1;
+      bool ok = true;
+      // staged[b] too: it orders the producers' norms cn[b] before these reads
+      // (its phase cannot move on before this warp releases the buffer)
+      for (int which = 0; which < 2 && ok; ++which)
+        for (long long w = 0; !tc::mbar_try_wait(&bar[which == 0 ? b : 2 + b], (t >> 1) & 1); ++w)
+          if (w > kTWait || *((volatile int*)&s_fail)) {
+            ok = false;
+            break;
+          }
+      if (!ok) {
+        s_fail = 1;
+        break;
+      }
+      tc::fence_after_sync();
+      const int cb = c0 + t * kTC;
+#pragma unroll 1
+      for (int c = 0; c < kTC; c += 8) {
+        float v[8];
+        tc::tmem_ld8(trow + (uint32_t)(b * kTC + c), v);
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int cand = cb + c + u;
+          const float d2 = qn + cn[b][c + u] - 2.f * v[u];
+          if (d2 < L.worst() && cand < c1 && cand != q) L.insert(d2, cand);
+        }
+      }
+      tc::fence_before_sync();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&bar[4 + b]);
+    }
+    if (q >= 0) {
+      const size_t base = ((size_t)q * nsplit + split) * KC;
+#pragma unroll
+      for (int r = 0; r < KC; ++r) {
+        part_d[base + r] = L.d[r];
+        part_i[base + r] = L.i[r];
+      }
+    }
+  } else if (warp < 8) {
+    // ---- producers: thread r stages candidate row r of each tile
+    const int r = tid - 128;
+    for (int t = 0; t < ntiles; ++t) {
+      const int b = t & 1;
+      if (t >= 2) {
+        bool ok = true;
+        for (long long w = 0; !tc::mbar_try_wait(&bar[4 + b], ((t - 2) >> 1) & 1); ++w)
+          if (w > kTWait || *((volatile int*)&s_fail)) {
+            ok = false;
+            break;
+          }
+        if (!ok) {
+          s_fail = 1;
+          break;
+        }
+      }
+      const int cand = c0 + t * kTC + r;
+      const bool on = cand < c1;
+      uint8_t* hi = Bb + 2 * b * OPB;
+      uint8_t* lo = hi + OPB;
+      float nrm = 0.f;
+#pragma unroll
+      for (int s = 0; s < NS; ++s)
+#pragma unroll
+        for (int kc = 0; kc < 8; ++kc) {
+          float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+          if (on) {
+            const float4 y = *reinterpret_cast<const float4*>(Xf + (size_t)cand * DP + s * 32 + kc * 4);
+            const int j = s * 32 + kc * 4;
+            v = make_float4(y.x - cen[j], y.y - cen[j + 1], y.z - cen[j + 2], y.w - cen[j + 3]);
+            nrm = fmaf(v.x, v.x, nrm);
+            nrm = fmaf(v.y, v.y, nrm);
+            nrm = fmaf(v.z, v.z, nrm);
+            nrm = fmaf(v.w, v.w, nrm);
+          }
+          put4(hi, lo, r, s, kc, v);
+        }
+      cn[b][r] = on ? nrm : FLT_MAX;
+      tc::fence_async_smem();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&bar[b]);
+    }
+  } else if (lane == 0) {
+    // ---- MMA issuer
+    const uint32_t idesc = tc::idesc_tf32(kTQ, kTC);
+    const uint32_t ah = tc::smem_u32(Ahi), al = tc::smem_u32(Alo);
+    for (int t = 0; t < ntiles; ++t) {
+      const int b = t & 1;
+      bool ok = true;
+      for (long long w = 0; !tc::mbar_try_wait(&bar[b], (t >> 1) & 1); ++w)
+        if (w > kTWait || *((volatile int*)&s_fail)) {
+          ok = false;
+          break;
+        }
+      if (!ok) {
+        s_fail = 1;
+        break;
+      }
+      tc::fence_after_sync();
+      const uint32_t bh = tc::smem_u32(Bb + 2 * b * OPB), bl = bh + OPB;
+      const uint32_t d = tmem + (uint32_t)(b * kTC);
+#pragma unroll
+      for (int s = 0; s < NS; ++s)
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk) {
+          const uint32_t o = s * kSlabBytes + kk * 32;
+          tc::mma_tf32(d, tc::desc_sw128(ah + o), tc::desc_sw128(bh + o), idesc, (s == 0 && kk == 0) ? 0u : 1u);
+          tc::mma_tf32(d, tc::desc_sw128(ah + o), tc::desc_sw128(bl + o), idesc, 1u);
+          tc::mma_tf32(d, tc::desc_sw128(al + o), tc::desc_sw128(bh + o), idesc, 1u);
+        }
+      tc::mma_commit(&bar[2 + b]);
+    }
+  }
+  // every MMA issued has completed before TMEM is released: on the normal
+  // path the epilogue waited for the last tile; after a timeout the issuer
+  // commits once more and waits (bounded)
+  __syncthreads();
+  if (s_fail && warp == 8 && lane == 0) {
+    tc::mma_commit(&bar[6]);
+    tc::mbar_wait(&bar[6], 0, kTWait);
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, kTTmemCols);
+  if (tid == 0 && s_fail) atomicExch(err, 1);
+}
+
+template <int DP>
+int launch_dp(int kc, dim3 grid, size_t smem, cudaStream_t st, const float* Xf, int n, const int* order, int nsplit,
+              float* pd, int* pi, float* r2q, int* err) {
+#define RVGP_KTC(KCv)                                                                                              \
+  case KCv: {                                                                                                      \
+    if (cudaFuncSetAttribute(knn_tc_screen<DP, KCv>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=   \
+        cudaSuccess)                                                                                               \
+      return check_launch("knn_tc_screen");                                                                        \
+    rvgp::note_launch();                                                                                           \
+    knn_tc_screen<DP, KCv><<<grid, kTThreads, smem, st>>>(Xf, n, order, nsplit, pd, pi, r2q, err);                 \
+    break;                                                                                                         \
+  }
+  switch (kc) {
+    RVGP_KTC(16)
+    RVGP_KTC(32)
+    RVGP_KTC(48)
+    default: RVGP_KTC(72)
+  }
+#undef RVGP_KTC
+  return check_launch("knn_tc_screen");
+}
+
+}  // namespace
+
+// The screen's launch (kc in 16/32/48/72; DP 32 or 64): part_d / part_i
+// (n x nsplit x kc, the candidates' f² and indices), r2q (n) = |x'|².
+int knn_tc_screen_launch(int DP, int kc, const float* Xf, int n, const int* order, int nsplit, float* part_d,
+                         int* part_i, float* r2q, int* err, cudaStream_t st) {
+  const int NS = DP / 32;
+  const size_t smem = 1024 + (size_t)2 * NS * kSlabBytes * 3;  // A hi/lo + two B buffers of hi/lo
+  dim3 grid((n + kTQ - 1) / kTQ, nsplit);
+  if (DP == 32) return launch_dp<32>(kc, grid, smem, st, Xf, n, order, nsplit, part_d, part_i, r2q, err);
+  return launch_dp<64>(kc, grid, smem, st, Xf, n, order, nsplit, part_d, part_i, r2q, err);
+}
+
+}  // namespace rvgp

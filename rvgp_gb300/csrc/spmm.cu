@@ -167,7 +167,11 @@ __global__ void __launch_bounds__(256) bspmm_kernel(int n, const int* __restrict
 // issued first, then the products in the row kernel's order (neighbour by
 // neighbour, block column by block column), so every variant gives the same
 // bits.
-template <typename T, int DB, int U, bool CG = false>
+// RB: CTA = 8 consecutive rows x one column chunk, chunk-major grid (the
+// rows of a CTA share most of their neighbours, and a chunk of X stays in L2
+// while its row blocks run); otherwise the chunks of a row are consecutive
+// warps.
+template <typename T, int DB, int U, bool CG = false, bool RB = false>
 __global__ void __launch_bounds__(256) bspmm_chunked_kernel(int n, int nch, const int* __restrict__ indptr,
                                                             const int* __restrict__ indices,
                                                             const T* __restrict__ vals, const T* __restrict__ X,
@@ -176,8 +180,16 @@ __global__ void __launch_bounds__(256) bspmm_chunked_kernel(int n, int nch, cons
   constexpr int V = Vec<T>::V;
   const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  const long long i = warp / nch;
-  const int chunk = (int)(warp % nch);
+  long long i;
+  int chunk;
+  if (RB) {
+    const long long nrb = ((long long)n + 7) / 8;
+    chunk = (int)(blockIdx.x / nrb);
+    i = (blockIdx.x % nrb) * 8 + (threadIdx.x >> 5);
+  } else {
+    i = warp / nch;
+    chunk = (int)(warp % nch);
+  }
   if (i >= n) return;
   const int grp = chunk * 32 + lane;
   const bool on = grp < b / V;
@@ -350,16 +362,16 @@ int launch_tile(int n, int DB, const int* indptr, const int* indices, const T* v
   return check_launch("rvgp_bspmm");
 }
 
-template <typename T, int U, bool CG = false>
+template <typename T, int U, bool CG = false, bool RB = false>
 int launch_chunked(int n, int DB, const int* indptr, const int* indices, const T* vals, const T* X, T* Y, const T* Z,
                    int b, int ld, T alpha, T beta, T gamma, cudaStream_t st) {
   constexpr int V = Vec<T>::V;
   const int nch = ceil_div(b / V, 32);
   const long long warps = (long long)n * nch;
-  const int grid = ceil_div(warps * 32, 256);
+  const int grid = RB ? (int)(((long long)n + 7) / 8 * nch) : ceil_div(warps * 32, 256);
   rvgp::note_launch();
 #define RVGP_SPMM_C(DBv) \
-  bspmm_chunked_kernel<T, DBv, U, CG><<<grid, 256, 0, st>>>(n, nch, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma)
+  bspmm_chunked_kernel<T, DBv, U, CG, RB><<<grid, 256, 0, st>>>(n, nch, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma)
   switch (DB) {
     case 1: RVGP_SPMM_C(1); break;
     case 2: RVGP_SPMM_C(2); break;
@@ -423,8 +435,9 @@ bool overlaps(const void* a, const void* b, size_t bytes) {
 // 2 / 4 neighbours per iteration, 3 / 4 = tile-mapped with 2 / 4, 5 / 6 =
 // chunked / tile-mapped (2 neighbours) with the neighbour gathers cached in
 // L2 only (a gather that misses L1 costs the L1 data path a fill and a read;
-// L2 has headroom).  The tuner (autotune.cuh) picks one per shape class
-// (RVGP_SPMM_VARIANT=v forces one); the same bits come out of all seven.
+// L2 has headroom), 7 = chunked with 8-row blocks per CTA, chunk-major.  The
+// tuner (autotune.cuh) picks one per shape class (RVGP_SPMM_VARIANT=v forces
+// one); the same bits come out of all eight.
 template <typename T>
 int launch(int n, int DB, const int* indptr, const int* indices, const T* vals, const T* X, T* Y, const T* Z, int b,
            int ld, T alpha, T beta, T gamma, cudaStream_t st) {
@@ -442,11 +455,13 @@ int launch(int n, int DB, const int* indptr, const int* indices, const T* vals, 
       case 3: return launch_tile<T, 2>(n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
       case 4: return launch_tile<T, 4>(n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
       case 5: return launch_chunked<T, 2, true>(n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
-      default: return launch_tile<T, 2, true>(n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
+      case 6: return launch_tile<T, 2, true>(n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
+      default:
+        return launch_chunked<T, 2, false, true>(n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
     }
   };
   int def = groups >= chunk_min_groups() ? 1 : 0;
-  if (const char* fv = getenv("RVGP_SPMM_VARIANT")) def = std::min(6, std::max(0, atoi(fv)));  // tests: one variant
+  if (const char* fv = getenv("RVGP_SPMM_VARIANT")) def = std::min(7, std::max(0, atoi(fv)));  // tests: one variant
   // tuning runs the product several times into Y: only when Y overlaps neither input
   const size_t bytes = (size_t)n * DB * ld * sizeof(T);
   const bool independent = !overlaps(Y, X, bytes) && !(Z && overlaps(Y, Z, bytes));
@@ -455,7 +470,7 @@ int launch(int n, int DB, const int* indptr, const int* indices, const T* vals, 
     char key[160];
     snprintf(key, sizeof(key), "bspmm %s DB%d b%d n2^%d", sizeof(T) == 4 ? "f32" : "f64", DB, b,
              autotune::log2_bucket(n));
-    v = autotune::tune(key, 7, def, st, 3, run);
+    v = autotune::tune(key, 8, def, st, 3, run);
     if (v < 0) return v;
   }
   return run(v);

@@ -52,7 +52,7 @@ def run(tmp_path, tag, b, env_extra):
 def test_autotune_cache_and_identical_variants(tmp_path, b):
     cache = str(tmp_path / "tune.txt")
     b1, a1, path, y1 = run(tmp_path, "first", b, {"RVGP_AUTOTUNE_CACHE": cache})
-    assert path == cache and b1 == -1 and a1 in range(7)
+    assert path == cache and b1 == -1 and a1 in range(8)
     assert any(line.startswith(f"bspmm f32 DB2 b{b} n2^11 # ") for line in open(cache))
     b2, a2, _, y2 = run(tmp_path, "second", b, {"RVGP_AUTOTUNE_CACHE": cache})
     assert b2 == a1 and a2 == a1  # the second process starts from the cached choice
@@ -60,6 +60,6 @@ def test_autotune_cache_and_identical_variants(tmp_path, b):
     _, _, _, yc = run(tmp_path, "chunked", b, {"RVGP_AUTOTUNE_CACHE": cache, "RVGP_SPMM_CHUNK_MIN": "0"})
     _, _, _, yr = run(tmp_path, "rows", b, {"RVGP_AUTOTUNE_CACHE": cache, "RVGP_SPMM_CHUNK_MIN": "100000"})
     forced = [run(tmp_path, f"v{v}", b, {"RVGP_AUTOTUNE_CACHE": cache, "RVGP_SPMM_VARIANT": str(v)})[3]
-              for v in range(7)]
+              for v in range(8)]
     for y in [y2, yc, yr] + forced:
         assert np.array_equal(y, y1)
