@@ -706,8 +706,8 @@ int copy_cols(const float* src, int lds, int c0, float* dst, int ldd, int d0, lo
 }
 
 // The FP32 stage with locking.  After each Rayleigh-Ritz step the leading
-// active Ritz vectors whose residual passes (in multiples of 4, never beyond
-// m) move to Vl and leave the iteration: the filter, the orthonormalisation,
+// active Ritz vectors whose residual is below a tenth of the tolerance (in
+// multiples of 4, never beyond m) move to Vl and leave the iteration: the filter, the orthonormalisation,
 // the Rayleigh-Ritz products and the Jacobi then run on the p - nl active
 // columns, kept compact (ld = p - nl) so every kernel sees a plain block.
 // After each filter the active block is projected against Vl twice
@@ -716,6 +716,8 @@ int copy_cols(const float* src, int lds, int c0, float* dst, int ldd, int d0, lo
 // filter degree still bounds the gain of the lowest Ritz value overall
 // (locked or not), as without locking.  On return B.V is the N x p block
 // [locked | active] (ld p), theta / res the matching values.
+constexpr double kLockMargin = 0.1;  // lock at a tenth of the convergence tolerance
+
 int iterate_locked(const Problem& P, Block<float>& B, float* Vl, int ldl, Small& s, Stats& stt, double bup,
                    double tol, int max_iter, int first_deg, double range, std::vector<double>& theta,
                    std::vector<double>& res, int* nconv_out, cudaStream_t st) {
@@ -757,8 +759,10 @@ int iterate_locked(const Problem& P, Block<float>& B, float* Vl, int ldl, Small&
       if (nconv == ma) break;
     }
     if (lock_on) {
+      // a locked vector is never polished again: lock only those whose
+      // residual is well below the convergence tolerance
       int k = 0;
-      while (k < ma && res[k] <= tol * bup) ++k;
+      while (k < ma && res[k] <= kLockMargin * tol * bup) ++k;
       k = k / 4 * 4;
       if (k >= 8) {
         TRY(copy_cols(B.V, pa, 0, Vl, ldl, nl, N, k, st));

@@ -190,3 +190,49 @@ def test_bspmm_planned_same_bits(core, d, dtype, b):
     got = core.bspmm(ip, ix, vals, cu(X, dtype), Z=cu(Z, dtype), alpha=0.7, beta=-0.3, gamma=1.9, plan=plan)
     tol = 1e-12 if dtype == torch.float64 else 2e-5
     np.testing.assert_allclose(got.cpu().double().numpy(), want, atol=tol * np.abs(want).max())
+
+
+@pytest.mark.parametrize("D,n,k", [(20, 3001, 10), (33, 2500, 15), (64, 4100, 15), (64, 700, 1), (48, 1500, 60)])
+def test_knn_tensor_core_screen(core, D, n, k):
+    """The tensor-core screen (16 < D <= 64: block-centred split-TF32
+    distances, certified bound) gives the oracle's exact neighbour lists and
+    the SIMT screen's (RVGP_KNN_TC=0): a cloud near a 3-dimensional manifold
+    embedded in D dimensions, tiles cut short (n not a multiple of 128), two
+    duplicated points and a pair at exactly equal distances."""
+    import os
+    rng = np.random.default_rng(D * 1000 + n)
+    t = rng.uniform(0, 3, (n, 3))
+    Q, _ = np.linalg.qr(rng.standard_normal((D, D)))
+    X = np.concatenate([np.sin(t), np.cos(t)], axis=1) @ Q[:6] + 0.01 * rng.standard_normal((n, D))
+    X[5] = X[17]
+    X[40] = X[17]
+    X[41] = 2 * X[42] - X[43]  # 42 is the midpoint of 41 and 43
+    idx = core.knn(cu(X), k).cpu().numpy()
+    old = os.environ.get("RVGP_KNN_TC")
+    os.environ["RVGP_KNN_TC"] = "0"
+    try:
+        idx0 = core.knn(cu(X), k).cpu().numpy()
+    finally:
+        if old is None:
+            del os.environ["RVGP_KNN_TC"]
+        else:
+            os.environ["RVGP_KNN_TC"] = old
+    assert np.array_equal(idx, idx0)
+    assert np.array_equal(idx, O.knn(X, k))
+
+
+def test_knn_tensor_core_certifies_manifold_rows(core):
+    """On manifold data (the Swiss roll in R^64) the tensor-core screen's
+    certificate settles almost every row: at most 1 % go to the exact scan."""
+    from rvgp_gb300.workloads import make_points
+    X = make_points("swissroll64", 20000, seed=4)
+    idx = core.knn(cu(X), 15).cpu().numpy()
+    rows = core.lib().rvgp_knn_fallback_rows(len(X), 64, 15, core.ptr(core.knn.last_ws), core.stream())
+    assert 0 <= rows <= 200
+    sample = np.random.default_rng(0).choice(len(X), 300, replace=False)
+    d = np.zeros((300, len(X)))
+    for j in range(X.shape[1]):  # coordinates summed in order, as the contract states
+        d += (X[sample, j, None] - X[None, :, j]) ** 2
+    d[np.arange(300), sample] = np.inf
+    ref = np.argsort(d, axis=1, kind="stable")[:, :15]
+    assert np.array_equal(idx[sample], ref)
