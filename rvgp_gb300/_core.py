@@ -327,7 +327,7 @@ def eigsh(indptr, indices, vals64, vals32=None, m=10, mode="mixed", tol=None, to
     evecs = torch.empty((N, m), dtype=torch.float64, device=dev)
     stats = (ctypes.c_int * 16)()
     if tol32 is None:  # the FP32 stage's residual tolerance (relative to the Gershgorin bound)
-        tol32 = float(os.environ.get("RVGP_EIG_TOL32", "1e-5"))
+        tol32 = float(os.environ.get("RVGP_EIG_TOL32", "4e-6"))
     if tol is None:  # mixed: stop at the FP32 stage's accuracy; fp64: ARPACK-level residuals
         tol = tol32 if imode == 1 else 1e-11
     L = lib()

@@ -716,7 +716,11 @@ int copy_cols(const float* src, int lds, int c0, float* dst, int ldd, int d0, lo
 // filter degree still bounds the gain of the lowest Ritz value overall
 // (locked or not), as without locking.  On return B.V is the N x p block
 // [locked | active] (ld p), theta / res the matching values.
-constexpr double kLockMargin = 0.1;  // lock at a tenth of the convergence tolerance
+// lock at a tenth of the convergence tolerance (RVGP_EIG_LOCK_MARGIN overrides)
+double lock_margin() {
+  const char* e = getenv("RVGP_EIG_LOCK_MARGIN");
+  return e ? atof(e) : 0.1;
+}
 
 int iterate_locked(const Problem& P, Block<float>& B, float* Vl, int ldl, Small& s, Stats& stt, double bup,
                    double tol, int max_iter, int first_deg, double range, std::vector<double>& theta,
@@ -762,7 +766,8 @@ int iterate_locked(const Problem& P, Block<float>& B, float* Vl, int ldl, Small&
       // a locked vector is never polished again: lock only those whose
       // residual is well below the convergence tolerance
       int k = 0;
-      while (k < ma && res[k] <= kLockMargin * tol * bup) ++k;
+      const double lm = lock_margin();
+      while (k < ma && res[k] <= lm * tol * bup) ++k;
       k = k / 4 * 4;
       if (k >= 8) {
         TRY(copy_cols(B.V, pa, 0, Vl, ldl, nl, N, k, st));

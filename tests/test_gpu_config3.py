@@ -1,0 +1,67 @@
+"""GPU: the headline workload at full size, the Swiss roll in R^64 with
+n = 100 000, k = 15, m = 500 (20 % training rows, 200 Adam steps): the
+neighbour lists of a sample of rows are exact, the mixed form's Lc
+eigenpairs pass their residual test, and the mixed form agrees with the FP64
+form: eigenvalues, largest principal angle per cluster of the eigenvalues,
+posterior mean (the headline criterion, 1e-4) and log marginal likelihood.
+One pass of each form (about a minute)."""
+import os
+import sys
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import ROOT
+
+pytestmark = pytest.mark.gpu
+
+sys.path.insert(0, ROOT)
+
+
+@pytest.fixture(scope="module")
+def runs():
+    from rvgp_gb300 import _core
+    _core.require_cuda()
+    import bench
+    wl = dict(bench.WORKLOADS["swissroll64_n100000_k15_m500"])
+    X, train, test = bench.make_inputs(wl)
+    V = bench.make_field(X, wl)
+    Xd = torch.as_tensor(X, device="cuda")
+    out = {}
+    for precision in ("mixed", "fp64"):
+        keep = {}
+        mean, _ = bench.pipeline(Xd, V, train, test, wl, precision, keep=keep)
+        torch.cuda.synchronize()
+        out[precision] = (keep, mean)
+    return X, out, bench
+
+
+def test_knn_sample_rows_exact(runs):
+    X, _, _ = runs
+    from rvgp_gb300 import _core
+    idx = _core.knn(torch.as_tensor(X, device="cuda"), 15).cpu().numpy()
+    sample = np.random.default_rng(1).choice(len(X), 200, replace=False)
+    dist = np.zeros((200, len(X)))
+    for j in range(X.shape[1]):  # coordinates summed in order
+        dist += (X[sample, j, None] - X[None, :, j]) ** 2
+    dist[np.arange(200), sample] = np.inf
+    ref = np.argsort(dist, axis=1, kind="stable")[:, :15]
+    assert np.array_equal(idx[sample], ref)
+
+
+def test_mixed_eigenpairs_converged(runs):
+    _, out, _ = runs
+    info = out["mixed"][0]["data"]._dev.eig_info_Lc
+    assert info["converged"] == 500 and info["tensor_cores"]
+
+
+def test_mixed_matches_fp64(runs):
+    _, out, bench = runs
+    keep_m, mean_m = out["mixed"]
+    keep_64, mean_64 = out["fp64"]
+    e = bench.error_statements(keep_m, keep_64, mean_m, mean_64)
+    assert e["posterior_mean_rel_err"] <= 1e-4
+    assert e["eigenvalue_abs_err_over_max_Lc"] <= 1e-4
+    assert e["principal_angle_sin_whole_space_Lc"] <= 5e-2
+    assert e["rel_delta_lml"] <= 1e-5

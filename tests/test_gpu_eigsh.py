@@ -104,16 +104,22 @@ def test_eigsh_locking(core):
     L = O.laplacian(ip, ix, n)
     ev_ref, V_ref = O.spectrum_shift_invert(L, m)
     args = (cu(ip, torch.int32), cu(ix, torch.int32), cu(L.data))
-    ev, V, info = core.eigsh(*args, m=m, mode="mixed", scale=1.0)
-    old = os.environ.get("RVGP_EIG_LOCK")
-    os.environ["RVGP_EIG_LOCK"] = "0"
-    try:
-        ev0, V0, info0 = core.eigsh(*args, m=m, mode="mixed", scale=1.0)
-    finally:
-        if old is None:
-            del os.environ["RVGP_EIG_LOCK"]
-        else:
-            os.environ["RVGP_EIG_LOCK"] = old
+
+    def solve(env):
+        saved = {k: os.environ.get(k) for k in env}
+        os.environ.update(env)
+        try:
+            return core.eigsh(*args, m=m, mode="mixed", scale=1.0)
+        finally:
+            for k, v in saved.items():
+                if v is None:
+                    del os.environ[k]
+                else:
+                    os.environ[k] = v
+
+    # lock at the tolerance itself so that this size locks vectors
+    ev, V, info = solve({"RVGP_EIG_LOCK_MARGIN": "1.0"})
+    ev0, V0, info0 = solve({"RVGP_EIG_LOCK": "0"})
     assert info["locked"] > 0 and info0["locked"] == 0
     assert info["converged"] == m and info0["converged"] == m
     top = ev_ref.max()
