@@ -25,6 +25,7 @@
 #include "knn_top.cuh"
 #include <float.h>
 #include <limits.h>
+#include <algorithm>
 #include <mutex>
 
 namespace rvgp {
@@ -107,10 +108,14 @@ __global__ void prep_radius(const double* __restrict__ part_r2, int nblk, double
 
 template <int DP, int KC>
 __global__ void __launch_bounds__(kQB) knn_screen(const float* __restrict__ Xf, int n, int nsplit,
-                                                  float* __restrict__ part_d, int* __restrict__ part_i) {
+                                                  float* __restrict__ part_d, int* __restrict__ part_i,
+                                                  const int* __restrict__ qlist, const int* __restrict__ nq) {
   constexpr int kTile = kTileElems / DP;
   __shared__ float tile[kTile * DP];
-  const int q = blockIdx.x * kQB + threadIdx.x;
+  // every query, or the nq[0] queries of qlist (the rows another screen's
+  // certificate could not settle)
+  const int qi = blockIdx.x * kQB + threadIdx.x;
+  const int q = qlist ? (qi < *nq ? qlist[qi] : n) : qi;
   const int split = blockIdx.y;
   const long long chunk = ((long long)n + nsplit - 1) / nsplit;
   const int c0 = (int)min((long long)n, split * chunk);
@@ -197,9 +202,10 @@ __global__ void knn_finish(const double* __restrict__ X, int n, int D, int DP, i
                            const float* __restrict__ part_d, const int* __restrict__ part_i,
                            const double* __restrict__ radius, int* __restrict__ out_idx,
                            int* __restrict__ nflag, int* __restrict__ flag_list, const float* __restrict__ r2q,
-                           const int* __restrict__ tcerr) {
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= n) return;
+                           const int* __restrict__ tcerr, const int* __restrict__ qlist, const int* __restrict__ nq) {
+  const int qi = blockIdx.x * blockDim.x + threadIdx.x;
+  if (qlist ? qi >= *nq : qi >= n) return;
+  const int q = qlist ? qlist[qi] : qi;
   TopList L;
   L.init(kc);
   const size_t base = (size_t)q * nsplit * kc;
@@ -325,20 +331,32 @@ int kc_bucket(int k) {
 }
 
 template <int KC>
-void launch_screen(int DP, dim3 grid, cudaStream_t st, const float* Xf, int n, int nsplit, float* pd, int* pi) {
+void launch_screen(int DP, dim3 grid, cudaStream_t st, const float* Xf, int n, int nsplit, float* pd, int* pi,
+                   const int* qlist = nullptr, const int* nq = nullptr) {
   switch (DP) {
-    case 4: knn_screen<4, KC><<<grid, kQB, 0, st>>>(Xf, n, nsplit, pd, pi); break;
-    case 8: knn_screen<8, KC><<<grid, kQB, 0, st>>>(Xf, n, nsplit, pd, pi); break;
-    case 16: knn_screen<16, KC><<<grid, kQB, 0, st>>>(Xf, n, nsplit, pd, pi); break;
-    case 32: knn_screen<32, KC><<<grid, kQB, 0, st>>>(Xf, n, nsplit, pd, pi); break;
-    case 64: knn_screen<64, KC><<<grid, kQB, 0, st>>>(Xf, n, nsplit, pd, pi); break;
-    default: knn_screen<128, KC><<<grid, kQB, 0, st>>>(Xf, n, nsplit, pd, pi); break;
+    case 4: knn_screen<4, KC><<<grid, kQB, 0, st>>>(Xf, n, nsplit, pd, pi, qlist, nq); break;
+    case 8: knn_screen<8, KC><<<grid, kQB, 0, st>>>(Xf, n, nsplit, pd, pi, qlist, nq); break;
+    case 16: knn_screen<16, KC><<<grid, kQB, 0, st>>>(Xf, n, nsplit, pd, pi, qlist, nq); break;
+    case 32: knn_screen<32, KC><<<grid, kQB, 0, st>>>(Xf, n, nsplit, pd, pi, qlist, nq); break;
+    case 64: knn_screen<64, KC><<<grid, kQB, 0, st>>>(Xf, n, nsplit, pd, pi, qlist, nq); break;
+    default: knn_screen<128, KC><<<grid, kQB, 0, st>>>(Xf, n, nsplit, pd, pi, qlist, nq); break;
+  }
+}
+
+void screen_kc(int kc, int DP, dim3 grid, cudaStream_t st, const float* Xf, int n, int nsplit, float* pd, int* pi,
+               const int* qlist = nullptr, const int* nq = nullptr) {
+  switch (kc) {
+    case 16: launch_screen<16>(DP, grid, st, Xf, n, nsplit, pd, pi, qlist, nq); break;
+    case 32: launch_screen<32>(DP, grid, st, Xf, n, nsplit, pd, pi, qlist, nq); break;
+    case 48: launch_screen<48>(DP, grid, st, Xf, n, nsplit, pd, pi, qlist, nq); break;
+    default: launch_screen<72>(DP, grid, st, Xf, n, nsplit, pd, pi, qlist, nq); break;
   }
 }
 
 struct KnnPlan {
   int DP, kc, nsplit, nblk_prep;
-  bool tc;  // tensor-core screen (knn_tc.cu)
+  bool tc;      // tensor-core screen (knn_tc.cu)
+  int nsplit2;  // the SIMT screen's splits (its own plan, or the re-screen of the rows the TC certificate leaves)
 };
 
 // The tensor-core screen for 16 < D <= 64 (RVGP_KNN_TC=0, or
@@ -357,6 +375,7 @@ KnnPlan plan(int n, int D, int k, bool allow_tc = true) {
   p.tc = allow_tc && knn_tc_enabled(D);
   int qblocks = ceil_div(n, kQB);
   p.nsplit = max(1, min(16, ceil_div((p.tc ? 1 : 4) * num_sms(), qblocks)));
+  p.nsplit2 = max(1, min(16, ceil_div(4 * num_sms(), qblocks)));
   p.nblk_prep = min(num_sms() * 2, max(1, ceil_div(n, 256)));
   return p;
 }
@@ -364,7 +383,7 @@ KnnPlan plan(int n, int D, int k, bool allow_tc = true) {
 struct KnnBufs {
   double *part_mm, *centre, *part_r2, *radius;
   float *Xf, *part_d, *r2q;
-  int *part_i, *nflag, *flag_list, *order, *rank, *tcerr;
+  int *part_i, *nflag, *flag_list, *order, *rank, *tcerr, *nflag2, *flag_list2;
   void* lo_ws;
   size_t lo_bytes;
 };
@@ -382,7 +401,7 @@ namespace {
 KnnBufs carve(Workspace& ws, const KnnPlan& p, int n, int D) {
   KnnBufs b;
   b.r2q = nullptr;
-  b.order = b.rank = b.tcerr = nullptr;
+  b.order = b.rank = b.tcerr = b.nflag2 = b.flag_list2 = nullptr;
   b.lo_ws = nullptr;
   b.lo_bytes = 0;
   b.part_mm = ws.take<double>((size_t)p.nblk_prep * D * 2);
@@ -390,11 +409,14 @@ KnnBufs carve(Workspace& ws, const KnnPlan& p, int n, int D) {
   b.part_r2 = ws.take<double>(p.nblk_prep);
   b.radius = ws.take<double>(1);
   b.Xf = ws.take<float>((size_t)n * p.DP);
-  b.part_d = ws.take<float>((size_t)n * p.nsplit * p.kc);
-  b.part_i = ws.take<int>((size_t)n * p.nsplit * p.kc);
+  const int ns = std::max(p.nsplit, p.nsplit2);
+  b.part_d = ws.take<float>((size_t)n * ns * p.kc);
+  b.part_i = ws.take<int>((size_t)n * ns * p.kc);
   b.nflag = ws.take<int>(1);
   b.flag_list = ws.take<int>(n);
   if (p.tc) {
+    b.nflag2 = ws.take<int>(1);
+    b.flag_list2 = ws.take<int>(n);
     b.r2q = ws.take<float>(n);
     b.order = ws.take<int>(n);
     b.rank = ws.take<int>(n);
@@ -453,20 +475,32 @@ static int knn_impl(const double* X, int n, int D, int k, int* idx, void* worksp
     // queries in the locality order: a block of 128 is a compact patch
     TRY_RC(rvgp_locality_order(X, n, D, b.order, b.rank, b.lo_ws, b.lo_bytes, stream));
     cudaMemsetAsync(b.tcerr, 0, sizeof(int), st);
+    cudaMemsetAsync(b.nflag2, 0, sizeof(int), st);
     TRY_RC(knn_tc_screen_launch(p.DP, p.kc, b.Xf, n, b.order, p.nsplit, b.part_d, b.part_i, b.r2q, b.tcerr, st));
+    rvgp::note_launch();
+    knn_finish<<<ceil_div(n, 128), 128, 0, st>>>(X, n, D, p.DP, k, p.kc, p.nsplit, b.part_d, b.part_i, b.radius, idx,
+                                                 b.nflag, b.flag_list, b.r2q, b.tcerr, nullptr, nullptr);
+    // rows the tensor-core certificate could not settle (a query block
+    // straddling a jump of the Morton curve): the SIMT screen, whose
+    // direct-difference certificate does not depend on the block, then the
+    // exact scan for what remains
+    const int nsplit2 = p.nsplit2;
+    rvgp::note_launch();
+    screen_kc(p.kc, p.DP, dim3(ceil_div(n, kQB), nsplit2), st, b.Xf, n, nsplit2, b.part_d, b.part_i, b.flag_list,
+              b.nflag);
+    rvgp::note_launch();
+    knn_finish<<<ceil_div(n, 128), 128, 0, st>>>(X, n, D, p.DP, k, p.kc, nsplit2, b.part_d, b.part_i, b.radius, idx,
+                                                 b.nflag2, b.flag_list2, nullptr, nullptr, b.flag_list, b.nflag);
+    rvgp::note_launch(); knn_fallback<<<num_sms(), kFbThreads, 0, st>>>(X, n, D, k, b.nflag2, b.flag_list2, idx);
   } else {
     dim3 grid(ceil_div(n, kQB), p.nsplit);
     rvgp::note_launch();
-    switch (p.kc) {
-      case 16: launch_screen<16>(p.DP, grid, st, b.Xf, n, p.nsplit, b.part_d, b.part_i); break;
-      case 32: launch_screen<32>(p.DP, grid, st, b.Xf, n, p.nsplit, b.part_d, b.part_i); break;
-      case 48: launch_screen<48>(p.DP, grid, st, b.Xf, n, p.nsplit, b.part_d, b.part_i); break;
-      default: launch_screen<72>(p.DP, grid, st, b.Xf, n, p.nsplit, b.part_d, b.part_i); break;
-    }
+    screen_kc(p.kc, p.DP, grid, st, b.Xf, n, p.nsplit, b.part_d, b.part_i);
+    rvgp::note_launch();
+    knn_finish<<<ceil_div(n, 128), 128, 0, st>>>(X, n, D, p.DP, k, p.kc, p.nsplit, b.part_d, b.part_i, b.radius, idx,
+                                                 b.nflag, b.flag_list, nullptr, nullptr, nullptr, nullptr);
+    rvgp::note_launch(); knn_fallback<<<num_sms(), kFbThreads, 0, st>>>(X, n, D, k, b.nflag, b.flag_list, idx);
   }
-  rvgp::note_launch(); knn_finish<<<ceil_div(n, 128), 128, 0, st>>>(X, n, D, p.DP, k, p.kc, p.nsplit, b.part_d, b.part_i,
-                                                                 b.radius, idx, b.nflag, b.flag_list, b.r2q, b.tcerr);
-  rvgp::note_launch(); knn_fallback<<<num_sms(), kFbThreads, 0, st>>>(X, n, D, k, b.nflag, b.flag_list, idx);
   RVGP_LAUNCH_CHECK("rvgp_knn");
   return RVGP_OK;
 }
@@ -546,6 +580,7 @@ RVGP_API int rvgp_knn_fallback_rows(int n, int D, int k, void* workspace, void* 
   Workspace ws(workspace, SIZE_MAX);
   KnnBufs b = carve(ws, plan(n, D, k), n, D);
   int h = -1;
-  if (read_back(&h, b.nflag, sizeof(int), as_stream(stream)) != cudaSuccess) return -1;
+  // the tensor-core path's exact scan takes the rows its SIMT re-screen left
+  if (read_back(&h, b.nflag2 ? b.nflag2 : b.nflag, sizeof(int), as_stream(stream)) != cudaSuccess) return -1;
   return h;
 }

@@ -28,6 +28,11 @@ def runs():
     X, train, test = bench.make_inputs(wl)
     V = bench.make_field(X, wl)
     Xd = torch.as_tensor(X, device="cuda")
+    # the reference binds the positive minimum of σ_f only to parameters made
+    # after the process's first fit (GPflow's set_default_positive_minimum,
+    # RVGP/main.py:30 vs :52): one warm-up fit puts both forms under it, as
+    # the benchmark's warm-up steps do
+    bench.pipeline(Xd, V, train, test, wl, "mixed")
     out = {}
     for precision in ("mixed", "fp64"):
         keep = {}
