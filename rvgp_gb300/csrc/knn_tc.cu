@@ -184,10 +184,24 @@ __global__ void __launch_bounds__(kTThreads, 1)
       }
     }
   } else if (warp < 8) {
-    // ---- producers: thread r stages candidate row r of each tile
+    // ---- producers: thread r stages candidate row r of each tile; the next
+    // tile's row is loaded into registers before this one's buffer wait
     const int r = tid - 128;
+    float4 nxt[NS * 8];
+    auto fetch = [&](int t) {
+      const int cand = c0 + t * kTC + r;
+#pragma unroll
+      for (int e = 0; e < NS * 8; ++e)
+        nxt[e] = cand < c1 ? *reinterpret_cast<const float4*>(Xf + (size_t)cand * DP + e * 4)
+                           : make_float4(0.f, 0.f, 0.f, 0.f);
+    };
+    if (ntiles > 0) fetch(0);
     for (int t = 0; t < ntiles; ++t) {
       const int b = t & 1;
+      float4 cur[NS * 8];
+#pragma unroll
+      for (int e = 0; e < NS * 8; ++e) cur[e] = nxt[e];
+      if (t + 1 < ntiles) fetch(t + 1);
       if (t >= 2) {
         bool ok = true;
         for (long long w = 0; !tc::mbar_try_wait(&bar[4 + b], ((t - 2) >> 1) & 1); ++w)
@@ -200,8 +214,7 @@ __global__ void __launch_bounds__(kTThreads, 1)
           break;
         }
       }
-      const int cand = c0 + t * kTC + r;
-      const bool on = cand < c1;
+      const bool on = c0 + t * kTC + r < c1;
       uint8_t* hi = Bb + 2 * b * OPB;
       uint8_t* lo = hi + OPB;
       float nrm = 0.f;
@@ -209,16 +222,14 @@ __global__ void __launch_bounds__(kTThreads, 1)
       for (int s = 0; s < NS; ++s)
 #pragma unroll
         for (int kc = 0; kc < 8; ++kc) {
-          float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-          if (on) {
-            const float4 y = *reinterpret_cast<const float4*>(Xf + (size_t)cand * DP + s * 32 + kc * 4);
-            const int j = s * 32 + kc * 4;
-            v = make_float4(y.x - cen[j], y.y - cen[j + 1], y.z - cen[j + 2], y.w - cen[j + 3]);
-            nrm = fmaf(v.x, v.x, nrm);
-            nrm = fmaf(v.y, v.y, nrm);
-            nrm = fmaf(v.z, v.z, nrm);
-            nrm = fmaf(v.w, v.w, nrm);
-          }
+          const float4 y = cur[s * 8 + kc];
+          const int j = s * 32 + kc * 4;
+          const float4 v = on ? make_float4(y.x - cen[j], y.y - cen[j + 1], y.z - cen[j + 2], y.w - cen[j + 3])
+                              : make_float4(0.f, 0.f, 0.f, 0.f);
+          nrm = fmaf(v.x, v.x, nrm);
+          nrm = fmaf(v.y, v.y, nrm);
+          nrm = fmaf(v.z, v.z, nrm);
+          nrm = fmaf(v.w, v.w, nrm);
           put4(hi, lo, r, s, kc, v);
         }
       cn[b][r] = on ? nrm : FLT_MAX;
