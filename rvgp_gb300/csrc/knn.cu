@@ -114,6 +114,7 @@ __global__ void __launch_bounds__(kQB) knn_screen(const float* __restrict__ Xf, 
   __shared__ float tile[kTile * DP];
   // every query, or the nq[0] queries of qlist (the rows another screen's
   // certificate could not settle)
+  if (qlist && (int)(blockIdx.x * kQB) >= *nq) return;  // no listed row in this CTA (uniform)
   const int qi = blockIdx.x * kQB + threadIdx.x;
   const int q = qlist ? (qi < *nq ? qlist[qi] : n) : qi;
   const int split = blockIdx.y;

@@ -79,17 +79,17 @@ class data:
         # The eigenpairs of L feed nothing downstream (the kernel is built on
         # those of Lc), so they are computed on a second stream by a host
         # thread, off the critical path; every reader of evals_L / evecs_L
-        # waits for them (wait()).  In the mixed form the solve is deferred
-        # until the GP fit's one-CTA kernel occupies a single SM (fit() starts
-        # it then), so it fills the other SMs instead of competing with the Lc
-        # eigensolve; the FP64 form starts it at once.
+        # waits for them (wait()).  It starts at once, beside the gauges and the
+        # Lc eigensolve (their latency-bound phases leave SMs idle; measured on
+        # the Swiss roll at n = 100 000: 0.638 s per step against 0.663 s when
+        # deferred to the GP fit); RVGP_EIG_L_START=fit defers it to fit().
         m = n if n_eigenpairs is None else min(int(n_eigenpairs), n)
         mode = "mixed" if precision == "mixed" else "fp64"
         # nvtx: name of an NVTX range the concurrent eigensolve's host thread
         # opens around its work, so that a profiler that selects kernels by the
         # caller's range also sees the kernels of that thread
         self._eig_L = self._prepare_eig_L(dev, n, m, mode, eig_tol, seed, timings, nvtx)
-        if mode == "fp64" or os.environ.get("RVGP_EIG_L_START", "") == "now":
+        if os.environ.get("RVGP_EIG_L_START", "now") != "fit":
             self._release_eig_L()
 
         _log(verbose, "Fit tangent spaces")
