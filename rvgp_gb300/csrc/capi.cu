@@ -1,4 +1,6 @@
 // Error state and library-level entry points of librvgp_gb300.
+#include <mutex>
+#include <map>
 #include "common.cuh"
 #include <string.h>
 #include <atomic>
@@ -52,3 +54,19 @@ RVGP_API int rvgp_abi_version(void) { return 1; }
 
 // Kernels launched by this library since it was loaded (all host threads).
 RVGP_API long long rvgp_launch_count(void) { return rvgp::g_launches.load(std::memory_order_relaxed); }
+
+namespace rvgp {
+cudaError_t raise_dyn_smem(const void* fn, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<int, const void*>, size_t> set;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(mu);
+  size_t& cur = set[{dev, fn}];
+  if (bytes <= cur) return cudaSuccess;
+  const cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess) cur = bytes;
+  return e;
+}
+}  // namespace rvgp
+

@@ -210,7 +210,7 @@ size_t cholqr32_workspace(int p) {
 int chol32_gram(const double* G, int p, float* L, float* Mb, float* d, float first_order, int* info,
                 cudaStream_t st) {
   const size_t smem = chol_smem(p);
-  if (cudaFuncSetAttribute(chol32_gram_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+  if (raise_dyn_smem((const void*)chol32_gram_kernel, (size_t)(smem)) != cudaSuccess) {
     set_error("chol32_gram: cannot reserve %zu bytes of shared memory", smem);
     return RVGP_ELAUNCH;
   }
@@ -224,7 +224,7 @@ int trsm_rows_f32(float* V, int ldv, long long N, int p, const float* L, const f
   RVGP_CHECK_ARG(p % 4 == 0 && ldv % 4 == 0 && (uintptr_t)V % 16 == 0 && (uintptr_t)L % 16 == 0,
                  "trsm_rows_f32: p=%d and ldv=%d must be multiples of 4, V and L 16-byte aligned", p, ldv);
   const size_t smem = trsm_smem(p);
-  if (cudaFuncSetAttribute(trsm_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+  if (raise_dyn_smem((const void*)trsm_rows_kernel, (size_t)(smem)) != cudaSuccess) {
     set_error("trsm_rows_f32: cannot reserve %zu bytes of shared memory", smem);
     return RVGP_ELAUNCH;
   }

@@ -65,6 +65,12 @@ inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 // its workspace need on the device it runs on.
 int num_sms();
 
+// Raise (never lower) a kernel's dynamic shared-memory limit on the current
+// device: the limit is a per-function setting shared by every host thread,
+// so two threads launching one kernel with different sizes must not set it
+// down under each other's launch.
+cudaError_t raise_dyn_smem(const void* fn, size_t bytes);
+
 }  // namespace rvgp
 
 #define RVGP_CHECK_ARG(cond, ...)        \

@@ -940,7 +940,9 @@ static int eigsh_impl(const int* indptr, const int* indices, const double* vals6
 
   std::vector<double> theta, res;
   int nconv = 0;
-  const int first_deg = 12;
+  // degree of the first filter, from the random block (RVGP_EIG_FIRST_DEG overrides)
+  const char* fd = getenv("RVGP_EIG_FIRST_DEG");
+  const int first_deg = fd ? std::max(2, std::min(200, atoi(fd))) : 12;
   if (mode == 1) {
     rvgp::note_launch(); random_block<float><<<ceil_div(N * p, 256), 256, 0, st>>>(L.f.V, N, p, p, seed, perm, DB);
     // locked vectors live in the FP64 scratch block, unused until the refinement

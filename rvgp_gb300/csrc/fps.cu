@@ -808,7 +808,7 @@ RVGP_API int rvgp_fps_spatial(const double* X, int n, int D, int N_max, int star
     const size_t smem = fps_sp_smem(n, D);
 #define RVGP_FPS_SP(Dv)                                                                                        \
   case Dv: {                                                                                                   \
-    if (cudaFuncSetAttribute(fps_sp_select<Dv>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=    \
+    if (raise_dyn_smem((const void*)fps_sp_select<Dv>, (size_t)(smem)) !=    \
         cudaSuccess)                                                                                           \
       return check_launch("rvgp_fps_spatial");                                                                 \
     rvgp::note_launch();                                                                                       \

@@ -1207,7 +1207,7 @@ int gp_fit_cluster_max_m() {
     const int m = nb * FB;
     const size_t smem = clayout(m, nb).total;
     if (smem + 512 > (size_t)optin) break;
-    if (cudaFuncSetAttribute(gp_fit_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+    if (raise_dyn_smem((const void*)gp_fit_cluster, (size_t)(smem)) != cudaSuccess) {
       cudaGetLastError();
       break;
     }
@@ -1232,8 +1232,7 @@ int gp_fit_cluster_max_m() {
   // the wide form, for 16 < nb <= 32, when the 16-block form fits
   if (best == kMaxCluster * FB && wlayout().total + 1024 <= (size_t)optin &&
       cudaFuncSetAttribute(gp_fit_cluster_wide, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess &&
-      cudaFuncSetAttribute(gp_fit_cluster_wide, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)wlayout().total) == cudaSuccess) {
+      raise_dyn_smem((const void*)gp_fit_cluster_wide, wlayout().total) == cudaSuccess) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(kWideCS);
     cfg.blockDim = dim3(kNT);
@@ -1279,7 +1278,7 @@ int gp_fit_cluster_launch(const float* C32, const double* C, const double* b, co
       return RVGP_EARG;
     }
     const size_t smem = wlayout().total;
-    if (cudaFuncSetAttribute(gp_fit_cluster_wide, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+    if (raise_dyn_smem((const void*)gp_fit_cluster_wide, (size_t)(smem)) !=
         cudaSuccess) {
       set_error("gp_fit_cluster: cannot reserve %zu bytes of shared memory", smem);
       return RVGP_ELAUNCH;
@@ -1307,7 +1306,7 @@ int gp_fit_cluster_launch(const float* C32, const double* C, const double* b, co
     return RVGP_OK;
   }
   const size_t smem = clayout(m, nb).total;
-  if (cudaFuncSetAttribute(gp_fit_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+  if (raise_dyn_smem((const void*)gp_fit_cluster, (size_t)(smem)) != cudaSuccess) {
     set_error("gp_fit_cluster: cannot reserve %zu bytes of shared memory", smem);
     return RVGP_ELAUNCH;
   }

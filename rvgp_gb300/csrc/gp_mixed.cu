@@ -586,7 +586,7 @@ RVGP_API int rvgp_gp_fit_adam_mixed_launch(const double* C, const double* b, con
     return RVGP_OK;
   }
   const size_t smem = layout(m).total;
-  if (cudaFuncSetAttribute(gp_fit_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+  if (raise_dyn_smem((const void*)gp_fit_f32, (size_t)(smem)) != cudaSuccess) {
     set_error("rvgp_gp_fit_adam_mixed: cannot reserve %zu bytes of shared memory", smem);
     return RVGP_ELAUNCH;
   }
@@ -705,7 +705,7 @@ RVGP_API int rvgp_gp_fit_restarts(const double* C, const double* b, const double
                                  beta2, eps, theta_out, hist, status, st, R, 1, scratch));
   } else {
     const size_t smem = layout(m).total;
-    if (cudaFuncSetAttribute(gp_fit_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+    if (raise_dyn_smem((const void*)gp_fit_f32, (size_t)(smem)) != cudaSuccess) {
       set_error("rvgp_gp_fit_restarts: cannot reserve %zu bytes of shared memory", smem);
       return RVGP_ELAUNCH;
     }

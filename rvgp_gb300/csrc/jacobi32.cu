@@ -282,7 +282,7 @@ int jacobi32_eigh(const float* H, int p, float* w, float* V, int max_sweeps, dou
   int* perm = W.take<int>(p);
   int* sw = W.take<int>(4);
   const size_t smem = jac_smem(p);
-  if (cudaFuncSetAttribute(jacobi32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+  if (raise_dyn_smem((const void*)jacobi32_kernel, (size_t)(smem)) != cudaSuccess) {
     set_error("jacobi32_eigh: cannot reserve %zu bytes of shared memory", smem);
     return RVGP_ELAUNCH;
   }

@@ -287,8 +287,7 @@ int launch_dp(int kc, dim3 grid, size_t smem, cudaStream_t st, const float* Xf, 
               float* pd, int* pi, float* r2q, int* err) {
 #define RVGP_KTC(KCv)                                                                                              \
   case KCv: {                                                                                                      \
-    if (cudaFuncSetAttribute(knn_tc_screen<DP, KCv>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=   \
-        cudaSuccess)                                                                                               \
+    if (raise_dyn_smem((const void*)knn_tc_screen<DP, KCv>, smem) != cudaSuccess)                               \
       return check_launch("knn_tc_screen");                                                                        \
     rvgp::note_launch();                                                                                           \
     knn_tc_screen<DP, KCv><<<grid, kTThreads, smem, st>>>(Xf, n, order, nsplit, pd, pi, r2q, err);                 \

@@ -719,7 +719,7 @@ constexpr int kJB = 32;
 constexpr int kJP = 2 * kJB;   // pair width
 constexpr int kJLd = kJP + 1;  // shared-memory row stride
 constexpr int kJbThreads = 1024;
-constexpr int kJbMaxInner = 2;
+constexpr int kJbMaxInner = 2;  // default inner sweeps per pair solve
 
 __device__ __forceinline__ void jrot32(float a, float b, float c, float& cs, float& sn) {
   cs = 1.f;
@@ -764,7 +764,7 @@ __device__ __forceinline__ double cta_sum(double v, double* red) {
 
 // Diagonalise the 64 x 64 principal submatrix of the pair (I, J); Q (64 x 64, global) <- its factor.
 __device__ void jb_pair_solve(const float* __restrict__ H, int P, int I, int J, float* __restrict__ Qg, double tol2,
-                              float* sm, double* red) {
+                              float* sm, double* red, int max_inner) {
   float* S = sm;
   float* S2 = S + kJP * kJLd;
   float* Q = S2 + kJP * kJLd;
@@ -779,7 +779,7 @@ __device__ void jb_pair_solve(const float* __restrict__ H, int P, int I, int J, 
     Q[r * kJLd + c] = r == c ? 1.f : 0.f;
   }
   __syncthreads();
-  for (int sweep = 0; sweep < kJbMaxInner; ++sweep) {
+  for (int sweep = 0; sweep < max_inner; ++sweep) {
     double off = 0.0, tot = 0.0;
     for (int e = tid; e < kJP * kJP; e += kJbThreads) {
       const double v = S[(e / kJP) * kJLd + e % kJP];
@@ -901,7 +901,7 @@ __device__ void jb_apply_tile(float* __restrict__ X, int P, int rI, int rJ, int 
 __global__ void __launch_bounds__(kJbThreads) jacobi_block32(const float* __restrict__ H, int p, int P, float* Hp,
                                                              float* Vp, float* Qbuf, double* part, int max_sweeps,
                                                              double tol2, unsigned int* bar, int* err,
-                                                             int* sweeps_out, float* w, float* Vout) {
+                                                             int* sweeps_out, float* w, float* Vout, int max_inner) {
   extern __shared__ __align__(16) unsigned char jsm[];
   __shared__ double red[kJbThreads / 32];
   __shared__ double s_off, s_tot;
@@ -952,7 +952,7 @@ __global__ void __launch_bounds__(kJbThreads) jacobi_block32(const float* __rest
     for (int r = 0; r < nb - 1; ++r) {
       for (int k = blockIdx.x; k < npair; k += G) {
         const int2 pr = circle_pair(nb, r, k);
-        jb_pair_solve(Hp, P, pr.x, pr.y, Qbuf + (size_t)k * kJP * kJP, tol2, sm, red);
+        jb_pair_solve(Hp, P, pr.x, pr.y, Qbuf + (size_t)k * kJP * kJP, tol2, sm, red, max_inner);
         __syncthreads();
       }
       if (!grid_barrier(bar, err, G)) return;
@@ -1102,7 +1102,7 @@ int cholesky(T* A, int lda, int p, int* info, cudaStream_t st) {
   if (smem <= kSmallCholSmem) {
     static std::atomic<bool> attr_set{false};  // per kernel; setting it twice is harmless
     if (!attr_set.load()) {
-      if (cudaFuncSetAttribute(potrf_small<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmallCholSmem) !=
+      if (raise_dyn_smem((const void*)potrf_small<T>, (size_t)(kSmallCholSmem)) !=
           cudaSuccess) {
         set_error("cholesky: cannot reserve %zu bytes of shared memory", kSmallCholSmem);
         return RVGP_ELAUNCH;
@@ -1265,7 +1265,7 @@ int jacobi_block_eigh(const float* H, int p, float* w, float* V, int max_sweeps,
   unsigned int* bar = W.take<unsigned int>(kMaxCoopGrid + 1);
   int* flags = W.take<int>(2);
   const size_t smem = jacobi_block_smem();
-  if (cudaFuncSetAttribute(jacobi_block32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+  if (raise_dyn_smem((const void*)jacobi_block32, (size_t)(smem)) != cudaSuccess)
     return check_launch("jacobi_block_eigh");
   const int npair = P / kJP;
   const int ntask = npair * npair + (P / kJP) * npair;
@@ -1281,7 +1281,10 @@ int jacobi_block_eigh(const float* H, int p, float* w, float* V, int max_sweeps,
   double t2 = tol * tol;
   int* err_dev = flags;
   int* sweeps_dev = flags + 1;
-  void* args[] = {(void*)&H, &pv, &Pv, &Hp, &Vp, &Qb, &part, &ms, &t2, &bar, &err_dev, &sweeps_dev, &w, &V};
+  // inner sweeps per 64 x 64 pair solve (RVGP_JACOBI_BLOCK_INNER overrides)
+  const char* ie = getenv("RVGP_JACOBI_BLOCK_INNER");
+  int inner = ie ? std::max(1, std::min(8, atoi(ie))) : kJbMaxInner;
+  void* args[] = {(void*)&H, &pv, &Pv, &Hp, &Vp, &Qb, &part, &ms, &t2, &bar, &err_dev, &sweeps_dev, &w, &V, &inner};
   rvgp::note_launch();
   cudaError_t e = cudaLaunchCooperativeKernel((const void*)jacobi_block32, dim3(G), dim3(kJbThreads), args, smem, st);
   if (e != cudaSuccess) {

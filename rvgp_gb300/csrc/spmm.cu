@@ -718,8 +718,7 @@ int launch_tiled_db(int n, const PlanView& pv, const int* indptr, const int* ind
   constexpr int SEG = kSegBytes / (int)sizeof(T);
   const int nt = plan_tiles(n), nch = ceil_div(b, SEG);
   const size_t smem = (size_t)kHaloRows / DB * DB * kSegBytes;
-  if (cudaFuncSetAttribute(bspmm_tiled_kernel<T, DB, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-      cudaSuccess)
+  if (raise_dyn_smem((const void*)bspmm_tiled_kernel<T, DB, 2>, smem) != cudaSuccess)
     return check_launch("rvgp_bspmm (tiled)");
   rvgp::note_launch();
   bspmm_tiled_kernel<T, DB, 2><<<(unsigned)((long long)nt * nch), 256, smem, st>>>(

@@ -475,7 +475,7 @@ GramPlan gram_plan(long long N, int p) {
 }
 
 int set_smem(const void* fn, size_t bytes, const char* what) {
-  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess) {
+  if (raise_dyn_smem((const void*)fn, (size_t)(bytes)) != cudaSuccess) {
     set_error("%s: cannot reserve %zu bytes of shared memory", what, bytes);
     return RVGP_ELAUNCH;
   }

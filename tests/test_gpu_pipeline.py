@@ -163,12 +163,18 @@ def test_fit_optimises_likelihood(RVGP):
     assert mean.shape == (10, 3) and var.shape == (10, 3) and np.all(var >= 0)
 
 
-def test_deferred_eigsh_L_beside_mixed_fit(RVGP):
-    """Mixed form: the eigensolve of L waits for the GP fit's one-CTA kernel
-    and runs beside it; its eigenpairs equal a direct solve's."""
+def test_deferred_eigsh_L_beside_mixed_fit(RVGP, monkeypatch):
+    """The concurrent eigensolve of L, deferred to the GP fit
+    (RVGP_EIG_L_START=fit): it waits for the fit and runs beside it; by
+    default it starts at once.  Either way its eigenpairs equal a direct
+    solve's."""
     from rvgp_gb300 import _core
     g = load_golden("torus")
     m = int(g["m"])
+    d0 = RVGP.create_data_object(g["X"], n_neighbors=20, n_eigenpairs=m, precision="mixed", verbose=False)
+    assert d0._eig_L["thread"] is not None  # started by create_data_object
+    ev0 = d0.evals_L
+    monkeypatch.setenv("RVGP_EIG_L_START", "fit")
     d = RVGP.create_data_object(g["X"], n_neighbors=20, n_eigenpairs=m, precision="mixed", verbose=False)
     assert d._eig_L["thread"] is None  # not started by create_data_object
     d.random_vector_field(seed=2)
@@ -188,6 +194,7 @@ def test_deferred_eigsh_L_beside_mixed_fit(RVGP):
     # a data object whose L pairs are read before any fit solves them on demand
     d2 = RVGP.create_data_object(g["X"], n_neighbors=20, n_eigenpairs=m, precision="mixed", verbose=False)
     np.testing.assert_allclose(d2.evals_L, ev, rtol=0, atol=0)
+    np.testing.assert_allclose(ev0, ev, rtol=0, atol=0)
 
 
 @pytest.mark.parametrize("B", [1, 6])
