@@ -282,7 +282,8 @@ def spmm_roofline(d, wl, peaks, flush, reps=20):
     alone with CUDA events on the launching stream, L2 flushed before it.  The
     matrix is the Morton-renumbered one the eigensolver multiplies by, and the
     product the launch tuner's variant (what the eigensolver runs); the
-    shared-memory tiled plan is timed beside it for reference."""
+    product through the matrix's plan (the tuner then also tries the grouped
+    and tiled forms) is timed beside it for reference."""
     import torch
     from rvgp_gb300 import _core
     dev = d._dev
@@ -323,12 +324,14 @@ def spmm_roofline(d, wl, peaks, flush, reps=20):
     names = {0: f"bspmm_kernel<float,{k},G>", 1: f"bspmm_chunked_kernel<float,{k},2>",
              2: f"bspmm_chunked_kernel<float,{k},4>", 3: f"bspmm_tile_kernel<float,{k},2>",
              4: f"bspmm_tile_kernel<float,{k},4>", 5: f"bspmm_chunked_kernel<float,{k},2,L2>",
-             6: f"bspmm_tile_kernel<float,{k},2,L2>", 7: f"bspmm_chunked_kernel<float,{k},2,rowblocks>"}
+             6: f"bspmm_tile_kernel<float,{k},2,L2>", 7: f"bspmm_chunked_kernel<float,{k},2,rowblocks>",
+             8: f"bspmm_tiled_kernel<float,{k},2>", 9: f"bspmm_group_kernel<float,{k},2>",
+             10: f"bspmm_group_kernel<float,{k},1>"}
     return {"kernel": f"{names.get(variant, '?')} (Chebyshev step, Lc x block; launch tuner's variant {variant})",
             "bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
             "frac": round(achieved / peaks["hbm_gbs"], 4),
             "traffic": SPMM_TRAFFIC.get((n, k, p, E)), "algorithmic_bytes": int(alg),
-            "avg_launch_us": round(t * 1e6, 2), "smem_plan_avg_launch_us": round(t_plan * 1e6, 2),
+            "avg_launch_us": round(t * 1e6, 2), "planned_avg_launch_us": round(t_plan * 1e6, 2),
             "block_width": p, "l2": "flushed before every timed launch"}
 
 

@@ -95,13 +95,17 @@ int rvgp_bspmm_f32(int n, int DB, const int* indptr, const int* indices, const f
 int rvgp_bspmm_f64(int n, int DB, const int* indptr, const int* indices, const double* vals, const double* X,
                    double* Y, const double* Z, int b, int ld, double alpha, double beta, double gamma, void* stream);
 
-/* Tiled form of the same product for a matrix used many times (the
+/* Planned forms of the same product for a matrix used many times (the
  * eigensolver's filter, RVGP/geometry.py:73): a plan built once per matrix
- * (per tile of 32 block rows, the distinct columns its entries reference and
- * each entry's position among them) lets every CTA stage the rows it gathers
- * in shared memory.  nnz = indptr[n].  Same bits as rvgp_bspmm_*; a null plan
- * runs rvgp_bspmm_*.  rvgp_eigsh builds one itself when its workspace has
- * rvgp_spmm_plan_bytes + 256 bytes beyond rvgp_eigsh_workspace. */
+ * holds, per group of 4 consecutive block rows, the merged list of their
+ * columns (each shared neighbour's rows are gathered once for the group),
+ * and per tile of 32 block rows the distinct columns its entries reference
+ * (a shared-memory staged form).  The launch tuner picks among these and the
+ * plain variants.  nnz = indptr[n].  Same bits as rvgp_bspmm_*; a null plan
+ * runs rvgp_bspmm_*.  On request (RVGP_SPMM_PLAN=1) rvgp_eigsh builds one
+ * itself when its workspace has rvgp_spmm_plan_bytes + 256 bytes beyond
+ * rvgp_eigsh_workspace; on GB300 both planned forms measure slower than the
+ * chunked plain variant at the eigensolver's shapes. */
 size_t rvgp_spmm_plan_bytes(int n, int DB, long long nnz);
 int rvgp_spmm_plan_build(int n, int DB, const int* indptr, const int* indices, long long nnz, void* plan,
                          size_t plan_bytes, void* stream);

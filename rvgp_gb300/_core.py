@@ -262,9 +262,10 @@ def connections(T, d, indptr, indices, want_R=True, want64=True, want32=True):
 
 # ---------------------------------------------------------------------------- products
 def spmm_plan(indptr, indices, DB=1):
-    """The tiled product's plan of a block-CSR matrix (a byte tensor): per tile
-    of 32 block rows its halo of distinct columns and every entry's position
-    in it.  Build once per matrix, pass to ``bspmm(..., plan=)``."""
+    """The planned product's plan of a block-CSR matrix (a byte tensor): per
+    group of 4 block rows the merged list of their columns, per tile of 32
+    block rows its halo of distinct columns and every entry's position in it.
+    Build once per matrix, pass to ``bspmm(..., plan=)``."""
     n = indptr.numel() - 1
     nnz = indices.numel()
     L = lib()
@@ -277,7 +278,8 @@ def spmm_plan(indptr, indices, DB=1):
 
 def bspmm(indptr, indices, vals, X, Y=None, Z=None, alpha=1.0, beta=0.0, gamma=0.0, plan=None):
     """Y = alpha*(A X) + beta*X + gamma*Z for block-CSR A with square blocks
-    (tiled through ``plan`` when given: the same bits)."""
+    (through ``plan`` when given, grouped / tiled forms included: the same
+    bits)."""
     n = indptr.numel() - 1
     DB = 1 if vals.dim() == 1 else vals.shape[-1]
     rows, b = X.shape

@@ -911,12 +911,13 @@ static int eigsh_impl(const int* indptr, const int* indices, const double* vals6
   cudaMemsetAsync(s.tc_err, 0, sizeof(int), st);
   Problem P{n, DB, N, indptr, indices, vals64, vals32, m, p, SpmmPlan{}};
   Stats stt;
-  // the shared-memory tiled product's plan, in the workspace beyond `need`
-  // when the caller sized it for one (rvgp_spmm_plan_bytes), on request
-  // (RVGP_SPMM_TILED=1): on GB300 its staging costs more than the L1 reuse
-  // of the tile-mapped variant the tuner can pick
+  // the product's plan (grouped and tiled forms, spmm.cu), in the workspace
+  // beyond `need` when the caller sized it for one (rvgp_spmm_plan_bytes), on
+  // request (RVGP_SPMM_PLAN=1): on GB300 both planned forms are slower than
+  // the chunked variant (fewer resident warps, fewer gathers in flight), so
+  // by default the tuner chooses among the plain variants only
   {
-    const char* e = getenv("RVGP_SPMM_TILED");
+    const char* e = getenv("RVGP_SPMM_PLAN");
     int nnz = 0;
     if (e && e[0] == '1' && ws_bytes > need) {
       if (read_back(&nnz, indptr + n, sizeof(int), st) != cudaSuccess) return check_launch("rvgp_eigsh");

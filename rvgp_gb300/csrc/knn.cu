@@ -106,18 +106,25 @@ __global__ void prep_radius(const double* __restrict__ part_r2, int nblk, double
   *radius = sqrt(m) * (1.0 + 1e-12);
 }
 
+// Splits per listed row when the screen runs over a list of nlist rows (the
+// rows another screen's certificate could not settle): as many as the part
+// buffers hold (cap_rows row-lists), at most smax.  The screen and the finish
+// compute it alike from the device-side count.
+__device__ __forceinline__ int list_splits(int nlist, long long cap_rows, int smax) {
+  const long long s = nlist > 0 ? cap_rows / nlist : smax;
+  return (int)max(1ll, min((long long)smax, s));
+}
+
+// One CTA's work: queries qi0 .. qi0 + kQB - 1 (list slots in list mode)
+// against the candidates of split `split` of nsplit; their lists at
+// part[(qi * nsplit + split) * KC] in list mode, else at the query's row.
 template <int DP, int KC>
-__global__ void __launch_bounds__(kQB) knn_screen(const float* __restrict__ Xf, int n, int nsplit,
-                                                  float* __restrict__ part_d, int* __restrict__ part_i,
-                                                  const int* __restrict__ qlist, const int* __restrict__ nq) {
+__device__ __forceinline__ void screen_block(float* tile, const float* __restrict__ Xf, int n, int qi0, int split,
+                                             int nsplit, float* __restrict__ part_d, int* __restrict__ part_i,
+                                             const int* __restrict__ qlist, int nlist) {
   constexpr int kTile = kTileElems / DP;
-  __shared__ float tile[kTile * DP];
-  // every query, or the nq[0] queries of qlist (the rows another screen's
-  // certificate could not settle)
-  if (qlist && (int)(blockIdx.x * kQB) >= *nq) return;  // no listed row in this CTA (uniform)
-  const int qi = blockIdx.x * kQB + threadIdx.x;
-  const int q = qlist ? (qi < *nq ? qlist[qi] : n) : qi;
-  const int split = blockIdx.y;
+  const int qi = qi0 + threadIdx.x;
+  const int q = qlist ? (qi < nlist ? qlist[qi] : n) : qi;
   const long long chunk = ((long long)n + nsplit - 1) / nsplit;
   const int c0 = (int)min((long long)n, split * chunk);
   const int c1 = (int)min((long long)n, c0 + chunk);
@@ -145,12 +152,36 @@ __global__ void __launch_bounds__(kQB) knn_screen(const float* __restrict__ Xf, 
     }
   }
   if (q < n) {
-    const size_t base = ((size_t)q * nsplit + split) * KC;
+    const size_t base = ((size_t)(qlist ? qi : q) * nsplit + split) * KC;
 #pragma unroll
     for (int r = 0; r < KC; ++r) {
       part_d[base + r] = L.d[r];
       part_i[base + r] = L.i[r];
     }
+  }
+}
+
+// Every query (grid ceil(n / kQB) x nsplit), or, with qlist, the nq[0] listed
+// rows: each CTA then takes (list block, split) items in turn, with
+// list_splits(nq[0], cap_rows, nsplit) splits per row, so a short list still
+// spreads over the whole GPU.
+template <int DP, int KC>
+__global__ void __launch_bounds__(kQB) knn_screen(const float* __restrict__ Xf, int n, int nsplit,
+                                                  float* __restrict__ part_d, int* __restrict__ part_i,
+                                                  const int* __restrict__ qlist, const int* __restrict__ nq,
+                                                  long long cap_rows) {
+  constexpr int kTile = kTileElems / DP;
+  __shared__ float tile[kTile * DP];
+  if (!qlist) {
+    screen_block<DP, KC>(tile, Xf, n, blockIdx.x * kQB, blockIdx.y, nsplit, part_d, part_i, nullptr, 0);
+    return;
+  }
+  const int nlist = *nq;
+  const int S = list_splits(nlist, cap_rows, nsplit);
+  const long long items = (long long)((nlist + kQB - 1) / kQB) * S;
+  for (long long w = blockIdx.x; w < items; w += gridDim.x) {  // uniform in the CTA
+    __syncthreads();  // the previous item's tile reads are done
+    screen_block<DP, KC>(tile, Xf, n, (int)(w / S) * kQB, (int)(w % S), S, part_d, part_i, qlist, nlist);
   }
 }
 
@@ -203,13 +234,15 @@ __global__ void knn_finish(const double* __restrict__ X, int n, int D, int DP, i
                            const float* __restrict__ part_d, const int* __restrict__ part_i,
                            const double* __restrict__ radius, int* __restrict__ out_idx,
                            int* __restrict__ nflag, int* __restrict__ flag_list, const float* __restrict__ r2q,
-                           const int* __restrict__ tcerr, const int* __restrict__ qlist, const int* __restrict__ nq) {
+                           const int* __restrict__ tcerr, const int* __restrict__ qlist, const int* __restrict__ nq,
+                           long long cap_rows) {
   const int qi = blockIdx.x * blockDim.x + threadIdx.x;
   if (qlist ? qi >= *nq : qi >= n) return;
   const int q = qlist ? qlist[qi] : qi;
+  if (qlist) nsplit = list_splits(*nq, cap_rows, nsplit);  // the list screen's layout
   TopList L;
   L.init(kc);
-  const size_t base = (size_t)q * nsplit * kc;
+  const size_t base = (size_t)(qlist ? qi : q) * nsplit * kc;
   int total = 0;
   for (int e = 0; e < nsplit * kc; ++e) {
     int ci = part_i[base + e];
@@ -333,31 +366,31 @@ int kc_bucket(int k) {
 
 template <int KC>
 void launch_screen(int DP, dim3 grid, cudaStream_t st, const float* Xf, int n, int nsplit, float* pd, int* pi,
-                   const int* qlist = nullptr, const int* nq = nullptr) {
+                   const int* qlist = nullptr, const int* nq = nullptr, long long cap = 0) {
   switch (DP) {
-    case 4: knn_screen<4, KC><<<grid, kQB, 0, st>>>(Xf, n, nsplit, pd, pi, qlist, nq); break;
-    case 8: knn_screen<8, KC><<<grid, kQB, 0, st>>>(Xf, n, nsplit, pd, pi, qlist, nq); break;
-    case 16: knn_screen<16, KC><<<grid, kQB, 0, st>>>(Xf, n, nsplit, pd, pi, qlist, nq); break;
-    case 32: knn_screen<32, KC><<<grid, kQB, 0, st>>>(Xf, n, nsplit, pd, pi, qlist, nq); break;
-    case 64: knn_screen<64, KC><<<grid, kQB, 0, st>>>(Xf, n, nsplit, pd, pi, qlist, nq); break;
-    default: knn_screen<128, KC><<<grid, kQB, 0, st>>>(Xf, n, nsplit, pd, pi, qlist, nq); break;
+    case 4: knn_screen<4, KC><<<grid, kQB, 0, st>>>(Xf, n, nsplit, pd, pi, qlist, nq, cap); break;
+    case 8: knn_screen<8, KC><<<grid, kQB, 0, st>>>(Xf, n, nsplit, pd, pi, qlist, nq, cap); break;
+    case 16: knn_screen<16, KC><<<grid, kQB, 0, st>>>(Xf, n, nsplit, pd, pi, qlist, nq, cap); break;
+    case 32: knn_screen<32, KC><<<grid, kQB, 0, st>>>(Xf, n, nsplit, pd, pi, qlist, nq, cap); break;
+    case 64: knn_screen<64, KC><<<grid, kQB, 0, st>>>(Xf, n, nsplit, pd, pi, qlist, nq, cap); break;
+    default: knn_screen<128, KC><<<grid, kQB, 0, st>>>(Xf, n, nsplit, pd, pi, qlist, nq, cap); break;
   }
 }
 
 void screen_kc(int kc, int DP, dim3 grid, cudaStream_t st, const float* Xf, int n, int nsplit, float* pd, int* pi,
-               const int* qlist = nullptr, const int* nq = nullptr) {
+               const int* qlist = nullptr, const int* nq = nullptr, long long cap = 0) {
   switch (kc) {
-    case 16: launch_screen<16>(DP, grid, st, Xf, n, nsplit, pd, pi, qlist, nq); break;
-    case 32: launch_screen<32>(DP, grid, st, Xf, n, nsplit, pd, pi, qlist, nq); break;
-    case 48: launch_screen<48>(DP, grid, st, Xf, n, nsplit, pd, pi, qlist, nq); break;
-    default: launch_screen<72>(DP, grid, st, Xf, n, nsplit, pd, pi, qlist, nq); break;
+    case 16: launch_screen<16>(DP, grid, st, Xf, n, nsplit, pd, pi, qlist, nq, cap); break;
+    case 32: launch_screen<32>(DP, grid, st, Xf, n, nsplit, pd, pi, qlist, nq, cap); break;
+    case 48: launch_screen<48>(DP, grid, st, Xf, n, nsplit, pd, pi, qlist, nq, cap); break;
+    default: launch_screen<72>(DP, grid, st, Xf, n, nsplit, pd, pi, qlist, nq, cap); break;
   }
 }
 
 struct KnnPlan {
   int DP, kc, nsplit, nblk_prep;
   bool tc;      // tensor-core screen (knn_tc.cu)
-  int nsplit2;  // the SIMT screen's splits (its own plan, or the re-screen of the rows the TC certificate leaves)
+  int nsplit2;  // part-buffer room per row beside nsplit (the re-screen's list layout uses it)
 };
 
 // The tensor-core screen for 16 < D <= 64 (RVGP_KNN_TC=0, or
@@ -480,18 +513,21 @@ static int knn_impl(const double* X, int n, int D, int k, int* idx, void* worksp
     TRY_RC(knn_tc_screen_launch(p.DP, p.kc, b.Xf, n, b.order, p.nsplit, b.part_d, b.part_i, b.r2q, b.tcerr, st));
     rvgp::note_launch();
     knn_finish<<<ceil_div(n, 128), 128, 0, st>>>(X, n, D, p.DP, k, p.kc, p.nsplit, b.part_d, b.part_i, b.radius, idx,
-                                                 b.nflag, b.flag_list, b.r2q, b.tcerr, nullptr, nullptr);
+                                                 b.nflag, b.flag_list, b.r2q, b.tcerr, nullptr, nullptr, 0);
     // rows the tensor-core certificate could not settle (a query block
     // straddling a jump of the Morton curve): the SIMT screen, whose
     // direct-difference certificate does not depend on the block, then the
-    // exact scan for what remains
-    const int nsplit2 = p.nsplit2;
+    // exact scan for what remains.  The list is usually short (tens of rows
+    // at n = 100 000), so its rows get up to one split per SM, as many as the
+    // part buffers hold (list_splits).
+    const int smax = num_sms();
+    const long long cap = (long long)n * std::max(p.nsplit, p.nsplit2);
+    const int gx = (int)std::min<long long>((long long)ceil_div(n, kQB) * smax, 4ll * num_sms());
     rvgp::note_launch();
-    screen_kc(p.kc, p.DP, dim3(ceil_div(n, kQB), nsplit2), st, b.Xf, n, nsplit2, b.part_d, b.part_i, b.flag_list,
-              b.nflag);
+    screen_kc(p.kc, p.DP, dim3(gx, 1), st, b.Xf, n, smax, b.part_d, b.part_i, b.flag_list, b.nflag, cap);
     rvgp::note_launch();
-    knn_finish<<<ceil_div(n, 128), 128, 0, st>>>(X, n, D, p.DP, k, p.kc, nsplit2, b.part_d, b.part_i, b.radius, idx,
-                                                 b.nflag2, b.flag_list2, nullptr, nullptr, b.flag_list, b.nflag);
+    knn_finish<<<ceil_div(n, 128), 128, 0, st>>>(X, n, D, p.DP, k, p.kc, smax, b.part_d, b.part_i, b.radius, idx,
+                                                 b.nflag2, b.flag_list2, nullptr, nullptr, b.flag_list, b.nflag, cap);
     rvgp::note_launch(); knn_fallback<<<num_sms(), kFbThreads, 0, st>>>(X, n, D, k, b.nflag2, b.flag_list2, idx);
   } else {
     dim3 grid(ceil_div(n, kQB), p.nsplit);
@@ -499,7 +535,7 @@ static int knn_impl(const double* X, int n, int D, int k, int* idx, void* worksp
     screen_kc(p.kc, p.DP, grid, st, b.Xf, n, p.nsplit, b.part_d, b.part_i);
     rvgp::note_launch();
     knn_finish<<<ceil_div(n, 128), 128, 0, st>>>(X, n, D, p.DP, k, p.kc, p.nsplit, b.part_d, b.part_i, b.radius, idx,
-                                                 b.nflag, b.flag_list, nullptr, nullptr, nullptr, nullptr);
+                                                 b.nflag, b.flag_list, nullptr, nullptr, nullptr, nullptr, 0);
     rvgp::note_launch(); knn_fallback<<<num_sms(), kFbThreads, 0, st>>>(X, n, D, k, b.nflag, b.flag_list, idx);
   }
   RVGP_LAUNCH_CHECK("rvgp_knn");

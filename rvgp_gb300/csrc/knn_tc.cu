@@ -6,7 +6,13 @@
 // of its 128 queries), and x'·y' from split-TF32 tcgen05 MMAs (x' = hi + lo,
 // A B ≈ Ahi Bhi + Ahi Blo + Alo Bhi, FP32 accumulators in TMEM).  Queries are
 // taken in the locality (Morton) order, so a block is a compact patch and
-// |x'| is its radius scale.
+// |x'| is its radius scale.  Candidates are taken in the same order and each
+// split visits its tiles outwards from the query block's own position, so the
+// first tiles hold most of a block's neighbours: the kc-th distance, the
+// insertion threshold, is tight after a few tiles and later insertions (a
+// divergent register shift of the whole list) are rare.  Which candidates
+// tie at the kc-th value may depend on the visiting order; the certificate
+// below does not.
 //
 // Error bound (per pair, on the FP32 centred values): the dropped lo·lo term
 // and the TF32 truncation of lo, ≤ 1.2e-6 |x'||y'|; at most 3·64 FP32
@@ -19,7 +25,8 @@
 // (4.01 u R, as for the SIMT screen) and per-query |x'|² (r2q).
 //
 // CTA: 288 threads.  Warps 0-3: epilogue, thread i owns query row i = TMEM
-// lane i and its register top-kc list; warps 4-7: producers, thread r stages
+// lane i and its register top-kc list (of positions in the order, turned
+// into point indices when written); warps 4-7: producers, thread r stages
 // candidate row r of a tile (centred, split, 128-byte-swizzled K-major) and
 // its squared norm; warp 8: one thread issues the MMAs.  Two candidate
 // buffers and two TMEM accumulators; mbarriers: staged[b] (4 producer
@@ -40,6 +47,18 @@ constexpr int kTThreads = 288;
 constexpr uint32_t kTTmemCols = 256;  // two 128-column accumulators
 constexpr long long kTWait = 1ll << 22;
 constexpr int kSlabBytes = kTQ * 128;  // one 32-element K slab of a 128-row operand
+
+// Tile visited i-th of ntiles: t0, t0+1, t0-1, t0+2, ... then the rest of
+// the longer side.
+__device__ __forceinline__ int tile_of(int i, int t0, int ntiles) {
+  const int m = min(t0, ntiles - 1 - t0);
+  if (i <= 2 * m) {
+    const int j = (i + 1) >> 1;
+    return (i & 1) ? t0 + j : t0 - j;
+  }
+  const int r = i - 2 * m;
+  return (ntiles - 1 - t0 > t0) ? t0 + m + r : t0 - m - r;
+}
 
 __device__ __forceinline__ uint8_t* align1k(uint8_t* p) {
   const uint32_t a = tc::smem_u32(p);
@@ -79,12 +98,16 @@ __global__ void __launch_bounds__(kTThreads, 1)
   uint8_t* Ahi = smem;
   uint8_t* Alo = Ahi + OPB;
   uint8_t* Bb = Alo + OPB;                    // buffer b: hi at Bb + 2 b OPB, lo after it
+                                              // then the epilogue's hit staging
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int qb = blockIdx.x, split = blockIdx.y;
   const int q0 = qb * kTQ, nq = min(kTQ, n - q0);
   const long long chunk = ((long long)n + nsplit - 1) / nsplit;
   const int c0 = (int)min((long long)n, split * chunk), c1 = (int)min((long long)n, c0 + chunk);
   const int ntiles = (c1 - c0 + kTC - 1) / kTC;
+  // first tile: the one holding this block's own first position, or the
+  // split's end nearest to it
+  const int t0 = ntiles > 0 ? max(0, min(ntiles - 1, (q0 - c0) / kTC)) : 0;
 
   if (warp == 0) {
     tc::tmem_alloc(&tmem_slot, kTTmemCols);
@@ -142,6 +165,9 @@ __global__ void __launch_bounds__(kTThreads, 1)
     // ---- epilogue: thread i = TMEM lane i
     RegTop<KC> L;
     L.init();
+    // columns per TMEM load: 32 where the k-list leaves the registers
+    constexpr int kCh = KC > 48 ? 8 : 32;
+    float* sd = reinterpret_cast<float*>(Bb + 4 * OPB);  // kCh x 128 hit staging
     const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
     for (int t = 0; t < ntiles; ++t) {
       const int b = t & 1;
@@ -159,16 +185,39 @@ __global__ void __launch_bounds__(kTThreads, 1)
         break;
       }
       tc::fence_after_sync();
-      const int cb = c0 + t * kTC;
+      const int cb = c0 + tile_of(t, t0, ntiles) * kTC;
+      const int qp = q0 + tid;  // this query's own position
 #pragma unroll 1
-      for (int c = 0; c < kTC; c += 8) {
-        float v[8];
-        tc::tmem_ld8(trow + (uint32_t)(b * kTC + c), v);
+      for (int c = 0; c < kTC; c += kCh) {
+        float v[kCh];
+        if constexpr (kCh == 32) tc::tmem_ld32(trow + (uint32_t)(b * kTC + c), v);
+        else tc::tmem_ld8(trow + (uint32_t)(b * kTC + c), v);
+        // unrolled: f² and a mask of the columns under the threshold at the
+        // chunk's start (a superset of those that insert)
+        const float wst = L.worst();
+        uint32_t mask = 0;
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
-          const int cand = cb + c + u;
-          const float d2 = qn + cn[b][c + u] - 2.f * v[u];
-          if (d2 < L.worst() && cand < c1 && cand != q) L.insert(d2, cand);
+        for (int g = 0; g < kCh / 4; ++g) {
+          const float4 nv = *reinterpret_cast<const float4*>(&cn[b][c + 4 * g]);
+          const float nn[4] = {nv.x, nv.y, nv.z, nv.w};
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            v[4 * g + u] = fmaf(-2.f, v[4 * g + u], qn + nn[u]);
+            mask |= (v[4 * g + u] < wst ? 1u : 0u) << (4 * g + u);
+          }
+        }
+        // rare after the first tiles: the hits go through shared memory to a
+        // loop with one insertion site (one copy of the register shift)
+        if (mask) {
+#pragma unroll
+          for (int j = 0; j < kCh; ++j) sd[j * kTQ + tid] = v[j];
+          while (mask) {
+            const int j = __ffs(mask) - 1;
+            mask &= mask - 1;
+            const float d2 = sd[j * kTQ + tid];
+            const int cand = cb + c + j;
+            if (d2 < L.worst() && cand < c1 && cand != qp) L.insert(d2, cand);
+          }
         }
       }
       tc::fence_before_sync();
@@ -180,28 +229,24 @@ __global__ void __launch_bounds__(kTThreads, 1)
 #pragma unroll
       for (int r = 0; r < KC; ++r) {
         part_d[base + r] = L.d[r];
-        part_i[base + r] = L.i[r];
+        part_i[base + r] = L.i[r] >= 0 ? order[L.i[r]] : -1;
       }
     }
   } else if (warp < 8) {
     // ---- producers: thread r stages candidate row r of each tile; the next
-    // tile's row is loaded into registers before this one's buffer wait
+    // tile's row is loaded into registers before the next buffer wait
     const int r = tid - 128;
     float4 nxt[NS * 8];
     auto fetch = [&](int t) {
-      const int cand = c0 + t * kTC + r;
+      const int cand = c0 + tile_of(t, t0, ntiles) * kTC + r;
+      const float* y = cand < c1 ? Xf + (size_t)order[cand] * DP : nullptr;
 #pragma unroll
       for (int e = 0; e < NS * 8; ++e)
-        nxt[e] = cand < c1 ? *reinterpret_cast<const float4*>(Xf + (size_t)cand * DP + e * 4)
-                           : make_float4(0.f, 0.f, 0.f, 0.f);
+        nxt[e] = y ? *reinterpret_cast<const float4*>(y + e * 4) : make_float4(0.f, 0.f, 0.f, 0.f);
     };
     if (ntiles > 0) fetch(0);
     for (int t = 0; t < ntiles; ++t) {
       const int b = t & 1;
-      float4 cur[NS * 8];
-#pragma unroll
-      for (int e = 0; e < NS * 8; ++e) cur[e] = nxt[e];
-      if (t + 1 < ntiles) fetch(t + 1);
       if (t >= 2) {
         bool ok = true;
         for (long long w = 0; !tc::mbar_try_wait(&bar[4 + b], ((t - 2) >> 1) & 1); ++w)
@@ -214,7 +259,7 @@ __global__ void __launch_bounds__(kTThreads, 1)
           break;
         }
       }
-      const bool on = c0 + t * kTC + r < c1;
+      const bool on = c0 + tile_of(t, t0, ntiles) * kTC + r < c1;
       uint8_t* hi = Bb + 2 * b * OPB;
       uint8_t* lo = hi + OPB;
       float nrm = 0.f;
@@ -222,7 +267,7 @@ __global__ void __launch_bounds__(kTThreads, 1)
       for (int s = 0; s < NS; ++s)
 #pragma unroll
         for (int kc = 0; kc < 8; ++kc) {
-          const float4 y = cur[s * 8 + kc];
+          const float4 y = nxt[s * 8 + kc];
           const int j = s * 32 + kc * 4;
           const float4 v = on ? make_float4(y.x - cen[j], y.y - cen[j + 1], y.z - cen[j + 2], y.w - cen[j + 3])
                               : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -236,6 +281,7 @@ __global__ void __launch_bounds__(kTThreads, 1)
       tc::fence_async_smem();
       __syncwarp();
       if (lane == 0) tc::mbar_arrive(&bar[b]);
+      if (t + 1 < ntiles) fetch(t + 1);  // in flight during the next buffer wait
     }
   } else if (lane == 0) {
     // ---- MMA issuer
@@ -310,7 +356,8 @@ int launch_dp(int kc, dim3 grid, size_t smem, cudaStream_t st, const float* Xf, 
 int knn_tc_screen_launch(int DP, int kc, const float* Xf, int n, const int* order, int nsplit, float* part_d,
                          int* part_i, float* r2q, int* err, cudaStream_t st) {
   const int NS = DP / 32;
-  const size_t smem = 1024 + (size_t)2 * NS * kSlabBytes * 3;  // A hi/lo + two B buffers of hi/lo
+  // A hi/lo + two B buffers of hi/lo + the epilogue's 32 x 128 hit staging
+  const size_t smem = 1024 + (size_t)2 * NS * kSlabBytes * 3 + (size_t)32 * kTQ * sizeof(float);
   dim3 grid((n + kTQ - 1) / kTQ, nsplit);
   if (DP == 32) return launch_dp<32>(kc, grid, smem, st, Xf, n, order, nsplit, part_d, part_i, r2q, err);
   return launch_dp<64>(kc, grid, smem, st, Xf, n, order, nsplit, part_d, part_i, r2q, err);

@@ -48,6 +48,39 @@ __global__ void bbox_kernel(const double* __restrict__ X, int n, int D, unsigned
   }
 }
 
+// The same with per-thread extremes (D <= 256): T = a multiple of D threads
+// per CTA and a grid stride that is one too, so every thread stays on one
+// coordinate; the CTA combines its threads in shared memory and then makes
+// one global atomic per coordinate (the per-element form above serialises on
+// 2 D addresses).
+__global__ void bbox_kernel_rows(const double* __restrict__ X, int n, int D, unsigned long long* __restrict__ mm) {
+  __shared__ unsigned long long smin[256], smax[256];
+  const int T = (blockDim.x / D) * D;
+  for (int j = threadIdx.x; j < D; j += blockDim.x) {
+    smin[j] = ~0ull;
+    smax[j] = 0ull;
+  }
+  __syncthreads();
+  if ((int)threadIdx.x < T) {
+    const long long start = (long long)blockIdx.x * T + threadIdx.x;
+    const long long stride = (long long)gridDim.x * T;
+    unsigned long long lo = ~0ull, hi = 0ull;
+    for (long long e = start; e < (long long)n * D; e += stride) {
+      const unsigned long long b = ordered_bits(X[e]);
+      lo = b < lo ? b : lo;
+      hi = b > hi ? b : hi;
+    }
+    const int j = (int)(start % D);
+    atomicMin(&smin[j], lo);
+    atomicMax(&smax[j], hi);
+  }
+  __syncthreads();
+  for (int j = threadIdx.x; j < D; j += blockDim.x) {
+    atomicMin(&mm[2 * j], smin[j]);
+    atomicMax(&mm[2 * j + 1], smax[j]);
+  }
+}
+
 __global__ void bbox_init(unsigned long long* mm, int D) {
   for (int j = threadIdx.x; j < D; j += blockDim.x) {
     mm[2 * j] = ~0ull;
@@ -203,7 +236,10 @@ RVGP_API int rvgp_locality_order(const double* X, int n, int D, int* perm, int* 
   rvgp::note_launch();
   bbox_init<<<1, 128, 0, st>>>(b.mm, D);
   rvgp::note_launch();
-  bbox_kernel<<<std::min(num_sms() * 4, ceil_div((long long)n * D, 256)), 256, 0, st>>>(X, n, D, b.mm);
+  if (D <= 256)
+    bbox_kernel_rows<<<std::min(num_sms() * 4, ceil_div((long long)n * D, 256)), 256, 0, st>>>(X, n, D, b.mm);
+  else
+    bbox_kernel<<<std::min(num_sms() * 4, ceil_div((long long)n * D, 256)), 256, 0, st>>>(X, n, D, b.mm);
   std::vector<unsigned long long> hm(2 * (size_t)D);
   if (read_back(hm.data(), b.mm, sizeof(unsigned long long) * 2 * D, st) != cudaSuccess) return check_launch("rvgp_locality_order");
   auto dec = [](unsigned long long v) {

@@ -439,26 +439,39 @@ bool overlaps(const void* a, const void* b, size_t bytes) {
 // tuner (autotune.cuh) picks one per shape class (RVGP_SPMM_VARIANT=v forces
 // one); the same bits come out of all eight.
 template <typename T>
-int launch(int n, int DB, const int* indptr, const int* indices, const T* vals, const T* X, T* Y, const T* Z, int b,
-           int ld, T alpha, T beta, T gamma, cudaStream_t st) {
+int run_variant(int v, int n, int DB, const int* indptr, const int* indices, const T* vals, const T* X, T* Y,
+                const T* Z, int b, int ld, T alpha, T beta, T gamma, cudaStream_t st) {
+  switch (v) {
+    case 0: return launch_rows<T>(n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
+    case 1: return launch_chunked<T, 2>(n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
+    case 2: return launch_chunked<T, 4>(n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
+    case 3: return launch_tile<T, 2>(n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
+    case 4: return launch_tile<T, 4>(n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
+    case 5: return launch_chunked<T, 2, true>(n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
+    case 6: return launch_tile<T, 2, true>(n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
+    default:
+      return launch_chunked<T, 2, false, true>(n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
+  }
+}
+
+template <typename T>
+int check_args(int DB, const T* X, const T* Y, const T* Z, int b, int ld) {
   constexpr int V = Vec<T>::V;
   RVGP_CHECK_ARG(b % V == 0 && ld % V == 0 && b <= ld, "rvgp_bspmm: b=%d and ld=%d must be multiples of %d", b, ld, V);
   RVGP_CHECK_ARG(((uintptr_t)X | (uintptr_t)Y | (uintptr_t)(Z ? Z : X)) % 16 == 0, "rvgp_bspmm: 16-byte alignment");
-  const int groups = b / V;
-  RVGP_CHECK_ARG(groups <= 32 * 16, "rvgp_bspmm: block width b=%d too large", b);
+  RVGP_CHECK_ARG(b / V <= 32 * 16, "rvgp_bspmm: block width b=%d too large", b);
   RVGP_CHECK_ARG(DB >= 1 && DB <= 4, "rvgp_bspmm: block size %d not supported (1..4)", DB);
+  return RVGP_OK;
+}
+
+template <typename T>
+int launch(int n, int DB, const int* indptr, const int* indices, const T* vals, const T* X, T* Y, const T* Z, int b,
+           int ld, T alpha, T beta, T gamma, cudaStream_t st) {
+  constexpr int V = Vec<T>::V;
+  if (int rc = check_args<T>(DB, X, Y, Z, b, ld)) return rc;
+  const int groups = b / V;
   auto run = [&](int v) -> int {
-    switch (v) {
-      case 0: return launch_rows<T>(n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
-      case 1: return launch_chunked<T, 2>(n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
-      case 2: return launch_chunked<T, 4>(n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
-      case 3: return launch_tile<T, 2>(n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
-      case 4: return launch_tile<T, 4>(n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
-      case 5: return launch_chunked<T, 2, true>(n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
-      case 6: return launch_tile<T, 2, true>(n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
-      default:
-        return launch_chunked<T, 2, false, true>(n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
-    }
+    return run_variant<T>(v, n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
   };
   int def = groups >= chunk_min_groups() ? 1 : 0;
   if (const char* fv = getenv("RVGP_SPMM_VARIANT")) def = std::min(7, std::max(0, atoi(fv)));  // tests: one variant
@@ -495,15 +508,35 @@ constexpr int kTileRows = 32;
 constexpr int kHaloRows = 576;      // halo rows x DB per tile (72 KB of 128-byte chunks)
 constexpr int kPlanMaxEntries = 2048;
 constexpr int kSegBytes = 128;
+constexpr int kGroupRows = 4;       // block rows per group of the grouped form
+constexpr int kMergeWindow = 64;    // look-ahead of the group merge
 
 __host__ __device__ inline int plan_hmax(int DB) { return kHaloRows / DB; }
 inline int plan_tiles(int n) { return (n + kTileRows - 1) / kTileRows; }
+inline int plan_groups(int n) { return (n + kGroupRows - 1) / kGroupRows; }
 
+// The plan holds both forms' data: per tile of kTileRows rows its halo and the
+// local column of every entry (tiled form); per group of kGroupRows rows the
+// merged neighbour list (grouped form).
 struct PlanView {
   int* tile_h;
   int* halo;
   unsigned short* lidx;
+  int* gcnt;  // merged entries of group g, at gcol[indptr[g * kGroupRows] ...]
+  int* gcol;  // nnz slots: the merged entry's block column
+  int* gidx;  // nnz x kGroupRows: per row of the group, its CSR entry at that column, or -1
 };
+
+size_t plan_bytes_needed(int n, int DB, long long nnz) {
+  Workspace ws(nullptr, 0);
+  ws.take<int>(plan_tiles(n));
+  ws.take<int>((size_t)plan_tiles(n) * plan_hmax(DB));
+  ws.take<unsigned short>((size_t)nnz);
+  ws.take<int>(plan_groups(n));
+  ws.take<int>((size_t)nnz);
+  ws.take<int>((size_t)nnz * kGroupRows);
+  return ws.used;
+}
 
 PlanView plan_view(void* plan, size_t bytes, int n, int DB, long long nnz) {
   Workspace ws(plan, bytes);
@@ -511,7 +544,204 @@ PlanView plan_view(void* plan, size_t bytes, int n, int DB, long long nnz) {
   v.tile_h = ws.take<int>(plan_tiles(n));
   v.halo = ws.take<int>((size_t)plan_tiles(n) * plan_hmax(DB));
   v.lidx = ws.take<unsigned short>((size_t)nnz);
+  v.gcnt = ws.take<int>(plan_groups(n));
+  v.gcol = ws.take<int>((size_t)nnz);
+  v.gidx = ws.take<int>((size_t)nnz * kGroupRows);
   return v;
+}
+
+// ------------------------------------------------------------ grouped form
+// The rows of a group (consecutive in the locality-preserving order) share
+// most of their neighbours: at k = 15 on a surface, 4 rows reference ~54 %
+// as many distinct block rows as entries.  The plan merges the group's CSR
+// rows into one list of columns, each with the entry of every row that has
+// it, by taking list heads only, so every row's entries stay in its CSR order
+// (any order of the input rows is valid; when the rows are sorted by one
+// key, as CSR rows are, the merge finds every shared column).  A head is
+// taken together with the equal heads of the other rows unless it occurs
+// further down one of them, in which case another head goes first; when every
+// head does (rows in conflicting orders), the first row's head goes alone.
+// The search looks kMergeWindow entries ahead (a hub row costs no more; a
+// match further down is only a missed share).  One thread per group; the
+// merged list of group g fills the group's own entry range, which it never
+// outgrows (each merged entry takes at least one).
+__global__ void __launch_bounds__(256) spmm_group_plan_kernel(int n, int ngroups, const int* __restrict__ indptr,
+                                                              const int* __restrict__ indices, int* __restrict__ gcnt,
+                                                              int* __restrict__ gcol, int* __restrict__ gidx) {
+  constexpr int GR = kGroupRows;
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= ngroups) return;
+  const int i0 = g * GR;
+  int ptr[GR], end[GR];
+#pragma unroll
+  for (int r = 0; r < GR; ++r) {
+    const bool on = i0 + r < n;
+    ptr[r] = on ? indptr[i0 + r] : 0;
+    end[r] = on ? indptr[i0 + r + 1] : 0;
+  }
+  const int base = indptr[i0];
+  int out = base;
+  while (true) {
+    int chosen = -1, first = -1;
+#pragma unroll
+    for (int r = 0; r < GR; ++r) {
+      if (chosen >= 0 || ptr[r] >= end[r]) continue;
+      if (first < 0) first = r;
+      const int c = indices[ptr[r]];
+      bool later = false;
+#pragma unroll
+      for (int q = 0; q < GR; ++q) {
+        if (q == r || later) continue;
+        const int t1 = min(end[q], ptr[q] + 1 + kMergeWindow);
+        for (int t = ptr[q] + 1; t < t1; ++t)
+          if (indices[t] == c) {
+            later = true;
+            break;
+          }
+      }
+      if (!later) chosen = r;
+    }
+    if (first < 0) break;
+    const bool alone = chosen < 0;
+    if (alone) chosen = first;
+    int c = 0;
+#pragma unroll
+    for (int r = 0; r < GR; ++r)
+      if (r == chosen) c = indices[ptr[r]];
+    int id[GR];
+#pragma unroll
+    for (int r = 0; r < GR; ++r) {
+      const bool take = ptr[r] < end[r] && (alone ? r == chosen : indices[ptr[r]] == c);
+      id[r] = take ? ptr[r] : -1;
+      ptr[r] += take ? 1 : 0;
+    }
+    gcol[out] = c;
+    *reinterpret_cast<int4*>(gidx + (size_t)out * GR) = make_int4(id[0], id[1], id[2], id[3]);
+    ++out;
+  }
+  gcnt[g] = out - base;
+}
+
+// Warp per (group, 32-column-group chunk), as the chunked form, with the
+// accumulators of the group's GR rows: a merged entry's X rows are gathered
+// once and applied to every row that has the entry.  U entries per
+// iteration, loads first; each row accumulates its own entries in CSR order,
+// neighbour by neighbour and block column by block column: the same bits as
+// the other variants.
+template <typename T, int DB, int U>
+__global__ void __launch_bounds__(256) bspmm_group_kernel(int n, int nch, const int* __restrict__ gcnt,
+                                                          const int* __restrict__ gcol,
+                                                          const int* __restrict__ gidx,
+                                                          const int* __restrict__ indptr,
+                                                          const T* __restrict__ vals, const T* __restrict__ X,
+                                                          T* __restrict__ Y, const T* __restrict__ Z, int b, int ld,
+                                                          T alpha, T beta, T gamma) {
+  constexpr int V = Vec<T>::V;
+  constexpr int GR = kGroupRows;
+  const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const long long g = warp / nch;
+  const int chunk = (int)(warp % nch);
+  if (g * GR >= n) return;
+  const int grp = chunk * 32 + lane;
+  const bool on = grp < b / V;
+  const int col = grp * V;
+  T acc[GR][DB][V];
+#pragma unroll
+  for (int r = 0; r < GR; ++r)
+#pragma unroll
+    for (int p = 0; p < DB; ++p)
+#pragma unroll
+      for (int v = 0; v < V; ++v) acc[r][p][v] = T(0);
+  const int s = __ldg(indptr + g * GR), e = s + __ldg(gcnt + g);
+  auto apply = [&](const int4& id4, const T (&x)[DB][V]) {
+    const int id[GR] = {id4.x, id4.y, id4.z, id4.w};
+#pragma unroll
+    for (int r = 0; r < GR; ++r)
+      if (id[r] >= 0) {  // uniform in the warp
+        T blk[DB * DB];
+        load_block<T, DB>(vals, id[r], blk);
+#pragma unroll
+        for (int q = 0; q < DB; ++q)
+#pragma unroll
+          for (int p = 0; p < DB; ++p)
+#pragma unroll
+            for (int v = 0; v < V; ++v) acc[r][p][v] = fma(blk[p * DB + q], x[q][v], acc[r][p][v]);
+      }
+  };
+  int t = s;
+  for (; t + U <= e; t += U) {
+    T x[U][DB][V];
+    int4 id[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int j = __ldg(gcol + t + u);
+      id[u] = __ldg(reinterpret_cast<const int4*>(gidx) + t + u);
+      if (on)
+#pragma unroll
+        for (int q = 0; q < DB; ++q) vgather<T, false>(X + ((size_t)j * DB + q) * ld + col, x[u][q]);
+    }
+    if (on)
+#pragma unroll
+      for (int u = 0; u < U; ++u) apply(id[u], x[u]);
+  }
+  for (; t < e; ++t) {
+    T x[DB][V];
+    const int j = __ldg(gcol + t);
+    const int4 id = __ldg(reinterpret_cast<const int4*>(gidx) + t);
+    if (on) {
+#pragma unroll
+      for (int q = 0; q < DB; ++q) vgather<T, false>(X + ((size_t)j * DB + q) * ld + col, x[q]);
+      apply(id, x);
+    }
+  }
+  if (!on) return;
+#pragma unroll
+  for (int r = 0; r < GR; ++r) {
+    const long long i = g * GR + r;
+    if (i >= n) break;
+#pragma unroll
+    for (int p = 0; p < DB; ++p) {
+      const size_t row = ((size_t)i * DB + p) * ld + col;
+      T out[V], x[V];
+#pragma unroll
+      for (int v = 0; v < V; ++v) out[v] = alpha * acc[r][p][v];
+      if (beta != T(0)) {
+        vload(X + row, x);
+#pragma unroll
+        for (int v = 0; v < V; ++v) out[v] = fma(beta, x[v], out[v]);
+      }
+      if (Z && gamma != T(0)) {
+        vload(Z + row, x);
+#pragma unroll
+        for (int v = 0; v < V; ++v) out[v] = fma(gamma, x[v], out[v]);
+      }
+      vstore(Y + row, out);
+    }
+  }
+}
+
+template <typename T, int U>
+int launch_group(int n, int DB, const PlanView& pv, const int* indptr, const T* vals, const T* X, T* Y, const T* Z,
+                 int b, int ld, T alpha, T beta, T gamma, cudaStream_t st) {
+  constexpr int V = Vec<T>::V;
+  const int nch = ceil_div(b / V, 32);
+  const long long warps = (long long)plan_groups(n) * nch;
+  const unsigned grid = (unsigned)ceil_div(warps * 32, 256ll);
+  rvgp::note_launch();
+  switch (DB) {
+#define RVGP_GRP(DBv)                                                                                              \
+  case DBv:                                                                                                        \
+    bspmm_group_kernel<T, DBv, U><<<grid, 256, 0, st>>>(n, nch, pv.gcnt, pv.gcol, pv.gidx, indptr, vals, X, Y, Z,  \
+                                                        b, ld, alpha, beta, gamma);                                \
+    break;
+    RVGP_GRP(1)
+    RVGP_GRP(2)
+    RVGP_GRP(3)
+    default: RVGP_GRP(4)
+#undef RVGP_GRP
+  }
+  return check_launch("rvgp_bspmm (grouped)");
 }
 
 __global__ void __launch_bounds__(256) spmm_plan_kernel(int n, int hmax, const int* __restrict__ indptr,
@@ -726,21 +956,42 @@ int launch_tiled_db(int n, const PlanView& pv, const int* indptr, const int* ind
   return check_launch("rvgp_bspmm (tiled)");
 }
 
+// Through a plan: the eight plain variants, 8 = tiled (shared-memory halo),
+// 9 / 10 = grouped with 2 / 1 merged entries per iteration.  The tuner picks
+// one per shape class (RVGP_SPMM_VARIANT=v forces one); the same bits come
+// out of all eleven.
 template <typename T>
-int launch_tiled(const void* plan, size_t plan_bytes, int n, int DB, long long nnz, const int* indptr,
-                 const int* indices, const T* vals, const T* X, T* Y, const T* Z, int b, int ld, T alpha, T beta,
-                 T gamma, cudaStream_t st) {
-  constexpr int V = Vec<T>::V;
-  RVGP_CHECK_ARG(b % V == 0 && ld % V == 0 && b <= ld, "rvgp_bspmm: b=%d and ld=%d must be multiples of %d", b, ld, V);
-  RVGP_CHECK_ARG(((uintptr_t)X | (uintptr_t)Y | (uintptr_t)(Z ? Z : X)) % 16 == 0, "rvgp_bspmm: 16-byte alignment");
-  RVGP_CHECK_ARG(DB >= 1 && DB <= 4, "rvgp_bspmm: block size %d not supported (1..4)", DB);
+int launch_planned(const void* plan, size_t plan_bytes, int n, int DB, long long nnz, const int* indptr,
+                   const int* indices, const T* vals, const T* X, T* Y, const T* Z, int b, int ld, T alpha, T beta,
+                   T gamma, cudaStream_t st) {
+  if (int rc = check_args<T>(DB, X, Y, Z, b, ld)) return rc;
+  RVGP_CHECK_ARG(n >= 1 && nnz >= 0 && plan_bytes >= plan_bytes_needed(n, DB, nnz),
+                 "rvgp_bspmm_planned: plan of %zu bytes needed", plan_bytes_needed(n, DB, nnz));
   const PlanView pv = plan_view(const_cast<void*>(plan), plan_bytes, n, DB, nnz);
-  switch (DB) {
-    case 1: return launch_tiled_db<T, 1>(n, pv, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
-    case 2: return launch_tiled_db<T, 2>(n, pv, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
-    case 3: return launch_tiled_db<T, 3>(n, pv, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
-    default: return launch_tiled_db<T, 4>(n, pv, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
+  auto run = [&](int v) -> int {
+    if (v < 8) return run_variant<T>(v, n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
+    if (v == 9) return launch_group<T, 2>(n, DB, pv, indptr, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
+    if (v == 10) return launch_group<T, 1>(n, DB, pv, indptr, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
+    switch (DB) {
+      case 1: return launch_tiled_db<T, 1>(n, pv, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
+      case 2: return launch_tiled_db<T, 2>(n, pv, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
+      case 3: return launch_tiled_db<T, 3>(n, pv, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
+      default: return launch_tiled_db<T, 4>(n, pv, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
+    }
+  };
+  int def = 9;
+  if (const char* fv = getenv("RVGP_SPMM_VARIANT")) def = std::min(10, std::max(0, atoi(fv)));
+  const size_t bytes = (size_t)n * DB * ld * sizeof(T);
+  const bool independent = !overlaps(Y, X, bytes) && !(Z && overlaps(Y, Z, bytes));
+  int v = def;
+  if (independent && getenv("RVGP_SPMM_CHUNK_MIN") == nullptr && getenv("RVGP_SPMM_VARIANT") == nullptr) {
+    char key[160];
+    snprintf(key, sizeof(key), "bspmm-plan %s DB%d b%d n2^%d", sizeof(T) == 4 ? "f32" : "f64", DB, b,
+             autotune::log2_bucket(n));
+    v = autotune::tune(key, 11, def, st, 3, run);
+    if (v < 0) return v;
   }
+  return run(v);
 }
 
 }  // namespace
@@ -756,11 +1007,7 @@ int bspmm_f64(int n, int DB, const int* indptr, const int* indices, const double
 
 size_t spmm_plan_bytes(int n, int DB, long long nnz) {
   if (n < 1 || DB < 1 || DB > 4 || nnz < 0) return 0;
-  Workspace ws(nullptr, 0);
-  ws.take<int>(plan_tiles(n));
-  ws.take<int>((size_t)plan_tiles(n) * plan_hmax(DB));
-  ws.take<unsigned short>((size_t)nnz);
-  return ws.used;
+  return plan_bytes_needed(n, DB, nnz);
 }
 
 int spmm_plan_build(int n, int DB, const int* indptr, const int* indices, long long nnz, void* plan,
@@ -772,6 +1019,9 @@ int spmm_plan_build(int n, int DB, const int* indptr, const int* indices, long l
   const PlanView pv = plan_view(plan, plan_bytes, n, DB, nnz);
   rvgp::note_launch();
   spmm_plan_kernel<<<plan_tiles(n), 256, 0, st>>>(n, plan_hmax(DB), indptr, indices, pv.tile_h, pv.halo, pv.lidx);
+  rvgp::note_launch();
+  spmm_group_plan_kernel<<<ceil_div(plan_groups(n), 256), 256, 0, st>>>(n, plan_groups(n), indptr, indices, pv.gcnt,
+                                                                      pv.gcol, pv.gidx);
   return check_launch("rvgp_spmm_plan_build");
 }
 
@@ -779,15 +1029,15 @@ int bspmm_planned_f32(const void* plan, size_t plan_bytes, int n, int DB, long l
                       const int* indices, const float* vals, const float* X, float* Y, const float* Z, int b, int ld,
                       float alpha, float beta, float gamma, cudaStream_t st) {
   if (!plan) return launch<float>(n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
-  return launch_tiled<float>(plan, plan_bytes, n, DB, nnz, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma,
-                             st);
+  return launch_planned<float>(plan, plan_bytes, n, DB, nnz, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma,
+                               st);
 }
 int bspmm_planned_f64(const void* plan, size_t plan_bytes, int n, int DB, long long nnz, const int* indptr,
                       const int* indices, const double* vals, const double* X, double* Y, const double* Z, int b,
                       int ld, double alpha, double beta, double gamma, cudaStream_t st) {
   if (!plan) return launch<double>(n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, st);
-  return launch_tiled<double>(plan, plan_bytes, n, DB, nnz, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta,
-                              gamma, st);
+  return launch_planned<double>(plan, plan_bytes, n, DB, nnz, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta,
+                                gamma, st);
 }
 
 }  // namespace rvgp
@@ -804,19 +1054,22 @@ RVGP_API int rvgp_bspmm_f64(int n, int DB, const int* indptr, const int* indices
   return rvgp::bspmm_f64(n, DB, indptr, indices, vals, X, Y, Z, b, ld, alpha, beta, gamma, rvgp::as_stream(stream));
 }
 
-// Bytes of the tiled product's plan for a block-CSR matrix of n block rows
+// Bytes of the planned product's plan for a block-CSR matrix of n block rows
 // (DB x DB blocks) and nnz stored blocks.
 RVGP_API size_t rvgp_spmm_plan_bytes(int n, int DB, long long nnz) { return rvgp::spmm_plan_bytes(n, DB, nnz); }
 
 // Builds the plan (per tile of 32 block rows: its halo of distinct columns
-// and the local column of every entry) into caller memory.  Stream-ordered.
+// and the local column of every entry; per group of 4 block rows: the merged
+// list of their columns with each row's entry there) into caller memory.
+// Stream-ordered.
 RVGP_API int rvgp_spmm_plan_build(int n, int DB, const int* indptr, const int* indices, long long nnz, void* plan,
                                   size_t plan_bytes, void* stream) {
   return rvgp::spmm_plan_build(n, DB, indptr, indices, nnz, plan, plan_bytes, rvgp::as_stream(stream));
 }
 
 // rvgp_bspmm_f32 / _f64 through a plan of the same matrix (null plan: the
-// untiled variants).  The same bits as rvgp_bspmm_*.
+// plain variants); the tuner also considers the tiled and grouped forms.
+// The same bits as rvgp_bspmm_*.
 RVGP_API int rvgp_bspmm_planned_f32(const void* plan, size_t plan_bytes, int n, int DB, long long nnz,
                                     const int* indptr, const int* indices, const float* vals, const float* X,
                                     float* Y, const float* Z, int b, int ld, float alpha, float beta, float gamma,

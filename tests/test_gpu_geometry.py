@@ -160,12 +160,18 @@ def test_bspmm(core, d, dtype, b):
 @pytest.mark.parametrize("d,dtype,b", [(1, torch.float32, 564), (2, torch.float32, 564), (2, torch.float64, 130),
                                        (3, torch.float32, 40), (4, torch.float64, 8), (1, torch.float64, 6),
                                        (2, torch.float32, 4)])
-def test_bspmm_planned_same_bits(core, d, dtype, b):
-    """The tiled product (a plan per matrix, halo rows staged in shared memory)
-    gives the bits of the untiled product: tiles of 32 rows with ragged last
+@pytest.mark.parametrize("variant", [None, "8", "9", "10"])
+def test_bspmm_planned_same_bits(core, d, dtype, b, variant, monkeypatch):
+    """The planned product (tuned, or forced: 8 = tiled with halo rows staged
+    in shared memory, 9 / 10 = grouped, merged neighbour lists of 4 rows)
+    gives the bits of the plain product: tiles of 32 rows with ragged last
     column chunks, empty rows, a tile whose halo exceeds the shared-memory
     budget and one with more than 2048 entries (both gather from global
-    memory), and a last tile of fewer than 32 rows."""
+    memory), a last tile of fewer than 32 rows and a last group of one row,
+    a hub row longer than the merge's look-ahead, and rows whose entries are
+    in shuffled (conflicting) orders."""
+    if variant is not None:
+        monkeypatch.setenv("RVGP_SPMM_VARIANT", variant)
     rng = np.random.default_rng(7 * d + b)
     n = 1000 + 17
     A = sp.random(n, n, density=0.012, random_state=3, format="lil")
@@ -174,6 +180,11 @@ def test_bspmm_planned_same_bits(core, d, dtype, b):
     A[128:160, :] = sp.random(32, n, density=0.08, random_state=4).tolil()  # tile 4: > 2048 entries
     A = (A.tocsr() + sp.eye(n)).tocsr()
     A.sort_indices()
+    ind = A.indices.copy()
+    for i in range(200, 240):  # rows 200..239 in shuffled orders
+        s0, s1 = A.indptr[i], A.indptr[i + 1]
+        ind[s0:s1] = rng.permutation(ind[s0:s1])
+    A = sp.csr_matrix((A.data, ind, A.indptr), shape=A.shape)
     blocks = rng.standard_normal((A.nnz, d, d))
     X = rng.standard_normal((n * d, b))
     Z = rng.standard_normal((n * d, b))
@@ -181,11 +192,14 @@ def test_bspmm_planned_same_bits(core, d, dtype, b):
     ip, ix = cu(A.indptr, torch.int32), cu(A.indices, torch.int32)
     plan = core.spmm_plan(ip, ix, d)
     for beta, Zt in ((-0.3, cu(Z, dtype)), (0.0, None)):
+        monkeypatch.delenv("RVGP_SPMM_VARIANT", raising=False)
         ref = core.bspmm(ip, ix, vals, cu(X, dtype), Z=Zt, alpha=0.7, beta=beta, gamma=1.9)
+        if variant is not None:
+            monkeypatch.setenv("RVGP_SPMM_VARIANT", variant)
         got = core.bspmm(ip, ix, vals, cu(X, dtype), Z=Zt, alpha=0.7, beta=beta, gamma=1.9, plan=plan)
         torch.cuda.synchronize()
         assert torch.equal(got, ref)
-    M = sp.bsr_matrix((blocks, A.indices, A.indptr), shape=(n * d, n * d))
+    M = sp.bsr_matrix((blocks, ind, A.indptr), shape=(n * d, n * d))
     want = 0.7 * (M @ X) - 0.3 * X + 1.9 * Z
     got = core.bspmm(ip, ix, vals, cu(X, dtype), Z=cu(Z, dtype), alpha=0.7, beta=-0.3, gamma=1.9, plan=plan)
     tol = 1e-12 if dtype == torch.float64 else 2e-5
@@ -207,6 +221,40 @@ def test_knn_tensor_core_screen(core, D, n, k):
     X[5] = X[17]
     X[40] = X[17]
     X[41] = 2 * X[42] - X[43]  # 42 is the midpoint of 41 and 43
+    idx = core.knn(cu(X), k).cpu().numpy()
+    old = os.environ.get("RVGP_KNN_TC")
+    os.environ["RVGP_KNN_TC"] = "0"
+    try:
+        idx0 = core.knn(cu(X), k).cpu().numpy()
+    finally:
+        if old is None:
+            del os.environ["RVGP_KNN_TC"]
+        else:
+            os.environ["RVGP_KNN_TC"] = old
+    assert np.array_equal(idx, idx0)
+    assert np.array_equal(idx, O.knn(X, k))
+
+
+@pytest.mark.parametrize("kind", ["clusters", "manifold_and_clusters"])
+def test_knn_tensor_core_rescreen_lists(core, kind):
+    """Rows the tensor-core certificate cannot settle go to the SIMT re-screen
+    as a list (its partial lists indexed by list slot, splits per row sized
+    on the device from the list's length).  Tight clusters far apart make a
+    query block straddle clusters, so its centred norms dwarf the neighbour
+    gaps and most rows (all, or a part beside a manifold) are listed; the
+    result equals the oracle's and the SIMT screen's."""
+    import os
+    D, k = 64, 15
+    rng = np.random.default_rng(11)
+    cen = 100.0 * rng.standard_normal((40, D))
+    Xc = cen[rng.integers(0, 40, 3000)] + 0.01 * rng.standard_normal((3000, D))
+    if kind == "clusters":
+        X = Xc
+    else:
+        t = rng.uniform(0, 3, (2000, 3))
+        Q, _ = np.linalg.qr(rng.standard_normal((D, D)))
+        Xm = np.concatenate([np.sin(t), np.cos(t)], axis=1) @ Q[:6] + 0.01 * rng.standard_normal((2000, D))
+        X = np.concatenate([Xm, Xc])[rng.permutation(5000)]
     idx = core.knn(cu(X), k).cpu().numpy()
     old = os.environ.get("RVGP_KNN_TC")
     os.environ["RVGP_KNN_TC"] = "0"
