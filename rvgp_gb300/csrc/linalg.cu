@@ -399,6 +399,61 @@ __global__ void trinv_kernel(const T* __restrict__ L, int ldl, int p, T* __restr
   }
 }
 
+// The same columns with the loads off the dependent chain: at step i the
+// column i of L below the pivot (this lane's rows) is already in shared
+// memory, copied by cp.async two steps earlier into a ring of three column
+// buffers, so a step costs the pivot's multiply, one shuffle and the updates,
+// not an L2 round trip.  Every lane copies and reads only its own rows, so
+// its own cp.async.wait_group orders the ring; the arithmetic and its order
+// are the plain kernel's (the same bits).  One warp per CTA, so the heavy
+// leading columns land on different SMs.
+template <typename T>
+__device__ __forceinline__ void cp_async_el(T* smem, const T* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(s), "l"(gmem), "n"(sizeof(T)) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+template <typename T>
+__global__ void __launch_bounds__(32) trinv_pf_kernel(const T* __restrict__ L, int ldl, int p, T* __restrict__ X,
+                                                      int ldx) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* y = reinterpret_cast<T*>(smem_raw);
+  T* rinv = y + p;
+  T* ring = rinv + p;  // 3 x p
+  const int lane = threadIdx.x;
+  const int j = blockIdx.x;
+  for (int i = lane; i < j; i += 32) X[(size_t)i * ldx + j] = T(0);
+  for (int k = j + ((lane - j) & 31); k < p; k += 32) {
+    y[k] = k == j ? T(1) : T(0);
+    rinv[k] = rcp_nr(L[(size_t)k * ldl + k]);
+  }
+  auto fetch = [&](int c) {  // column c below its pivot, this lane's rows, into slot c % 3
+    if (c < p) {
+      T* dst = ring + (size_t)(c % 3) * p;
+      for (int k = c + 1 + ((lane - c - 1) & 31); k < p; k += 32) cp_async_el(dst + k, L + (size_t)k * ldl + c);
+    }
+    cp_async_commit();  // possibly empty: one group per column keeps the count
+  };
+  fetch(j);
+  fetch(j + 1);
+  for (int i = j; i < p; ++i) {
+    fetch(i + 2);
+    cp_async_wait<2>();  // column i (this lane's part) has landed
+    T xi = T(0);
+    if (lane == (i & 31)) {
+      xi = y[i] * rinv[i];
+      X[(size_t)i * ldx + j] = xi;
+    }
+    xi = __shfl_sync(0xffffffffu, xi, i & 31);
+    const T* ci = ring + (size_t)(i % 3) * p;
+    for (int k = i + 1 + ((lane - i - 1) & 31); k < p; k += 32) y[k] -= ci[k] * xi;
+  }
+  cp_async_wait<0>();
+}
+
 // ------------------------------------------------------------------ Jacobi eigensolver
 template <typename T>
 struct Eps;
@@ -1126,6 +1181,12 @@ int cholesky(T* A, int lda, int p, int* info, cudaStream_t st) {
 
 template <typename T>
 int tri_inv_lower(const T* L, int ldl, int p, T* Linv, int ldi, cudaStream_t st) {
+  const size_t pf_smem = sizeof(T) * 5 * (size_t)p;  // y, 1/L_kk and three columns
+  if (pf_smem <= 200 * 1024) {
+    if (raise_dyn_smem((const void*)trinv_pf_kernel<T>, pf_smem) != cudaSuccess) return check_launch("tri_inv_lower");
+    rvgp::note_launch(); trinv_pf_kernel<T><<<p, 32, pf_smem, st>>>(L, ldl, p, Linv, ldi);
+    return check_launch("tri_inv_lower");
+  }
   // shared memory: 2p values per warp, at most 48 KB per CTA
   const int warps = (int)std::max<size_t>(1, std::min<size_t>(4, (48 * 1024) / (2 * sizeof(T) * (size_t)p)));
   const size_t smem = sizeof(T) * 2 * (size_t)warps * p;
