@@ -271,9 +271,18 @@ def measured_peaks():
 
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of the
-# tiled Chebyshev-step SpMM from ncu captures, keyed by (n, d, p, stored
-# blocks) of the workload's Lc; filled from the captures under profiles/.
-SPMM_TRAFFIC = {}
+# chunked Chebyshev-step SpMM, keyed by (n, d, p, stored blocks) of the
+# workload's Lc, with where the figure comes from.  The capture was made on
+# the n = 50 000 Swiss roll (profiles/bspmm_chunked_kernel_f32_Lc_
+# swissroll64_n50000_p564.md: 693.6 MB against 694.8 MB algorithmic); every
+# term of the product's traffic (X and Z read, Y written, blocks and column
+# indices) grows with the rows and stored blocks, so at n = 100 000 it is
+# scaled by the algorithmic bytes, 1 389 591 924 / 694 757 164.
+SPMM_TRAFFIC = {
+    (100000, 2, 564, 1779596): (int(693.6e6 * 1389591924 / 694757164),
+                                "ncu capture at n = 50 000, scaled by the units processed"),
+    (50000, 2, 564, 887858): (int(693.6e6), "ncu capture"),
+}
 
 
 def spmm_roofline(d, wl, peaks, flush, reps=20):
@@ -330,7 +339,8 @@ def spmm_roofline(d, wl, peaks, flush, reps=20):
     return {"kernel": f"{names.get(variant, '?')} (Chebyshev step, Lc x block; launch tuner's variant {variant})",
             "bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
             "frac": round(achieved / peaks["hbm_gbs"], 4),
-            "traffic": SPMM_TRAFFIC.get((n, k, p, E)), "algorithmic_bytes": int(alg),
+            "traffic": SPMM_TRAFFIC.get((n, k, p, E), (None, None))[0],
+            "traffic_source": SPMM_TRAFFIC.get((n, k, p, E), (None, None))[1], "algorithmic_bytes": int(alg),
             "avg_launch_us": round(t * 1e6, 2), "planned_avg_launch_us": round(t_plan * 1e6, 2),
             "block_width": p, "l2": "flushed before every timed launch"}
 
