@@ -206,13 +206,16 @@ def test_bspmm_planned_same_bits(core, d, dtype, b, variant, monkeypatch):
     np.testing.assert_allclose(got.cpu().double().numpy(), want, atol=tol * np.abs(want).max())
 
 
-@pytest.mark.parametrize("D,n,k", [(20, 3001, 10), (33, 2500, 15), (64, 4100, 15), (64, 700, 1), (48, 1500, 60)])
+@pytest.mark.parametrize("D,n,k", [(20, 3001, 10), (33, 2500, 15), (64, 4100, 15), (64, 700, 1), (48, 1500, 60),
+                                   (40, 50, 5), (17, 129, 8), (64, 129, 20)])
 def test_knn_tensor_core_screen(core, D, n, k):
     """The tensor-core screen (16 < D <= 64: block-centred split-TF32
     distances, certified bound) gives the oracle's exact neighbour lists and
     the SIMT screen's (RVGP_KNN_TC=0): a cloud near a 3-dimensional manifold
-    embedded in D dimensions, tiles cut short (n not a multiple of 128), two
-    duplicated points and a pair at exactly equal distances."""
+    embedded in D dimensions, tiles cut short (n not a multiple of 128, a
+    single partial block, a full block and one more point, the smallest D
+    routed to the tensor cores), two duplicated points and a pair at exactly
+    equal distances."""
     import os
     rng = np.random.default_rng(D * 1000 + n)
     t = rng.uniform(0, 3, (n, 3))
