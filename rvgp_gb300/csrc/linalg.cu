@@ -403,10 +403,15 @@ __global__ void trinv_kernel(const T* __restrict__ L, int ldl, int p, T* __restr
 // column i of L below the pivot (this lane's rows) is already in shared
 // memory, copied by cp.async two steps earlier into a ring of three column
 // buffers, so a step costs the pivot's multiply, one shuffle and the updates,
-// not an L2 round trip.  Every lane copies and reads only its own rows, so
-// its own cp.async.wait_group orders the ring; the arithmetic and its order
-// are the plain kernel's (the same bits).  One warp per CTA, so the heavy
-// leading columns land on different SMs.
+// not an L2 round trip.  The columns are read from a transposed copy (the
+// strictly-lower part of L written into the strictly-upper part of the
+// output first, `lower_to_upper`), so a step's copies are contiguous: a
+// column of row-major L has one element per row, and at p = 800 its lines
+// no longer stay in L1.  The output's upper part is zeroed afterwards.
+// Every lane copies and reads only its own rows, so its own
+// cp.async.wait_group orders the ring; the arithmetic and its order are the
+// plain kernel's (the same bits).  One warp per CTA, so the heavy leading
+// columns land on different SMs.
 template <typename T>
 __device__ __forceinline__ void cp_async_el(T* smem, const T* gmem) {
   const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
@@ -416,16 +421,45 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
+// U[i][k] = L[k][i] for k > i (32 x 32 tiles through shared memory)
 template <typename T>
-__global__ void __launch_bounds__(32) trinv_pf_kernel(const T* __restrict__ L, int ldl, int p, T* __restrict__ X,
-                                                      int ldx) {
+__global__ void __launch_bounds__(256) lower_to_upper(const T* __restrict__ L, int ldl, int p, T* __restrict__ U,
+                                                      int ldu) {
+  __shared__ T tile[32][33];
+  const int kb = blockIdx.y, ib = blockIdx.x;
+  if (kb < ib) return;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  for (int r = ty; r < 32; r += 8) {
+    const int k = kb * 32 + r, i = ib * 32 + tx;
+    tile[r][tx] = (k < p && i < p && k > i) ? L[(size_t)k * ldl + i] : T(0);
+  }
+  __syncthreads();
+  for (int r = ty; r < 32; r += 8) {
+    const int i = ib * 32 + r, k = kb * 32 + tx;
+    if (k < p && i < p && k > i) U[(size_t)i * ldu + k] = tile[tx][r];
+  }
+}
+
+template <typename T>
+__global__ void zero_strict_upper(T* __restrict__ X, int ldx, int p) {
+  const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e >= (long long)p * p) return;
+  const int i = (int)(e / p), j = (int)(e % p);
+  if (j > i) X[(size_t)i * ldx + j] = T(0);
+}
+
+// LT: the transposed strictly-lower part of L (row c holds column c below
+// its pivot), in the strictly-upper part of X itself: the kernel writes only
+// the lower part of X, so the two never meet.
+template <typename T>
+__global__ void __launch_bounds__(32) trinv_pf_kernel(const T* __restrict__ L, int ldl, const T* LT, int ldt, int p,
+                                                      T* X, int ldx) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* y = reinterpret_cast<T*>(smem_raw);
   T* rinv = y + p;
   T* ring = rinv + p;  // 3 x p
   const int lane = threadIdx.x;
   const int j = blockIdx.x;
-  for (int i = lane; i < j; i += 32) X[(size_t)i * ldx + j] = T(0);
   for (int k = j + ((lane - j) & 31); k < p; k += 32) {
     y[k] = k == j ? T(1) : T(0);
     rinv[k] = rcp_nr(L[(size_t)k * ldl + k]);
@@ -433,7 +467,8 @@ __global__ void __launch_bounds__(32) trinv_pf_kernel(const T* __restrict__ L, i
   auto fetch = [&](int c) {  // column c below its pivot, this lane's rows, into slot c % 3
     if (c < p) {
       T* dst = ring + (size_t)(c % 3) * p;
-      for (int k = c + 1 + ((lane - c - 1) & 31); k < p; k += 32) cp_async_el(dst + k, L + (size_t)k * ldl + c);
+      const T* src = LT + (size_t)c * ldt;
+      for (int k = c + 1 + ((lane - c - 1) & 31); k < p; k += 32) cp_async_el(dst + k, src + k);
     }
     cp_async_commit();  // possibly empty: one group per column keeps the count
   };
@@ -1184,7 +1219,10 @@ int tri_inv_lower(const T* L, int ldl, int p, T* Linv, int ldi, cudaStream_t st)
   const size_t pf_smem = sizeof(T) * 5 * (size_t)p;  // y, 1/L_kk and three columns
   if (pf_smem <= 200 * 1024) {
     if (raise_dyn_smem((const void*)trinv_pf_kernel<T>, pf_smem) != cudaSuccess) return check_launch("tri_inv_lower");
-    rvgp::note_launch(); trinv_pf_kernel<T><<<p, 32, pf_smem, st>>>(L, ldl, p, Linv, ldi);
+    const int nb = ceil_div(p, 32);
+    rvgp::note_launch(); lower_to_upper<T><<<dim3(nb, nb), 256, 0, st>>>(L, ldl, p, Linv, ldi);
+    rvgp::note_launch(); trinv_pf_kernel<T><<<p, 32, pf_smem, st>>>(L, ldl, Linv, ldi, p, Linv, ldi);
+    rvgp::note_launch(); zero_strict_upper<T><<<ceil_div((long long)p * p, 256), 256, 0, st>>>(Linv, ldi, p);
     return check_launch("tri_inv_lower");
   }
   // shared memory: 2p values per warp, at most 48 KB per CTA
