@@ -443,7 +443,7 @@ KnnBufs carve(Workspace& ws, const KnnPlan& p, int n, int D) {
   b.part_r2 = ws.take<double>(p.nblk_prep);
   b.radius = ws.take<double>(1);
   b.Xf = ws.take<float>((size_t)n * p.DP);
-  const int ns = std::max(p.nsplit, p.nsplit2);
+  const int ns = std::max(p.tc ? 2 * p.nsplit : p.nsplit, p.nsplit2);  // the TC screen writes two halves
   b.part_d = ws.take<float>((size_t)n * ns * p.kc);
   b.part_i = ws.take<int>((size_t)n * ns * p.kc);
   b.nflag = ws.take<int>(1);
@@ -512,8 +512,8 @@ static int knn_impl(const double* X, int n, int D, int k, int* idx, void* worksp
     cudaMemsetAsync(b.nflag2, 0, sizeof(int), st);
     TRY_RC(knn_tc_screen_launch(p.DP, p.kc, b.Xf, n, b.order, p.nsplit, b.part_d, b.part_i, b.r2q, b.tcerr, st));
     rvgp::note_launch();
-    knn_finish<<<ceil_div(n, 128), 128, 0, st>>>(X, n, D, p.DP, k, p.kc, p.nsplit, b.part_d, b.part_i, b.radius, idx,
-                                                 b.nflag, b.flag_list, b.r2q, b.tcerr, nullptr, nullptr, 0);
+    knn_finish<<<ceil_div(n, 128), 128, 0, st>>>(X, n, D, p.DP, k, p.kc, 2 * p.nsplit, b.part_d, b.part_i, b.radius,
+                                                 idx, b.nflag, b.flag_list, b.r2q, b.tcerr, nullptr, nullptr, 0);
     // rows the tensor-core certificate could not settle (a query block
     // straddling a jump of the Morton curve): the SIMT screen, whose
     // direct-difference certificate does not depend on the block, then the
@@ -521,7 +521,7 @@ static int knn_impl(const double* X, int n, int D, int k, int* idx, void* worksp
     // at n = 100 000), so its rows get up to one split per SM, as many as the
     // part buffers hold (list_splits).
     const int smax = num_sms();
-    const long long cap = (long long)n * std::max(p.nsplit, p.nsplit2);
+    const long long cap = (long long)n * std::max(2 * p.nsplit, p.nsplit2);
     const int gx = (int)std::min<long long>((long long)ceil_div(n, kQB) * smax, 4ll * num_sms());
     rvgp::note_launch();
     screen_kc(p.kc, p.DP, dim3(gx, 1), st, b.Xf, n, smax, b.part_d, b.part_i, b.flag_list, b.nflag, cap);

@@ -24,13 +24,16 @@
 // finish kernel turns it into a certificate with the FP32 copy's own rounding
 // (4.01 u R, as for the SIMT screen) and per-query |x'|² (r2q).
 //
-// CTA: 288 threads.  Warps 0-3: epilogue, thread i owns query row i = TMEM
-// lane i and its register top-kc list (of positions in the order, turned
-// into point indices when written); warps 4-7: producers, thread r stages
+// CTA: 416 threads.  Warps 0-7: epilogue, two per SMSP (the epilogue is
+// latency-bound with one): warp w owns query rows 32 (w % 4) .. = TMEM lanes
+// and the column half w / 4 of every tile, each thread a register top-kc
+// list for its row and half (of positions in the order, turned into point
+// indices when written; the two halves are written as two splits); warps
+// 0-3 also stage the queries.  Warps 8-11: producers, thread r stages
 // candidate row r of a tile (centred, split, 128-byte-swizzled K-major) and
-// its squared norm; warp 8: one thread issues the MMAs.  Two candidate
+// its squared norm; warp 12: one thread issues the MMAs.  Two candidate
 // buffers and two TMEM accumulators; mbarriers: staged[b] (4 producer
-// warps), full[b] (MMA commit), free[b] (4 epilogue warps).  Every wait is
+// warps), full[b] (MMA commit), free[b] (8 epilogue warps).  Every wait is
 // bounded; on a timeout the CTA raises the error flag, drains its MMAs and
 // frees its TMEM.
 #include "common.cuh"
@@ -43,7 +46,8 @@ namespace {
 
 constexpr int kTQ = 128;             // queries per CTA (MMA M)
 constexpr int kTC = 128;             // candidates per tile (MMA N)
-constexpr int kTThreads = 288;
+constexpr int kEpiWarps = 8;           // two per SMSP: column halves of each tile
+constexpr int kTThreads = (kEpiWarps + 4 + 1) * 32;  // + 4 producer warps + the MMA warp
 constexpr uint32_t kTTmemCols = 256;  // two 128-column accumulators
 constexpr long long kTWait = 1ll << 22;
 constexpr int kSlabBytes = kTQ * 128;  // one 32-element K slab of a 128-row operand
@@ -94,6 +98,8 @@ __global__ void __launch_bounds__(kTThreads, 1)
   __shared__ int s_fail;
   __shared__ float cen[DP];
   __shared__ float cn[2][kTC];
+  __shared__ float s_qn[kTQ];  // each query's |x'|², for both epilogue warps of its row
+  __shared__ int s_q[kTQ];     // and its point index (-1 past the end)
   uint8_t* smem = align1k(smem_raw);
   uint8_t* Ahi = smem;
   uint8_t* Alo = Ahi + OPB;
@@ -117,7 +123,7 @@ __global__ void __launch_bounds__(kTThreads, 1)
     for (int b = 0; b < 2; ++b) {
       tc::mbar_init(&bar[b], 4);
       tc::mbar_init(&bar[2 + b], 1);
-      tc::mbar_init(&bar[4 + b], 4);
+      tc::mbar_init(&bar[4 + b], kEpiWarps);
     }
     tc::mbar_init(&bar[6], 1);
     tc::fence_mbar_init();
@@ -157,18 +163,25 @@ __global__ void __launch_bounds__(kTThreads, 1)
         put4(Ahi, Alo, i, s, kc, v);
       }
     if (on && split == 0) r2q[q] = qn;
+    s_qn[i] = qn;
+    s_q[i] = q;
   }
   tc::fence_async_smem();
   __syncthreads();
 
-  if (warp < 4) {
-    // ---- epilogue: thread i = TMEM lane i
+  if (warp < kEpiWarps) {
+    // ---- epilogue: warp w reads TMEM lanes 32 (w % 4) .. (its query rows)
+    // and columns [64 h, 64 h + 64) of each tile, h = w / 4; the two halves of
+    // a row keep their own lists, written as two splits
+    const int row = (warp & 3) * 32 + lane, half = warp >> 2, e = warp * 32 + lane;
+    const float qn_r = s_qn[row];
+    const int q_r = s_q[row];
     RegTop<KC> L;
     L.init();
-    // columns per TMEM load: 32 where the k-list leaves the registers
-    constexpr int kCh = KC > 48 ? 8 : 32;
-    float* sd = reinterpret_cast<float*>(Bb + 4 * OPB);  // kCh x 128 hit staging
-    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+    // columns per TMEM load: 16 where the k-list leaves the registers
+    constexpr int kCh = KC > 48 ? 8 : 16;
+    float* sd = reinterpret_cast<float*>(Bb + 4 * OPB);  // kCh x 256 hit staging
+    const uint32_t trow = tmem + ((uint32_t)((warp & 3) * 32) << 16);
     for (int t = 0; t < ntiles; ++t) {
       const int b = t & 1;
       bool ok = true;
@@ -186,11 +199,11 @@ __global__ void __launch_bounds__(kTThreads, 1)
       }
       tc::fence_after_sync();
       const int cb = c0 + tile_of(t, t0, ntiles) * kTC;
-      const int qp = q0 + tid;  // this query's own position
+      const int qp = q0 + row;  // this query's own position
 #pragma unroll 1
-      for (int c = 0; c < kTC; c += kCh) {
+      for (int c = half * (kTC / 2); c < (half + 1) * (kTC / 2); c += kCh) {
         float v[kCh];
-        if constexpr (kCh == 32) tc::tmem_ld32(trow + (uint32_t)(b * kTC + c), v);
+        if constexpr (kCh == 16) tc::tmem_ld16(trow + (uint32_t)(b * kTC + c), v);
         else tc::tmem_ld8(trow + (uint32_t)(b * kTC + c), v);
         // unrolled: f² and a mask of the columns under the threshold at the
         // chunk's start (a superset of those that insert)
@@ -202,7 +215,7 @@ __global__ void __launch_bounds__(kTThreads, 1)
           const float nn[4] = {nv.x, nv.y, nv.z, nv.w};
 #pragma unroll
           for (int u = 0; u < 4; ++u) {
-            v[4 * g + u] = fmaf(-2.f, v[4 * g + u], qn + nn[u]);
+            v[4 * g + u] = fmaf(-2.f, v[4 * g + u], qn_r + nn[u]);
             mask |= (v[4 * g + u] < wst ? 1u : 0u) << (4 * g + u);
           }
         }
@@ -210,11 +223,11 @@ __global__ void __launch_bounds__(kTThreads, 1)
         // loop with one insertion site (one copy of the register shift)
         if (mask) {
 #pragma unroll
-          for (int j = 0; j < kCh; ++j) sd[j * kTQ + tid] = v[j];
+          for (int j = 0; j < kCh; ++j) sd[j * (kEpiWarps * 32) + e] = v[j];
           while (mask) {
             const int j = __ffs(mask) - 1;
             mask &= mask - 1;
-            const float d2 = sd[j * kTQ + tid];
+            const float d2 = sd[j * (kEpiWarps * 32) + e];
             const int cand = cb + c + j;
             if (d2 < L.worst() && cand < c1 && cand != qp) L.insert(d2, cand);
           }
@@ -224,18 +237,18 @@ __global__ void __launch_bounds__(kTThreads, 1)
       __syncwarp();
       if (lane == 0) tc::mbar_arrive(&bar[4 + b]);
     }
-    if (q >= 0) {
-      const size_t base = ((size_t)q * nsplit + split) * KC;
+    if (q_r >= 0) {
+      const size_t base = ((size_t)q_r * (2 * nsplit) + 2 * split + half) * KC;
 #pragma unroll
       for (int r = 0; r < KC; ++r) {
         part_d[base + r] = L.d[r];
         part_i[base + r] = L.i[r] >= 0 ? order[L.i[r]] : -1;
       }
     }
-  } else if (warp < 8) {
+  } else if (warp < kEpiWarps + 4) {
     // ---- producers: thread r stages candidate row r of each tile; the next
     // tile's row is loaded into registers before the next buffer wait
-    const int r = tid - 128;
+    const int r = tid - kEpiWarps * 32;
     float4 nxt[NS * 8];
     auto fetch = [&](int t) {
       const int cand = c0 + tile_of(t, t0, ntiles) * kTC + r;
@@ -318,7 +331,7 @@ __global__ void __launch_bounds__(kTThreads, 1)
   // path the epilogue waited for the last tile; after a timeout the issuer
   // commits once more and waits (bounded)
   __syncthreads();
-  if (s_fail && warp == 8 && lane == 0) {
+  if (s_fail && warp == kEpiWarps + 4 && lane == 0) {
     tc::mma_commit(&bar[6]);
     tc::mbar_wait(&bar[6], 0, kTWait);
   }
@@ -352,12 +365,13 @@ int launch_dp(int kc, dim3 grid, size_t smem, cudaStream_t st, const float* Xf, 
 }  // namespace
 
 // The screen's launch (kc in 16/32/48/72; DP 32 or 64): part_d / part_i
-// (n x nsplit x kc, the candidates' f² and indices), r2q (n) = |x'|².
+// (n x 2 nsplit x kc, the candidates' f² and indices: each split's two column
+// halves), r2q (n) = |x'|².
 int knn_tc_screen_launch(int DP, int kc, const float* Xf, int n, const int* order, int nsplit, float* part_d,
                          int* part_i, float* r2q, int* err, cudaStream_t st) {
   const int NS = DP / 32;
-  // A hi/lo + two B buffers of hi/lo + the epilogue's 32 x 128 hit staging
-  const size_t smem = 1024 + (size_t)2 * NS * kSlabBytes * 3 + (size_t)32 * kTQ * sizeof(float);
+  // A hi/lo + two B buffers of hi/lo + the epilogue's 16 x 256 hit staging
+  const size_t smem = 1024 + (size_t)2 * NS * kSlabBytes * 3 + (size_t)16 * kEpiWarps * 32 * sizeof(float);
   dim3 grid((n + kTQ - 1) / kTQ, nsplit);
   if (DP == 32) return launch_dp<32>(kc, grid, smem, st, Xf, n, order, nsplit, part_d, part_i, r2q, err);
   return launch_dp<64>(kc, grid, smem, st, Xf, n, order, nsplit, part_d, part_i, r2q, err);
